@@ -1,0 +1,258 @@
+"""TEST INFRASTRUCTURE -- the CPU oracle, never the product.
+
+ctypes bindings for the plain-C FP64 restatement of the reference's tree-code
+path (``oracle/treecode_oracle.c``) and, when it has been built in this
+container, for the reference's own solvers compiled from its sources
+(``oracle/_ref/libref_oracle.so``).  Only the tests, the smoke check and the
+CPU-baseline leg of ``bench.py`` use this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libref_oracle.so")
+
+KERNEL_TSNE = 0
+KERNEL_GRAVITY = 1
+
+# orc_node in treecode_oracle.h (NodeFMM_MORTON_2D flattened), 208 bytes
+NODE_DTYPE = np.dtype([
+    ("bb_c", "f8", 2), ("bb_len", "f8"),
+    ("first_child", "u4"), ("first_part", "u4"), ("count", "u4"), ("pad", "u4"),
+    ("com", "f8", 2), ("m0", "f8"), ("m2", "f8", 4),
+    ("c1", "f8", 2), ("c2", "f8", 4), ("c3", "f8", 8),
+])
+assert NODE_DTYPE.itemsize == 208
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle.so with gcc (FP contraction off: same bits on x86 and Arm)."""
+    src = os.path.join(HERE, "treecode_oracle.c")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(
+            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "treecode_oracle.h"))):
+        subprocess.check_call(["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
+                               "-o", LIB_PATH, src, "-lm", "-lpthread"])
+    return LIB_PATH
+
+
+def build_ref(ref_root: str = "/root/reference") -> str | None:
+    """Compile the reference's own solvers (only where the reference sources exist)."""
+    if not os.path.isdir(os.path.join(ref_root, "src")):
+        return None
+    repo = os.path.dirname(HERE)
+    subprocess.check_call(["make", "-s", "-f", "oracle/Makefile.ref", f"REF={ref_root}"], cwd=repo)
+    return REF_PATH
+
+
+_lib = None
+_ref = None
+P = ctypes.c_void_p
+I64 = ctypes.c_int64
+D = ctypes.c_double
+I = ctypes.c_int
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.orc_get_depth.restype = ctypes.c_uint32
+        L.orc_get_depth.argtypes = [I, I64]
+        L.orc_node_count.restype = I64
+        L.orc_node_count.argtypes = [ctypes.c_uint32]
+        L.orc_morton_codes.argtypes = [I64, P, P, P, P]
+        L.orc_sort_perm.argtypes = [I64, P, P]
+        L.orc_build_tree.argtypes = [ctypes.c_uint32, I64, P, P, P, P]
+        L.orc_sym_fmm_solve.argtypes = [I, D, ctypes.c_uint32, D, I64, P, P, P, P]
+        L.orc_sym_fmm.argtypes = [I, D, I, I, D, I64, P, P, P, P, P, P, P, P, P]
+        L.orc_naive.argtypes = [I, D, I64, P, P, P, I]
+        L.orc_direct_rows.argtypes = [I, D, I64, P, I64, P, P, I]
+        L.orc_bh.argtypes = [I, D, I, D, I64, P, P, P]
+        L.orc_bh.restype = I
+        L.orc_tsne_attractive.argtypes = [I64, P, P, P, P, D, P]
+        L.orc_tsne_step.argtypes = [I64, P, P, P, P, P, I, I, D, D, D, D, P, P, P]
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The reference's own solvers, or None where they were not built."""
+    global _ref
+    if _ref is None and os.path.exists(REF_PATH):
+        R = ctypes.CDLL(REF_PATH)
+        R.ref_get_depth.restype = ctypes.c_uint
+        R.ref_get_depth.argtypes = [I, I]
+        R.ref_sym_fmm.argtypes = [I, D, I, I, D, I64] + [P] * 9 + [I]
+        R.ref_naive.argtypes = [I, D, I64, P, P, P]
+        R.ref_bh.argtypes = [I, D, I, D, I64, P, P, P, P]
+        _ref = R
+    return _ref
+
+
+def get_depth(max_children: int, n: int) -> int:
+    return int(lib().orc_get_depth(max_children, n))
+
+
+def node_count(depth: int) -> int:
+    return int(lib().orc_node_count(depth))
+
+
+def bbox(pos: np.ndarray):
+    return pos.min(0).astype(np.float64), pos.max(0).astype(np.float64)
+
+
+def morton_codes(pos, mn, mx):
+    pos = np.ascontiguousarray(pos, np.float64)
+    out = np.empty(len(pos), np.uint32)
+    lib().orc_morton_codes(len(pos), _p(pos), _p(np.asarray(mn, np.float64)),
+                           _p(np.asarray(mx, np.float64)), _p(out))
+    return out
+
+
+def sort_perm(codes):
+    codes = np.ascontiguousarray(codes, np.uint32)
+    perm = np.empty(len(codes), np.int32)
+    lib().orc_sort_perm(len(codes), _p(codes), _p(perm))
+    return perm
+
+
+def sym_fmm(pos, *, kernel=KERNEL_TSNE, eps=0.0, max_children=16, depth=-1, theta=0.5,
+            mn=None, mx=None, want_nodes=True):
+    """updateTree + solveNbody of the symmetric Morton FMM (sorted-order outputs)."""
+    pos = np.ascontiguousarray(pos, np.float64)
+    n = len(pos)
+    if mn is None:
+        mn, mx = bbox(pos)
+    d = depth if depth >= 0 else get_depth(max_children, n)
+    codes = np.empty(n, np.uint32)
+    ids = np.empty(n, np.int32)
+    ps = np.empty((n, 2))
+    g = np.zeros((n, 2))
+    tot = np.zeros(1)
+    nodes = np.zeros(node_count(d), NODE_DTYPE) if want_nodes else None
+    lib().orc_sym_fmm(kernel, eps, max_children, d, theta, n, _p(pos),
+                      _p(np.asarray(mn, np.float64)), _p(np.asarray(mx, np.float64)),
+                      _p(codes), _p(ids), _p(ps), _p(g), _p(tot), _p(nodes))
+    return dict(codes=codes, ids=ids, pos=ps, grad=g, total=float(tot[0]), nodes=nodes, depth=d)
+
+
+def naive(pos, *, kernel=KERNEL_TSNE, eps=0.0, nthreads=None):
+    pos = np.ascontiguousarray(pos, np.float64)
+    g = np.zeros_like(pos)
+    tot = np.zeros(1)
+    lib().orc_naive(kernel, eps, len(pos), _p(pos), _p(g), _p(tot), nthreads or os.cpu_count() or 1)
+    return g, float(tot[0])
+
+
+def direct_rows(pos, rows, *, kernel=KERNEL_TSNE, eps=0.0, nthreads=None):
+    pos = np.ascontiguousarray(pos, np.float64)
+    rows = np.ascontiguousarray(rows, np.int64)
+    g = np.zeros((len(rows), 2))
+    lib().orc_direct_rows(kernel, eps, len(pos), _p(pos), len(rows), _p(rows), _p(g),
+                          nthreads or os.cpu_count() or 1)
+    return g
+
+
+def bh(pos, *, kernel=KERNEL_TSNE, eps=0.0, max_children=16, theta=0.5):
+    pos = np.ascontiguousarray(pos, np.float64)
+    g = np.zeros_like(pos)
+    tot = np.zeros(1)
+    lib().orc_bh(kernel, eps, max_children, theta, len(pos), _p(pos), _p(g), _p(tot))
+    return g, float(tot[0])
+
+
+def tsne_attractive(row_ptr, col, val, pos, exag, grad):
+    lib().orc_tsne_attractive(len(pos), _p(row_ptr), _p(col), _p(val), _p(pos), exag, _p(grad))
+
+
+def tsne_step(y, y_prev, row_ptr, col, val, *, max_children=16, depth=-1, theta=0.5,
+              exag_code=16.0, lr=None, momentum=0.5):
+    y = np.ascontiguousarray(y, np.float64)
+    y_prev = np.ascontiguousarray(y_prev, np.float64)
+    n = len(y)
+    d = depth if depth >= 0 else get_depth(max_children, n)
+    lr = n / 15.0 if lr is None else lr
+    yn = np.empty_like(y)
+    g = np.zeros_like(y)
+    z = np.zeros(1)
+    lib().orc_tsne_step(n, _p(y), _p(y_prev), _p(np.ascontiguousarray(row_ptr, np.uint32)),
+                        _p(np.ascontiguousarray(col, np.uint32)),
+                        _p(np.ascontiguousarray(val, np.float64)), max_children, d, theta,
+                        exag_code, lr, momentum, _p(yn), _p(g), _p(z))
+    return yn, g, float(z[0])
+
+
+# ---------------------------------------------------------------- reference
+def ref_sym_fmm(pos, *, kernel=KERNEL_TSNE, eps=0.0, max_children=16, depth=-1, theta=0.5,
+                mn=None, mx=None, symmetric=True):
+    R = ref_lib()
+    if R is None:
+        return None
+    pos = np.ascontiguousarray(pos, np.float64)
+    n = len(pos)
+    if mn is None:
+        mn, mx = bbox(pos)
+    d = depth if depth >= 0 else int(R.ref_get_depth(max_children, n))
+    mm = np.array([mn[0], mn[1], mx[0], mx[1]], np.float64)
+    codes = np.empty(n, np.uint32)
+    ids = np.empty(n, np.int32)
+    ps = np.empty((n, 2))
+    g = np.zeros((n, 2))
+    tot = np.zeros(1)
+    nodes = np.zeros((node_count(d), 27))
+    tm = np.zeros(2)
+    R.ref_sym_fmm(kernel, eps, max_children, d, theta, n, _p(pos), _p(mm), _p(codes), _p(ids),
+                  _p(ps), _p(g), _p(tot), _p(nodes), _p(tm), 1 if symmetric else 0)
+    return dict(codes=codes, ids=ids, pos=ps, grad=g, total=float(tot[0]), nodes=nodes,
+                depth=d, times=tm)
+
+
+def ref_naive(pos, *, kernel=KERNEL_TSNE, eps=0.0):
+    R = ref_lib()
+    if R is None:
+        return None
+    pos = np.ascontiguousarray(pos, np.float64)
+    g = np.zeros_like(pos)
+    tot = np.zeros(1)
+    R.ref_naive(kernel, eps, len(pos), _p(pos), _p(g), _p(tot))
+    return g, float(tot[0])
+
+
+def ref_bh(pos, *, kernel=KERNEL_TSNE, eps=0.0, max_children=16, theta=0.5):
+    R = ref_lib()
+    if R is None:
+        return None
+    pos = np.ascontiguousarray(pos, np.float64)
+    g = np.zeros_like(pos)
+    tot = np.zeros(1)
+    tm = np.zeros(2)
+    R.ref_bh(kernel, eps, max_children, theta, len(pos), _p(pos), _p(g), _p(tot), _p(tm))
+    return g, float(tot[0])
+
+
+def ref_nodes_to_struct(ref_nodes: np.ndarray) -> np.ndarray:
+    """Map the reference harness's 27-double node rows onto NODE_DTYPE."""
+    out = np.zeros(len(ref_nodes), NODE_DTYPE)
+    out["bb_c"] = ref_nodes[:, 0:2]
+    out["bb_len"] = ref_nodes[:, 2]
+    out["first_child"] = ref_nodes[:, 3].astype(np.uint32)
+    out["first_part"] = ref_nodes[:, 4].astype(np.uint32)
+    out["count"] = ref_nodes[:, 5].astype(np.uint32)
+    out["com"] = ref_nodes[:, 6:8]
+    out["m0"] = ref_nodes[:, 8]
+    out["m2"] = ref_nodes[:, 9:13]
+    out["c1"] = ref_nodes[:, 13:15]
+    out["c2"] = ref_nodes[:, 15:19]
+    out["c3"] = ref_nodes[:, 19:27]
+    return out

@@ -1,0 +1,823 @@
+/*
+ * TEST INFRASTRUCTURE -- NOT PART OF THE PRODUCT.
+ * Plain-C FP64 restatement of the reference's CPU tree-code path; see
+ * treecode_oracle.h for the contract.  Reference paths are relative to the
+ * reference project.  Operation order follows the reference expression by
+ * expression so that, compiled with -ffp-contract=off, results are bitwise
+ * identical to the compiled reference on the same inputs.
+ */
+#include "treecode_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------ */
+/* kernel radial factors                                               */
+/* ------------------------------------------------------------------ */
+
+/* t-SNE: nBodySolverFMM_SYM_MORTON.h:624-636 (D1 = rS^-2, D2 = -4 rS^-3,
+ * D3 = 24 rS^-4).  Gravity: F(R) = R g(s), g = -(s + eps^2)^-3/2,
+ * D1 = g, D2 = 2g', D3 = 4g''; pair term t = -(s + eps^2)^-1/2.          */
+typedef struct { double D1, D2, D3, t; } derivs;
+
+static inline derivs tsne_derivs(double sq_r)
+{
+    derivs d;
+    double rS = 1.0 + sq_r;
+    double inv = 1.0 / rS;
+    double inv2 = inv * inv;
+    double inv3 = inv2 * inv;
+    double inv4 = inv3 * inv;
+    d.D1 = inv2;
+    d.D2 = -4.0 * inv3;
+    d.D3 = 24.0 * inv4;
+    d.t = rS; /* callers divide by rS as the reference does */
+    return d;
+}
+
+static inline derivs grav_derivs(double s, double eps2)
+{
+    derivs d;
+    double u = s + eps2;
+    double iu = 1.0 / u;
+    double isq = 1.0 / sqrt(u);
+    double g = -isq * iu;
+    d.D1 = g;
+    d.D2 = -3.0 * g * iu;
+    d.D3 = -5.0 * d.D2 * iu;
+    d.t = -isq;
+    return d;
+}
+
+/* C1 from a source of mass MB0 and second moment MB2 at offset R
+ * (nBodySolverFMM_SYM_MORTON.h:638-655).                                   */
+static inline void far_c1(double Rx, double Ry, double MB0, const double* MB2,
+                          double D1, double D2, double D3, double* out)
+{
+    double inv = 1.0 / MB0;
+    double T00 = inv * MB2[0], T01 = inv * MB2[1], T10 = inv * MB2[2], T11 = inv * MB2[3];
+    double S1 = T00 + T11;
+    double S2 = (Rx * Rx * T00) + (Rx * Ry * T01) + (Ry * Rx * T10) + (Ry * Ry * T11);
+    double S30 = Rx * T00 + Ry * T01;
+    double S31 = Rx * T10 + Ry * T11;
+    out[0] = MB0 * (Rx * (D1 + 0.5 * (S1)*D2 + 0.5 * (S2)*D3) + (S30)*D2);
+    out[1] = MB0 * (Ry * (D1 + 0.5 * (S1)*D2 + 0.5 * (S2)*D3) + (S31)*D2);
+}
+
+/* C2/C3 block (nBodySolverFMM_SYM_MORTON.h:657-697): C2 = MA0*(MB0*(...)).
+ * has_mb selects the P2L form (:764-804) that has no MB0 factor.            */
+static inline void c2c3(double Rx, double Ry, double MA0, double MB0, int has_mb,
+                        double D1, double D2, double D3, double* C2, double* C3)
+{
+    double r[2] = {Rx, Ry};
+    double e2[4], e3[8];
+    e2[0] = (D1 + Rx * Rx * D2);
+    e2[1] = (Rx * Ry * D2);
+    e2[2] = (Ry * Rx * D2);
+    e2[3] = (D1 + Ry * Ry * D2);
+    e3[0] = ((Rx + Rx + Rx) * D2 + Rx * Rx * Rx * D3);
+    e3[1] = ((Ry)*D2 + Rx * Rx * Ry * D3);
+    e3[2] = ((Ry)*D2 + Rx * Ry * Rx * D3);
+    e3[3] = ((Rx)*D2 + Rx * Ry * Ry * D3);
+    e3[4] = ((Ry)*D2 + Ry * Rx * Rx * D3);
+    e3[5] = ((Rx)*D2 + Ry * Rx * Ry * D3);
+    e3[6] = ((Rx)*D2 + Ry * Ry * Rx * D3);
+    e3[7] = ((Ry + Ry + Ry) * D2 + Ry * Ry * Ry * D3);
+    (void)r;
+    for (int i = 0; i < 4; i++) C2[i] = has_mb ? MA0 * (MB0 * e2[i]) : MA0 * e2[i];
+    for (int i = 0; i < 8; i++) C3[i] = has_mb ? MA0 * (MB0 * e3[i]) : MA0 * e3[i];
+}
+
+/* Gravity kernels use the same expression layout as the t-SNE kernels.
+ * The gravity C2/C3 are built with (MA0*MB0) as one factor, matching the
+ * reference-side gravity kernels in oracle/ref_harness.cpp.               */
+static inline void c2c3_grav(double Rx, double Ry, double scale, double D1, double D2,
+                             double D3, double* C2, double* C3)
+{
+    double r[2] = {Rx, Ry};
+    for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 2; j++) {
+            C2[i * 2 + j] = scale * ((i == j ? D1 : 0.0) + r[i] * r[j] * D2);
+            for (int k = 0; k < 2; k++) {
+                double d = ((i == j) ? r[k] : 0.0) + ((i == k) ? r[j] : 0.0) + ((j == k) ? r[i] : 0.0);
+                C3[i * 4 + j * 2 + k] = scale * (d * D2 + r[i] * r[j] * r[k] * D3);
+            }
+        }
+}
+
+typedef struct {
+    int kernel;
+    double eps2;
+    double theta;
+    const double* pos;
+    double* grad;
+    orc_node* nodes;
+    double total;
+} sym_ctx;
+
+/* TSNE_FMM_SYM_MORTON_NN_Kernel (:622-723) / gravity counterpart */
+static void kernel_nn(sym_ctx* c, orc_node* A, orc_node* B)
+{
+    double Rx = A->com[0] - B->com[0];
+    double Ry = A->com[1] - B->com[1];
+    double sq = Rx * Rx + Ry * Ry;
+    double C1[2], C2[4], C3[8];
+    if (c->kernel == ORC_KERNEL_TSNE) {
+        derivs d = tsne_derivs(sq);
+        far_c1(Rx, Ry, B->m0, B->m2, d.D1, d.D2, d.D3, C1);
+        c2c3(Rx, Ry, A->m0, B->m0, 1, d.D1, d.D2, d.D3, C2, C3);
+        A->c1[0] += C1[0]; A->c1[1] += C1[1];
+        for (int i = 0; i < 4; i++) A->c2[i] += C2[i];
+        for (int i = 0; i < 8; i++) A->c3[i] += C3[i];
+        far_c1(-Rx, -Ry, A->m0, A->m2, d.D1, d.D2, d.D3, C1);
+        B->c1[0] += C1[0]; B->c1[1] += C1[1];
+        for (int i = 0; i < 4; i++) B->c2[i] += C2[i];
+        for (int i = 0; i < 8; i++) B->c3[i] += -C3[i];
+        c->total += 2.0 * (A->m0 * B->m0) / d.t;
+    } else {
+        derivs d = grav_derivs(sq, c->eps2);
+        far_c1(Rx, Ry, B->m0, B->m2, d.D1, d.D2, d.D3, C1);
+        c2c3_grav(Rx, Ry, A->m0 * B->m0, d.D1, d.D2, d.D3, C2, C3);
+        A->c1[0] += C1[0]; A->c1[1] += C1[1];
+        for (int i = 0; i < 4; i++) A->c2[i] += C2[i];
+        for (int i = 0; i < 8; i++) A->c3[i] += C3[i];
+        far_c1(-Rx, -Ry, A->m0, A->m2, d.D1, d.D2, d.D3, C1);
+        B->c1[0] += C1[0]; B->c1[1] += C1[1];
+        for (int i = 0; i < 4; i++) B->c2[i] += C2[i];
+        for (int i = 0; i < 8; i++) B->c3[i] += -C3[i];
+        c->total += 2.0 * (A->m0 * B->m0) * d.t;
+    }
+}
+
+/* TSNE_FMM_SYM_MORTON_PN_Kernel (:726-815) / gravity counterpart */
+static void kernel_pn(sym_ctx* c, int64_t p, orc_node* B)
+{
+    const double* x = c->pos + 2 * p;
+    double Rx = x[0] - B->com[0];
+    double Ry = x[1] - B->com[1];
+    double sq = Rx * Rx + Ry * Ry;
+    double C1[2], C2[4], C3[8];
+    derivs d = (c->kernel == ORC_KERNEL_TSNE) ? tsne_derivs(sq) : grav_derivs(sq, c->eps2);
+    far_c1(Rx, Ry, B->m0, B->m2, d.D1, d.D2, d.D3, C1);
+    c->grad[2 * p] += C1[0];
+    c->grad[2 * p + 1] += C1[1];
+    Rx = -Rx;
+    Ry = -Ry;
+    if (c->kernel == ORC_KERNEL_TSNE) {
+        c2c3(Rx, Ry, B->m0, 1.0, 0, d.D1, d.D2, d.D3, C2, C3);
+    } else {
+        c2c3_grav(Rx, Ry, B->m0, d.D1, d.D2, d.D3, C2, C3);
+    }
+    B->c1[0] += (Rx * d.D1);
+    B->c1[1] += (Ry * d.D1);
+    for (int i = 0; i < 4; i++) B->c2[i] += C2[i];
+    for (int i = 0; i < 8; i++) B->c3[i] += C3[i];
+    if (c->kernel == ORC_KERNEL_TSNE)
+        c->total += 2.0 * B->m0 / d.t;
+    else
+        c->total += 2.0 * B->m0 * d.t;
+}
+
+/* TSNE_FMM_SYM_MORTON_PP_Kernel (:818-836) / gravity counterpart */
+static void kernel_pp(sym_ctx* c, int64_t a, int64_t b)
+{
+    const double* xa = c->pos + 2 * a;
+    const double* xb = c->pos + 2 * b;
+    double Rx = xa[0] - xb[0];
+    double Ry = xa[1] - xb[1];
+    double sq = Rx * Rx + Ry * Ry;
+    if (c->kernel == ORC_KERNEL_TSNE) {
+        double fd = 1.0 / (1.0 + sq);
+        c->grad[2 * a] += fd * fd * Rx;
+        c->grad[2 * a + 1] += fd * fd * Ry;
+        c->grad[2 * b] += fd * fd * (-Rx);
+        c->grad[2 * b + 1] += fd * fd * (-Ry);
+        c->total += 2.0 * fd;
+    } else {
+        derivs d = grav_derivs(sq, c->eps2);
+        c->grad[2 * a] += d.D1 * Rx;
+        c->grad[2 * a + 1] += d.D1 * Ry;
+        c->grad[2 * b] += d.D1 * (-Rx);
+        c->grad[2 * b + 1] += d.D1 * (-Ry);
+        c->total += 2.0 * d.t;
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* tree construction                                                   */
+/* ------------------------------------------------------------------ */
+
+uint32_t orc_get_depth(int max_children, int64_t n)
+{
+    /* N / max_children is integer division in the reference (int / int).   */
+    const double circle_area = 3.141592653589793238462643383279502884 / 4.0;
+    double depth_real = log((1.0 / circle_area) * (double)((int)n / max_children)) / log(4.0);
+    return (uint32_t)ceil(depth_real);
+}
+
+int64_t orc_node_count(uint32_t depth)
+{
+    int64_t total = 0, s = 1;
+    for (uint32_t l = 0; l <= depth; l++) {
+        total += s;
+        s *= 4;
+    }
+    return total;
+}
+
+static int64_t level_index(uint32_t l) { return (((int64_t)1 << (2 * l)) - 1) / 3; }
+
+static inline uint32_t spread16(uint32_t x)
+{
+    x = (x | (x << 8)) & 0x00FF00FFu;
+    x = (x | (x << 4)) & 0x0F0F0F0Fu;
+    x = (x | (x << 2)) & 0x33333333u;
+    x = (x | (x << 1)) & 0x55555555u;
+    return x;
+}
+
+static inline double dmin(double a, double b) { return (b < a) ? b : a; }
+static inline double dmax(double a, double b) { return (a < b) ? b : a; }
+
+void orc_morton_codes(int64_t n, const double* pos, const double min_xy[2],
+                      const double max_xy[2], uint32_t* codes)
+{
+    double nmx = -min_xy[0], nmy = -min_xy[1];
+    double L = dmax(max_xy[0] + nmx, max_xy[1] + nmy); /* compMax (:84-85) */
+    for (int64_t i = 0; i < n; i++) {
+        double px = (pos[2 * i] + nmx) / (L);
+        double py = (pos[2 * i + 1] + nmy) / (L);
+        px = dmin(dmax(px * 65536.0, 0.0), 65535.0);
+        py = dmin(dmax(py * 65536.0, 0.0), 65535.0);
+        codes[i] = (spread16((uint32_t)py) << 1) | spread16((uint32_t)px);
+    }
+}
+
+static const uint32_t* g_sort_codes;
+static int cmp_code_idx(const void* a, const void* b)
+{
+    int32_t ia = *(const int32_t*)a, ib = *(const int32_t*)b;
+    uint32_t ca = g_sort_codes[ia], cb = g_sort_codes[ib];
+    if (ca != cb) return ca < cb ? -1 : 1;
+    return (ia > ib) - (ia < ib);
+}
+
+void orc_sort_perm(int64_t n, const uint32_t* codes, int32_t* perm)
+{
+    for (int64_t i = 0; i < n; i++) perm[i] = (int32_t)i;
+    g_sort_codes = codes;
+    qsort(perm, (size_t)n, sizeof(int32_t), cmp_code_idx);
+}
+
+void orc_build_tree(uint32_t depth, int64_t n, const double* pos, const double min_xy[2],
+                    const double max_xy[2], orc_node* nodes)
+{
+    int64_t nn = orc_node_count(depth);
+    memset(nodes, 0, (size_t)nn * sizeof(orc_node));
+    double nmx = -min_xy[0], nmy = -min_xy[1];
+    double L = dmax(max_xy[0] + nmx, max_xy[1] + nmy);
+    uint32_t W = 1u << depth;
+    double h = L / (double)W;
+    int64_t base = level_index(depth);
+    /* createLeafNodes (:328-379) */
+    for (int64_t i = 0; i < n; i++) {
+        double gx = (double)W * (pos[2 * i] + nmx) / (L);
+        double gy = (double)W * (pos[2 * i + 1] + nmy) / (L);
+        uint32_t ux = (uint32_t)gx, uy = (uint32_t)gy;
+        if (ux > W - 1u) ux = W - 1u;
+        if (uy > W - 1u) uy = W - 1u;
+        orc_node* q = &nodes[base + ((spread16(uy) << 1) | spread16(ux))];
+        if (q->count == 0u) {
+            q->bb_c[0] = min_xy[0] + h * (double)ux + 0.5 * h;
+            q->bb_c[1] = min_xy[1] + h * (double)uy + 0.5 * h;
+            q->bb_len = h;
+            q->first_part = (uint32_t)i;
+        }
+        q->count += 1u;
+        q->com[0] += pos[2 * i];
+        q->com[1] += pos[2 * i + 1];
+    }
+    for (int64_t k = base; k < base + ((int64_t)1 << (2 * depth)); k++) {
+        orc_node* q = &nodes[k];
+        if (q->count == 0u) continue;
+        q->m0 = q->count;
+        q->com[0] /= q->m0;
+        q->com[1] /= q->m0;
+        for (uint32_t p = q->first_part; p < q->first_part + q->count; p++) {
+            double rx = pos[2 * p] - q->com[0];
+            double ry = pos[2 * p + 1] - q->com[1];
+            q->m2[0] += rx * rx;
+            q->m2[1] += rx * ry;
+            q->m2[2] += ry * rx;
+            q->m2[3] += ry * ry;
+        }
+    }
+    /* bottomUpNodeConstruction (:381-470) */
+    static const double off[4][2] = {{0.5, 0.5}, {-0.5, 0.5}, {0.5, -0.5}, {-0.5, -0.5}};
+    for (int l = (int)depth - 1; l >= 0; l--) {
+        int64_t li = level_index((uint32_t)l), lc = level_index((uint32_t)l + 1);
+        int64_t ls = (int64_t)1 << (2 * l);
+        for (int64_t i = 0; i < ls; i++) {
+            orc_node* q = &nodes[li + i];
+            int64_t fc = lc + 4 * i;
+            for (int j = 3; j >= 0; j--) {
+                orc_node* ch = &nodes[fc + j];
+                if (ch->count == 0u) continue;
+                q->first_child = (uint32_t)fc;
+                q->bb_c[0] = off[j][0] * ch->bb_len + ch->bb_c[0];
+                q->bb_c[1] = off[j][1] * ch->bb_len + ch->bb_c[1];
+                q->bb_len = 2.0 * ch->bb_len;
+                q->first_part = ch->first_part;
+                q->count += ch->count;
+                q->com[0] += ch->m0 * ch->com[0];
+                q->com[1] += ch->m0 * ch->com[1];
+                q->m0 += ch->m0;
+            }
+            if (q->count == 0u) continue;
+            q->com[0] /= q->m0;
+            q->com[1] /= q->m0;
+            for (int64_t c = q->first_child; c < (int64_t)q->first_child + 4; c++) {
+                orc_node* ch = &nodes[c];
+                if (ch->m0 == 0.0) continue;
+                double rx = ch->com[0] - q->com[0];
+                double ry = ch->com[1] - q->com[1];
+                q->m2[0] += rx * rx;
+                q->m2[1] += rx * ry;
+                q->m2[2] += ry * rx;
+                q->m2[3] += ry * ry;
+                for (int t = 0; t < 4; t++) q->m2[t] += ch->m2[t];
+            }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* symmetric dual-tree traversal                                       */
+/* ------------------------------------------------------------------ */
+
+/* traverse_SYM_PN (:272-313) */
+static void trav_pn(sym_ctx* c, int64_t p, orc_node* B)
+{
+    const double* x = c->pos + 2 * p;
+    double dx = x[0] - B->com[0], dy = x[1] - B->com[1];
+    double dist = dx * dx + dy * dy;
+    double thr = B->bb_len / c->theta;
+    if (dist > thr * thr) {
+        kernel_pn(c, p, B);
+    } else if (B->first_child == 0) {
+        for (int64_t q = B->first_part; q < (int64_t)B->first_part + B->count; q++)
+            if (q != p) kernel_pp(c, p, q);
+    } else {
+        for (uint32_t k = B->first_child; k < B->first_child + 4; k++)
+            if (c->nodes[k].count != 0) trav_pn(c, p, &c->nodes[k]);
+    }
+}
+
+/* traverse_SYM_NN (:154-270).  Point identity uses the sorted index, which is
+ * equivalent to the reference's ID check when IDs are unique.              */
+static void trav_nn(sym_ctx* c, orc_node* A, orc_node* B)
+{
+    double dx = A->com[0] - B->com[0], dy = A->com[1] - B->com[1];
+    double dist = dx * dx + dy * dy;
+    double thr = (A->bb_len + B->bb_len) / c->theta;
+    if (dist > thr * thr) {
+        if (A->count != 0 && B->count != 0) kernel_nn(c, A, B);
+    } else if (A->first_child == 0) {
+        if (A == B) {
+            for (int64_t i = A->first_part; i < (int64_t)A->first_part + A->count; i++)
+                if (B->count != 0)
+                    for (int64_t j = i; j < (int64_t)B->first_part + B->count; j++)
+                        if (i != j) kernel_pp(c, i, j);
+        } else {
+            for (int64_t i = A->first_part; i < (int64_t)A->first_part + A->count; i++)
+                if (B->count != 0) trav_pn(c, i, B);
+        }
+    } else if (B->first_child == 0) {
+        if (A == B) {
+            for (int64_t j = B->first_part; j < (int64_t)B->first_part + B->count; j++)
+                if (A->count != 0)
+                    for (int64_t i = j; i < (int64_t)A->first_part + A->count; i++)
+                        if (i != j) kernel_pp(c, i, j);
+        } else {
+            for (int64_t j = B->first_part; j < (int64_t)B->first_part + B->count; j++)
+                if (A->count != 0) trav_pn(c, j, A);
+        }
+    } else {
+        for (uint32_t a = A->first_child; a < A->first_child + 4; a++) {
+            uint32_t b0 = (A == B) ? a : B->first_child;
+            for (uint32_t b = b0; b < B->first_child + 4; b++)
+                if (c->nodes[a].count != 0 && c->nodes[b].count != 0)
+                    trav_nn(c, &c->nodes[a], &c->nodes[b]);
+        }
+    }
+}
+
+/* einsum<Index<0>,Index<0,1>>(d, C2)_j = sum_i d_i C2_ij                   */
+static inline void contract2(const double* d, const double* C2, double* out)
+{
+    out[0] = d[0] * C2[0] + d[1] * C2[2];
+    out[1] = d[0] * C2[1] + d[1] * C2[3];
+}
+/* einsum<Index<0>,Index<0,1,2>>(d, C3)_jk = sum_i d_i C3_ijk               */
+static inline void contract3(const double* d, const double* C3, double* out)
+{
+    for (int jk = 0; jk < 4; jk++) out[jk] = d[0] * C3[jk] + d[1] * C3[4 + jk];
+}
+
+/* applyForces (:482-536): L2L into non-empty children, L2P at leaves.      */
+static void apply_forces(sym_ctx* c, orc_node* q)
+{
+    if (q->first_child != 0) {
+        for (uint32_t k = q->first_child; k < q->first_child + 4; k++) {
+            orc_node* ch = &c->nodes[k];
+            if (ch->count == 0) continue;
+            double inv = 1.0 / ch->m0;
+            for (int i = 0; i < 4; i++) ch->c2[i] *= inv;
+            for (int i = 0; i < 8; i++) ch->c3[i] *= inv;
+            double d[2] = {ch->com[0] - q->com[0], ch->com[1] - q->com[1]};
+            double e1[2], e3[4], e31[2], e2[4];
+            contract2(d, q->c2, e1);
+            contract3(d, q->c3, e3);
+            contract2(d, e3, e31);
+            for (int i = 0; i < 2; i++) ch->c1[i] += q->c1[i] + e1[i] + 0.5 * e31[i];
+            for (int i = 0; i < 4; i++) e2[i] = q->c2[i] + e3[i];
+            for (int i = 0; i < 4; i++) ch->c2[i] += e2[i];
+            for (int i = 0; i < 8; i++) ch->c3[i] += q->c3[i];
+            apply_forces(c, ch);
+        }
+    } else {
+        for (int64_t p = q->first_part; p < (int64_t)q->first_part + q->count; p++) {
+            double d[2] = {c->pos[2 * p] - q->com[0], c->pos[2 * p + 1] - q->com[1]};
+            double e1[2], e3[4], e31[2];
+            contract2(d, q->c2, e1);
+            contract3(d, q->c3, e3);
+            contract2(d, e3, e31);
+            c->grad[2 * p] += q->c1[0] + e1[0] + 0.5 * e31[0];
+            c->grad[2 * p + 1] += q->c1[1] + e1[1] + 0.5 * e31[1];
+        }
+    }
+}
+
+void orc_sym_fmm_solve(int kernel, double eps, uint32_t depth, double theta, int64_t n,
+                       const double* pos, orc_node* nodes, double* grad, double* total)
+{
+    (void)depth;
+    (void)n;
+    sym_ctx c;
+    c.kernel = kernel;
+    c.eps2 = eps * eps;
+    c.theta = theta;
+    c.pos = pos;
+    c.grad = grad;
+    c.nodes = nodes;
+    c.total = *total;
+    trav_nn(&c, &nodes[0], &nodes[0]);
+    double inv = 1.0 / nodes[0].m0;
+    for (int i = 0; i < 4; i++) nodes[0].c2[i] *= inv;
+    for (int i = 0; i < 8; i++) nodes[0].c3[i] *= inv;
+    apply_forces(&c, &nodes[0]);
+    *total = c.total;
+}
+
+void orc_sym_fmm(int kernel, double eps, int max_children, int depth, double theta, int64_t n,
+                 const double* pos, const double min_xy[2], const double max_xy[2],
+                 uint32_t* codes_sorted, int32_t* ids_sorted, double* pos_sorted,
+                 double* grad_sorted, double* total, orc_node* nodes)
+{
+    uint32_t d = depth >= 0 ? (uint32_t)depth : orc_get_depth(max_children, n);
+    uint32_t* codes = (uint32_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(uint32_t));
+    orc_morton_codes(n, pos, min_xy, max_xy, codes);
+    orc_sort_perm(n, codes, ids_sorted);
+    for (int64_t k = 0; k < n; k++) {
+        int32_t i = ids_sorted[k];
+        codes_sorted[k] = codes[i];
+        pos_sorted[2 * k] = pos[2 * i];
+        pos_sorted[2 * k + 1] = pos[2 * i + 1];
+    }
+    free(codes);
+    int64_t nn = orc_node_count(d);
+    orc_node* own = NULL;
+    if (!nodes) nodes = own = (orc_node*)malloc((size_t)nn * sizeof(orc_node));
+    orc_build_tree(d, n, pos_sorted, min_xy, max_xy, nodes);
+    if (n > 0) orc_sym_fmm_solve(kernel, eps, d, theta, n, pos_sorted, nodes, grad_sorted, total);
+    free(own);
+}
+
+/* ------------------------------------------------------------------ */
+/* direct sums                                                         */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+    int kernel;
+    double eps2;
+    int64_t n;
+    const double* pos;
+    const int64_t* rows;
+    int64_t r0, r1;
+    double* grad;
+    double total;
+    int row_out_compact;
+} naive_job;
+
+/* TSNEnaiveKernel (nBodySolverNaive.h:124-141): uses |diff| then squares it */
+static void* naive_worker(void* arg)
+{
+    naive_job* j = (naive_job*)arg;
+    double tot = 0.0;
+    for (int64_t r = j->r0; r < j->r1; r++) {
+        int64_t i = j->rows ? j->rows[r] : r;
+        double gx = 0.0, gy = 0.0;
+        for (int64_t k = 0; k < j->n; k++) {
+            if (k == i) continue;
+            double dx = j->pos[2 * i] - j->pos[2 * k];
+            double dy = j->pos[2 * i + 1] - j->pos[2 * k + 1];
+            if (j->kernel == ORC_KERNEL_TSNE) {
+                double dist = sqrt(dx * dx + dy * dy);
+                double fd = 1.0 / (1.0 + (dist * dist));
+                tot += fd;
+                gx += fd * fd * dx;
+                gy += fd * fd * dy;
+            } else {
+                derivs d = grav_derivs(dx * dx + dy * dy, j->eps2);
+                tot += d.t;
+                gx += d.D1 * dx;
+                gy += d.D1 * dy;
+            }
+        }
+        int64_t o = j->row_out_compact ? r : i;
+        j->grad[2 * o] = gx;
+        j->grad[2 * o + 1] = gy;
+    }
+    j->total = tot;
+    return NULL;
+}
+
+static void run_rows(int kernel, double eps, int64_t n, const double* pos, int64_t m,
+                     const int64_t* rows, double* grad, double* total, int nthreads, int compact)
+{
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    pthread_t th[256];
+    naive_job jobs[256];
+    int64_t chunk = (m + nthreads - 1) / nthreads;
+    for (int t = 0; t < nthreads; t++) {
+        jobs[t].kernel = kernel;
+        jobs[t].eps2 = eps * eps;
+        jobs[t].n = n;
+        jobs[t].pos = pos;
+        jobs[t].rows = rows;
+        jobs[t].r0 = t * chunk < m ? t * chunk : m;
+        jobs[t].r1 = (t + 1) * chunk < m ? (t + 1) * chunk : m;
+        jobs[t].grad = grad;
+        jobs[t].total = 0.0;
+        jobs[t].row_out_compact = compact;
+        pthread_create(&th[t], NULL, naive_worker, &jobs[t]);
+    }
+    double tot = 0.0;
+    for (int t = 0; t < nthreads; t++) {
+        pthread_join(th[t], NULL);
+        tot += jobs[t].total;
+    }
+    if (total) *total = tot;
+}
+
+void orc_naive(int kernel, double eps, int64_t n, const double* pos, double* grad,
+               double* total, int nthreads)
+{
+    run_rows(kernel, eps, n, pos, n, NULL, grad, total, nthreads, 0);
+}
+
+void orc_direct_rows(int kernel, double eps, int64_t n, const double* pos, int64_t m,
+                     const int64_t* idx, double* grad_rows, int nthreads)
+{
+    run_rows(kernel, eps, n, pos, m, idx, grad_rows, NULL, nthreads, 1);
+}
+
+/* ------------------------------------------------------------------ */
+/* Barnes-Hut (pointer quadtree)                                       */
+/* ------------------------------------------------------------------ */
+
+typedef struct bh_node {
+    float total_mass;        /* QuadTree::totalMass is float (quadtree.h:17) */
+    double com[2];
+    double lo[2], hi[2];
+    int32_t* occ;
+    int64_t nocc;
+    struct bh_node* ch[4];
+    int nch;
+} bh_node;
+
+/* QuadTree::createTree (quadtree.h:100-172).  The return value is
+ * std::pair<float, glm::vec2>, so the parent sees float-rounded child COMs. */
+static void bh_create(bh_node* q, const double* pos, int maxc, float* ret_m, float ret_c[2])
+{
+    if (q->nocc > maxc) {
+        int32_t* part[4];
+        int64_t cnt[4] = {0, 0, 0, 0};
+        for (int k = 0; k < 4; k++) part[k] = (int32_t*)malloc((size_t)q->nocc * sizeof(int32_t));
+        double l = (q->hi[0] - q->lo[0]) / 2.0;
+        double mx = q->lo[0] + l, my = q->lo[1] + l;
+        for (int64_t i = 0; i < q->nocc; i++) {
+            int32_t id = q->occ[i];
+            double x = pos[2 * id], y = pos[2 * id + 1];
+            int k;
+            if (x >= mx && y >= my) k = 0;          /* HH */
+            else if (x >= mx && y < my) k = 1;      /* HL */
+            else if (x < mx && y >= my) k = 2;      /* LH */
+            else k = 3;                             /* LL */
+            part[k][cnt[k]++] = id;
+        }
+        double blo[4][2] = {{mx, my}, {mx, q->lo[1]}, {q->lo[0], my}, {q->lo[0], q->lo[1]}};
+        double bhi[4][2] = {{q->hi[0], q->hi[1]}, {q->hi[0], my}, {mx, q->hi[1]}, {mx, my}};
+        q->nch = 0;
+        for (int k = 0; k < 4; k++) {
+            if (cnt[k] == 0) {
+                free(part[k]);
+                continue;
+            }
+            bh_node* c = (bh_node*)calloc(1, sizeof(bh_node));
+            c->occ = part[k];
+            c->nocc = cnt[k];
+            c->lo[0] = blo[k][0]; c->lo[1] = blo[k][1];
+            c->hi[0] = bhi[k][0]; c->hi[1] = bhi[k][1];
+            q->ch[q->nch++] = c;
+        }
+        q->total_mass = 0.0f;
+        q->com[0] = q->com[1] = 0.0;
+        for (int k = 0; k < q->nch; k++) {
+            float cm, cc[2];
+            bh_create(q->ch[k], pos, maxc, &cm, cc);
+            double m = (double)cm;
+            q->total_mass = (float)((double)q->total_mass + m);
+            q->com[0] += m * (double)cc[0];
+            q->com[1] += m * (double)cc[1];
+        }
+    } else {
+        q->total_mass = 0.0f;
+        q->com[0] = q->com[1] = 0.0;
+        for (int64_t i = 0; i < q->nocc; i++) {
+            q->total_mass = (float)((double)q->total_mass + 1.0);
+            q->com[0] += 1.0 * pos[2 * q->occ[i]];
+            q->com[1] += 1.0 * pos[2 * q->occ[i] + 1];
+        }
+    }
+    q->com[0] /= (double)q->total_mass;
+    q->com[1] /= (double)q->total_mass;
+    *ret_m = q->total_mass;
+    ret_c[0] = (float)q->com[0];
+    ret_c[1] = (float)q->com[1];
+}
+
+static void bh_free(bh_node* q)
+{
+    for (int k = 0; k < q->nch; k++) {
+        bh_free(q->ch[k]);
+        free(q->ch[k]);
+    }
+    free(q->occ);
+}
+
+typedef struct {
+    int kernel;
+    double eps2;
+    double theta;
+    const double* pos;
+    double total;
+} bh_ctx;
+
+/* NBodySolverBH::traverseBH (nBodySolverBH.h:56-89) + TSNEBHPNKernel /
+ * TSNEBHPPKernel (:94-116); gravity uses the softened kernel.             */
+static void bh_trav(bh_ctx* c, int64_t p, const bh_node* q, double* g)
+{
+    double l = q->hi[0] - q->lo[0];
+    double dx = c->pos[2 * p] - q->com[0], dy = c->pos[2 * p + 1] - q->com[1];
+    double len = sqrt(dx * dx + dy * dy);
+    if (l / len < c->theta) {
+        double sq = dx * dx + dy * dy;
+        double tm = (double)q->total_mass;
+        if (c->kernel == ORC_KERNEL_TSNE) {
+            double fd = 1.0 / (1.0 + sq);
+            c->total += tm * fd;
+            g[0] += tm * fd * fd * dx;
+            g[1] += tm * fd * fd * dy;
+        } else {
+            derivs d = grav_derivs(sq, c->eps2);
+            c->total += tm * d.t;
+            g[0] += tm * d.D1 * dx;
+            g[1] += tm * d.D1 * dy;
+        }
+    } else if (q->nch <= 1) {
+        for (int64_t i = 0; i < q->nocc; i++) {
+            int64_t o = q->occ[i];
+            if (o == p) continue;
+            double ex = c->pos[2 * p] - c->pos[2 * o], ey = c->pos[2 * p + 1] - c->pos[2 * o + 1];
+            double sq = ex * ex + ey * ey;
+            if (c->kernel == ORC_KERNEL_TSNE) {
+                double fd = 1.0 / (1.0 + sq);
+                c->total += fd;
+                g[0] += fd * fd * ex;
+                g[1] += fd * fd * ey;
+            } else {
+                derivs d = grav_derivs(sq, c->eps2);
+                c->total += d.t;
+                g[0] += d.D1 * ex;
+                g[1] += d.D1 * ey;
+            }
+        }
+    } else {
+        for (int k = 0; k < q->nch; k++) bh_trav(c, p, q->ch[k], g);
+    }
+}
+
+int orc_bh(int kernel, double eps, int max_children, double theta, int64_t n,
+           const double* pos, double* grad, double* total)
+{
+    if (n <= 0) {
+        if (total) *total = 0.0;
+        return 0;
+    }
+    bh_node root;
+    memset(&root, 0, sizeof(root));
+    root.occ = (int32_t*)malloc((size_t)n * sizeof(int32_t));
+    root.nocc = n;
+    double lo[2] = {INFINITY, INFINITY}, hi[2] = {-INFINITY, -INFINITY};
+    for (int64_t i = 0; i < n; i++) {
+        root.occ[i] = (int32_t)i;
+        for (int a = 0; a < 2; a++) {
+            lo[a] = dmin(lo[a], pos[2 * i + a]);
+            hi[a] = dmax(hi[a], pos[2 * i + a]);
+        }
+    }
+    double ld = dmax(hi[0] - lo[0], hi[1] - lo[1]);
+    root.lo[0] = lo[0];
+    root.lo[1] = lo[1];
+    root.hi[0] = lo[0] + ld + 0.0001;
+    root.hi[1] = lo[1] + ld + 0.0001;
+    float m, cc[2];
+    bh_create(&root, pos, max_children, &m, cc);
+    bh_ctx c = {kernel, eps * eps, theta, pos, 0.0};
+    for (int64_t i = 0; i < n; i++) {
+        grad[2 * i] = grad[2 * i + 1] = 0.0;
+        bh_trav(&c, i, &root, grad + 2 * i);
+    }
+    if (total) *total = c.total;
+    bh_free(&root);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* t-SNE composition                                                   */
+/* ------------------------------------------------------------------ */
+
+void orc_tsne_attractive(int64_t n, const uint32_t* row_ptr, const uint32_t* col,
+                         const double* val, const double* pos, double exag, double* grad)
+{
+    for (int64_t r = 0; r < n; r++) {
+        double ax = 0.0, ay = 0.0;
+        for (uint32_t i = row_ptr[r]; i < row_ptr[r + 1]; i++) {
+            uint32_t c = col[i];
+            double dx = pos[2 * c] - pos[2 * r];
+            double dy = pos[2 * c + 1] - pos[2 * r + 1];
+            double d = dx * dx + dy * dy;
+            double q = 1.0 / (1.0 + d);
+            ax += exag * val[i] * q * dx;
+            ay += exag * val[i] * q * dy;
+        }
+        grad[2 * r] += ax;
+        grad[2 * r + 1] += ay;
+    }
+}
+
+void orc_tsne_step(int64_t n, const double* y, const double* y_prev, const uint32_t* row_ptr,
+                   const uint32_t* col, const double* val, int max_children, int depth,
+                   double theta, double exag_code, double lr, double momentum, double* y_next,
+                   double* grad_out, double* z_out)
+{
+    double mn[2] = {INFINITY, INFINITY}, mx[2] = {-INFINITY, -INFINITY};
+    for (int64_t i = 0; i < n; i++)
+        for (int a = 0; a < 2; a++) {
+            mn[a] = dmin(mn[a], y[2 * i + a]);
+            mx[a] = dmax(mx[a], y[2 * i + a]);
+        }
+    uint32_t* cs = (uint32_t*)malloc((size_t)n * sizeof(uint32_t));
+    int32_t* ids = (int32_t*)malloc((size_t)n * sizeof(int32_t));
+    double* ps = (double*)malloc((size_t)n * 2 * sizeof(double));
+    double* gs = (double*)calloc((size_t)n * 2, sizeof(double));
+    double z = 0.0;
+    orc_sym_fmm(ORC_KERNEL_TSNE, 0.0, max_children, depth, theta, n, y, mn, mx, cs, ids, ps, gs, &z, NULL);
+    double s = 4.0 / z; /* updateRepulsive (tsne.h:287-301) */
+    for (int64_t k = 0; k < n; k++) {
+        grad_out[2 * ids[k]] = gs[2 * k] * s;
+        grad_out[2 * ids[k] + 1] = gs[2 * k + 1] * s;
+    }
+    orc_tsne_attractive(n, row_ptr, col, val, y, exag_code, grad_out);
+    for (int64_t i = 0; i < 2 * n; i++) /* updatePoints (tsne.h:179-206) */
+        y_next[i] = y[i] + lr * grad_out[i] + momentum * (y[i] - y_prev[i]);
+    if (z_out) *z_out = z;
+    free(cs);
+    free(ids);
+    free(ps);
+    free(gs);
+}

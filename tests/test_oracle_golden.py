@@ -1,0 +1,91 @@
+"""The C oracle against golden fixtures produced by the reference's own solvers.
+
+The fixtures were made by tests/golden/make_golden.py from the reference
+compiled from its sources.  The oracle must reproduce them bit for bit.
+"""
+import numpy as np
+import pytest
+
+import oracle
+
+SYM_CASES = ["sym_tsne_gauss_3000", "sym_grav_mixture_4096", "sym_tsne_ties_1000",
+             "sym_tsne_deep_2000_theta1", "sym_grav_disks_3000_theta03", "sym_tsne_tiny_2",
+             "sym_tsne_tiny_3", "sym_tsne_tiny_17", "sym_tsne_tiny_64"]
+
+
+@pytest.mark.parametrize("case", SYM_CASES)
+def test_sym_fmm_bit_exact(golden, case):
+    g = golden(case)
+    mn, mx = g["minmax"][:2], g["minmax"][2:]
+    r = oracle.sym_fmm(g["pos"], kernel=int(g["kernel"]), eps=float(g["eps"]),
+                       max_children=int(g["max_children"]), depth=int(g["depth"]),
+                       theta=float(g["theta"]), mn=mn, mx=mx)
+    assert r["depth"] == int(g["depth"])
+    np.testing.assert_array_equal(r["codes"], g["codes"])
+    np.testing.assert_array_equal(r["ids"], g["ids"])
+    np.testing.assert_array_equal(r["pos"], g["pos_sorted"])
+    ref_nodes = oracle.ref_nodes_to_struct(g["nodes"])
+    for f in ("bb_c", "bb_len", "first_child", "first_part", "count", "com", "m0", "m2",
+              "c1", "c2", "c3"):
+        np.testing.assert_array_equal(r["nodes"][f], ref_nodes[f], err_msg=f)
+    np.testing.assert_array_equal(r["grad"], g["grad"])
+    assert r["total"] == float(g["total"])
+
+
+def test_depth_rule_matches_reference(golden):
+    # getDepth(16, N) = ceil(log((4/pi) * (N/16)) / log 4) with integer N/16
+    assert oracle.get_depth(16, 70000) == 7
+    assert oracle.get_depth(16, 65536) == 7
+    assert oracle.get_depth(64, 4194304) == 9
+    assert oracle.get_depth(16, 3000) == int(golden("sym_tsne_gauss_3000")["depth"])
+
+
+@pytest.mark.parametrize("tag", ["tsne", "grav"])
+def test_naive_bit_exact(golden, tag):
+    g = golden(f"naive_{tag}_1500")
+    grad, total = oracle.naive(g["pos"], kernel=int(g["kernel"]), eps=float(g["eps"]))
+    np.testing.assert_array_equal(grad, g["grad"])
+    # the total is summed in per-thread chunks; only the partition differs
+    assert total == pytest.approx(float(g["total"]), rel=1e-12)
+
+
+@pytest.mark.parametrize("tag", ["tsne", "grav"])
+def test_bh_bit_exact(golden, tag):
+    g = golden(f"bh_{tag}_3000")
+    grad, total = oracle.bh(g["pos"], kernel=int(g["kernel"]), eps=float(g["eps"]),
+                            max_children=int(g["max_children"]), theta=float(g["theta"]))
+    np.testing.assert_array_equal(grad, g["grad"])
+    assert total == float(g["total"])
+
+
+def test_tsne_step_matches_reference_composition(golden):
+    g = golden("tsne_step_600")
+    ys = [g["y0"], g["y0"]]
+    for it in range(len(g["zs"])):
+        yn, grad, z = oracle.tsne_step(ys[-1], ys[-2], g["row_ptr"], g["col"], g["val"],
+                                       theta=float(g["theta"]), exag_code=float(g["exag_code"]),
+                                       lr=float(g["lr"]), momentum=float(g["momentum"]))
+        assert z == float(g["zs"][it])
+        np.testing.assert_allclose(grad, g["grads"][it], rtol=1e-12, atol=1e-15)
+        np.testing.assert_allclose(yn, g["ys"][it], rtol=1e-12, atol=1e-14)
+        ys.append(g["ys"][it])  # continue from the reference trajectory
+
+
+def test_morton_codes_and_stable_tie_order():
+    pos = np.array([[0.0, 0.0], [1.0, 1.0], [0.0, 0.0], [0.5, 0.25], [1.0, 1.0]])
+    codes = oracle.morton_codes(pos, [0.0, 0.0], [1.0, 1.0])
+    # u = 1 clamps to 65535 on both axes -> all 32 bits set
+    assert codes[1] == 0xFFFFFFFF and codes[0] == 0
+    perm = oracle.sort_perm(codes)
+    np.testing.assert_array_equal(perm, [0, 2, 3, 1, 4])
+
+
+def test_reference_harness_agrees_when_built():
+    """Cross-check against the reference compiled here (skipped where absent)."""
+    if oracle.ref_lib() is None:
+        pytest.skip("reference not compiled in this container")
+    pos = np.random.default_rng(7).normal(0, 2, (1200, 2))
+    a = oracle.sym_fmm(pos)
+    b = oracle.ref_sym_fmm(pos)
+    np.testing.assert_array_equal(a["grad"], b["grad"])
+    np.testing.assert_array_equal(a["codes"], b["codes"])
