@@ -1,0 +1,158 @@
+/*
+ * treecode.h -- C ABI of the GB300 2D tree-code library (libtreecode.so).
+ *
+ * Drop-in boundary for the per-step force/gradient call of the reference's
+ * tree solvers.  The reference interface is the abstract class
+ *
+ *   template <class T> class NBodySolver {                       // src/nbodysolvers/cpu/nBodySolver.h:9-23
+ *     int maxChildren; double theta; double cell_size;
+ *     virtual void solveNbody(double& total, std::vector<T>& points) = 0;
+ *     virtual void updateTree(std::vector<T>& points, glm::dvec2 minPos, glm::dvec2 maxPos) = 0;
+ *     virtual std::vector<VertexPos2Col3> getNodesBufferData(int level) = 0;
+ *   };
+ *
+ * implemented by NBodySolverFMM_SYM_MORTON<TsnePoint2D>
+ * (src/nbodysolvers/cpu/nBodySolverFMM_SYM_MORTON.h:29-614).  A handle plays
+ * the solver object; positions cross the boundary as interleaved (x, y)
+ * doubles and the particle identity (TsnePoint2D::ID) as int32.
+ *
+ * Conventions: every entry point returns TC_OK (0) or a negative TC_ERR_*
+ * status and never aborts; tc_last_error() describes the last failure of the
+ * calling thread.  Host pointers are borrowed for the duration of the call;
+ * device buffers belong to the handle.  A handle is not thread-safe and runs
+ * on one CUDA stream (tc_config.stream, or one it creates).
+ */
+#ifndef TREECODE_H
+#define TREECODE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TC_OK 0
+#define TC_ERR_INVALID -1   /* bad argument or input (NaN, point outside box) */
+#define TC_ERR_CUDA -2      /* CUDA runtime error                            */
+#define TC_ERR_NOMEM -3     /* device allocation failed                      */
+#define TC_ERR_STATE -4     /* call out of order (solve before update_tree)  */
+#define TC_ERR_TIMEOUT -5   /* a bounded device wait gave up                 */
+
+#define TC_KERNEL_TSNE 0     /* Student-t repulsion (TSNE_FMM_SYM_MORTON_*_Kernel) */
+#define TC_KERNEL_GRAVITY 1  /* 2D Plummer-softened gravity                        */
+
+#define TC_PREC_FP32 0  /* expansions and P2P in FP32 (tree build, MACs and Z in FP64) */
+#define TC_PREC_FP64 1  /* everything in FP64 (parity diagnostics)                     */
+
+typedef struct tc_handle tc_handle;
+
+typedef struct tc_config {
+    int kernel;        /* TC_KERNEL_*                                           */
+    int max_children;  /* NBodySolver::maxChildren (leaf size for getDepth)     */
+    int depth;         /* tree depth; < 0 selects getDepth(max_children, n)     */
+    double theta;      /* NBodySolver::theta, opening criterion                 */
+    double softening;  /* gravity softening length eps                          */
+    int precision;     /* TC_PREC_*                                             */
+    int device;        /* CUDA device ordinal                                   */
+    void* stream;      /* cudaStream_t to run on, or NULL for a private stream  */
+} tc_config;
+
+/* Defaults: t-SNE kernel, leaf 16, automatic depth, theta 0.5, FP32. */
+int tc_config_init(tc_config* cfg);
+
+/* Constructor of NBodySolverFMM_SYM_MORTON (nBodySolverFMM_SYM_MORTON.h:49-67). */
+int tc_create(const tc_config* cfg, tc_handle** out);
+int tc_destroy(tc_handle* h);
+
+/* NBodySolver::theta is a public field the caller changes between iterations
+ * (TSNE::setThetaForAll, src/nBodyInstances/tsne.h:245-252).               */
+int tc_set_theta(tc_handle* h, double theta);
+
+/* getDepth (nBodySolverFMM_SYM_MORTON.h:106-115), clamped at 0 for n < leaf. */
+int tc_get_depth(int max_children, int64_t n, uint32_t* depth);
+/* node count of the level-dense tree, initNodesSize (:117-151).             */
+int tc_node_count(uint32_t depth, int64_t* count);
+
+/* updateTree (nBodySolverFMM_SYM_MORTON.h:79-95).  pos_xy (n x 2, host) and
+ * ids (n, host, may be NULL) are reordered in place into Morton order, as the
+ * reference sorts its particle vector.  min_xy/max_xy are the caller's
+ * bounding box (TSNE::updateMinMaxPos); every point must lie inside it.      */
+int tc_update_tree(tc_handle* h, double* pos_xy, int32_t* ids, int64_t n, const double min_xy[2],
+                   const double max_xy[2]);
+
+/* solveNbody (nBodySolverFMM_SYM_MORTON.h:69-77).  Adds the repulsive force
+ * (t-SNE: sum q_ij^2 (y_i - y_j), unnormalised; gravity: acceleration of unit
+ * masses) into grad_xy (host, sorted order) and the kernel's pair sum into
+ * *total (t-SNE: Z).  pos_xy must be the positions passed to the preceding
+ * tc_update_tree, in the order it returned (it may be NULL).              */
+int tc_solve(tc_handle* h, double* total, const double* pos_xy, double* grad_xy, int64_t n);
+
+/* Device-resident variants (pointers are device memory on the handle's
+ * device).  d_pos_xy is in the caller's order and is not modified; when
+ * min_xy is NULL the bounding box is computed on the device.  Results of
+ * tc_solve_device are written in Morton order, or scattered back to the
+ * caller's order when scatter != 0; accumulate selects += over =.         */
+int tc_update_tree_device(tc_handle* h, const double* d_pos_xy, int64_t n, const double* min_xy,
+                          const double* max_xy);
+int tc_solve_device(tc_handle* h, double* d_grad_xy, double* d_total, int accumulate, int scatter);
+
+/* Reads back the tree of the last update: Morton codes, permutation (input
+ * index of each sorted point), sorted positions, and 27 doubles per node in
+ * the order BBcentre(2) BBlength firstChildIndex firstParticleIndex
+ * particleIndexAmount centreOfMass(2) M0 M2(4) C1(2) C2(4) C3(8), the fields
+ * of NodeFMM_MORTON_2D (src/trees/cpu/nodeFMM_MORTON_2D.h:8-25).  The C
+ * fields hold the final local expansions of the last solve, after the L2L
+ * pass, in the solve's precision.  Any pointer may be NULL.             */
+int tc_get_tree(tc_handle* h, uint32_t* codes, int32_t* perm, double* pos_sorted, double* nodes);
+
+/* Interaction-list statistics of the last update: per level the number of
+ * accepted node pairs (directed) and near pairs.  Arrays of depth+1.    */
+int tc_get_list_stats(tc_handle* h, uint32_t* nn_pairs, uint32_t* near_pairs);
+
+/* getNodesBufferData (nBodySolverFMM_SYM_MORTON.h:97-104): boxes of the
+ * non-empty nodes of one level (level < 0: all levels) as (cx, cy, length)
+ * triples.  *count receives how many exist; at most cap are written.     */
+int tc_get_node_boxes(tc_handle* h, int level, double* boxes, int64_t cap, int64_t* count);
+
+/* Kernels launched by the last update/solve call on this handle. */
+int tc_last_launch_count(tc_handle* h);
+
+/* ---------------------------------------------------------------- direct sums
+ * NBodySolverNaive::solveNbody (src/nbodysolvers/cpu/nBodySolverNaive.h:53-112)
+ * and the GPU naive step cudaTsneNaiveStepRep
+ * (src/nbodysolvers/gpu/nBodySolverGpuNaive.cu:50-81): O(N^2) force on the
+ * sink rows `rows` (NULL: all n points, then m is ignored) from all n points,
+ * written (not accumulated) to grad_rows (m x 2); *total receives the pair
+ * sum over those rows.  TC_PREC_FP64 is the error oracle of the tree code.  */
+int tc_direct(int kernel, double softening, int precision, const double* pos_xy, int64_t n,
+              const int64_t* rows, int64_t m, double* grad_rows, double* total);
+int tc_direct_device(int kernel, double softening, int precision, const double* d_pos_xy, int64_t n,
+                     const int64_t* d_rows, int64_t m, double* d_grad_rows, double* d_total, void* stream);
+
+/* ---------------------------------------------------------------- t-SNE step
+ * The TSNE class around the solver (src/nBodyInstances/tsne.h:42-563),
+ * device resident.  P is the symmetric affinity matrix as CSR (rows and
+ * columns sorted, as TSNE::setupEfficientPmatrix builds it, tsne.h:462-520);
+ * values are stored as FP32.  y0 (n x 2) initialises both the current and the
+ * previous embedding (TSNE::generateInitialPoints, tsne.h:522-562).         */
+typedef struct tc_tsne tc_tsne;
+int tc_tsne_create(const tc_config* cfg, int64_t n, const uint32_t* row_ptr, const uint32_t* col,
+                   const double* val, const double* y0, tc_tsne** out);
+int tc_tsne_destroy(tc_tsne* t);
+int tc_tsne_set_theta(tc_tsne* t, double theta);
+/* One TSNE_buffers::timeStep (tsne_buffers.h:125-168): updateTree on the
+ * current embedding, updateRepulsive (tsne.h:287-301), updateAttractive
+ * (:356-381) with factor exag_code (the reference uses 16 for the first 250
+ * iterations, then 4), updatePoints (:179-206) with the given momentum and
+ * learning rate.  *z_out (may be NULL) receives the repulsive normaliser Z. */
+int tc_tsne_step(tc_tsne* t, double exag_code, double momentum, double lr, double* z_out);
+/* Current embedding, previous embedding and last gradient, in ID order.    */
+int tc_tsne_get(tc_tsne* t, double* y, double* y_prev, double* grad);
+int tc_tsne_last_launch_count(tc_tsne* t);
+
+const char* tc_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

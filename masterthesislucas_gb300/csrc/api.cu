@@ -1,0 +1,528 @@
+// C ABI of libtreecode.so (declared in include/treecode.h): handle lifetime,
+// host <-> device staging, and the update/solve entry points that stand in
+// for NBodySolver::updateTree / solveNbody (src/nbodysolvers/cpu/nBodySolver.h:17-18).
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "state.cuh"
+
+static thread_local char g_err[512] = "";
+
+void tc_set_error(const char* fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+int tc_cuda_fail(cudaError_t e, const char* what)
+{
+    tc_set_error("CUDA error %s (%s) in %s", cudaGetErrorName(e), cudaGetErrorString(e), what);
+    return e == cudaErrorMemoryAllocation ? TC_ERR_NOMEM : TC_ERR_CUDA;
+}
+
+namespace tc {
+
+int ensure(Buf& b, size_t bytes)
+{
+    if (bytes == 0) bytes = 16;
+    if (b.bytes >= bytes) return TC_OK;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    cudaError_t e = cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        return tc_cuda_fail(e, "cudaMalloc");
+    }
+    b.bytes = bytes;
+    return TC_OK;
+}
+
+void release(Buf& b)
+{
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+}
+
+namespace {
+
+__global__ void k_bbox(const double2* __restrict__ pos, int64_t n, double* __restrict__ out, uint32_t* err)
+{
+    double mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double2 p = pos[i];
+        if (!(isfinite(p.x) && isfinite(p.y))) atomicOr(err, 1u);
+        mnx = fmin(mnx, p.x);
+        mny = fmin(mny, p.y);
+        mxx = fmax(mxx, p.x);
+        mxy = fmax(mxy, p.y);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mnx = fmin(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+        mny = fmin(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+        mxx = fmax(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+        mxy = fmax(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+    }
+    __shared__ double s[4][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        s[0][w] = mnx;
+        s[1][w] = mny;
+        s[2][w] = mxx;
+        s[3][w] = mxy;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < (int)(blockDim.x >> 5); k++) {
+            mnx = fmin(mnx, s[0][k]);
+            mny = fmin(mny, s[1][k]);
+            mxx = fmax(mxx, s[2][k]);
+            mxy = fmax(mxy, s[3][k]);
+        }
+        // min/max are exact and order-independent: atomics on the ordered
+        // integer image of the doubles are deterministic
+        auto key = [](double v) {
+            unsigned long long u = (unsigned long long)__double_as_longlong(v);
+            return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+        };
+        unsigned long long* o = reinterpret_cast<unsigned long long*>(out);
+        atomicMin(o + 0, key(mnx));
+        atomicMin(o + 1, key(mny));
+        atomicMax(o + 2, key(mxx));
+        atomicMax(o + 3, key(mxy));
+    }
+}
+
+__global__ void k_bbox_init(double* out)
+{
+    unsigned long long* o = reinterpret_cast<unsigned long long*>(out);
+    o[0] = o[1] = 0xFFFFFFFFFFFFFFFFull;
+    o[2] = o[3] = 0ull;
+}
+
+inline double unkey(unsigned long long k)
+{
+    unsigned long long u = (k & 0x8000000000000000ull) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
+    double d;
+    std::memcpy(&d, &u, 8);
+    return d;
+}
+
+// refreshes the compute copy of the positions after tc_solve received new ones
+template <typename real>
+__global__ void k_prel(const double2* __restrict__ pos64, const uint32_t* __restrict__ codes, int64_t n, int depth,
+                       double minx, double miny, double h, real* __restrict__ prel)
+{
+    const int shift = 32 - 2 * depth;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t leaf = depth ? (codes[k] >> shift) : 0u;
+        double cx = minx + ((double)compact16(leaf) + 0.5) * h;
+        double cy = miny + ((double)compact16(leaf >> 1) + 0.5) * h;
+        double2 p = pos64[k];
+        prel[2 * k] = (real)(p.x - cx);
+        prel[2 * k + 1] = (real)(p.y - cy);
+    }
+}
+
+}  // namespace
+
+int device_bbox(Handle& h, const double* d_pos, int64_t n, double mn[2], double mx[2])
+{
+    int rc;
+    if ((rc = ensure(h.err, 64)) || (rc = ensure(h.dtotal, 64))) return rc;
+    double* o = P<double>(h.dtotal) + 2;
+    TC_CUDA_TRY(cudaMemsetAsync(h.err.p, 0, 4, h.stream));
+    k_bbox_init<<<1, 1, 0, h.stream>>>(o);
+    k_bbox<<<grid_for(n, 256, kSMs * 4), 256, 0, h.stream>>>((const double2*)d_pos, n, o, P<uint32_t>(h.err));
+    h.launches += 2;
+    TC_CUDA_TRY(cudaMemcpyAsync(h.h_words, o, 32, cudaMemcpyDeviceToHost, h.stream));
+    TC_CUDA_TRY(cudaMemcpyAsync(h.h_words + 8, h.err.p, 4, cudaMemcpyDeviceToHost, h.stream));
+    TC_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    if (h.h_words[8]) {
+        tc_set_error("positions contain NaN or infinity");
+        return TC_ERR_INVALID;
+    }
+    unsigned long long k[4];
+    std::memcpy(k, h.h_words, 32);
+    mn[0] = unkey(k[0]);
+    mn[1] = unkey(k[1]);
+    mx[0] = unkey(k[2]);
+    mx[1] = unkey(k[3]);
+    return TC_OK;
+}
+
+int refresh_positions(Handle& h)
+{
+    const double hl = h.L / (double)(1u << h.depth);
+    if (h.cfg.precision == TC_PREC_FP64)
+        k_prel<double><<<grid_for(h.n, 256), 256, 0, h.stream>>>(P<double2>(h.pos64), P<uint32_t>(h.codes), h.n,
+                                                                h.depth, h.minx, h.miny, hl, P<double>(h.prel));
+    else
+        k_prel<float><<<grid_for(h.n, 256), 256, 0, h.stream>>>(P<double2>(h.pos64), P<uint32_t>(h.codes), h.n,
+                                                               h.depth, h.minx, h.miny, hl, P<float>(h.prel));
+    h.launches++;
+    TC_CUDA_TRY(cudaGetLastError());
+    return TC_OK;
+}
+
+int dump_final_locals(Handle& h, std::vector<double>& out);
+
+}  // namespace tc
+
+using namespace tc;
+
+
+extern "C" {
+
+const char* tc_last_error(void) { return g_err; }
+
+int tc_config_init(tc_config* cfg)
+{
+    if (!cfg) return TC_ERR_INVALID;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->kernel = TC_KERNEL_TSNE;
+    cfg->max_children = 16;
+    cfg->depth = -1;
+    cfg->theta = 0.5;
+    cfg->softening = 1e-3;
+    cfg->precision = TC_PREC_FP32;
+    cfg->device = 0;
+    cfg->stream = nullptr;
+    return TC_OK;
+}
+
+int tc_get_depth(int max_children, int64_t n, uint32_t* depth)
+{
+    if (!depth || max_children <= 0 || n < 0) {
+        tc_set_error("tc_get_depth: invalid arguments");
+        return TC_ERR_INVALID;
+    }
+    // N / max_children is an integer division in the reference
+    const double circle_area = 3.141592653589793238462643383279502884 / 4.0;
+    int64_t q = (int64_t)(int)n / max_children;
+    if (q < 1) {
+        *depth = 0;
+        return TC_OK;
+    }
+    double d = std::log((1.0 / circle_area) * (double)q) / std::log(4.0);
+    double c = std::ceil(d);
+    *depth = c < 0 ? 0u : (uint32_t)c;
+    return TC_OK;
+}
+
+int tc_node_count(uint32_t depth, int64_t* count)
+{
+    if (!count || depth > 20) return TC_ERR_INVALID;
+    int64_t t = 0, s = 1;
+    for (uint32_t l = 0; l <= depth; l++) {
+        t += s;
+        s *= 4;
+    }
+    *count = t;
+    return TC_OK;
+}
+
+int tc_create(const tc_config* cfg, tc_handle** out)
+{
+    if (!cfg || !out) {
+        tc_set_error("tc_create: null argument");
+        return TC_ERR_INVALID;
+    }
+    *out = nullptr;
+    if (!(cfg->theta > 0.0) || cfg->max_children <= 0 || (cfg->kernel != TC_KERNEL_TSNE && cfg->kernel != TC_KERNEL_GRAVITY) ||
+        (cfg->precision != TC_PREC_FP32 && cfg->precision != TC_PREC_FP64) || cfg->depth > 15 ||
+        !(cfg->softening >= 0.0) || (cfg->kernel == TC_KERNEL_GRAVITY && !(cfg->softening > 0.0))) {
+        tc_set_error("tc_create: invalid configuration");
+        return TC_ERR_INVALID;
+    }
+    TC_CUDA_TRY(cudaSetDevice(cfg->device));
+    tc_handle* t = new (std::nothrow) tc_handle();
+    if (!t) return TC_ERR_NOMEM;
+    t->h.cfg = *cfg;
+    if (cfg->stream) {
+        t->h.stream = (cudaStream_t)cfg->stream;
+    } else {
+        cudaError_t e = cudaStreamCreateWithFlags(&t->h.stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            delete t;
+            return tc_cuda_fail(e, "cudaStreamCreate");
+        }
+        t->h.own_stream = true;
+    }
+    cudaError_t e = cudaMallocHost(&t->h.h_total, 64);
+    if (e == cudaSuccess) e = cudaMallocHost(&t->h.h_words, 64 * 4);
+    if (e != cudaSuccess) {
+        tc_destroy(t);
+        return tc_cuda_fail(e, "cudaMallocHost");
+    }
+    *out = t;
+    return TC_OK;
+}
+
+int tc_destroy(tc_handle* t)
+{
+    if (!t) return TC_OK;
+    Handle& h = t->h;
+    cudaSetDevice(h.cfg.device);
+    if (h.stream) cudaStreamSynchronize(h.stream);
+    Buf* bufs[] = {&h.codes, &h.perm, &h.alt_keys, &h.alt_vals, &h.pos_in, &h.pos64, &h.prel, &h.grad_acc,
+                   &h.count, &h.first, &h.com64, &h.m0, &h.m2, &h.bbc, &h.bblen, &h.comrel, &h.m0r, &h.m2t,
+                   &h.loc, &h.locfin, &h.ptr_pool, &h.idx_pool, &h.cnt_tmp, &h.tmp, &h.err, &h.zpart, &h.dtotal,
+                   &h.host_stage};
+    for (Buf* b : bufs) release(*b);
+    if (h.h_total) cudaFreeHost(h.h_total);
+    if (h.h_words) cudaFreeHost(h.h_words);
+    if (h.own_stream && h.stream) cudaStreamDestroy(h.stream);
+    delete t;
+    return TC_OK;
+}
+
+int tc_set_theta(tc_handle* t, double theta)
+{
+    if (!t || !(theta > 0.0)) return TC_ERR_INVALID;
+    t->h.cfg.theta = theta;
+    // the lists depend on theta: a new update_tree is needed before solving
+    t->h.tree_ready = false;
+    return TC_OK;
+}
+
+static int update_common(Handle& h, const double* d_pos, int64_t n, const double* mn, const double* mx)
+{
+    if (n <= 0 || n > (int64_t)0x7FFFFFFF) {
+        tc_set_error("n must be in [1, 2^31)");
+        return TC_ERR_INVALID;
+    }
+    if (!std::isfinite(mn[0]) || !std::isfinite(mn[1]) || !std::isfinite(mx[0]) || !std::isfinite(mx[1])) {
+        tc_set_error("bounding box is not finite");
+        return TC_ERR_INVALID;
+    }
+    int rc = build_tree(h, d_pos, n, mn[0], mn[1], mx[0], mx[1]);
+    if (rc) return rc;
+    rc = build_lists(h);  // synchronises the stream (list sizes)
+    if (rc) return rc;
+    TC_CUDA_TRY(cudaMemcpyAsync(h.h_words + 8, h.err.p, 4, cudaMemcpyDeviceToHost, h.stream));
+    TC_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    if (h.h_words[8]) {
+        h.tree_ready = false;
+        tc_set_error("a position is NaN or lies outside the bounding box");
+        return TC_ERR_INVALID;
+    }
+    return TC_OK;
+}
+
+int tc_update_tree(tc_handle* t, double* pos_xy, int32_t* ids, int64_t n, const double min_xy[2],
+                   const double max_xy[2])
+{
+    if (!t || !pos_xy || !min_xy || !max_xy) {
+        tc_set_error("tc_update_tree: null argument");
+        return TC_ERR_INVALID;
+    }
+    Handle& h = t->h;
+    TC_CUDA_TRY(cudaSetDevice(h.cfg.device));
+    h.launches = 0;
+    int rc;
+    if ((rc = ensure(h.pos_in, (size_t)n * 16))) return rc;
+    TC_CUDA_TRY(cudaMemcpyAsync(h.pos_in.p, pos_xy, (size_t)n * 16, cudaMemcpyHostToDevice, h.stream));
+    if ((rc = update_common(h, P<double>(h.pos_in), n, min_xy, max_xy))) return rc;
+    TC_CUDA_TRY(cudaMemcpyAsync(pos_xy, h.pos64.p, (size_t)n * 16, cudaMemcpyDeviceToHost, h.stream));
+    if (ids) {
+        std::vector<uint32_t> perm(n);
+        TC_CUDA_TRY(cudaMemcpyAsync(perm.data(), h.perm.p, (size_t)n * 4, cudaMemcpyDeviceToHost, h.stream));
+        TC_CUDA_TRY(cudaStreamSynchronize(h.stream));
+        std::vector<int32_t> old(ids, ids + n);
+        for (int64_t k = 0; k < n; k++) ids[k] = old[perm[k]];
+    } else {
+        TC_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    }
+    return TC_OK;
+}
+
+int tc_update_tree_device(tc_handle* t, const double* d_pos_xy, int64_t n, const double* min_xy,
+                          const double* max_xy)
+{
+    if (!t || !d_pos_xy || (!min_xy) != (!max_xy)) {
+        tc_set_error("tc_update_tree_device: invalid arguments");
+        return TC_ERR_INVALID;
+    }
+    Handle& h = t->h;
+    TC_CUDA_TRY(cudaSetDevice(h.cfg.device));
+    h.launches = 0;
+    double mn[2], mx[2];
+    if (min_xy) {
+        mn[0] = min_xy[0];
+        mn[1] = min_xy[1];
+        mx[0] = max_xy[0];
+        mx[1] = max_xy[1];
+    } else {
+        int rc = device_bbox(h, d_pos_xy, n, mn, mx);
+        if (rc) return rc;
+    }
+    return update_common(h, d_pos_xy, n, mn, mx);
+}
+
+int tc_solve_device(tc_handle* t, double* d_grad_xy, double* d_total, int accumulate, int scatter)
+{
+    if (!t || !d_grad_xy || !d_total) return TC_ERR_INVALID;
+    Handle& h = t->h;
+    if (!h.tree_ready) {
+        tc_set_error("tc_solve: no tree (call tc_update_tree first)");
+        return TC_ERR_STATE;
+    }
+    TC_CUDA_TRY(cudaSetDevice(h.cfg.device));
+    h.launches = 0;
+    return solve_fmm(h, d_grad_xy, d_total, accumulate, scatter);
+}
+
+int tc_solve(tc_handle* t, double* total, const double* pos_xy, double* grad_xy, int64_t n)
+{
+    if (!t || !total || !grad_xy) {
+        tc_set_error("tc_solve: null argument");
+        return TC_ERR_INVALID;
+    }
+    Handle& h = t->h;
+    if (!h.tree_ready) {
+        tc_set_error("tc_solve: no tree (call tc_update_tree first)");
+        return TC_ERR_STATE;
+    }
+    if (n != h.n) {
+        tc_set_error("tc_solve: n (%lld) differs from the tree's (%lld)", (long long)n, (long long)h.n);
+        return TC_ERR_INVALID;
+    }
+    TC_CUDA_TRY(cudaSetDevice(h.cfg.device));
+    h.launches = 0;
+    int rc;
+    if ((rc = ensure(h.grad_acc, (size_t)n * 16)) || (rc = ensure(h.dtotal, 64))) return rc;
+    if (pos_xy) {
+        TC_CUDA_TRY(cudaMemcpyAsync(h.pos64.p, pos_xy, (size_t)n * 16, cudaMemcpyHostToDevice, h.stream));
+        if ((rc = refresh_positions(h))) return rc;
+    }
+    TC_CUDA_TRY(cudaMemsetAsync(h.dtotal.p, 0, 8, h.stream));
+    if ((rc = solve_fmm(h, P<double>(h.grad_acc), P<double>(h.dtotal), 0, 0))) return rc;
+    std::vector<double> g((size_t)n * 2);
+    TC_CUDA_TRY(cudaMemcpyAsync(g.data(), h.grad_acc.p, (size_t)n * 16, cudaMemcpyDeviceToHost, h.stream));
+    TC_CUDA_TRY(cudaMemcpyAsync(h.h_total, h.dtotal.p, 8, cudaMemcpyDeviceToHost, h.stream));
+    TC_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    for (int64_t i = 0; i < 2 * n; i++) grad_xy[i] += g[i];
+    *total += h.h_total[0];
+    return TC_OK;
+}
+
+int tc_get_tree(tc_handle* t, uint32_t* codes, int32_t* perm, double* pos_sorted, double* nodes)
+{
+    if (!t) return TC_ERR_INVALID;
+    Handle& h = t->h;
+    if (h.depth < 0 || h.n == 0) return TC_ERR_STATE;
+    TC_CUDA_TRY(cudaSetDevice(h.cfg.device));
+    cudaStream_t s = h.stream;
+    const int64_t n = h.n, nn = h.nnodes;
+    if (codes) TC_CUDA_TRY(cudaMemcpyAsync(codes, h.codes.p, n * 4, cudaMemcpyDeviceToHost, s));
+    if (perm) TC_CUDA_TRY(cudaMemcpyAsync(perm, h.perm.p, n * 4, cudaMemcpyDeviceToHost, s));
+    if (pos_sorted) TC_CUDA_TRY(cudaMemcpyAsync(pos_sorted, h.pos64.p, n * 16, cudaMemcpyDeviceToHost, s));
+    if (nodes) {
+        std::vector<uint32_t> cnt(nn), fst(nn);
+        std::vector<double> com(2 * nn), m0(nn), m2(3 * nn), bbc(2 * nn), len(nn);
+        TC_CUDA_TRY(cudaMemcpyAsync(cnt.data(), h.count.p, nn * 4, cudaMemcpyDeviceToHost, s));
+        TC_CUDA_TRY(cudaMemcpyAsync(fst.data(), h.first.p, nn * 4, cudaMemcpyDeviceToHost, s));
+        TC_CUDA_TRY(cudaMemcpyAsync(com.data(), h.com64.p, nn * 16, cudaMemcpyDeviceToHost, s));
+        TC_CUDA_TRY(cudaMemcpyAsync(m0.data(), h.m0.p, nn * 8, cudaMemcpyDeviceToHost, s));
+        TC_CUDA_TRY(cudaMemcpyAsync(m2.data(), h.m2.p, nn * 24, cudaMemcpyDeviceToHost, s));
+        TC_CUDA_TRY(cudaMemcpyAsync(bbc.data(), h.bbc.p, nn * 16, cudaMemcpyDeviceToHost, s));
+        TC_CUDA_TRY(cudaMemcpyAsync(len.data(), h.bblen.p, nn * 8, cudaMemcpyDeviceToHost, s));
+        std::vector<double> fin;
+        int rc = dump_final_locals(h, fin);
+        if (rc) return rc;
+        TC_CUDA_TRY(cudaStreamSynchronize(s));
+        for (int64_t k = 0; k < nn; k++) {
+            double* o = nodes + k * 27;
+            int l = 0;
+            while (l < h.depth && (int64_t)level_index(l + 1) <= k) l++;
+            const int64_t i = k - level_index(l);
+            o[0] = bbc[2 * k];
+            o[1] = bbc[2 * k + 1];
+            o[2] = len[k];
+            o[3] = (cnt[k] != 0 && l < h.depth) ? (double)(level_index(l + 1) + 4 * i) : 0.0;
+            o[4] = fst[k];
+            o[5] = cnt[k];
+            o[6] = com[2 * k];
+            o[7] = com[2 * k + 1];
+            o[8] = m0[k];
+            o[9] = m2[3 * k];
+            o[10] = m2[3 * k + 1];
+            o[11] = m2[3 * k + 1];
+            o[12] = m2[3 * k + 2];
+            const double* c = fin.empty() ? nullptr : fin.data() + 9 * k;
+            double C[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+            if (c && cnt[k] != 0)
+                for (int j = 0; j < 9; j++) C[j] = c[j];
+            o[13] = C[L_C1X];
+            o[14] = C[L_C1Y];
+            o[15] = C[L_C2XX];
+            o[16] = C[L_C2XY];
+            o[17] = C[L_C2XY];
+            o[18] = C[L_C2YY];
+            // C3 in i*4 + j*2 + k order: xxx xxy xyx xyy yxx yxy yyx yyy
+            o[19] = C[L_C3XXX];
+            o[20] = C[L_C3XXY];
+            o[21] = C[L_C3XXY];
+            o[22] = C[L_C3XYY];
+            o[23] = C[L_C3XXY];
+            o[24] = C[L_C3XYY];
+            o[25] = C[L_C3XYY];
+            o[26] = C[L_C3YYY];
+        }
+    } else {
+        TC_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    return TC_OK;
+}
+
+int tc_get_list_stats(tc_handle* t, uint32_t* nn_pairs, uint32_t* near_pairs)
+{
+    if (!t || t->h.depth < 0) return TC_ERR_STATE;
+    for (int l = 0; l <= t->h.depth; l++) {
+        if (nn_pairs) nn_pairs[l] = t->h.lists.nn_total.size() > (size_t)l ? t->h.lists.nn_total[l] : 0;
+        if (near_pairs) near_pairs[l] = t->h.lists.near_total.size() > (size_t)l ? t->h.lists.near_total[l] : 0;
+    }
+    return TC_OK;
+}
+
+int tc_get_node_boxes(tc_handle* t, int level, double* boxes, int64_t cap, int64_t* count)
+{
+    if (!t || !count) return TC_ERR_INVALID;
+    Handle& h = t->h;
+    if (h.depth < 0) return TC_ERR_STATE;
+    TC_CUDA_TRY(cudaSetDevice(h.cfg.device));
+    const int64_t nn = h.nnodes;
+    std::vector<uint32_t> cnt(nn);
+    std::vector<double> bbc(2 * nn), len(nn);
+    TC_CUDA_TRY(cudaMemcpyAsync(cnt.data(), h.count.p, nn * 4, cudaMemcpyDeviceToHost, h.stream));
+    TC_CUDA_TRY(cudaMemcpyAsync(bbc.data(), h.bbc.p, nn * 16, cudaMemcpyDeviceToHost, h.stream));
+    TC_CUDA_TRY(cudaMemcpyAsync(len.data(), h.bblen.p, nn * 8, cudaMemcpyDeviceToHost, h.stream));
+    TC_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    int64_t c = 0;
+    for (int l = 0; l <= h.depth; l++) {
+        if (level >= 0 && l != level) continue;
+        for (int64_t k = level_index(l); k < (int64_t)level_index(l + 1); k++) {
+            if (cnt[k] == 0) continue;
+            if (boxes && c < cap) {
+                boxes[3 * c] = bbc[2 * k];
+                boxes[3 * c + 1] = bbc[2 * k + 1];
+                boxes[3 * c + 2] = len[k];
+            }
+            c++;
+        }
+    }
+    *count = c;
+    return TC_OK;
+}
+
+int tc_last_launch_count(tc_handle* t) { return t ? t->h.launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,107 @@
+// Shared device helpers for the GB300 tree-code library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/treecode.h"
+
+#define TC_CUDA_TRY(expr)                                   \
+    do {                                                    \
+        cudaError_t _e = (expr);                            \
+        if (_e != cudaSuccess) return tc_cuda_fail(_e, #expr); \
+    } while (0)
+
+int tc_cuda_fail(cudaError_t e, const char* what);
+void tc_set_error(const char* fmt, ...);
+
+namespace tc {
+
+constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs
+
+__host__ __device__ inline uint32_t spread16(uint32_t x)
+{
+    x = (x | (x << 8)) & 0x00FF00FFu;
+    x = (x | (x << 4)) & 0x0F0F0F0Fu;
+    x = (x | (x << 2)) & 0x33333333u;
+    x = (x | (x << 1)) & 0x55555555u;
+    return x;
+}
+
+__host__ __device__ inline uint32_t compact16(uint32_t x)
+{
+    x &= 0x55555555u;
+    x = (x | (x >> 1)) & 0x33333333u;
+    x = (x | (x >> 2)) & 0x0F0F0F0Fu;
+    x = (x | (x >> 4)) & 0x00FF00FFu;
+    x = (x | (x >> 8)) & 0x0000FFFFu;
+    return x;
+}
+
+// first node of level l in the level-dense layout: (4^l - 1) / 3
+__host__ __device__ inline uint32_t level_index(int l) { return (uint32_t)((((uint64_t)1 << (2 * l)) - 1) / 3); }
+
+template <typename T>
+__device__ inline T warp_sum(T v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// exclusive scan of one value per thread across the block; returns the block total
+__device__ inline uint32_t block_exclusive_scan(uint32_t v, uint32_t& total)
+{
+    __shared__ uint32_t warp_tot[32];
+    __shared__ uint32_t blk_total;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    const int nw = blockDim.x >> 5;
+    if (warp == 0) {
+        uint32_t t = lane < nw ? warp_tot[lane] : 0u;
+        uint32_t s = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < nw) warp_tot[lane] = s - t;
+        if (lane == nw - 1) blk_total = s;
+    }
+    __syncthreads();
+    total = blk_total;
+    uint32_t r = warp_tot[warp] + x - v;
+    __syncthreads();
+    return r;
+}
+
+
+inline int grid_for(int64_t n, int block, int cap = kSMs * 32)
+{
+    int64_t g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (int)g;
+}
+
+// ---------------------------------------------------------------- scan
+// Exclusive scan of n u32 values; out must hold n+1 entries and receives the
+// total in out[n].  tmp must hold scan_tmp_words(n) u32.
+int64_t scan_tmp_words(int64_t n);
+int exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* tmp, cudaStream_t s);
+
+// ---------------------------------------------------------------- sort
+// Stable LSD radix sort of 32-bit keys with 32-bit values (4 passes of 8 bits).
+// keys/vals are sorted in place; alt_* are scratch of n entries each.
+int64_t radix_tmp_words(int64_t n);
+int radix_sort_u32(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32_t* alt_vals, int64_t n,
+                   uint32_t* tmp, cudaStream_t s, int* launches);
+
+}  // namespace tc

@@ -1,0 +1,69 @@
+// Radial interaction kernels shared by the tree code and the direct sums.
+// A kernel gives, for s = |R|^2, the radial factors of the force
+// F(R) = R g(s): D1 = g, D2 = 2 g', D3 = 4 g'' (the derivative terms of the
+// reference's TSNE_FMM_SYM_MORTON_*_Kernel, nBodySolverFMM_SYM_MORTON.h:622-636)
+// and the scalar pair term t(s) summed into the solver's total.
+#pragma once
+
+#include "common.cuh"
+
+namespace tc {
+
+template <typename real>
+__device__ inline real rcp(real x);
+template <>
+__device__ inline float rcp<float>(float x) { return __fdividef(1.0f, x); }
+template <>
+__device__ inline double rcp<double>(double x) { return 1.0 / x; }
+template <typename real>
+__device__ inline real rsq(real x);
+template <>
+__device__ inline float rsq<float>(float x) { return rsqrtf(x); }
+template <>
+__device__ inline double rsq<double>(double x) { return 1.0 / sqrt(x); }
+
+// Student-t kernel of the t-SNE repulsion: F(R) = R (1+r^2)^-2, pair term (1+r^2)^-1
+template <typename real>
+struct KTsne {
+    __device__ inline void far(real s, real& D1, real& D2, real& D3, real& t) const
+    {
+        real inv = rcp<real>(real(1) + s);
+        real i2 = inv * inv;
+        D1 = i2;
+        D2 = real(-4) * i2 * inv;
+        D3 = real(24) * i2 * i2;
+        t = inv;
+    }
+    __device__ inline void near(real s, real& D1, real& t) const
+    {
+        real fd = rcp<real>(real(1) + s);
+        D1 = fd * fd;
+        t = fd;
+    }
+};
+
+// 2D Plummer-softened gravity: F(R) = -R (r^2+eps^2)^-3/2, pair term -(r^2+eps^2)^-1/2
+template <typename real>
+struct KGrav {
+    real eps2;
+    __device__ inline void far(real s, real& D1, real& D2, real& D3, real& t) const
+    {
+        real u = s + eps2;
+        real iu = rcp<real>(u);
+        real isq = rsq<real>(u);
+        real g = -isq * iu;
+        D1 = g;
+        D2 = real(-3) * g * iu;
+        D3 = real(-5) * D2 * iu;
+        t = -isq;
+    }
+    __device__ inline void near(real s, real& D1, real& t) const
+    {
+        real isq = rsq<real>(s + eps2);
+        D1 = -isq * isq * isq;
+        t = -isq;
+    }
+};
+
+
+}  // namespace tc

@@ -1,0 +1,154 @@
+// Interaction lists: the recursion of traverse_SYM_NN
+// (src/nbodysolvers/cpu/nBodySolverFMM_SYM_MORTON.h:154-270) turned into a
+// level-synchronous, per-sink-node construction.
+//
+// The reference walks unordered node pairs (A, B) of the same level from
+// (root, root).  A pair is accepted for the symmetric M2L when
+// |com_A - com_B|^2 > ((L_A + L_B) / theta)^2; otherwise, above the leaf level,
+// every pair of non-empty children is visited (j >= i when A == B); at the
+// leaf level a non-accepted pair becomes a point-level interaction.
+//
+// Here each node A stores the partners of every visited pair it belongs to,
+// in both directions, split into
+//   nn(A)   - partners accepted by the MAC (M2L sources for A),
+//   near(A) - partners not accepted (refined at the next level; at the leaf
+//             level they are the P2P / PN partners, including A itself).
+// Since near(child) and nn(child) are drawn from the non-empty children of
+// near(parent), the lists hold exactly the reference's visited pairs.  The
+// MAC is evaluated in FP64 from the bit-exact COMs, so the decisions are the
+// reference's decisions.
+#include "state.cuh"
+
+namespace tc {
+namespace {
+
+__device__ inline bool mac_accept(double2 a, double2 b, double len, double inv_theta)
+{
+    double dx = a.x - b.x, dy = a.y - b.y;
+    double dist = dx * dx + dy * dy;
+    double thr = (len + len) * inv_theta;
+    return dist > thr * thr;
+}
+
+// one thread per node of level l; fill == 0 counts, fill == 1 writes
+__global__ void k_lists(int l, double inv_theta, const uint32_t* __restrict__ count, const double2* __restrict__ com64,
+                        const double* __restrict__ bblen, const uint32_t* __restrict__ pnear_ptr,
+                        const uint32_t* __restrict__ pnear_idx, uint32_t* __restrict__ nn_cnt,
+                        uint32_t* __restrict__ near_cnt, const uint32_t* __restrict__ nn_ptr,
+                        uint32_t* __restrict__ nn_idx, const uint32_t* __restrict__ near_ptr,
+                        uint32_t* __restrict__ near_idx, int fill)
+{
+    const uint32_t li = level_index(l);
+    const int64_t nl = (int64_t)1 << (2 * l);
+    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < nl; a += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t nn = 0, nr = 0;
+        if (count[li + a] != 0) {
+            if (l == 0) {
+                nr = 1;
+                if (fill) near_idx[near_ptr[a]] = 0;
+            } else {
+                const double2 ca = com64[li + a];
+                const double len = bblen[li + a];
+                const uint32_t p = (uint32_t)(a >> 2);
+                const uint32_t nb = fill ? nn_ptr[a] : 0, rb = fill ? near_ptr[a] : 0;
+                for (uint32_t e = pnear_ptr[p]; e < pnear_ptr[p + 1]; e++) {
+                    const uint32_t bp = pnear_idx[e];
+                    for (uint32_t j = 0; j < 4; j++) {
+                        const uint32_t b = 4 * bp + j;
+                        if (count[li + b] == 0) continue;
+                        if (mac_accept(ca, com64[li + b], len, inv_theta)) {
+                            if (fill) nn_idx[nb + nn] = b;
+                            nn++;
+                        } else {
+                            if (fill) near_idx[rb + nr] = b;
+                            nr++;
+                        }
+                    }
+                }
+            }
+        }
+        if (!fill) {
+            nn_cnt[a] = nn;
+            near_cnt[a] = nr;
+        }
+    }
+}
+
+}  // namespace
+
+int build_lists(Handle& h)
+{
+    cudaStream_t s = h.stream;
+    const int depth = h.depth;
+    Lists& L = h.lists;
+    L.nn_total.assign(depth + 1, 0);
+    L.near_total.assign(depth + 1, 0);
+    L.nn_ptr_off.assign(depth + 1, 0);
+    L.near_ptr_off.assign(depth + 1, 0);
+    L.nn_idx_off.assign(depth + 1, 0);
+    L.near_idx_off.assign(depth + 1, 0);
+    // pointer pool: two (4^l + 1)-word CSR pointer arrays per level
+    int64_t ptr_words = 0;
+    for (int l = 0; l <= depth; l++) {
+        int64_t nl = (int64_t)1 << (2 * l);
+        L.nn_ptr_off[l] = ptr_words;
+        ptr_words += nl + 1;
+        L.near_ptr_off[l] = ptr_words;
+        ptr_words += nl + 1;
+    }
+    const int64_t nleaf = (int64_t)1 << (2 * depth);
+    int rc;
+    if ((rc = ensure(h.ptr_pool, ptr_words * 4)) || (rc = ensure(h.cnt_tmp, 2 * nleaf * 4 + 64)) ||
+        (rc = ensure(h.tmp, (radix_tmp_words(h.n) > scan_tmp_words(nleaf) ? radix_tmp_words(h.n)
+                                                                           : scan_tmp_words(nleaf)) * 4)))
+        return rc;
+    uint32_t* ptr = P<uint32_t>(h.ptr_pool);
+    uint32_t* nn_cnt = P<uint32_t>(h.cnt_tmp);
+    uint32_t* near_cnt = nn_cnt + nleaf;
+    int64_t idx_words = 0;
+    std::vector<int64_t> idx_cap;
+    const double inv_theta = 1.0 / h.cfg.theta;
+    // first pass over all levels needs the previous level's near lists
+    // resident, so the index pool grows level by level (host reads totals).
+    for (int l = 0; l <= depth; l++) {
+        const int64_t nl = (int64_t)1 << (2 * l);
+        const uint32_t* pnp = l ? ptr + L.near_ptr_off[l - 1] : nullptr;
+        const uint32_t* pni = l ? P<uint32_t>(h.idx_pool) + L.near_idx_off[l - 1] : nullptr;
+        k_lists<<<grid_for(nl, 128), 128, 0, s>>>(l, inv_theta, P<uint32_t>(h.count), P<double2>(h.com64),
+                                                 P<double>(h.bblen), pnp, pni, nn_cnt, near_cnt, nullptr, nullptr,
+                                                 nullptr, nullptr, 0);
+        uint32_t* nnp = ptr + L.nn_ptr_off[l];
+        uint32_t* nrp = ptr + L.near_ptr_off[l];
+        if ((rc = exclusive_scan_u32(nn_cnt, nnp, nl, P<uint32_t>(h.tmp), s))) return rc;
+        if ((rc = exclusive_scan_u32(near_cnt, nrp, nl, P<uint32_t>(h.tmp), s))) return rc;
+        TC_CUDA_TRY(cudaMemcpyAsync(h.h_words, nnp + nl, 4, cudaMemcpyDeviceToHost, s));
+        TC_CUDA_TRY(cudaMemcpyAsync(h.h_words + 1, nrp + nl, 4, cudaMemcpyDeviceToHost, s));
+        TC_CUDA_TRY(cudaStreamSynchronize(s));
+        L.nn_total[l] = h.h_words[0];
+        L.near_total[l] = h.h_words[1];
+        L.nn_idx_off[l] = idx_words;
+        idx_words += L.nn_total[l];
+        L.near_idx_off[l] = idx_words;
+        idx_words += L.near_total[l];
+        // grow the pool keeping the earlier levels (needed as parents)
+        if ((size_t)idx_words * 4 > h.idx_pool.bytes) {
+            Buf nb;
+            if ((rc = ensure(nb, (size_t)(idx_words * 4 * 3 / 2 + 1024)))) return rc;
+            if (h.idx_pool.p && L.nn_idx_off[l] > 0)
+                TC_CUDA_TRY(cudaMemcpyAsync(nb.p, h.idx_pool.p, L.nn_idx_off[l] * 4, cudaMemcpyDeviceToDevice, s));
+            TC_CUDA_TRY(cudaStreamSynchronize(s));
+            release(h.idx_pool);
+            h.idx_pool = nb;
+        }
+        pni = l ? P<uint32_t>(h.idx_pool) + L.near_idx_off[l - 1] : nullptr;
+        k_lists<<<grid_for(nl, 128), 128, 0, s>>>(l, inv_theta, P<uint32_t>(h.count), P<double2>(h.com64),
+                                                 P<double>(h.bblen), pnp, pni, nullptr, nullptr, nnp,
+                                                 P<uint32_t>(h.idx_pool) + L.nn_idx_off[l], nrp,
+                                                 P<uint32_t>(h.idx_pool) + L.near_idx_off[l], 1);
+        h.launches += 8;
+    }
+    TC_CUDA_TRY(cudaGetLastError());
+    return TC_OK;
+}
+
+}  // namespace tc

@@ -1,0 +1,85 @@
+// Device-wide exclusive prefix sum of u32 (reduce -> scan partials -> scan).
+#include "common.cuh"
+
+namespace tc {
+namespace {
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanChunk = kScanThreads * kScanItems;
+
+__global__ void k_scan_reduce(const uint32_t* __restrict__ in, int64_t n, uint32_t* __restrict__ partial)
+{
+    int64_t base = (int64_t)blockIdx.x * kScanChunk;
+    uint32_t s = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++) {
+        int64_t k = base + (int64_t)i * kScanThreads + threadIdx.x;
+        if (k < n) s += in[k];
+    }
+    s = warp_sum(s);
+    __shared__ uint32_t ws[kScanThreads / 32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int w = 0; w < kScanThreads / 32; w++) t += ws[w];
+        partial[blockIdx.x] = t;
+    }
+}
+
+__global__ void k_scan_partials(uint32_t* partial, int64_t nb)
+{
+    uint32_t carry = 0;
+    for (int64_t base = 0; base < nb; base += blockDim.x) {
+        int64_t k = base + threadIdx.x;
+        uint32_t v = k < nb ? partial[k] : 0u;
+        uint32_t tot;
+        uint32_t ex = block_exclusive_scan(v, tot);
+        if (k < nb) partial[k] = carry + ex;
+        carry += tot;
+    }
+}
+
+__global__ void k_scan_final(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, int64_t n,
+                             const uint32_t* __restrict__ partial, int64_t nb)
+{
+    int64_t base = (int64_t)blockIdx.x * kScanChunk + (int64_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t s = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++) {
+        int64_t k = base + i;
+        v[i] = k < n ? in[k] : 0u;
+        s += v[i];
+    }
+    uint32_t tot;
+    uint32_t ex = block_exclusive_scan(s, tot) + partial[blockIdx.x];
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++) {
+        int64_t k = base + i;
+        if (k < n) out[k] = ex;
+        ex += v[i];
+    }
+    if (blockIdx.x == nb - 1 && threadIdx.x == 0) out[n] = partial[blockIdx.x] + tot;
+}
+
+}  // namespace
+
+int64_t scan_tmp_words(int64_t n) { return (n + kScanChunk - 1) / kScanChunk + 1; }
+
+int exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* tmp, cudaStream_t s)
+{
+    if (n <= 0) {
+        TC_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(uint32_t), s));
+        return TC_OK;
+    }
+    int64_t nb = (n + kScanChunk - 1) / kScanChunk;
+    k_scan_reduce<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, tmp);
+    k_scan_partials<<<1, 1024, 0, s>>>(tmp, nb);
+    k_scan_final<<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, tmp, nb);
+    TC_CUDA_TRY(cudaGetLastError());
+    return TC_OK;
+}
+
+}  // namespace tc

@@ -1,0 +1,137 @@
+// Stable LSD radix sort of (u32 key, u32 value): 4 passes of 8 bits, each a
+// per-tile digit histogram, a device-wide scan of the digit-major histogram
+// table, and a stable scatter.  The scatter ranks keys in their input order
+// with warp match-any groups, stages the tile digit-sorted in shared memory
+// and writes each digit run contiguously.  Stability makes ties between equal
+// Morton codes keep input order, which defines the permutation where the
+// reference's unstable integer_sort (nBodySolverFMM_SYM_MORTON.h:89) does not.
+#include "common.cuh"
+
+namespace tc {
+namespace {
+
+constexpr int RT = 256;           // threads per tile
+constexpr int RI = 8;             // keys per thread
+constexpr int RTILE = RT * RI;    // keys per tile
+constexpr int RADIX = 256;
+constexpr int NW = RT / 32;
+
+__global__ void __launch_bounds__(RT) k_radix_hist(const uint32_t* __restrict__ keys, int64_t n, int shift,
+                                                   uint32_t* __restrict__ hist, int nblocks)
+{
+    __shared__ uint32_t h[RADIX];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    int64_t base = (int64_t)blockIdx.x * RTILE;
+#pragma unroll
+    for (int r = 0; r < RI; r++) {
+        int64_t p = base + (int64_t)r * RT + threadIdx.x;
+        if (p < n) atomicAdd(&h[(keys[p] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[(int64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(RT) k_radix_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                                      uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                      int64_t n, int shift, const uint32_t* __restrict__ offs,
+                                                      int nblocks, int iota_vals)
+{
+    __shared__ uint32_t s_keys[RTILE];
+    __shared__ uint32_t s_vals[RTILE];
+    __shared__ uint32_t s_wh[NW][RADIX];
+    __shared__ uint32_t s_run[RADIX];
+    __shared__ uint32_t s_start[RADIX];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    s_run[tid] = 0;
+    uint32_t key[RI], val[RI], rank[RI], dig[RI];
+    const int64_t base = (int64_t)blockIdx.x * RTILE;
+#pragma unroll
+    for (int r = 0; r < RI; r++) {
+        const int64_t p = base + (int64_t)r * RT + tid;
+        const bool valid = p < n;
+        uint32_t k = valid ? kin[p] : 0xFFFFFFFFu;
+        uint32_t v = valid ? (iota_vals ? (uint32_t)p : vin[p]) : 0u;
+        uint32_t d = valid ? ((k >> shift) & 255u) : 256u;
+        for (int i = tid; i < NW * RADIX; i += RT) (&s_wh[0][0])[i] = 0;
+        __syncthreads();
+        uint32_t peers = __match_any_sync(0xffffffffu, d);
+        int leader = __ffs(peers) - 1;
+        uint32_t rw = __popc(peers & lt_mask);
+        if (lane == leader && d < 256u) s_wh[warp][d] = __popc(peers);
+        __syncthreads();
+        {
+            uint32_t run = s_run[tid];
+#pragma unroll
+            for (int w = 0; w < NW; w++) {
+                uint32_t c = s_wh[w][tid];
+                s_wh[w][tid] = run;
+                run += c;
+            }
+            s_run[tid] = run;
+        }
+        __syncthreads();
+        rank[r] = d < 256u ? s_wh[warp][d] + rw : 0u;
+        key[r] = k;
+        val[r] = v;
+        dig[r] = d;
+        __syncthreads();
+    }
+    uint32_t tot;
+    uint32_t st = block_exclusive_scan(s_run[tid], tot);
+    s_start[tid] = st;
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RI; r++) {
+        if (dig[r] < 256u) {
+            uint32_t idx = s_start[dig[r]] + rank[r];
+            s_keys[idx] = key[r];
+            s_vals[idx] = val[r];
+        }
+    }
+    __syncthreads();
+    int64_t rem = n - base;
+    const int cnt = rem < RTILE ? (int)rem : RTILE;
+    for (int j = tid; j < cnt; j += RT) {
+        uint32_t k = s_keys[j];
+        uint32_t d = (k >> shift) & 255u;
+        uint32_t o = offs[(int64_t)d * nblocks + blockIdx.x] + (uint32_t)j - s_start[d];
+        kout[o] = k;
+        vout[o] = s_vals[j];
+    }
+}
+
+}  // namespace
+
+int64_t radix_tmp_words(int64_t n)
+{
+    int64_t nb = (n + RTILE - 1) / RTILE;
+    int64_t h = nb * RADIX;
+    return 2 * (h + 1) + scan_tmp_words(h) + 8;
+}
+
+int radix_sort_u32(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32_t* alt_vals, int64_t n,
+                   uint32_t* tmp, cudaStream_t s, int* launches)
+{
+    if (n <= 0) return TC_OK;
+    const int nb = (int)((n + RTILE - 1) / RTILE);
+    const int64_t h = (int64_t)nb * RADIX;
+    uint32_t* hist = tmp;
+    uint32_t* offs = tmp + (h + 1);
+    uint32_t* stmp = offs + (h + 1);
+    uint32_t *ki = keys, *vi = vals, *ko = alt_keys, *vo = alt_vals;
+    for (int pass = 0; pass < 4; pass++) {
+        k_radix_hist<<<nb, RT, 0, s>>>(ki, n, pass * 8, hist, nb);
+        int rc = exclusive_scan_u32(hist, offs, h, stmp, s);
+        if (rc) return rc;
+        k_radix_scatter<<<nb, RT, 0, s>>>(ki, vi, ko, vo, n, pass * 8, offs, nb, pass == 0);
+        if (launches) *launches += 5;
+        uint32_t* t = ki; ki = ko; ko = t;
+        t = vi; vi = vo; vo = t;
+    }
+    TC_CUDA_TRY(cudaGetLastError());
+    return TC_OK;
+}
+
+}  // namespace tc

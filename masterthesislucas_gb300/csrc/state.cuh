@@ -1,0 +1,80 @@
+// Device-resident state of one solver handle (the GB300 counterpart of the
+// reference's NodeFMM_MORTON_2D vector plus the particle buffer it sorts).
+//
+// HBM layout (structure of arrays, everything sized once and reused):
+//   particles, Morton order    codes u32, perm u32 (input index = reference ID),
+//                              pos64 double2 (bit-exact tree build),
+//                              prel real2 (position relative to its leaf's cell
+//                              centre, the compute copy for P2P/M2P/L2P)
+//   nodes, level-dense         count u32, first u32, com64 double2, m0 double,
+//   (levelIndex[l] + i)        m2 double3 (xx, xy, yy), bbc double2, bblen double
+//                              comrel real2 (COM - ideal cell centre), m0r real,
+//                              m2t real3 (M2 / M0), loc real[9] local expansion
+//   interaction lists          per level: NN (accepted M2L partners) and near
+//                              (partners to refine / leaf partners), CSR u32
+#pragma once
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace tc {
+
+// local expansion layout (9 unique coefficients of C1, C2, C3)
+enum { L_C1X = 0, L_C1Y, L_C2XX, L_C2XY, L_C2YY, L_C3XXX, L_C3XXY, L_C3XYY, L_C3YYY, L_NCOEF };
+
+struct Buf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+struct Lists {
+    // per level l (0..depth): CSR over the 4^l nodes of the level (dense index)
+    std::vector<uint32_t> nn_total, near_total;  // host copies of the totals
+    std::vector<int64_t> nn_ptr_off, near_ptr_off;   // word offsets into ptr pool
+    std::vector<int64_t> nn_idx_off, near_idx_off;   // word offsets into idx pool
+};
+
+struct Handle {
+    tc_config cfg;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int depth = -1;
+    int64_t n = 0;
+    int64_t nnodes = 0;
+    double minx = 0, miny = 0, L = 0;
+    bool tree_ready = false;
+    int launches = 0;   // kernels launched by the last call
+
+    // particles
+    Buf codes, perm, alt_keys, alt_vals, pos_in, pos64, prel, grad_acc;
+    // nodes
+    Buf count, first, com64, m0, m2, bbc, bblen, comrel, m0r, m2t, loc, locfin;
+    // lists
+    Buf ptr_pool, idx_pool, cnt_tmp;
+    Lists lists;
+    // scratch
+    Buf tmp, err, zpart, dtotal, host_stage;
+    double* h_total = nullptr;     // pinned
+    uint32_t* h_words = nullptr;   // pinned, 64 words
+};
+
+int ensure(Buf& b, size_t bytes);
+void release(Buf& b);
+
+template <typename T>
+inline T* P(const Buf& b) { return reinterpret_cast<T*>(b.p); }
+
+// tree.cu
+int build_tree(Handle& h, const double* d_pos, int64_t n, double minx, double miny, double maxx, double maxy);
+// lists.cu
+int build_lists(Handle& h);
+// fmm.cu
+int solve_fmm(Handle& h, double* d_grad, double* d_total, int accumulate, int scatter);
+
+}  // namespace tc
+
+// the opaque handle of the C ABI
+struct tc_handle {
+    tc::Handle h;
+};

@@ -1,0 +1,301 @@
+// Tree construction, bit-exact to NBodySolverFMM_SYM_MORTON::updateTree
+// (src/nbodysolvers/cpu/nBodySolverFMM_SYM_MORTON.h:79-95):
+//   createMortonCode (:538-561)  -> k_morton         (FP64, same op order)
+//   integer_sort (:89)           -> radix_sort_u32   (stable on input order)
+//   createLeafNodes (:328-379)   -> k_gather_bounds + k_leaf_moments
+//   bottomUpNodeConstruction (:381-470) -> k_bottom_up, one launch per level
+// Leaf moments are summed sequentially in sorted order by one thread per
+// leaf and internal nodes combine children in the reference's j = 3..0 order,
+// so COM, M0 and M2 come out bit-identical to the reference's FP64 values.
+// Alongside the FP64 node record the kernels write the compute copies in
+// cell-relative coordinates (COM minus the ideal cell centre), which keep
+// FP32 differences accurate to a fraction of the cell size.
+#include <cmath>
+
+#include "state.cuh"
+
+namespace tc {
+namespace {
+
+__global__ void k_morton(const double2* __restrict__ pos, int64_t n, double minx, double miny, double maxx,
+                         double maxy, double L, uint32_t* __restrict__ codes, uint32_t* __restrict__ err)
+{
+    const double nmx = -minx, nmy = -miny;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double2 p = pos[i];
+        if (!(p.x >= minx && p.x <= maxx && p.y >= miny && p.y <= maxy)) atomicOr(err, 1u);
+        double px = (p.x + nmx) / (L);
+        double py = (p.y + nmy) / (L);
+        px = px * 65536.0;
+        py = py * 65536.0;
+        px = (px < 0.0) ? 0.0 : px;     // glm::max(v, 0)
+        py = (py < 0.0) ? 0.0 : py;
+        px = (65535.0 < px) ? 65535.0 : px;  // glm::min(v, 65535)
+        py = (65535.0 < py) ? 65535.0 : py;
+        codes[i] = (spread16((uint32_t)py) << 1) | spread16((uint32_t)px);
+    }
+}
+
+template <typename real>
+__global__ void k_gather_bounds(const uint32_t* __restrict__ codes, const uint32_t* __restrict__ perm,
+                                const double2* __restrict__ pos_in, int64_t n, int depth, double minx, double miny,
+                                double h, double2* __restrict__ pos64, real* __restrict__ prel,
+                                uint32_t* __restrict__ first, uint32_t* __restrict__ endp)
+{
+    const int shift = 32 - 2 * depth;
+    const uint32_t li = level_index(depth);
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t leaf = depth ? (codes[k] >> shift) : 0u;
+        double2 p = pos_in[perm[k]];
+        pos64[k] = p;
+        uint32_t ix = compact16(leaf), iy = compact16(leaf >> 1);
+        double cx = minx + ((double)ix + 0.5) * h;
+        double cy = miny + ((double)iy + 0.5) * h;
+        prel[2 * k] = (real)(p.x - cx);
+        prel[2 * k + 1] = (real)(p.y - cy);
+        if (k == 0 || (depth ? (codes[k - 1] >> shift) : 0u) != leaf) first[li + leaf] = (uint32_t)k;
+        if (k == n - 1 || (depth ? (codes[k + 1] >> shift) : 0u) != leaf) endp[li + leaf] = (uint32_t)(k + 1);
+    }
+}
+
+template <typename real>
+__device__ inline void write_compute(int64_t node, double comx, double comy, double m0, double m2xx, double m2xy,
+                                     double m2yy, double cx, double cy, real* comrel, real* m0r, real* m2t)
+{
+    comrel[2 * node] = (real)(comx - cx);
+    comrel[2 * node + 1] = (real)(comy - cy);
+    m0r[node] = (real)m0;
+    double inv = m0 > 0.0 ? 1.0 / m0 : 0.0;
+    m2t[3 * node] = (real)(inv * m2xx);
+    m2t[3 * node + 1] = (real)(inv * m2xy);
+    m2t[3 * node + 2] = (real)(inv * m2yy);
+}
+
+// createLeafNodes, second loop (:355-377) plus the first-occupant box (:343-350)
+template <typename real>
+__global__ void k_leaf_moments(const double2* __restrict__ pos64, int depth, double minx, double miny, double h,
+                               uint32_t* __restrict__ count, const uint32_t* __restrict__ first,
+                               double2* __restrict__ com64, double* __restrict__ m0, double* __restrict__ m2,
+                               double2* __restrict__ bbc, double* __restrict__ bblen, real* __restrict__ comrel,
+                               real* __restrict__ m0r, real* __restrict__ m2t)
+{
+    const uint32_t li = level_index(depth);
+    const int64_t nl = (int64_t)1 << (2 * depth);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t node = li + i;
+        uint32_t f = first[node];
+        uint32_t c = count[node] - f;  // count holds the end index here
+        count[node] = c;
+        uint32_t ix = compact16((uint32_t)i), iy = compact16((uint32_t)i >> 1);
+        double cx = minx + ((double)ix + 0.5) * h;
+        double cy = miny + ((double)iy + 0.5) * h;
+        if (c == 0) {
+            com64[node] = make_double2(0.0, 0.0);
+            m0[node] = 0.0;
+            m2[3 * node] = m2[3 * node + 1] = m2[3 * node + 2] = 0.0;
+            bbc[node] = make_double2(0.0, 0.0);
+            bblen[node] = 0.0;
+            write_compute<real>(node, cx, cy, 0.0, 0.0, 0.0, 0.0, cx, cy, comrel, m0r, m2t);
+            continue;
+        }
+        double sx = 0.0, sy = 0.0;
+        for (uint32_t p = f; p < f + c; p++) {
+            double2 q = pos64[p];
+            sx += q.x;
+            sy += q.y;
+        }
+        double M0 = (double)c;
+        sx /= M0;
+        sy /= M0;
+        double a = 0.0, b = 0.0, d = 0.0;
+        for (uint32_t p = f; p < f + c; p++) {
+            double2 q = pos64[p];
+            double rx = q.x - sx, ry = q.y - sy;
+            a += rx * rx;
+            b += rx * ry;
+            d += ry * ry;
+        }
+        com64[node] = make_double2(sx, sy);
+        m0[node] = M0;
+        m2[3 * node] = a;
+        m2[3 * node + 1] = b;
+        m2[3 * node + 2] = d;
+        // BBcentre = minPos + h * g + 0.5 * h (:345)
+        bbc[node] = make_double2(minx + h * (double)ix + 0.5 * h, miny + h * (double)iy + 0.5 * h);
+        bblen[node] = h;
+        write_compute<real>(node, sx, sy, M0, a, b, d, cx, cy, comrel, m0r, m2t);
+    }
+}
+
+// bottomUpNodeConstruction (:381-470) for one level l
+template <typename real>
+__global__ void k_bottom_up(int l, double minx, double miny, double hl, uint32_t* __restrict__ count,
+                            uint32_t* __restrict__ first, double2* __restrict__ com64, double* __restrict__ m0,
+                            double* __restrict__ m2, double2* __restrict__ bbc, double* __restrict__ bblen,
+                            real* __restrict__ comrel, real* __restrict__ m0r, real* __restrict__ m2t)
+{
+    const uint32_t li = level_index(l), lc = level_index(l + 1);
+    const int64_t nl = (int64_t)1 << (2 * l);
+    const double offx[4] = {0.5, -0.5, 0.5, -0.5};
+    const double offy[4] = {0.5, 0.5, -0.5, -0.5};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t node = li + i;
+        const int64_t fc = lc + 4 * i;
+        uint32_t cnt = 0, fp = 0;
+        double cx = 0.0, cy = 0.0, M0 = 0.0, bx = 0.0, by = 0.0, len = 0.0;
+        for (int j = 3; j >= 0; j--) {
+            const int64_t ch = fc + j;
+            uint32_t cc = count[ch];
+            if (cc == 0) continue;
+            double clen = bblen[ch];
+            double2 cb = bbc[ch];
+            bx = offx[j] * clen + cb.x;
+            by = offy[j] * clen + cb.y;
+            len = 2.0 * clen;
+            fp = first[ch];
+            cnt += cc;
+            double cm = m0[ch];
+            double2 cc2 = com64[ch];
+            cx += cm * cc2.x;
+            cy += cm * cc2.y;
+            M0 += cm;
+        }
+        uint32_t ix = compact16((uint32_t)i), iy = compact16((uint32_t)i >> 1);
+        double ccx = minx + ((double)ix + 0.5) * hl;
+        double ccy = miny + ((double)iy + 0.5) * hl;
+        count[node] = cnt;
+        first[node] = fp;
+        if (cnt == 0) {
+            com64[node] = make_double2(0.0, 0.0);
+            m0[node] = 0.0;
+            m2[3 * node] = m2[3 * node + 1] = m2[3 * node + 2] = 0.0;
+            bbc[node] = make_double2(0.0, 0.0);
+            bblen[node] = 0.0;
+            write_compute<real>(node, ccx, ccy, 0.0, 0.0, 0.0, 0.0, ccx, ccy, comrel, m0r, m2t);
+            continue;
+        }
+        cx /= M0;
+        cy /= M0;
+        double a = 0.0, b = 0.0, d = 0.0;
+        for (int j = 0; j < 4; j++) {
+            const int64_t ch = fc + j;
+            double cm = m0[ch];
+            if (cm == 0.0) continue;
+            double2 cc2 = com64[ch];
+            double rx = cc2.x - cx, ry = cc2.y - cy;
+            a += rx * rx;
+            b += rx * ry;
+            d += ry * ry;
+            a += m2[3 * ch];
+            b += m2[3 * ch + 1];
+            d += m2[3 * ch + 2];
+        }
+        com64[node] = make_double2(cx, cy);
+        m0[node] = M0;
+        m2[3 * node] = a;
+        m2[3 * node + 1] = b;
+        m2[3 * node + 2] = d;
+        bbc[node] = make_double2(bx, by);
+        bblen[node] = len;
+        write_compute<real>(node, cx, cy, M0, a, b, d, ccx, ccy, comrel, m0r, m2t);
+    }
+}
+
+}  // namespace
+
+int build_tree(Handle& h, const double* d_pos, int64_t n, double minx, double miny, double maxx, double maxy)
+{
+    cudaStream_t s = h.stream;
+    const double nmx = -minx, nmy = -miny;
+    const double ax = maxx + nmx, ay = maxy + nmy;
+    const double L = (ax < ay) ? ay : ax;  // compMax(maxPos - minPos) (:84-85)
+    if (!(L > 0.0) || !std::isfinite(L)) {
+        tc_set_error("bounding box must have a positive finite extent (got %g)", L);
+        return TC_ERR_INVALID;
+    }
+    int depth = h.cfg.depth;
+    if (depth < 0) {
+        uint32_t d = 0;
+        tc_get_depth(h.cfg.max_children, n, &d);
+        depth = (int)d;
+    }
+    if (depth > 15) {
+        tc_set_error("tree depth %d exceeds the 15 levels that 32-bit Morton codes resolve", depth);
+        return TC_ERR_INVALID;
+    }
+    int64_t nn = 0;
+    tc_node_count((uint32_t)depth, &nn);
+    h.depth = depth;
+    h.n = n;
+    h.nnodes = nn;
+    h.minx = minx;
+    h.miny = miny;
+    h.L = L;
+    h.tree_ready = false;
+    h.launches = 0;
+    const bool f64 = h.cfg.precision == TC_PREC_FP64;
+    const size_t rs = f64 ? 8 : 4;
+    int rc = 0;
+    if ((rc = ensure(h.codes, n * 4)) || (rc = ensure(h.perm, n * 4)) || (rc = ensure(h.alt_keys, n * 4)) ||
+        (rc = ensure(h.alt_vals, n * 4)) || (rc = ensure(h.pos64, n * 16)) || (rc = ensure(h.prel, n * 2 * rs)) ||
+        (rc = ensure(h.count, nn * 4)) || (rc = ensure(h.first, nn * 4)) || (rc = ensure(h.com64, nn * 16)) ||
+        (rc = ensure(h.m0, nn * 8)) || (rc = ensure(h.m2, nn * 24)) || (rc = ensure(h.bbc, nn * 16)) ||
+        (rc = ensure(h.bblen, nn * 8)) || (rc = ensure(h.comrel, nn * 2 * rs)) || (rc = ensure(h.m0r, nn * rs)) ||
+        (rc = ensure(h.m2t, nn * 3 * rs)) || (rc = ensure(h.tmp, radix_tmp_words(n) * 4)) ||
+        (rc = ensure(h.err, 64)))
+        return rc;
+
+    TC_CUDA_TRY(cudaMemsetAsync(h.err.p, 0, sizeof(uint32_t), s));
+    k_morton<<<grid_for(n, 256), 256, 0, s>>>((const double2*)d_pos, n, minx, miny, maxx, maxy, L,
+                                               P<uint32_t>(h.codes), P<uint32_t>(h.err));
+    h.launches++;
+    TC_CUDA_TRY(cudaGetLastError());
+    rc = radix_sort_u32(P<uint32_t>(h.codes), P<uint32_t>(h.perm), P<uint32_t>(h.alt_keys), P<uint32_t>(h.alt_vals), n,
+                        P<uint32_t>(h.tmp), s, &h.launches);
+    if (rc) return rc;
+    const uint32_t li = level_index(depth);
+    const int64_t nleaf = (int64_t)1 << (2 * depth);
+    TC_CUDA_TRY(cudaMemsetAsync(P<uint32_t>(h.count) + li, 0, nleaf * 4, s));
+    TC_CUDA_TRY(cudaMemsetAsync(P<uint32_t>(h.first) + li, 0, nleaf * 4, s));
+    const double hleaf = L / (double)(1u << depth);
+    if (f64) {
+        k_gather_bounds<double><<<grid_for(n, 256), 256, 0, s>>>(P<uint32_t>(h.codes), P<uint32_t>(h.perm),
+                                                                 (const double2*)d_pos, n, depth, minx, miny, hleaf,
+                                                                 P<double2>(h.pos64), P<double>(h.prel),
+                                                                 P<uint32_t>(h.first), P<uint32_t>(h.count));
+        k_leaf_moments<double><<<grid_for(nleaf, 128), 128, 0, s>>>(
+            P<double2>(h.pos64), depth, minx, miny, hleaf, P<uint32_t>(h.count), P<uint32_t>(h.first),
+            P<double2>(h.com64), P<double>(h.m0), P<double>(h.m2), P<double2>(h.bbc), P<double>(h.bblen),
+            P<double>(h.comrel), P<double>(h.m0r), P<double>(h.m2t));
+    } else {
+        k_gather_bounds<float><<<grid_for(n, 256), 256, 0, s>>>(P<uint32_t>(h.codes), P<uint32_t>(h.perm),
+                                                                (const double2*)d_pos, n, depth, minx, miny, hleaf,
+                                                                P<double2>(h.pos64), P<float>(h.prel),
+                                                                P<uint32_t>(h.first), P<uint32_t>(h.count));
+        k_leaf_moments<float><<<grid_for(nleaf, 128), 128, 0, s>>>(
+            P<double2>(h.pos64), depth, minx, miny, hleaf, P<uint32_t>(h.count), P<uint32_t>(h.first),
+            P<double2>(h.com64), P<double>(h.m0), P<double>(h.m2), P<double2>(h.bbc), P<double>(h.bblen),
+            P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t));
+    }
+    h.launches += 2;
+    for (int l = depth - 1; l >= 0; l--) {
+        const double hl = L / (double)(1u << l);
+        const int64_t nl = (int64_t)1 << (2 * l);
+        if (f64)
+            k_bottom_up<double><<<grid_for(nl, 128), 128, 0, s>>>(
+                l, minx, miny, hl, P<uint32_t>(h.count), P<uint32_t>(h.first), P<double2>(h.com64), P<double>(h.m0),
+                P<double>(h.m2), P<double2>(h.bbc), P<double>(h.bblen), P<double>(h.comrel), P<double>(h.m0r),
+                P<double>(h.m2t));
+        else
+            k_bottom_up<float><<<grid_for(nl, 128), 128, 0, s>>>(
+                l, minx, miny, hl, P<uint32_t>(h.count), P<uint32_t>(h.first), P<double2>(h.com64), P<double>(h.m0),
+                P<double>(h.m2), P<double2>(h.bbc), P<double>(h.bblen), P<float>(h.comrel), P<float>(h.m0r),
+                P<float>(h.m2t));
+        h.launches++;
+    }
+    TC_CUDA_TRY(cudaGetLastError());
+    h.tree_ready = true;
+    return TC_OK;
+}
+
+}  // namespace tc

@@ -1,0 +1,192 @@
+"""Host-side mirror of the reference's solver interface over the C ABI.
+
+``NBodySolverFMM_SYM_MORTON`` keeps the names and argument meaning of
+``NBodySolver<T>`` (src/nbodysolvers/cpu/nBodySolver.h:9-23) as implemented by
+``NBodySolverFMM_SYM_MORTON<TsnePoint2D>``
+(src/nbodysolvers/cpu/nBodySolverFMM_SYM_MORTON.h:29-614):
+
+* ``updateTree(points, minPos, maxPos)`` sorts ``points`` into Morton order in
+  place (positions, derivatives, labels and IDs move together, as the
+  reference's AoS sort moves whole ``TsnePoint2D`` records);
+* ``solveNbody(total, points)`` adds the repulsive force into
+  ``points.derivative`` and returns ``total`` plus the kernel's pair sum (the
+  reference's ``double& total`` argument);
+* ``getNodesBufferData(level)`` returns the boxes of the non-empty nodes.
+
+``Points`` is the structure-of-arrays form of ``std::vector<TsnePoint2D>``
+(src/particles/tsnePoint2D.h:6-37).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, lib, ptr
+
+
+@dataclass
+class Points:
+    position: np.ndarray               # (n, 2) float64
+    derivative: np.ndarray             # (n, 2) float64
+    ID: np.ndarray                     # (n,) int32
+    label: np.ndarray | None = None    # (n,) int32
+
+    @classmethod
+    def from_positions(cls, pos) -> "Points":
+        pos = np.ascontiguousarray(pos, np.float64)
+        n = len(pos)
+        return cls(pos.copy(), np.zeros((n, 2)), np.arange(n, dtype=np.int32), np.zeros(n, np.int32))
+
+    def __len__(self):
+        return len(self.position)
+
+
+KERNELS = {"tsne": _lib.TC_KERNEL_TSNE, "gravity": _lib.TC_KERNEL_GRAVITY}
+PRECISIONS = {"fp32": _lib.TC_PREC_FP32, "fp64": _lib.TC_PREC_FP64}
+
+
+def get_depth(max_children: int, n: int) -> int:
+    d = ctypes.c_uint32(0)
+    check(lib().tc_get_depth(max_children, n, ctypes.byref(d)))
+    return int(d.value)
+
+
+def node_count(depth: int) -> int:
+    c = ctypes.c_int64(0)
+    check(lib().tc_node_count(depth, ctypes.byref(c)))
+    return int(c.value)
+
+
+class NBodySolverFMM_SYM_MORTON:
+    """GPU symmetric Morton FMM behind the reference's solver interface."""
+
+    def __init__(self, kernel: str = "tsne", max_children: int = 16, tree_depth: int | None = None,
+                 theta: float = 0.5, softening: float = 1e-3, precision: str = "fp32", device: int = 0,
+                 stream=None):
+        cfg = _lib.TcConfig()
+        check(lib().tc_config_init(ctypes.byref(cfg)))
+        cfg.kernel = KERNELS[kernel]
+        cfg.max_children = max_children
+        cfg.depth = -1 if tree_depth is None else int(tree_depth)
+        cfg.theta = theta
+        cfg.softening = softening
+        cfg.precision = PRECISIONS[precision]
+        cfg.device = device
+        cfg.stream = stream
+        self._h = ctypes.c_void_p()
+        check(lib().tc_create(ctypes.byref(cfg), ctypes.byref(self._h)))
+        self.maxChildren = max_children
+        self._cfg_depth = cfg.depth
+        self._theta = theta
+        self.kernel = kernel
+        self.precision = precision
+        self.treeDepth = None
+        self.n = 0
+
+    # -- NBodySolver fields
+    @property
+    def theta(self) -> float:
+        return self._theta
+
+    @theta.setter
+    def theta(self, v: float):
+        check(lib().tc_set_theta(self._h, float(v)))
+        self._theta = float(v)
+
+    def close(self):
+        if self._h:
+            lib().tc_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- NBodySolver methods
+    def updateTree(self, points: Points, minPos, maxPos):
+        n = len(points)
+        pos = np.ascontiguousarray(points.position, np.float64)
+        ids = np.ascontiguousarray(points.ID, np.int32)
+        mn = np.asarray(minPos, np.float64)
+        mx = np.asarray(maxPos, np.float64)
+        check(lib().tc_update_tree(self._h, ptr(pos), None, n, ptr(mn), ptr(mx)))
+        perm = np.empty(n, np.int32)
+        check(lib().tc_get_tree(self._h, None, ptr(perm), None, None))
+        points.position[...] = pos
+        points.ID[...] = ids[perm]
+        points.derivative[...] = points.derivative[perm]
+        if points.label is not None:
+            points.label[...] = points.label[perm]
+        self.n = n
+        self.treeDepth = get_depth(self.maxChildren, n) if self._depth_cfg() < 0 else self._depth_cfg()
+        return perm
+
+    def _depth_cfg(self):
+        return -1 if not hasattr(self, "_cfg_depth") else self._cfg_depth
+
+    def solveNbody(self, total: float, points: Points) -> float:
+        tot = ctypes.c_double(total)
+        grad = np.ascontiguousarray(points.derivative, np.float64)
+        check(lib().tc_solve(self._h, ctypes.byref(tot), None, ptr(grad), len(points)))
+        points.derivative[...] = grad
+        return float(tot.value)
+
+    def getNodesBufferData(self, level: int = -1) -> np.ndarray:
+        cnt = ctypes.c_int64(0)
+        check(lib().tc_get_node_boxes(self._h, level, None, 0, ctypes.byref(cnt)))
+        boxes = np.zeros((cnt.value, 3))
+        check(lib().tc_get_node_boxes(self._h, level, ptr(boxes), cnt.value, ctypes.byref(cnt)))
+        return boxes
+
+    # -- extras used by the tests and the benchmark
+    def tree_dump(self):
+        """Morton codes, permutation, sorted positions and the 27-double node rows."""
+        n = self.n
+        codes = np.empty(n, np.uint32)
+        perm = np.empty(n, np.int32)
+        pos = np.empty((n, 2))
+        nodes = np.empty((node_count(self.depth()), 27))
+        check(lib().tc_get_tree(self._h, ptr(codes), ptr(perm), ptr(pos), ptr(nodes)))
+        return dict(codes=codes, perm=perm, pos=pos, nodes=nodes)
+
+    def depth(self) -> int:
+        return self.treeDepth
+
+    def list_stats(self):
+        d = self.depth()
+        nn = np.zeros(d + 1, np.uint32)
+        nr = np.zeros(d + 1, np.uint32)
+        check(lib().tc_get_list_stats(self._h, ptr(nn), ptr(nr)))
+        return nn, nr
+
+    def launches(self) -> int:
+        return int(lib().tc_last_launch_count(self._h))
+
+    # device-resident entry points (torch tensors on the handle's device)
+    def update_tree_device(self, pos, minPos=None, maxPos=None):
+        mn = None if minPos is None else np.asarray(minPos, np.float64)
+        mx = None if maxPos is None else np.asarray(maxPos, np.float64)
+        check(lib().tc_update_tree_device(self._h, ptr(pos), pos.shape[0], ptr(mn), ptr(mx)))
+        self.n = pos.shape[0]
+        self.treeDepth = get_depth(self.maxChildren, self.n) if self._depth_cfg() < 0 else self._depth_cfg()
+
+    def solve_device(self, grad, total, accumulate: bool = False, scatter: bool = True):
+        check(lib().tc_solve_device(self._h, ptr(grad), ptr(total), int(accumulate), int(scatter)))
+
+
+def direct(pos, *, kernel="tsne", softening=1e-3, precision="fp64", rows=None):
+    """O(N^2) force on `rows` (all points when None) on the GPU."""
+    pos = np.ascontiguousarray(pos, np.float64)
+    n = len(pos)
+    r = None if rows is None else np.ascontiguousarray(rows, np.int64)
+    m = n if r is None else len(r)
+    g = np.zeros((m, 2))
+    tot = ctypes.c_double(0.0)
+    check(lib().tc_direct(KERNELS[kernel], softening, PRECISIONS[precision], ptr(pos), n, ptr(r), m, ptr(g),
+                          ctypes.byref(tot)))
+    return g, float(tot.value)

@@ -1,0 +1,62 @@
+"""CPU-side checks of the C ABI: the library loads and exports every symbol
+the public headers declare; host-only helpers agree with the oracle."""
+import ctypes
+import os
+import re
+
+import pytest
+
+import oracle
+from masterthesislucas_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for f in os.listdir(inc):
+        if f.endswith(".h"):
+            src = open(os.path.join(inc, f)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names |= set(re.findall(r"\b(tc_\w+)\s*\(", src))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def L():
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("libtreecode.so not built")
+    return _lib.lib()
+
+
+def test_every_declared_symbol_is_exported(L):
+    names = declared_symbols()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(L, n), n
+        assert n in _lib.SIGNATURES, f"{n} has no ctypes signature"
+
+
+def test_get_depth_matches_reference_rule(L):
+    for leaf, n in [(16, 70000), (16, 65536), (64, 4194304), (16, 3000), (16, 17), (16, 15), (8, 3000), (1, 1)]:
+        d = ctypes.c_uint32()
+        assert L.tc_get_depth(leaf, n, ctypes.byref(d)) == 0
+        expect = oracle.get_depth(leaf, n) if n // leaf >= 1 else 0
+        assert d.value == expect, (leaf, n)
+
+
+def test_node_count(L):
+    c = ctypes.c_int64()
+    for d in range(0, 10):
+        assert L.tc_node_count(d, ctypes.byref(c)) == 0
+        assert c.value == oracle.node_count(d)
+
+
+def test_invalid_config_rejected_without_gpu(L):
+    cfg = _lib.TcConfig()
+    L.tc_config_init(ctypes.byref(cfg))
+    cfg.theta = -1.0
+    h = ctypes.c_void_p()
+    assert L.tc_create(ctypes.byref(cfg), ctypes.byref(h)) == _lib.TC_ERR_INVALID
+    assert b"invalid" in L.tc_last_error()
