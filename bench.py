@@ -1,0 +1,374 @@
+#!/usr/bin/env python
+"""Benchmark of the tree-code force step on GB300.
+
+Metric: particles/s per force step at <= 1e-4 median relative force error
+(median over 4,096 seeded sample particles of |F - F_direct| / |F_direct|,
+F_direct an FP64 direct sum on the GPU).
+
+Default workload (the metric's configuration): the 2D N-body force step on
+N = 4,194,304 particles in two exponential disks (scale lengths 0.1 and 0.05,
+centres 0.6 apart, masses 1/N), Plummer-softened gravity eps = 1e-3, leaf size
+64 (tree depth 9), FP32 expansions and P2P.  A step is one updateTree +
+solveNbody of the symmetric Morton FMM at the reference's fixed expansion
+order; the opening angle is the largest of a candidate list whose measured
+median error is <= 1e-4 (calibrated before timing, untimed).
+
+Arms:
+  --impl ours       (default) the CUDA library on 1..N GPUs (replicas: each
+                    rank advances its own independent system; weak scaling)
+  --impl reference  the reference's CPU algorithm (the C oracle port of
+                    NBodySolverFMM_SYM_MORTON, single-threaded per system as
+                    in the reference) on all host cores, each core solving an
+                    independent bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particles/s per force step at 1e-4 rel err: learned-order vs plain FMM, 1 GB300"
+UNIT = "particles/s"
+TARGET_ERR = 1e-4
+N_SAMPLES = 4096
+THETAS = (0.4, 0.35, 0.3, 0.25, 0.2, 0.15, 0.1)
+
+WORKLOADS = {
+    "nbody_two_disks_4m": dict(n=4194304, dist="two_disks", kernel="gravity", softening=1e-3, max_children=64),
+    "nbody_two_disks_1m": dict(n=1048576, dist="two_disks", kernel="gravity", softening=1e-3, max_children=64),
+    "bh_mixture_65k": dict(n=65536, dist="mixture", kernel="gravity", softening=1e-3, max_children=16),
+}
+
+
+def positions(w, seed):
+    from masterthesislucas_gb300 import datasets
+    if w["dist"] == "two_disks":
+        p = datasets.two_disks(w["n"], seed=seed)
+    else:
+        p = datasets.gaussian_mixture(w["n"], seed=seed)
+    return np.ascontiguousarray(p.astype(np.float64))
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms in the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def median_error(grad, ref):
+    e = np.linalg.norm(grad - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    return float(np.median(e)), float(np.percentile(e, 90)), float(e.max())
+
+
+def run_ours(args, w, rank, world):
+    import torch
+
+    from masterthesislucas_gb300 import NBodySolverFMM_SYM_MORTON
+    from masterthesislucas_gb300._lib import check, lib, ptr
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(device=dev)
+    n = w["n"]
+    pos_h = positions(w, seed=1000 + rank)
+    pos_d = torch.from_numpy(pos_h).to(dev)
+    grad_d = torch.zeros((n, 2), dtype=torch.float64, device=dev)
+    tot_d = torch.zeros(1, dtype=torch.float64, device=dev)
+    rows = np.sort(np.random.default_rng(7).choice(n, N_SAMPLES, replace=False)).astype(np.int64)
+    rows_d = torch.from_numpy(rows).to(dev)
+    ref_d = torch.zeros((N_SAMPLES, 2), dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    # FP64 direct-sum oracle on the sampled sinks (untimed)
+    check(lib().tc_direct_device(1 if w["kernel"] == "gravity" else 0, w["softening"], 1, ptr(pos_d), n,
+                                 ptr(rows_d), N_SAMPLES, ptr(ref_d), None, None))
+    torch.cuda.synchronize()
+    ref = ref_d.cpu().numpy()
+
+    def make(theta):
+        return NBodySolverFMM_SYM_MORTON(w["kernel"], max_children=w["max_children"], theta=theta,
+                                         softening=w["softening"], precision="fp32",
+                                         device=dev.index, stream=stream.cuda_stream)
+
+    def step(s):
+        s.update_tree_device(pos_d)
+        s.solve_device(grad_d, tot_d, accumulate=False, scatter=True)
+
+    # opening-angle calibration: largest theta meeting the error target
+    chosen, calib = None, []
+    for th in (args.theta,) if args.theta else THETAS:
+        s = make(th)
+        step(s)
+        torch.cuda.synchronize()
+        g = grad_d[rows_d].cpu().numpy()
+        med, p90, emax = median_error(g, ref)
+        calib.append({"theta": th, "median": med})
+        if med <= TARGET_ERR or args.theta:
+            chosen = (th, s, (med, p90, emax))
+            break
+        s.close()
+    if chosen is None:
+        raise SystemExit("no opening angle met the error target")
+    theta, s, err = chosen
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > L2 (129 MB)
+    for _ in range(args.warmup):
+        step(s)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    stage_sum = None
+    launches = 0
+    with ClockSampler(dev.index) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(k))
+            ev0[k].record(stream)
+            s.update_tree_device(pos_d)
+            launches += s.launches()
+            s.solve_device(grad_d, tot_d, accumulate=False, scatter=True)
+            launches += s.launches()
+            ev1[k].record(stream)
+            st = s.stage_times()
+            stage_sum = st if stage_sum is None else {a: stage_sum[a] + st[a] for a in st}
+        torch.cuda.synchronize()
+    ms = [ev0[k].elapsed_time(ev1[k]) for k in range(args.steps)]
+    t_total = sum(ms) / 1e3
+    if world > 1:
+        t = torch.tensor([t_total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_total = float(t.item())
+    counters = s.counters()
+    stages = {a: v / args.steps for a, v in stage_sum.items()}
+    g = grad_d[rows_d].cpu().numpy()
+    err = median_error(g, ref)
+
+    # end to end through the C ABI with pinned host buffers
+    from masterthesislucas_gb300._lib import check as chk
+    import ctypes
+    pos_pin = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
+    grad_pin = torch.zeros((n, 2), dtype=torch.float64, pin_memory=True)
+    ids_pin = torch.empty(n, dtype=torch.int32, pin_memory=True)
+    pos_np, grad_np, ids_np = pos_pin.numpy(), grad_pin.numpy(), ids_pin.numpy()
+    mn, mx = pos_h.min(0), pos_h.max(0)
+    e2e_ms = []
+    for k in range(max(2, args.steps // 2) + 2):
+        np.copyto(pos_np, pos_h)
+        ids_np[:] = np.arange(n, dtype=np.int32)
+        grad_np[:] = 0.0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        chk(lib().tc_update_tree(s._h, ptr(pos_np), ptr(ids_np), n, ptr(mn), ptr(mx)))
+        tot = ctypes.c_double(0.0)
+        chk(lib().tc_solve(s._h, ctypes.byref(tot), None, ptr(grad_np), n))
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms = e2e_ms[2:]
+    return dict(theta=theta, calib=calib, ms=ms, t_total=t_total, stages=stages, counters=counters, err=err,
+                clocks=clk.summary(), launches=launches, e2e_ms=e2e_ms, depth=s.depth())
+
+
+def cpu_baseline(w, theta, n_sample, threads=1, seeds=None):
+    """The reference's algorithm (C oracle port), single-threaded per system."""
+    import ctypes
+    import oracle
+    from masterthesislucas_gb300 import datasets
+
+    seeds = seeds or list(range(threads))
+    L = oracle.lib()
+    jobs = []
+    for sd in seeds:
+        if w["dist"] == "two_disks":
+            p = datasets.two_disks(n_sample, seed=5000 + sd)
+        else:
+            p = datasets.gaussian_mixture(n_sample, seed=5000 + sd)
+        p = np.ascontiguousarray(p.astype(np.float64))
+        jobs.append(p)
+    depth = oracle.get_depth(w["max_children"], n_sample)
+    kern = 1 if w["kernel"] == "gravity" else 0
+
+    def solve(p):
+        n = len(p)
+        mn, mx = p.min(0), p.max(0)
+        codes = np.empty(n, np.uint32)
+        ids = np.empty(n, np.int32)
+        ps = np.empty((n, 2))
+        g = np.zeros((n, 2))
+        tot = np.zeros(1)
+        L.orc_sym_fmm(kern, w["softening"], w["max_children"], depth, theta, n, oracle._p(p), oracle._p(mn),
+                      oracle._p(mx), oracle._p(codes), oracle._p(ids), oracle._p(ps), oracle._p(g), oracle._p(tot),
+                      None)
+
+    t0 = time.perf_counter()
+    ths = [threading.Thread(target=solve, args=(p,)) for p in jobs]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    dt = time.perf_counter() - t0
+    return len(jobs) * n_sample / dt, dt, depth
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="nbody_two_disks_4m", choices=sorted(WORKLOADS))
+    ap.add_argument("--theta", type=float, default=None)
+    ap.add_argument("--cpu-sample", type=int, default=262144)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    w = WORKLOADS[args.workload]
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    config = {"workload": args.workload, "n": w["n"], "distribution": w["dist"], "kernel": w["kernel"],
+              "softening": w["softening"], "leaf_size": w["max_children"], "expansion": "reference order (M0+M2 / C1-C3)",
+              "precision": "fp32 expansions and P2P; fp64 tree build, MACs and Z",
+              "error_target": TARGET_ERR, "error_samples": N_SAMPLES}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        theta = args.theta or 0.3
+        threads = os.cpu_count() or 1
+        n_s = 131072
+        vals = []
+        dts = []
+        for k in range(args.warmup + args.steps):
+            v, dt, depth = cpu_baseline(w, theta, n_s, threads=threads, seeds=[k * 1000 + i for i in range(threads)])
+            if k >= args.warmup:
+                vals.append(v)
+                dts.append(dt)
+        value = float(np.mean(vals))
+        config.update({"theta": theta, "sample_n": n_s, "sample_depth": depth})
+        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(dts)),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded two-disk positions)", "config": config,
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": f"{threads} independent {n_s}-particle systems of the same distribution, "
+                                           f"leaf {w['max_children']}, theta {theta}, one per core"},
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        dist.init_process_group("nccl")
+    r = run_ours(args, w, rank, world)
+    if rank != 0:
+        return
+    n = w["n"]
+    value = n * world * args.steps / r["t_total"]
+    e2e_s = float(np.mean(r["e2e_ms"])) / 1e3
+    peaks, peak_src = load_peaks()
+    sm_mhz = peaks.get("sm_max_mhz", 2070.0)
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12  # TFLOP/s, nominal at the max SM clock
+    t_near = r["stages"]["near"] / 1e3
+    flops = 20.0 * r["counters"]["p2p_pairs"]
+    achieved = flops / t_near / 1e12 if t_near > 0 else None
+    config.update({"theta": r["theta"], "depth": r["depth"], "theta_calibration": r["calib"],
+                   "l2": "256 MB buffer written between timed steps (inputs also exceed L2)"})
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * r["t_total"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded two-disk positions; no published dataset for this workload)",
+        "config": config,
+        "method": "plain fixed-order symmetric Morton FMM (reference order); learned-order controller not built",
+        "error": {"median": r["err"][0], "p90": r["err"][1], "max": r["err"][2], "vs": "fp64 direct sum",
+                  "samples": N_SAMPLES},
+        "stages_ms": r["stages"],
+        "counters": r["counters"],
+        "roofline": {"kernel": "k_leaf_near (P2P + M2P + L2P)", "bound": "fp32",
+                     "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": (achieved / fp32_peak) if achieved else None, "traffic": None,
+                     "flops_per_pair": 20, "peak_source": f"nominal: 152 SMs x 128 FP32 lanes x 2 x {sm_mhz:.0f} MHz "
+                                                          f"(MEASURED_PEAKS.json holds no FP32 figure; {peak_src})"},
+        "e2e": {"value": n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * 16,
+                "d2h_bytes_per_step": n * 16 + n * 4 + n * 16 + 8},
+        "gpu_launches": r["launches"],
+        "clocks": r["clocks"],
+    }
+    if not args.no_cpu_baseline:
+        v, dt, depth = cpu_baseline(w, r["theta"], args.cpu_sample, threads=1, seeds=[0])
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": f"one {args.cpu_sample}-particle system of the same distribution, "
+                                          f"leaf {w['max_children']} (depth {depth}), theta {r['theta']}, "
+                                          f"{dt:.1f} s"}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -117,6 +117,16 @@ int tc_get_node_boxes(tc_handle* h, int level, double* boxes, int64_t cap, int64
 /* Kernels launched by the last update/solve call on this handle. */
 int tc_last_launch_count(tc_handle* h);
 
+/* Device time of the stages of the last update + solve, in milliseconds,
+ * from CUDA events on the handle's stream: [0] Morton codes + radix sort,
+ * [1] leaf build + upward pass, [2] interaction lists, [3] M2L,
+ * [4] near field (P2P, M2P, P2L, L2P), [5] Z reduction.  Synchronises.   */
+#define TC_NSTAGES 6
+int tc_get_stage_times(tc_handle* h, double* ms);
+/* Interaction counts of the last solve: [0] P2P pair evaluations, [1] M2P,
+ * [2] P2L, [3] M2L (directed; each unordered reference pair counts twice). */
+int tc_get_counters(tc_handle* h, uint64_t* counts);
+
 /* ---------------------------------------------------------------- direct sums
  * NBodySolverNaive::solveNbody (src/nbodysolvers/cpu/nBodySolverNaive.h:53-112)
  * and the GPU naive step cudaTsneNaiveStepRep

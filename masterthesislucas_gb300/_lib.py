@@ -57,6 +57,8 @@ SIGNATURES = {
     "tc_get_list_stats": (_I, [_P, _P, _P]),
     "tc_get_node_boxes": (_I, [_P, _I, _P, _I64, _P]),
     "tc_last_launch_count": (_I, [_P]),
+    "tc_get_stage_times": (_I, [_P, _P]),
+    "tc_get_counters": (_I, [_P, _P]),
     "tc_last_error": (ctypes.c_char_p, []),
     "tc_direct": (_I, [_I, _D, _I, _P, _I64, _P, _I64, _P, _P]),
     "tc_direct_device": (_I, [_I, _D, _I, _P, _I64, _P, _I64, _P, _P, _P]),

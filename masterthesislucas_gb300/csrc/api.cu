@@ -51,6 +51,16 @@ void release(Buf& b)
     b.bytes = 0;
 }
 
+int record(Handle& h, int i)
+{
+    if (!h.ev_ready) {
+        for (auto& e : h.ev) TC_CUDA_TRY(cudaEventCreate(&e));
+        h.ev_ready = true;
+    }
+    TC_CUDA_TRY(cudaEventRecord(h.ev[i], h.stream));
+    return TC_OK;
+}
+
 namespace {
 
 __global__ void k_bbox(const double2* __restrict__ pos, int64_t n, double* __restrict__ out, uint32_t* err)
@@ -274,7 +284,7 @@ int tc_destroy(tc_handle* t)
     if (h.stream) cudaStreamSynchronize(h.stream);
     Buf* bufs[] = {&h.codes, &h.perm, &h.alt_keys, &h.alt_vals, &h.pos_in, &h.pos64, &h.prel, &h.grad_acc,
                    &h.count, &h.first, &h.com64, &h.m0, &h.m2, &h.bbc, &h.bblen, &h.comrel, &h.m0r, &h.m2t,
-                   &h.loc, &h.locfin, &h.ptr_pool, &h.idx_pool, &h.cnt_tmp, &h.tmp, &h.err, &h.zpart, &h.dtotal,
+                   &h.loc, &h.locfin, &h.chunk, &h.zwork, &h.zloc, &h.counters, &h.ptr_pool, &h.idx_pool, &h.cnt_tmp, &h.tmp, &h.err, &h.zpart, &h.dtotal,
                    &h.host_stage};
     for (Buf* b : bufs) release(*b);
     if (h.h_total) cudaFreeHost(h.h_total);
@@ -524,5 +534,38 @@ int tc_get_node_boxes(tc_handle* t, int level, double* boxes, int64_t cap, int64
 }
 
 int tc_last_launch_count(tc_handle* t) { return t ? t->h.launches : 0; }
+
+int tc_get_stage_times(tc_handle* t, double* ms)
+{
+    if (!t || !ms) return TC_ERR_INVALID;
+    Handle& h = t->h;
+    if (!h.ev_ready) return TC_ERR_STATE;
+    TC_CUDA_TRY(cudaSetDevice(h.cfg.device));
+    TC_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    // stage k spans events (a, b)
+    const int a[TC_NSTAGES] = {0, 1, 2, 4, 5, 6};
+    const int b[TC_NSTAGES] = {1, 2, 3, 5, 6, 7};
+    for (int k = 0; k < TC_NSTAGES; k++) {
+        float f = 0.f;
+        cudaError_t e = cudaEventElapsedTime(&f, h.ev[a[k]], h.ev[b[k]]);
+        ms[k] = e == cudaSuccess ? (double)f : -1.0;
+    }
+    cudaGetLastError();
+    return TC_OK;
+}
+
+int tc_get_counters(tc_handle* t, uint64_t* counts)
+{
+    if (!t || !counts) return TC_ERR_INVALID;
+    Handle& h = t->h;
+    if (!h.counters.p) return TC_ERR_STATE;
+    TC_CUDA_TRY(cudaSetDevice(h.cfg.device));
+    TC_CUDA_TRY(cudaMemcpyAsync(counts, h.counters.p, 3 * 8, cudaMemcpyDeviceToHost, h.stream));
+    TC_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    uint64_t m2l = 0;
+    for (size_t l = 0; l < h.lists.nn_total.size(); l++) m2l += h.lists.nn_total[l];
+    counts[3] = m2l;
+    return TC_OK;
+}
 
 }  // extern "C"

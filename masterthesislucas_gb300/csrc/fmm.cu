@@ -154,17 +154,19 @@ __device__ inline bool pn_pass(double2 x, double2 com, double len, double inv_th
 
 constexpr int kLeafWarps = 4;
 
+// phase A, one warp per non-empty leaf S: the final local expansion of S at
+// com_S (own M2L + shifted ancestors + P2L from the passing points of
+// partners T < S), and the number of 32-sink chunks of S
 template <typename real, typename K>
 __global__ void __launch_bounds__(32 * kLeafWarps)
-    k_leaf(K ker, Geo geo, const uint32_t* __restrict__ count, const uint32_t* __restrict__ first,
-           const double2* __restrict__ com64, const double* __restrict__ bblen, const real* __restrict__ comrel,
-           const real* __restrict__ m0r, const real* __restrict__ m2t, const real* __restrict__ loc,
-           const uint32_t* __restrict__ near_ptr, const uint32_t* __restrict__ near_idx,
-           const double2* __restrict__ pos64, const real* __restrict__ prel, const uint32_t* __restrict__ perm,
-           double* __restrict__ grad, int accumulate, int scatter, double* __restrict__ zleaf,
-           real* __restrict__ locfin)
+    k_leaf_local(K ker, Geo geo, const uint32_t* __restrict__ count, const uint32_t* __restrict__ first,
+                 const double2* __restrict__ com64, const double* __restrict__ bblen, const real* __restrict__ comrel,
+                 const real* __restrict__ m0r, const real* __restrict__ loc, const uint32_t* __restrict__ near_ptr,
+                 const uint32_t* __restrict__ near_idx, const double2* __restrict__ pos64,
+                 const real* __restrict__ prel, real* __restrict__ locfin, double* __restrict__ zloc,
+                 uint32_t* __restrict__ nchunk, unsigned long long* __restrict__ counters)
 {
-    __shared__ real s_src[kLeafWarps][32][2];
+    uint32_t n_p2l = 0;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int dep = geo.depth;
     const uint32_t li = level_index(dep);
@@ -175,25 +177,23 @@ __global__ void __launch_bounds__(32 * kLeafWarps)
     for (int64_t si = blockIdx.x * (int64_t)kLeafWarps + w; si < nl; si += wstride) {
         const int64_t S = li + si;
         const uint32_t cS = count[S];
+        if (lane == 0) nchunk[si] = (cS + 31u) / 32u;
         if (cS == 0) {
-            if (lane == 0) zleaf[si] = 0.0;
+            if (lane == 0) zloc[si] = 0.0;
             continue;
         }
-        const uint32_t fS = first[S];
         const int isx = (int)compact16((uint32_t)si), isy = (int)compact16((uint32_t)si >> 1);
         const double2 comS64 = com64[S];
         const double lenS = bblen[S];
         const real csx = comrel[2 * S], csy = comrel[2 * S + 1];
         const real mS = m0r[S];
         const uint32_t e0 = near_ptr[si], e1 = near_ptr[si + 1];
-
-        // ---- phase A: local expansion of S at com_S
         real C[L_NCOEF];
 #pragma unroll
         for (int c = 0; c < L_NCOEF; c++) C[c] = real(0);
         real zA = real(0);
         if (lane <= dep) {
-            // lane k handles the ancestor at level k (k == dep is S itself)
+            // lane k shifts the expansion of the ancestor at level k (k == dep is S)
             const int k = lane;
             const uint32_t ai = (uint32_t)((uint64_t)si >> (2 * (dep - k)));
             const int64_t A = level_index(k) + ai;
@@ -207,7 +207,6 @@ __global__ void __launch_bounds__(32 * kLeafWarps)
             const real dy = h * (((real)isy + real(0.5)) - (iay + real(0.5)) * scale) + (csy - comrel[2 * A + 1]);
             add_shifted(CA, dx, dy, C);
         }
-        // P2L from partners T < S whose points pass the MAC against S
         for (uint32_t e = e0; e < e1; e++) {
             const uint32_t ti = near_idx[e];
             if (ti >= (uint32_t)si) continue;
@@ -226,33 +225,118 @@ __global__ void __launch_bounds__(32 * kLeafWarps)
                 C[L_C1Y] += Ry * D1;
                 add_c2c3(Rx, Ry, real(1), D1, D2, D3, C);
                 zA += mS * tt;
+                n_p2l++;
             }
         }
 #pragma unroll
         for (int c = 0; c < L_NCOEF; c++) C[c] = warp_sum(C[c]);
-        double zsum = (double)warp_sum(zA);
+        const double z = (double)warp_sum(zA);
         if (lane == 0) {
 #pragma unroll
             for (int c = 0; c < L_NCOEF; c++) locfin[si * L_NCOEF + c] = C[c];
+            zloc[si] = z;
         }
+    }
+    const unsigned long long c = warp_sum((unsigned long long)n_p2l);
+    if (lane == 0 && c) atomicAdd(counters + 2, c);
+}
 
-        // ---- phase B: sinks in chunks of 32
-        for (uint32_t c0 = 0; c0 < cS; c0 += 32) {
-            const uint32_t sl = c0 + lane;
-            const bool act = sl < cS;
-            const uint32_t s = fS + (act ? sl : 0);
-            const real px = prel[2 * s], py = prel[2 * s + 1];
-            const double2 x64 = pos64[s];
-            real gx = real(0), gy = real(0), zs = real(0);
-            if (act) eval_c1(C, px - csx, py - csy, gx, gy);
-            for (uint32_t e = e0; e < e1; e++) {
-                const uint32_t ti = near_idx[e];
-                const int64_t T = li + ti;
-                const uint32_t fT = first[T], cT = count[T];
-                const real ox = real(isx - (int)compact16(ti)) * h, oy = real(isy - (int)compact16(ti >> 1)) * h;
-                // base = x_s - (cell centre of T); source offset subtracts prel_t
-                const real bx = ox + px, by = oy + py;
-                if (ti == (uint32_t)si) {
+// phase B, one warp per work item (leaf S, chunk of up to 32 sinks of S)
+template <typename real, typename K>
+__global__ void __launch_bounds__(32 * kLeafWarps)
+    k_leaf_near(K ker, Geo geo, const uint32_t* __restrict__ count, const uint32_t* __restrict__ first,
+                const double2* __restrict__ com64, const double* __restrict__ bblen, const real* __restrict__ comrel,
+                const real* __restrict__ m0r, const real* __restrict__ m2t, const real* __restrict__ locfin,
+                const uint32_t* __restrict__ near_ptr, const uint32_t* __restrict__ near_idx,
+                const uint32_t* __restrict__ chunk_ptr, const double2* __restrict__ pos64,
+                const real* __restrict__ prel, const uint32_t* __restrict__ perm, double* __restrict__ grad,
+                int accumulate, int scatter, double* __restrict__ zwork, unsigned long long* __restrict__ counters)
+{
+    __shared__ real s_src[kLeafWarps][32][2];
+    uint32_t n_pp = 0, n_m2p = 0;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int dep = geo.depth;
+    const uint32_t li = level_index(dep);
+    const int64_t nl = (int64_t)1 << (2 * dep);
+    const real h = (real)geo.h_leaf;
+    const double inv_theta = geo.inv_theta;
+    const uint32_t nwork = chunk_ptr[nl];
+    const int64_t wstride = (int64_t)gridDim.x * kLeafWarps;
+    for (int64_t wi = blockIdx.x * (int64_t)kLeafWarps + w; wi < nwork; wi += wstride) {
+        // leaf of this work item: last si with chunk_ptr[si] <= wi
+        int64_t lo = 0, hi = nl;
+        while (hi - lo > 1) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (chunk_ptr[mid] <= (uint32_t)wi) lo = mid; else hi = mid;
+        }
+        const int64_t si = lo;
+        const int64_t S = li + si;
+        const uint32_t cS = count[S];
+        const uint32_t fS = first[S];
+        const uint32_t c0 = ((uint32_t)wi - chunk_ptr[si]) * 32u;
+        const int isx = (int)compact16((uint32_t)si), isy = (int)compact16((uint32_t)si >> 1);
+        const double2 comS64 = com64[S];
+        const double lenS = bblen[S];
+        const real csx = comrel[2 * S], csy = comrel[2 * S + 1];
+        const uint32_t e0 = near_ptr[si], e1 = near_ptr[si + 1];
+        real C[L_NCOEF];
+#pragma unroll
+        for (int c = 0; c < L_NCOEF; c++) C[c] = locfin[si * L_NCOEF + c];
+
+        const uint32_t sl = c0 + lane;
+        const bool act = sl < cS;
+        const uint32_t s = fS + (act ? sl : 0);
+        const real px = prel[2 * s], py = prel[2 * s + 1];
+        const double2 x64 = pos64[s];
+        real gx = real(0), gy = real(0), zs = real(0);
+        if (act) eval_c1(C, px - csx, py - csy, gx, gy);
+        for (uint32_t e = e0; e < e1; e++) {
+            const uint32_t ti = near_idx[e];
+            const int64_t T = li + ti;
+            const uint32_t fT = first[T], cT = count[T];
+            const real ox = real(isx - (int)compact16(ti)) * h, oy = real(isy - (int)compact16(ti >> 1)) * h;
+            // base = x_s - (cell centre of T); each source subtracts its prel
+            const real bx = ox + px, by = oy + py;
+            if (ti == (uint32_t)si) {
+                for (uint32_t q0 = 0; q0 < cT; q0 += 32) {
+                    const uint32_t q = q0 + lane;
+                    if (q < cT) {
+                        s_src[w][lane][0] = prel[2 * (fT + q)];
+                        s_src[w][lane][1] = prel[2 * (fT + q) + 1];
+                    }
+                    __syncwarp();
+                    const uint32_t m = min(32u, cT - q0);
+                    if (act) {
+                        n_pp += m - ((sl >= q0 && sl < q0 + m) ? 1u : 0u);
+                        for (uint32_t j = 0; j < m; j++) {
+                            if (q0 + j == sl) continue;
+                            const real Rx = bx - s_src[w][j][0], Ry = by - s_src[w][j][1];
+                            real D1, t;
+                            ker.near(Rx * Rx + Ry * Ry, D1, t);
+                            gx += D1 * Rx;
+                            gy += D1 * Ry;
+                            zs += t;
+                        }
+                    }
+                    __syncwarp();
+                }
+            } else if (ti > (uint32_t)si) {
+                // S is the first node of the pair: each sink is tested against T
+                const bool pass = act && pn_pass(x64, com64[T], bblen[T], inv_theta);
+                if (pass) {
+                    const real Rx = bx - comrel[2 * T], Ry = by - comrel[2 * T + 1];
+                    real D1, D2, D3, t;
+                    ker.far(Rx * Rx + Ry * Ry, D1, D2, D3, t);
+                    const real mT = m0r[T];
+                    real c1x, c1y;
+                    far_c1(Rx, Ry, mT, m2t[3 * T], m2t[3 * T + 1], m2t[3 * T + 2], D1, D2, D3, c1x, c1y);
+                    gx += c1x;
+                    gy += c1y;
+                    zs += mT * t;
+                    n_m2p++;
+                }
+                const bool direct = act && !pass;
+                if (__any_sync(0xffffffffu, direct)) {
                     for (uint32_t q0 = 0; q0 < cT; q0 += 32) {
                         const uint32_t q = q0 + lane;
                         if (q < cT) {
@@ -261,9 +345,9 @@ __global__ void __launch_bounds__(32 * kLeafWarps)
                         }
                         __syncwarp();
                         const uint32_t m = min(32u, cT - q0);
-                        if (act)
+                        if (direct) {
+                            n_pp += m;
                             for (uint32_t j = 0; j < m; j++) {
-                                if (q0 + j == sl) continue;
                                 const real Rx = bx - s_src[w][j][0], Ry = by - s_src[w][j][1];
                                 real D1, t;
                                 ker.near(Rx * Rx + Ry * Ry, D1, t);
@@ -271,101 +355,78 @@ __global__ void __launch_bounds__(32 * kLeafWarps)
                                 gy += D1 * Ry;
                                 zs += t;
                             }
-                        __syncwarp();
-                    }
-                } else if (ti > (uint32_t)si) {
-                    // S is the first node of the pair: test each sink against T
-                    const bool pass = act && pn_pass(x64, com64[T], bblen[T], inv_theta);
-                    if (pass) {
-                        const real Rx = bx - comrel[2 * T], Ry = by - comrel[2 * T + 1];
-                        real D1, D2, D3, t;
-                        ker.far(Rx * Rx + Ry * Ry, D1, D2, D3, t);
-                        const real mT = m0r[T];
-                        real c1x, c1y;
-                        far_c1(Rx, Ry, mT, m2t[3 * T], m2t[3 * T + 1], m2t[3 * T + 2], D1, D2, D3, c1x, c1y);
-                        gx += c1x;
-                        gy += c1y;
-                        zs += mT * t;
-                    }
-                    const bool direct = act && !pass;
-                    if (__any_sync(0xffffffffu, direct)) {
-                        for (uint32_t q0 = 0; q0 < cT; q0 += 32) {
-                            const uint32_t q = q0 + lane;
-                            if (q < cT) {
-                                s_src[w][lane][0] = prel[2 * (fT + q)];
-                                s_src[w][lane][1] = prel[2 * (fT + q) + 1];
-                            }
-                            __syncwarp();
-                            const uint32_t m = min(32u, cT - q0);
-                            if (direct)
-                                for (uint32_t j = 0; j < m; j++) {
-                                    const real Rx = bx - s_src[w][j][0], Ry = by - s_src[w][j][1];
-                                    real D1, t;
-                                    ker.near(Rx * Rx + Ry * Ry, D1, t);
-                                    gx += D1 * Rx;
-                                    gy += D1 * Ry;
-                                    zs += t;
-                                }
-                            __syncwarp();
                         }
-                    }
-                } else {
-                    // S is the second node: the points of T that fail the MAC
-                    // against S interact with every sink directly
-                    for (uint32_t q0 = 0; q0 < cT; q0 += 32) {
-                        const uint32_t q = q0 + lane;
-                        bool fail = false;
-                        real tx = real(0), ty = real(0);
-                        if (q < cT) {
-                            fail = !pn_pass(pos64[fT + q], comS64, lenS, inv_theta);
-                            tx = prel[2 * (fT + q)];
-                            ty = prel[2 * (fT + q) + 1];
-                        }
-                        const uint32_t bal = __ballot_sync(0xffffffffu, fail);
-                        if (fail) {
-                            const int slot = __popc(bal & ((1u << lane) - 1u));
-                            s_src[w][slot][0] = tx;
-                            s_src[w][slot][1] = ty;
-                        }
-                        __syncwarp();
-                        const int m = __popc(bal);
-                        if (act)
-                            for (int j = 0; j < m; j++) {
-                                const real Rx = bx - s_src[w][j][0], Ry = by - s_src[w][j][1];
-                                real D1, t;
-                                ker.near(Rx * Rx + Ry * Ry, D1, t);
-                                gx += D1 * Rx;
-                                gy += D1 * Ry;
-                                zs += t;
-                            }
                         __syncwarp();
                     }
                 }
-            }
-            if (act) {
-                const int64_t o = scatter ? (int64_t)perm[s] : (int64_t)s;
-                double ox2 = (double)gx, oy2 = (double)gy;
-                if (accumulate) {
-                    ox2 += grad[2 * o];
-                    oy2 += grad[2 * o + 1];
+            } else {
+                // S is the second node: the points of T that fail the MAC
+                // against S interact with every sink directly
+                for (uint32_t q0 = 0; q0 < cT; q0 += 32) {
+                    const uint32_t q = q0 + lane;
+                    bool fail = false;
+                    real tx = real(0), ty = real(0);
+                    if (q < cT) {
+                        fail = !pn_pass(pos64[fT + q], comS64, lenS, inv_theta);
+                        tx = prel[2 * (fT + q)];
+                        ty = prel[2 * (fT + q) + 1];
+                    }
+                    const uint32_t bal = __ballot_sync(0xffffffffu, fail);
+                    if (fail) {
+                        const int slot = __popc(bal & ((1u << lane) - 1u));
+                        s_src[w][slot][0] = tx;
+                        s_src[w][slot][1] = ty;
+                    }
+                    __syncwarp();
+                    const int m = __popc(bal);
+                    if (act) {
+                        n_pp += (uint32_t)m;
+                        for (int j = 0; j < m; j++) {
+                            const real Rx = bx - s_src[w][j][0], Ry = by - s_src[w][j][1];
+                            real D1, t;
+                            ker.near(Rx * Rx + Ry * Ry, D1, t);
+                            gx += D1 * Rx;
+                            gy += D1 * Ry;
+                            zs += t;
+                        }
+                    }
+                    __syncwarp();
                 }
-                grad[2 * o] = ox2;
-                grad[2 * o + 1] = oy2;
             }
-            zsum += warp_sum(act ? (double)zs : 0.0);
         }
-        if (lane == 0) zleaf[si] = zsum;
+        if (act) {
+            const int64_t o = scatter ? (int64_t)perm[s] : (int64_t)s;
+            double ox2 = (double)gx, oy2 = (double)gy;
+            if (accumulate) {
+                ox2 += grad[2 * o];
+                oy2 += grad[2 * o + 1];
+            }
+            grad[2 * o] = ox2;
+            grad[2 * o + 1] = oy2;
+        }
+        const double z = warp_sum(act ? (double)zs : 0.0);
+        if (lane == 0) zwork[wi] = z;
+    }
+    const unsigned long long a = warp_sum((unsigned long long)n_pp);
+    const unsigned long long b = warp_sum((unsigned long long)n_m2p);
+    if (lane == 0 && (a | b)) {
+        atomicAdd(counters + 0, a);
+        atomicAdd(counters + 1, b);
     }
 }
 
-// deterministic sum of the per-node and per-leaf Z partials
+// deterministic sum of the Z partials: per node (M2L), per leaf (P2L) and
+// per work item (near field; the count is read from the chunk offsets)
 __global__ void k_sum_z(const double* __restrict__ a, int64_t na, const double* __restrict__ b, int64_t nb,
-                        double* __restrict__ out, int accumulate)
+                        const double* __restrict__ c, const uint32_t* __restrict__ nc, double* __restrict__ out,
+                        int accumulate)
 {
     __shared__ double ws[32];
     double s = 0.0;
+    const int64_t ncv = *nc;
     for (int64_t i = threadIdx.x; i < na; i += blockDim.x) s += a[i];
     for (int64_t i = threadIdx.x; i < nb; i += blockDim.x) s += b[i];
+    for (int64_t i = threadIdx.x; i < ncv; i += blockDim.x) s += c[i];
     s = warp_sum(s);
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
     __syncthreads();
@@ -424,10 +485,11 @@ int solve_t(Handle& h, K ker, double* d_grad, int accumulate, int scatter, doubl
     const int64_t nleaf = (int64_t)1 << (2 * dep);
     int rc;
     if ((rc = ensure(h.loc, nn * L_NCOEF * sizeof(real))) || (rc = ensure(h.locfin, nleaf * L_NCOEF * sizeof(real))) ||
-        (rc = ensure(h.zpart, (nn + nleaf) * 8 + 64)))
+        (rc = ensure(h.zpart, nn * 8 + 64)))
         return rc;
+    if ((rc = ensure(h.counters, 64)) || (rc = record(h, 4))) return rc;
+    TC_CUDA_TRY(cudaMemsetAsync(h.counters.p, 0, 64, s));
     double* zp = P<double>(h.zpart);
-    double* zl = zp + nn;
     real* loc = P<real>(h.loc);
     // the root has no M2L partners
     TC_CUDA_TRY(cudaMemsetAsync(loc, 0, L_NCOEF * sizeof(real), s));
@@ -446,16 +508,33 @@ int solve_t(Handle& h, K ker, double* d_grad, int accumulate, int scatter, doubl
     geo.depth = dep;
     geo.inv_theta = 1.0 / h.cfg.theta;
     geo.h_leaf = h.L / (double)(1u << dep);
+    // work items of the near field: 32-sink chunks of the non-empty leaves
+    const int64_t wmax = h.n / 32 + (h.n < nleaf ? h.n : nleaf) + 1;
+    if ((rc = ensure(h.chunk, (nleaf + 1) * 4)) || (rc = ensure(h.zwork, wmax * 8)) ||
+        (rc = ensure(h.zloc, nleaf * 8)) || (rc = ensure(h.cnt_tmp, nleaf * 4 + 64)) ||
+        (rc = ensure(h.tmp, scan_tmp_words(nleaf) * 4)))
+        return rc;
+    uint32_t* nchunk = P<uint32_t>(h.cnt_tmp);
+    uint32_t* chunk_ptr = P<uint32_t>(h.chunk);
     const int64_t nblk = (nleaf + kLeafWarps - 1) / kLeafWarps;
-    k_leaf<real, K><<<(unsigned)(nblk < kSMs * 256 ? nblk : kSMs * 256), 32 * kLeafWarps, 0, s>>>(
+    k_leaf_local<real, K><<<(unsigned)(nblk < kSMs * 256 ? nblk : kSMs * 256), 32 * kLeafWarps, 0, s>>>(
         ker, geo, P<uint32_t>(h.count), P<uint32_t>(h.first), P<double2>(h.com64), P<double>(h.bblen),
-        P<real>(h.comrel), P<real>(h.m0r), P<real>(h.m2t), loc, ptr + h.lists.near_ptr_off[dep],
-        idx + h.lists.near_idx_off[dep], P<double2>(h.pos64), P<real>(h.prel), P<uint32_t>(h.perm), d_grad,
-        accumulate, scatter, zl, P<real>(h.locfin));
-    k_sum_z<<<1, 1024, 0, s>>>(zp, nn, zl, nleaf, d_total, 1);
-    h.launches += 2;
+        P<real>(h.comrel), P<real>(h.m0r), loc, ptr + h.lists.near_ptr_off[dep], idx + h.lists.near_idx_off[dep],
+        P<double2>(h.pos64), P<real>(h.prel), P<real>(h.locfin), P<double>(h.zloc), nchunk,
+        P<unsigned long long>(h.counters));
+    if ((rc = exclusive_scan_u32(nchunk, chunk_ptr, nleaf, P<uint32_t>(h.tmp), s))) return rc;
+    if ((rc = record(h, 5))) return rc;
+    const int64_t wblk = (wmax + kLeafWarps - 1) / kLeafWarps;
+    k_leaf_near<real, K><<<(unsigned)(wblk < kSMs * 256 ? wblk : kSMs * 256), 32 * kLeafWarps, 0, s>>>(
+        ker, geo, P<uint32_t>(h.count), P<uint32_t>(h.first), P<double2>(h.com64), P<double>(h.bblen),
+        P<real>(h.comrel), P<real>(h.m0r), P<real>(h.m2t), P<real>(h.locfin), ptr + h.lists.near_ptr_off[dep],
+        idx + h.lists.near_idx_off[dep], chunk_ptr, P<double2>(h.pos64), P<real>(h.prel), P<uint32_t>(h.perm),
+        d_grad, accumulate, scatter, P<double>(h.zwork), P<unsigned long long>(h.counters));
+    if ((rc = record(h, 6))) return rc;
+    k_sum_z<<<1, 1024, 0, s>>>(zp, nn, P<double>(h.zloc), nleaf, P<double>(h.zwork), chunk_ptr + nleaf, d_total, 1);
+    h.launches += 6;
     TC_CUDA_TRY(cudaGetLastError());
-    return TC_OK;
+    return record(h, 7);
 }
 
 }  // namespace

@@ -148,7 +148,7 @@ int build_lists(Handle& h)
         h.launches += 8;
     }
     TC_CUDA_TRY(cudaGetLastError());
-    return TC_OK;
+    return record(h, 3);
 }
 
 }  // namespace tc

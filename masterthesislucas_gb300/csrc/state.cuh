@@ -49,18 +49,27 @@ struct Handle {
     // particles
     Buf codes, perm, alt_keys, alt_vals, pos_in, pos64, prel, grad_acc;
     // nodes
-    Buf count, first, com64, m0, m2, bbc, bblen, comrel, m0r, m2t, loc, locfin;
+    Buf count, first, com64, m0, m2, bbc, bblen, comrel, m0r, m2t, loc, locfin, chunk, zwork, zloc;
     // lists
     Buf ptr_pool, idx_pool, cnt_tmp;
     Lists lists;
     // scratch
     Buf tmp, err, zpart, dtotal, host_stage;
+    // stage timing (CUDA events on the handle's stream) and interaction counters
+    cudaEvent_t ev[TC_NSTAGES + 2] = {};
+    bool ev_ready = false;
+    Buf counters;  // u64: p2p pairs, m2p, p2l (device)
     double* h_total = nullptr;     // pinned
     uint32_t* h_words = nullptr;   // pinned, 64 words
 };
 
 int ensure(Buf& b, size_t bytes);
 void release(Buf& b);
+
+// stage boundaries recorded on the handle's stream (index into Handle::ev):
+// 0 update start, 1 sorted, 2 tree built, 3 lists built, 4 solve start,
+// 5 M2L done, 6 near field done, 7 solve done
+int record(Handle& h, int i);
 
 template <typename T>
 inline T* P(const Buf& b) { return reinterpret_cast<T*>(b.p); }

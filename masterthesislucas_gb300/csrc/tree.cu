@@ -232,7 +232,6 @@ int build_tree(Handle& h, const double* d_pos, int64_t n, double minx, double mi
     h.miny = miny;
     h.L = L;
     h.tree_ready = false;
-    h.launches = 0;
     const bool f64 = h.cfg.precision == TC_PREC_FP64;
     const size_t rs = f64 ? 8 : 4;
     int rc = 0;
@@ -245,6 +244,7 @@ int build_tree(Handle& h, const double* d_pos, int64_t n, double minx, double mi
         (rc = ensure(h.err, 64)))
         return rc;
 
+    if ((rc = record(h, 0))) return rc;
     TC_CUDA_TRY(cudaMemsetAsync(h.err.p, 0, sizeof(uint32_t), s));
     k_morton<<<grid_for(n, 256), 256, 0, s>>>((const double2*)d_pos, n, minx, miny, maxx, maxy, L,
                                                P<uint32_t>(h.codes), P<uint32_t>(h.err));
@@ -252,7 +252,7 @@ int build_tree(Handle& h, const double* d_pos, int64_t n, double minx, double mi
     TC_CUDA_TRY(cudaGetLastError());
     rc = radix_sort_u32(P<uint32_t>(h.codes), P<uint32_t>(h.perm), P<uint32_t>(h.alt_keys), P<uint32_t>(h.alt_vals), n,
                         P<uint32_t>(h.tmp), s, &h.launches);
-    if (rc) return rc;
+    if (rc || (rc = record(h, 1))) return rc;
     const uint32_t li = level_index(depth);
     const int64_t nleaf = (int64_t)1 << (2 * depth);
     TC_CUDA_TRY(cudaMemsetAsync(P<uint32_t>(h.count) + li, 0, nleaf * 4, s));
@@ -294,6 +294,7 @@ int build_tree(Handle& h, const double* d_pos, int64_t n, double minx, double mi
         h.launches++;
     }
     TC_CUDA_TRY(cudaGetLastError());
+    if ((rc = record(h, 2))) return rc;
     h.tree_ready = true;
     return TC_OK;
 }

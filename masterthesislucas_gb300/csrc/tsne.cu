@@ -15,8 +15,17 @@
 namespace tc {
 namespace {
 
+template <typename real>
+__device__ inline real rcp1(real x);
+template <>
+__device__ inline float rcp1<float>(float x) { return __fdividef(1.0f, x); }
+template <>
+__device__ inline double rcp1<double>(double x) { return 1.0 / x; }
+
+// real: precision of the attractive products (FP32 product path, FP64 parity path)
+template <typename real, typename vreal>
 __global__ void k_tsne_attr_update(int64_t n, const uint32_t* __restrict__ row_ptr, const uint32_t* __restrict__ col,
-                                   const float* __restrict__ val, const double2* __restrict__ y,
+                                   const vreal* __restrict__ val, const double2* __restrict__ y,
                                    const double2* __restrict__ y_prev, const double* __restrict__ grad_rep,
                                    const double* __restrict__ z, double exag, double lr, double mom,
                                    double2* __restrict__ y_next, double* __restrict__ grad_out)
@@ -27,12 +36,12 @@ __global__ void k_tsne_attr_update(int64_t n, const uint32_t* __restrict__ row_p
     for (int64_t i = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += wstride) {
         const double2 yi = y[i];
         const uint32_t e0 = row_ptr[i], e1 = row_ptr[i + 1];
-        float ax = 0.f, ay = 0.f;
+        real ax = 0, ay = 0;
         for (uint32_t e = e0 + lane; e < e1; e += 32) {
             const double2 yj = y[col[e]];
-            const float dx = (float)(yj.x - yi.x), dy = (float)(yj.y - yi.y);
-            const float q = __fdividef(1.0f, 1.0f + (dx * dx + dy * dy));
-            const float w = val[e] * q;
+            const real dx = (real)(yj.x - yi.x), dy = (real)(yj.y - yi.y);
+            const real q = rcp1<real>(real(1) + (dx * dx + dy * dy));
+            const real w = (real)val[e] * q;
             ax += w * dx;
             ay += w * dy;
         }
@@ -102,12 +111,16 @@ int tc_tsne_create(const tc_config* cfg, int64_t n, const uint32_t* row_ptr, con
         delete t;
         return rc;
     }
-    std::vector<float> vf(t->nnz);
-    for (int64_t e = 0; e < t->nnz; e++) vf[e] = (float)val[e];
+    // FP32 affinities on the product path, FP64 in the parity precision
+    const bool f64 = c.precision == TC_PREC_FP64;
+    const size_t vbytes = f64 ? 8 : 4;
+    std::vector<float> vf(f64 ? 0 : t->nnz);
+    for (int64_t e = 0; e < (int64_t)vf.size(); e++) vf[e] = (float)val[e];
+    const void* vsrc = f64 ? (const void*)val : (const void*)vf.data();
     for (int k = 0; k < 3 && rc == TC_OK; k++) rc = ensure(t->y[k], (size_t)n * 16);
     if (!rc) rc = ensure(t->row_ptr, (size_t)(n + 1) * 4);
     if (!rc) rc = ensure(t->col, (size_t)t->nnz * 4 + 16);
-    if (!rc) rc = ensure(t->val, (size_t)t->nnz * 4 + 16);
+    if (!rc) rc = ensure(t->val, (size_t)t->nnz * vbytes + 16);
     if (!rc) rc = ensure(t->grad_rep, (size_t)n * 16);
     if (!rc) rc = ensure(t->grad, (size_t)n * 16);
     if (!rc) rc = ensure(t->z, 64);
@@ -115,7 +128,7 @@ int tc_tsne_create(const tc_config* cfg, int64_t n, const uint32_t* row_ptr, con
     if (!rc) e = cudaMemcpyAsync(t->row_ptr.p, row_ptr, (n + 1) * 4, cudaMemcpyHostToDevice, h.stream);
     if (!rc && e == cudaSuccess && t->nnz) e = cudaMemcpyAsync(t->col.p, col, t->nnz * 4, cudaMemcpyHostToDevice, h.stream);
     if (!rc && e == cudaSuccess && t->nnz)
-        e = cudaMemcpyAsync(t->val.p, vf.data(), t->nnz * 4, cudaMemcpyHostToDevice, h.stream);
+        e = cudaMemcpyAsync(t->val.p, vsrc, t->nnz * vbytes, cudaMemcpyHostToDevice, h.stream);
     if (!rc && e == cudaSuccess) e = cudaMemcpyAsync(t->y[0].p, y0, n * 16, cudaMemcpyHostToDevice, h.stream);
     if (!rc && e == cudaSuccess) e = cudaMemcpyAsync(t->y[1].p, y0, n * 16, cudaMemcpyHostToDevice, h.stream);
     if (!rc && e == cudaSuccess) e = cudaStreamSynchronize(h.stream);
@@ -161,10 +174,16 @@ int tc_tsne_step(tc_tsne* t, double exag_code, double momentum, double lr, doubl
     rc = tc_solve_device(t->solver, P<double>(t->grad_rep), P<double>(t->z), 0, 1);
     if (rc) return rc;
     launches += h.launches;
-    k_tsne_attr_update<<<grid_for(t->n * 32, 256, kSMs * 32), 256, 0, h.stream>>>(
-        t->n, P<uint32_t>(t->row_ptr), P<uint32_t>(t->col), P<float>(t->val), P<double2>(t->y[t->cur]),
-        P<double2>(t->y[t->prev]), P<double>(t->grad_rep), P<double>(t->z), exag_code, lr, momentum,
-        P<double2>(t->y[t->next]), P<double>(t->grad));
+    if (h.cfg.precision == TC_PREC_FP64)
+        k_tsne_attr_update<double, double><<<grid_for(t->n * 32, 256, kSMs * 32), 256, 0, h.stream>>>(
+            t->n, P<uint32_t>(t->row_ptr), P<uint32_t>(t->col), P<double>(t->val), P<double2>(t->y[t->cur]),
+            P<double2>(t->y[t->prev]), P<double>(t->grad_rep), P<double>(t->z), exag_code, lr, momentum,
+            P<double2>(t->y[t->next]), P<double>(t->grad));
+    else
+        k_tsne_attr_update<float, float><<<grid_for(t->n * 32, 256, kSMs * 32), 256, 0, h.stream>>>(
+            t->n, P<uint32_t>(t->row_ptr), P<uint32_t>(t->col), P<float>(t->val), P<double2>(t->y[t->cur]),
+            P<double2>(t->y[t->prev]), P<double>(t->grad_rep), P<double>(t->z), exag_code, lr, momentum,
+            P<double2>(t->y[t->next]), P<double>(t->grad));
     TC_CUDA_TRY(cudaGetLastError());
     t->launches = launches + 1;
     int c = t->cur, p = t->prev, nx = t->next;

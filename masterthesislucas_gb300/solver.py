@@ -167,6 +167,19 @@ class NBodySolverFMM_SYM_MORTON:
     def launches(self) -> int:
         return int(lib().tc_last_launch_count(self._h))
 
+    STAGES = ("sort", "build", "lists", "far", "near", "reduce")
+
+    def stage_times(self) -> dict:
+        """Device milliseconds per stage of the last update + solve (CUDA events)."""
+        ms = np.zeros(len(self.STAGES))
+        check(lib().tc_get_stage_times(self._h, ptr(ms)))
+        return dict(zip(self.STAGES, ms.tolist()))
+
+    def counters(self) -> dict:
+        c = np.zeros(4, np.uint64)
+        check(lib().tc_get_counters(self._h, ptr(c)))
+        return dict(p2p_pairs=int(c[0]), m2p=int(c[1]), p2l=int(c[2]), m2l=int(c[3]))
+
     # device-resident entry points (torch tensors on the handle's device)
     def update_tree_device(self, pos, minPos=None, maxPos=None):
         mn = None if minPos is None else np.asarray(minPos, np.float64)

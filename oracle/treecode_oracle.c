@@ -255,20 +255,24 @@ void orc_morton_codes(int64_t n, const double* pos, const double min_xy[2],
     }
 }
 
-static const uint32_t* g_sort_codes;
-static int cmp_code_idx(const void* a, const void* b)
-{
-    int32_t ia = *(const int32_t*)a, ib = *(const int32_t*)b;
-    uint32_t ca = g_sort_codes[ia], cb = g_sort_codes[ib];
-    if (ca != cb) return ca < cb ? -1 : 1;
-    return (ia > ib) - (ia < ib);
-}
-
+/* stable LSD counting sort on 8-bit digits (re-entrant; ties keep input order) */
 void orc_sort_perm(int64_t n, const uint32_t* codes, int32_t* perm)
 {
+    int32_t* tmp = (int32_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int32_t));
+    int32_t *src = perm, *dst = tmp;
     for (int64_t i = 0; i < n; i++) perm[i] = (int32_t)i;
-    g_sort_codes = codes;
-    qsort(perm, (size_t)n, sizeof(int32_t), cmp_code_idx);
+    for (int shift = 0; shift < 32; shift += 8) {
+        int64_t cnt[257];
+        memset(cnt, 0, sizeof(cnt));
+        for (int64_t i = 0; i < n; i++) cnt[((codes[src[i]] >> shift) & 255u) + 1]++;
+        for (int d = 0; d < 256; d++) cnt[d + 1] += cnt[d];
+        for (int64_t i = 0; i < n; i++) dst[cnt[(codes[src[i]] >> shift) & 255u]++] = src[i];
+        int32_t* t = src;
+        src = dst;
+        dst = t;
+    }
+    /* four passes: the result is back in perm */
+    free(tmp);
 }
 
 void orc_build_tree(uint32_t depth, int64_t n, const double* pos, const double min_xy[2],
