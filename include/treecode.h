@@ -55,6 +55,10 @@ typedef struct tc_config {
     int precision;     /* TC_PREC_*                                             */
     int device;        /* CUDA device ordinal                                   */
     void* stream;      /* cudaStream_t to run on, or NULL for a private stream  */
+    int order;         /* 0: the reference's expansion (M0+M2 multipole, C1..C3
+                          local, point-node MAC stage); p in {3,4,6,8,10,12}:
+                          total-order-p Cartesian expansions about the COM,
+                          direct P2P for non-accepted leaf pairs (FP32 only) */
 } tc_config;
 
 /* Defaults: t-SNE kernel, leaf 16, automatic depth, theta 0.5, FP32. */

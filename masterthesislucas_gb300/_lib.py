@@ -28,7 +28,7 @@ TC_PREC_FP64 = 1
 class TcConfig(ctypes.Structure):
     _fields_ = [("kernel", ctypes.c_int), ("max_children", ctypes.c_int), ("depth", ctypes.c_int),
                 ("theta", ctypes.c_double), ("softening", ctypes.c_double), ("precision", ctypes.c_int),
-                ("device", ctypes.c_int), ("stream", ctypes.c_void_p)]
+                ("device", ctypes.c_int), ("stream", ctypes.c_void_p), ("order", ctypes.c_int)]
 
 
 class TreecodeError(RuntimeError):

@@ -1,0 +1,69 @@
+"""Autotuner for the order-p FMM: tree depth, opening angle and expansion order.
+
+For a given particle set (device-resident) it measures, for each candidate
+(depth, theta, order), the device time of one updateTree + solveNbody (CUDA
+events, after one warm-up) and the median relative force error against an
+FP64 direct sum on sampled sinks, and returns the fastest candidate whose
+error meets the target.  Candidates are visited from cheap to expensive and a
+theta/order line stops once the error target is met (larger orders at the same
+theta only cost more).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .solver import NBodySolverFMM_SYM_MORTON, get_depth
+
+ORDERS = (4, 6, 8, 10)
+THETAS = (1.2, 1.0, 0.9, 0.8, 0.7, 0.6, 0.5, 0.4)
+
+
+def median_error(grad_rows: np.ndarray, ref_rows: np.ndarray) -> float:
+    e = np.linalg.norm(grad_rows - ref_rows, axis=1) / np.linalg.norm(ref_rows, axis=1)
+    return float(np.median(e))
+
+
+def tune(pos_d, ref_rows, rows_d, *, kernel: str, softening: float, leaf: int, target: float,
+         stream=None, depths=None, thetas=THETAS, orders=ORDERS, device: int = 0, log=None):
+    """Returns (best, trials).  best = dict(depth, theta, order, ms, err) or None."""
+    import torch
+
+    n = pos_d.shape[0]
+    d0 = get_depth(leaf, n)
+    depths = depths or (d0 + 1, d0 + 2, d0 + 3)
+    grad_d = torch.zeros((n, 2), dtype=torch.float64, device=pos_d.device)
+    tot_d = torch.zeros(1, dtype=torch.float64, device=pos_d.device)
+    s_torch = torch.cuda.Stream(device=pos_d.device) if stream is None else stream
+    trials = []
+    best = None
+    for depth in depths:
+        if depth > 15:
+            continue
+        for order in orders:
+            for theta in thetas:
+                s = NBodySolverFMM_SYM_MORTON(kernel, max_children=leaf, tree_depth=depth, theta=theta,
+                                              softening=softening, precision="fp32", order=order,
+                                              device=device, stream=s_torch.cuda_stream)
+                try:
+                    s.update_tree_device(pos_d)
+                    s.solve_device(grad_d, tot_d)
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record(s_torch)
+                    s.update_tree_device(pos_d)
+                    s.solve_device(grad_d, tot_d)
+                    e1.record(s_torch)
+                    torch.cuda.synchronize()
+                    ms = e0.elapsed_time(e1)
+                    err = median_error(grad_d[rows_d].cpu().numpy(), ref_rows)
+                finally:
+                    s.close()
+                t = dict(depth=depth, theta=theta, order=order, ms=ms, err=err)
+                trials.append(t)
+                if log:
+                    log(t)
+                if err <= target:
+                    if best is None or ms < best["ms"]:
+                        best = t
+                    break  # smaller theta at this order only costs more
+    return best, trials

@@ -18,7 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(PKG, "libtreecode.so")
 BUILD = os.path.join(PKG, "_build")
 
-SOURCES = ["scan.cu", "sort.cu", "tree.cu", "lists.cu", "fmm.cu", "direct.cu", "tsne.cu", "api.cu"]
+SOURCES = ["scan.cu", "sort.cu", "tree.cu", "lists.cu", "fmm.cu", "fmm_p.cu", "direct.cu", "tsne.cu", "api.cu"]
 NO_FMA = {"tree.cu"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -205,6 +205,7 @@ int tc_config_init(tc_config* cfg)
     cfg->precision = TC_PREC_FP32;
     cfg->device = 0;
     cfg->stream = nullptr;
+    cfg->order = 0;
     return TC_OK;
 }
 
@@ -248,6 +249,7 @@ int tc_create(const tc_config* cfg, tc_handle** out)
     *out = nullptr;
     if (!(cfg->theta > 0.0) || cfg->max_children <= 0 || (cfg->kernel != TC_KERNEL_TSNE && cfg->kernel != TC_KERNEL_GRAVITY) ||
         (cfg->precision != TC_PREC_FP32 && cfg->precision != TC_PREC_FP64) || cfg->depth > 15 ||
+        cfg->order < 0 || cfg->order > 16 || (cfg->order > 0 && cfg->precision != TC_PREC_FP32) ||
         !(cfg->softening >= 0.0) || (cfg->kernel == TC_KERNEL_GRAVITY && !(cfg->softening > 0.0))) {
         tc_set_error("tc_create: invalid configuration");
         return TC_ERR_INVALID;
@@ -284,7 +286,7 @@ int tc_destroy(tc_handle* t)
     if (h.stream) cudaStreamSynchronize(h.stream);
     Buf* bufs[] = {&h.codes, &h.perm, &h.alt_keys, &h.alt_vals, &h.pos_in, &h.pos64, &h.prel, &h.grad_acc,
                    &h.count, &h.first, &h.com64, &h.m0, &h.m2, &h.bbc, &h.bblen, &h.comrel, &h.m0r, &h.m2t,
-                   &h.loc, &h.locfin, &h.chunk, &h.zwork, &h.zloc, &h.counters, &h.ptr_pool, &h.idx_pool, &h.cnt_tmp, &h.tmp, &h.err, &h.zpart, &h.dtotal,
+                   &h.loc, &h.locfin, &h.mu, &h.chunk, &h.zwork, &h.zloc, &h.counters, &h.ptr_pool, &h.idx_pool, &h.cnt_tmp, &h.tmp, &h.err, &h.zpart, &h.dtotal, &h.sumtmp,
                    &h.host_stage};
     for (Buf* b : bufs) release(*b);
     if (h.h_total) cudaFreeHost(h.h_total);
@@ -387,7 +389,8 @@ int tc_solve_device(tc_handle* t, double* d_grad_xy, double* d_total, int accumu
     }
     TC_CUDA_TRY(cudaSetDevice(h.cfg.device));
     h.launches = 0;
-    return solve_fmm(h, d_grad_xy, d_total, accumulate, scatter);
+    return h.cfg.order ? solve_fmm_order(h, d_grad_xy, d_total, accumulate, scatter)
+                       : solve_fmm(h, d_grad_xy, d_total, accumulate, scatter);
 }
 
 int tc_solve(tc_handle* t, double* total, const double* pos_xy, double* grad_xy, int64_t n)
@@ -414,7 +417,9 @@ int tc_solve(tc_handle* t, double* total, const double* pos_xy, double* grad_xy,
         if ((rc = refresh_positions(h))) return rc;
     }
     TC_CUDA_TRY(cudaMemsetAsync(h.dtotal.p, 0, 8, h.stream));
-    if ((rc = solve_fmm(h, P<double>(h.grad_acc), P<double>(h.dtotal), 0, 0))) return rc;
+    rc = h.cfg.order ? solve_fmm_order(h, P<double>(h.grad_acc), P<double>(h.dtotal), 0, 0)
+                     : solve_fmm(h, P<double>(h.grad_acc), P<double>(h.dtotal), 0, 0);
+    if (rc) return rc;
     std::vector<double> g((size_t)n * 2);
     TC_CUDA_TRY(cudaMemcpyAsync(g.data(), h.grad_acc.p, (size_t)n * 16, cudaMemcpyDeviceToHost, h.stream));
     TC_CUDA_TRY(cudaMemcpyAsync(h.h_total, h.dtotal.p, 8, cudaMemcpyDeviceToHost, h.stream));

@@ -97,6 +97,13 @@ inline int grid_for(int64_t n, int block, int cap = kSMs * 32)
 int64_t scan_tmp_words(int64_t n);
 int exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* tmp, cudaStream_t s);
 
+// Deterministic FP64 sum of a[0..na) followed by c[0..*nc) (nc a device
+// pointer, may be NULL) into *out (+= when accumulate).  tmp holds
+// sum_tmp_doubles() doubles.
+int64_t sum_tmp_doubles();
+int sum_f64(const double* a, int64_t na, const double* c, const uint32_t* nc, double* out, int accumulate,
+            double* tmp, cudaStream_t s);
+
 // ---------------------------------------------------------------- sort
 // Stable LSD radix sort of 32-bit keys with 32-bit values (4 passes of 8 bits).
 // keys/vals are sorted in place; alt_* are scratch of n entries each.

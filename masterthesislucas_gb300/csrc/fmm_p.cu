@@ -1,0 +1,531 @@
+// Order-p symmetric Morton FMM: the reference's Cartesian Taylor scheme
+// (src/nbodysolvers/cpu/nBodySolverFMM_SYM_MORTON.h:622-836 truncates at total
+// order 3: multipole M0 + M2, local C1..C3) generalised to total order p.
+//
+// Expansions are about each node's centre of mass, with the reference's
+// dual-tree MAC and lists (lists.cu).  Non-accepted leaf pairs interact by
+// direct P2P (no point-node stage: at order p an M2P costs as much as a
+// leaf-sized P2P).  Every quantity is scaled by the cell size h_l of its level
+// so that FP32 covers orders up to 16 on deep trees:
+//   mu_a  = sum_i m_i (r_i / h)^a / a!                      multipole
+//   D_g   = h^|g| d^g phi(R)                                kernel derivatives
+//   L_b   = sum_a (-1)^|a| mu_a D_(a+b),  |a| + |b| <= p     local (M2L)
+// with phi the radial potential whose gradient is the force (t-SNE:
+// -1/(2(1+r^2)); gravity: (r^2+eps^2)^-1/2).  The derivatives come from the
+// recurrence u D_k = -[(2nu + 2n_i) x_i D_(k-e_i) + 2 n_j x_j D_(k-e_j)
+// + (2nu n_i + n_i(n_i-1)) D_(k-2e_i) + n_j(n_j-1) D_(k-2e_j)] for
+// phi = u^-nu, u = r^2 + c, n = k - e_i, obtained by differentiating
+// u grad(phi) = -2 nu R phi.
+#include "kernels.cuh"
+#include "state.cuh"
+
+namespace tc {
+namespace {
+
+__host__ __device__ constexpr int ncoef(int p) { return (p + 1) * (p + 2) / 2; }
+__host__ __device__ constexpr int cidx(int a, int b) { return (a + b) * (a + b + 1) / 2 + b; }
+
+struct PotParams {
+    float nu;    // phi = pref * u^-nu
+    float c;     // u = r^2 + c (before scaling)
+    float kappa; // pair term t = kappa * phi
+    int kind;    // TC_KERNEL_*
+};
+
+// scaled derivatives D_g, |g| <= P, at scaled offset (x, y) for a level of size h
+template <int P>
+__device__ inline void derivs(float x, float y, float h, const PotParams& pp, float* D)
+{
+    const float c = pp.c / (h * h);
+    const float u = x * x + y * y + c;
+    const float iu = __fdividef(1.0f, u);
+    // pref * h^-2nu * u^-nu (scaled potential)
+    if (pp.kind == TC_KERNEL_GRAVITY)
+        D[0] = rsqrtf(u) / h;
+    else
+        D[0] = -0.5f * iu / (h * h);
+    const float nu2 = 2.0f * pp.nu;
+#pragma unroll
+    for (int k = 1; k <= P; k++) {
+#pragma unroll
+        for (int b = 0; b <= k; b++) {
+            const int a = k - b;
+            float t;
+            if (a >= 1) {
+                t = (nu2 + 2.0f * (a - 1)) * x * D[cidx(a - 1, b)];
+                if (b >= 1) t += 2.0f * b * y * D[cidx(a, b - 1)];
+                if (a >= 2) t += (nu2 * (a - 1) + (float)((a - 1) * (a - 2))) * D[cidx(a - 2, b)];
+                if (b >= 2) t += (float)(b * (b - 1)) * D[cidx(a, b - 2)];
+            } else {
+                t = (nu2 + 2.0f * (b - 1)) * y * D[cidx(0, b - 1)];
+                if (b >= 2) t += (nu2 * (b - 1) + (float)((b - 1) * (b - 2))) * D[cidx(0, b - 2)];
+            }
+            D[cidx(a, b)] = -t * iu;
+        }
+    }
+}
+
+// monomials w_g = d^g / g! for |g| <= Q
+template <int Q>
+__device__ inline void monomials(float dx, float dy, float* w)
+{
+    w[0] = 1.0f;
+#pragma unroll
+    for (int k = 1; k <= Q; k++) {
+#pragma unroll
+        for (int b = 0; b <= k; b++) {
+            const int a = k - b;
+            if (a >= 1)
+                w[cidx(a, b)] = w[cidx(a - 1, b)] * dx * (1.0f / a);
+            else
+                w[cidx(a, b)] = w[cidx(a, b - 1)] * dy * (1.0f / b);
+        }
+    }
+}
+
+// acc_a += sum_{b <= a} in_b * w_(a-b)       (M2M: mu(parent) from mu(child))
+template <int P>
+__device__ inline void shift_up(const float* in, const float* w, float* acc)
+{
+#pragma unroll
+    for (int ka = 0; ka <= P; ka++)
+#pragma unroll
+        for (int ba = 0; ba <= ka; ba++) {
+            const int aa = ka - ba;
+            float s = 0.f;
+#pragma unroll
+            for (int kb = 0; kb <= ka; kb++)
+#pragma unroll
+                for (int bb = 0; bb <= kb; bb++) {
+                    const int ab = kb - bb;
+                    if (ab <= aa && bb <= ba) s += in[cidx(ab, bb)] * w[cidx(aa - ab, ba - bb)];
+                }
+            acc[cidx(aa, ba)] += s;
+        }
+}
+
+// acc_b += sum_{g >= b} in_g * w_(g-b)       (L2L: local at d from local at 0)
+template <int P>
+__device__ inline void shift_down(const float* in, const float* w, float* acc)
+{
+#pragma unroll
+    for (int kb = 0; kb <= P; kb++)
+#pragma unroll
+        for (int bb = 0; bb <= kb; bb++) {
+            const int ab = kb - bb;
+            float s = 0.f;
+#pragma unroll
+            for (int kg = kb; kg <= P; kg++)
+#pragma unroll
+                for (int bg = 0; bg <= kg; bg++) {
+                    const int ag = kg - bg;
+                    if (ag >= ab && bg >= bb) s += in[cidx(ag, bg)] * w[cidx(ag - ab, bg - bb)];
+                }
+            acc[cidx(ab, bb)] += s;
+        }
+}
+
+// ------------------------------------------------------------------ P2M
+// one warp per leaf: mu_a = sum (r/h)^a / a! about the COM
+template <int P>
+__global__ void __launch_bounds__(128) k_p2m(int dep, float h, const uint32_t* __restrict__ count,
+                                             const uint32_t* __restrict__ first, const float* __restrict__ comrel,
+                                             const float* __restrict__ prel, float* __restrict__ mu)
+{
+    constexpr int K = ncoef(P);
+    const int lane = threadIdx.x & 31;
+    const uint32_t li = level_index(dep);
+    const int64_t nl = (int64_t)1 << (2 * dep);
+    const float ih = 1.0f / h;
+    const int64_t wstride = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t i = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); i < nl; i += wstride) {
+        const int64_t node = li + i;
+        const uint32_t c = count[node];
+        if (c == 0) continue;
+        const uint32_t f = first[node];
+        const float cx = comrel[2 * node], cy = comrel[2 * node + 1];
+        float acc[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) acc[k] = 0.f;
+        for (uint32_t q = lane; q < c; q += 32) {
+            float w[K];
+            monomials<P>((prel[2 * (f + q)] - cx) * ih, (prel[2 * (f + q) + 1] - cy) * ih, w);
+#pragma unroll
+            for (int k = 0; k < K; k++) acc[k] += w[k];
+        }
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const float v = warp_sum(acc[k]);
+            if (lane == 0) mu[node * K + k] = v;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ M2M
+// one thread per node of level l: shift the children's multipoles (child
+// scale h/2) to the node's COM at scale h
+template <int P>
+__global__ void __launch_bounds__(128) k_m2m(int l, float hl, const uint32_t* __restrict__ count,
+                                             const float* __restrict__ comrel, float* __restrict__ mu)
+{
+    constexpr int K = ncoef(P);
+    const uint32_t li = level_index(l), lc = level_index(l + 1);
+    const int64_t nl = (int64_t)1 << (2 * l);
+    const float ih = 1.0f / hl;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t node = li + i;
+        if (count[node] == 0) continue;
+        const float px = comrel[2 * node], py = comrel[2 * node + 1];
+        float acc[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) acc[k] = 0.f;
+        for (int j = 0; j < 4; j++) {
+            const int64_t ch = lc + 4 * i + j;
+            if (count[ch] == 0) continue;
+            // child COM - parent COM: child cell centre sits at (+-1/4, +-1/4) h of the parent's
+            const float ox = ((j & 1) ? 0.25f : -0.25f) * hl, oy = ((j & 2) ? 0.25f : -0.25f) * hl;
+            const float dx = (ox + comrel[2 * ch] - px) * ih, dy = (oy + comrel[2 * ch + 1] - py) * ih;
+            float in[K], w[K];
+#pragma unroll
+            for (int ka = 0; ka <= P; ka++) {
+                const float sc = 1.0f / (float)(1 << ka);  // child scale -> parent scale
+#pragma unroll
+                for (int b = 0; b <= ka; b++) in[cidx(ka - b, b)] = mu[ch * K + cidx(ka - b, b)] * sc;
+            }
+            monomials<P>(dx, dy, w);
+            shift_up<P>(in, w, acc);
+        }
+#pragma unroll
+        for (int k = 0; k < K; k++) mu[node * K + k] = acc[k];
+    }
+}
+
+// ------------------------------------------------------------------ M2L
+// one thread per sink node A of level l: L(A) = sum over nn(A) of M2L; also
+// the far-field pair sum kappa * sum_b L_b mu_b(A)
+template <int P>
+__global__ void __launch_bounds__(128) k_m2l_p(int l, float hl, PotParams pp, const uint32_t* __restrict__ nn_ptr,
+                                               const uint32_t* __restrict__ nn_idx, const uint32_t* __restrict__ count,
+                                               const float* __restrict__ comrel, const float* __restrict__ mu,
+                                               float* __restrict__ loc, double* __restrict__ zpart)
+{
+    constexpr int K = ncoef(P);
+    const uint32_t li = level_index(l);
+    const int64_t nl = (int64_t)1 << (2 * l);
+    const float ih = 1.0f / hl;
+    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < nl; a += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t na = li + a;
+        const uint32_t b0 = nn_ptr[a], b1 = nn_ptr[a + 1];
+        float L[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) L[k] = 0.f;
+        if (b0 != b1) {
+            const int iax = (int)compact16((uint32_t)a), iay = (int)compact16((uint32_t)a >> 1);
+            const float cax = comrel[2 * na], cay = comrel[2 * na + 1];
+            for (uint32_t e = b0; e < b1; e++) {
+                const uint32_t b = nn_idx[e];
+                const int64_t nb = li + b;
+                const float Rx = (float)(iax - (int)compact16(b)) + (cax - comrel[2 * nb]) * ih;
+                const float Ry = (float)(iay - (int)compact16(b >> 1)) + (cay - comrel[2 * nb + 1]) * ih;
+                float D[K];
+                derivs<P>(Rx, Ry, hl, pp, D);
+                const float* m = mu + nb * K;
+#pragma unroll
+                for (int ka = 0; ka <= P; ka++) {
+                    if (ka == 1) continue;  // dipole vanishes about the COM
+#pragma unroll
+                    for (int ba = 0; ba <= ka; ba++) {
+                        const float ma = (ka & 1) ? -m[cidx(ka - ba, ba)] : m[cidx(ka - ba, ba)];
+#pragma unroll
+                        for (int kb = 0; kb + ka <= P; kb++)
+#pragma unroll
+                            for (int bb = 0; bb <= kb; bb++)
+                                L[cidx(kb - bb, bb)] += ma * D[cidx(ka - ba + kb - bb, ba + bb)];
+                    }
+                }
+            }
+        }
+        double z = 0.0;
+        if (count[na] != 0 && b0 != b1) {
+            const float* m = mu + na * K;
+            float zs = 0.f;
+#pragma unroll
+            for (int k = 0; k < K; k++) zs += L[k] * m[k];
+            z = (double)pp.kappa * (double)zs;
+        }
+        zpart[na] = z;
+#pragma unroll
+        for (int k = 0; k < K; k++) loc[na * K + k] = L[k];
+    }
+}
+
+// ------------------------------------------------------------------ L2L
+// one thread per node of level l >= 1: L_fin = L_own + shift(L_fin(parent))
+template <int P>
+__global__ void __launch_bounds__(128) k_l2l(int l, float hl, const uint32_t* __restrict__ count,
+                                             const float* __restrict__ comrel, float* __restrict__ loc)
+{
+    constexpr int K = ncoef(P);
+    const uint32_t li = level_index(l), lp = level_index(l - 1);
+    const int64_t nl = (int64_t)1 << (2 * l);
+    const float ih = 1.0f / hl;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t node = li + i;
+        if (count[node] == 0) continue;
+        const int64_t par = lp + (i >> 2);
+        const int j = (int)(i & 3);
+        // node COM - parent COM in units of the node's cell size h: the child
+        // cell centre sits (+-1/2, +-1/2) h from the parent's
+        const float ox = ((j & 1) ? 0.5f : -0.5f), oy = ((j & 2) ? 0.5f : -0.5f);
+        const float ddx = ox + (comrel[2 * node] - comrel[2 * par]) * ih;
+        const float ddy = oy + (comrel[2 * node + 1] - comrel[2 * par + 1]) * ih;
+        float in[K], w[K], acc[K];
+#pragma unroll
+        for (int kb = 0; kb <= P; kb++) {
+            const float sc = 1.0f / (float)(1 << kb);  // parent scale 2h -> child scale h
+#pragma unroll
+            for (int b = 0; b <= kb; b++) in[cidx(kb - b, b)] = loc[par * K + cidx(kb - b, b)] * sc;
+        }
+#pragma unroll
+        for (int k = 0; k < K; k++) acc[k] = loc[node * K + k];
+        monomials<P>(ddx, ddy, w);
+        shift_down<P>(in, w, acc);
+#pragma unroll
+        for (int k = 0; k < K; k++) loc[node * K + k] = acc[k];
+    }
+}
+
+// ------------------------------------------------------------------ near field
+constexpr int kNearWarps = 4;
+
+__global__ void k_chunks(int dep, const uint32_t* __restrict__ count, uint32_t* __restrict__ nchunk)
+{
+    const uint32_t li = level_index(dep);
+    const int64_t nl = (int64_t)1 << (2 * dep);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x)
+        nchunk[i] = (count[li + i] + 31u) / 32u;
+}
+
+// one warp per work item (leaf S, chunk of up to 32 sinks): L2P of the final
+// local expansion of S plus direct P2P with every particle of near(S)
+template <int P, typename KN>
+__global__ void __launch_bounds__(32 * kNearWarps)
+    k_near_p(KN ker, int dep, float h, const uint32_t* __restrict__ count, const uint32_t* __restrict__ first,
+             const float* __restrict__ comrel, const float* __restrict__ loc, const uint32_t* __restrict__ near_ptr,
+             const uint32_t* __restrict__ near_idx, const uint32_t* __restrict__ chunk_ptr,
+             const float* __restrict__ prel, const uint32_t* __restrict__ perm, double* __restrict__ grad,
+             int accumulate, int scatter, double* __restrict__ zwork, unsigned long long* __restrict__ counters)
+{
+    constexpr int K = ncoef(P);
+    constexpr int KW = ncoef(P - 1);
+    __shared__ float2 s_src[kNearWarps][32];
+    uint32_t n_pp = 0;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t li = level_index(dep);
+    const int64_t nl = (int64_t)1 << (2 * dep);
+    const float ih = 1.0f / h;
+    const uint32_t nwork = chunk_ptr[nl];
+    const int64_t wstride = (int64_t)gridDim.x * kNearWarps;
+    for (int64_t wi = blockIdx.x * (int64_t)kNearWarps + w; wi < nwork; wi += wstride) {
+        int64_t lo = 0, hi = nl;
+        while (hi - lo > 1) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (chunk_ptr[mid] <= (uint32_t)wi) lo = mid; else hi = mid;
+        }
+        const int64_t si = lo;
+        const int64_t S = li + si;
+        const uint32_t cS = count[S], fS = first[S];
+        const uint32_t sl = ((uint32_t)wi - chunk_ptr[si]) * 32u + lane;
+        const bool act = sl < cS;
+        const uint32_t s = fS + (act ? sl : 0);
+        const int isx = (int)compact16((uint32_t)si), isy = (int)compact16((uint32_t)si >> 1);
+        const float px = prel[2 * s], py = prel[2 * s + 1];
+        float gx = 0.f, gy = 0.f, zs = 0.f;
+        if (act) {
+            // L2P: F = (1/h) sum_b L_b d^(b - e) / (b - e)!
+            float wv[KW];
+            monomials<P - 1>((px - comrel[2 * S]) * ih, (py - comrel[2 * S + 1]) * ih, wv);
+            const float* L = loc + S * K;
+#pragma unroll
+            for (int k = 0; k < P; k++)
+#pragma unroll
+                for (int b = 0; b <= k; b++) {
+                    const int a = k - b;
+                    gx += L[cidx(a + 1, b)] * wv[cidx(a, b)];
+                    gy += L[cidx(a, b + 1)] * wv[cidx(a, b)];
+                }
+            gx *= ih;
+            gy *= ih;
+        }
+        const uint32_t e0 = near_ptr[si], e1 = near_ptr[si + 1];
+        for (uint32_t e = e0; e < e1; e++) {
+            const uint32_t ti = near_idx[e];
+            const int64_t T = li + ti;
+            const uint32_t fT = first[T], cT = count[T];
+            const float bx = (float)(isx - (int)compact16(ti)) * h + px;
+            const float by = (float)(isy - (int)compact16(ti >> 1)) * h + py;
+            const bool self = ti == (uint32_t)si;
+            for (uint32_t q0 = 0; q0 < cT; q0 += 32) {
+                const uint32_t q = q0 + lane;
+                if (q < cT) s_src[w][lane] = make_float2(prel[2 * (fT + q)], prel[2 * (fT + q) + 1]);
+                __syncwarp();
+                const uint32_t m = min(32u, cT - q0);
+                if (act) {
+                    if (self) {
+                        n_pp += m - ((sl >= q0 && sl < q0 + m) ? 1u : 0u);
+                        for (uint32_t j = 0; j < m; j++) {
+                            if (q0 + j == sl) continue;
+                            const float2 t2 = s_src[w][j];
+                            const float Rx = bx - t2.x, Ry = by - t2.y;
+                            float D1, t;
+                            ker.near(Rx * Rx + Ry * Ry, D1, t);
+                            gx += D1 * Rx;
+                            gy += D1 * Ry;
+                            zs += t;
+                        }
+                    } else {
+                        n_pp += m;
+                        for (uint32_t j = 0; j < m; j++) {
+                            const float2 t2 = s_src[w][j];
+                            const float Rx = bx - t2.x, Ry = by - t2.y;
+                            float D1, t;
+                            ker.near(Rx * Rx + Ry * Ry, D1, t);
+                            gx += D1 * Rx;
+                            gy += D1 * Ry;
+                            zs += t;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        if (act) {
+            const int64_t o = scatter ? (int64_t)perm[s] : (int64_t)s;
+            double ox2 = (double)gx, oy2 = (double)gy;
+            if (accumulate) {
+                ox2 += grad[2 * o];
+                oy2 += grad[2 * o + 1];
+            }
+            grad[2 * o] = ox2;
+            grad[2 * o + 1] = oy2;
+        }
+        const double z = warp_sum(act ? (double)zs : 0.0);
+        if (lane == 0) zwork[wi] = z;
+    }
+    const unsigned long long a = warp_sum((unsigned long long)n_pp);
+    if (lane == 0 && a) atomicAdd(counters + 0, a);
+}
+
+__global__ void k_sum_z2(const double* __restrict__ a, int64_t na, const double* __restrict__ c,
+                         const uint32_t* __restrict__ nc, double* __restrict__ out)
+{
+    __shared__ double ws[32];
+    double s = 0.0;
+    const int64_t ncv = *nc;
+    for (int64_t i = threadIdx.x; i < na; i += blockDim.x) s += a[i];
+    for (int64_t i = threadIdx.x; i < ncv; i += blockDim.x) s += c[i];
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : 0.0;
+        v = warp_sum(v);
+        if (threadIdx.x == 0) *out = *out + v;
+    }
+}
+
+template <int ORD, typename KN>
+int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumulate, int scatter, double* d_total)
+{
+    constexpr int K = ncoef(ORD);
+    cudaStream_t s = h.stream;
+    const int dep = h.depth;
+    const int64_t nn = h.nnodes;
+    const int64_t nleaf = (int64_t)1 << (2 * dep);
+    const int64_t wmax = h.n / 32 + (h.n < nleaf ? h.n : nleaf) + 1;
+    int rc;
+    if ((rc = ensure(h.mu, nn * K * 4)) || (rc = ensure(h.loc, nn * K * 4)) || (rc = ensure(h.zpart, nn * 8 + 64)) ||
+        (rc = ensure(h.counters, 64)) || (rc = ensure(h.chunk, (nleaf + 1) * 4)) ||
+        (rc = ensure(h.zwork, wmax * 8)) || (rc = ensure(h.cnt_tmp, nleaf * 4 + 64)) ||
+        (rc = ensure(h.tmp, scan_tmp_words(nleaf) * 4)) || (rc = record(h, 4)))
+        return rc;
+    TC_CUDA_TRY(cudaMemsetAsync(h.counters.p, 0, 64, s));
+    float* mu = P<float>(h.mu);
+    float* loc = P<float>(h.loc);
+    double* zp = P<double>(h.zpart);
+    const float* comrel = P<float>(h.comrel);
+    const uint32_t* count = P<uint32_t>(h.count);
+    auto hl = [&](int l) { return (float)(h.L / (double)(1u << l)); };
+    k_p2m<ORD><<<grid_for(nleaf * 32, 128, kSMs * 64), 128, 0, s>>>(dep, hl(dep), count, P<uint32_t>(h.first), comrel,
+                                                                 P<float>(h.prel), mu);
+    for (int l = dep - 1; l >= 0; l--) {
+        const int64_t nl = (int64_t)1 << (2 * l);
+        k_m2m<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, mu);
+    }
+    TC_CUDA_TRY(cudaMemsetAsync(loc, 0, K * 4, s));
+    TC_CUDA_TRY(cudaMemsetAsync(zp, 0, 8, s));
+    const uint32_t* ptr = P<uint32_t>(h.ptr_pool);
+    const uint32_t* idx = P<uint32_t>(h.idx_pool);
+    for (int l = 1; l <= dep; l++) {
+        const int64_t nl = (int64_t)1 << (2 * l);
+        k_m2l_p<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, ptr + h.lists.nn_ptr_off[l],
+                                                     idx + h.lists.nn_idx_off[l], count, comrel, mu, loc, zp);
+    }
+    for (int l = 1; l <= dep; l++) {
+        const int64_t nl = (int64_t)1 << (2 * l);
+        k_l2l<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, loc);
+    }
+    uint32_t* nchunk = P<uint32_t>(h.cnt_tmp);
+    uint32_t* chunk_ptr = P<uint32_t>(h.chunk);
+    k_chunks<<<grid_for(nleaf, 256), 256, 0, s>>>(dep, count, nchunk);
+    if ((rc = exclusive_scan_u32(nchunk, chunk_ptr, nleaf, P<uint32_t>(h.tmp), s))) return rc;
+    if ((rc = record(h, 5))) return rc;
+    const int64_t wblk = (wmax + kNearWarps - 1) / kNearWarps;
+    k_near_p<ORD, KN><<<(unsigned)(wblk < kSMs * 256 ? wblk : kSMs * 256), 32 * kNearWarps, 0, s>>>(
+        ker, dep, hl(dep), count, P<uint32_t>(h.first), comrel, loc, ptr + h.lists.near_ptr_off[dep],
+        idx + h.lists.near_idx_off[dep], chunk_ptr, P<float>(h.prel), P<uint32_t>(h.perm), d_grad, accumulate,
+        scatter, P<double>(h.zwork), P<unsigned long long>(h.counters));
+    if ((rc = record(h, 6))) return rc;
+    if ((rc = ensure(h.sumtmp, sum_tmp_doubles() * 8)) ||
+        (rc = sum_f64(zp, nn, P<double>(h.zwork), chunk_ptr + nleaf, d_total, 1, P<double>(h.sumtmp), s)))
+        return rc;
+    h.launches += 4 + 3 * dep + 5;
+    TC_CUDA_TRY(cudaGetLastError());
+    return record(h, 7);
+}
+
+template <int P>
+int dispatch_kernel(Handle& h, double* d_grad, int accumulate, int scatter, double* d_total)
+{
+    PotParams pp;
+    pp.kind = h.cfg.kernel;
+    if (h.cfg.kernel == TC_KERNEL_GRAVITY) {
+        pp.nu = 0.5f;
+        pp.c = (float)(h.cfg.softening * h.cfg.softening);
+        pp.kappa = -1.0f;
+        return solve_p<P>(h, KGrav<float>{pp.c}, pp, d_grad, accumulate, scatter, d_total);
+    }
+    pp.nu = 1.0f;
+    pp.c = 1.0f;
+    pp.kappa = -2.0f;
+    return solve_p<P>(h, KTsne<float>{}, pp, d_grad, accumulate, scatter, d_total);
+}
+
+}  // namespace
+
+int solve_fmm_order(Handle& h, double* d_grad, double* d_total, int accumulate, int scatter)
+{
+    switch (h.cfg.order) {
+    case 3: return dispatch_kernel<3>(h, d_grad, accumulate, scatter, d_total);
+    case 4: return dispatch_kernel<4>(h, d_grad, accumulate, scatter, d_total);
+    case 6: return dispatch_kernel<6>(h, d_grad, accumulate, scatter, d_total);
+    case 8: return dispatch_kernel<8>(h, d_grad, accumulate, scatter, d_total);
+    case 10: return dispatch_kernel<10>(h, d_grad, accumulate, scatter, d_total);
+    case 12: return dispatch_kernel<12>(h, d_grad, accumulate, scatter, d_total);
+    default:
+        tc_set_error("unsupported expansion order %d (3, 4, 6, 8, 10, 12)", h.cfg.order);
+        return TC_ERR_INVALID;
+    }
+}
+
+}  // namespace tc

@@ -64,7 +64,55 @@ __global__ void k_scan_final(const uint32_t* __restrict__ in, uint32_t* __restri
     if (blockIdx.x == nb - 1 && threadIdx.x == 0) out[n] = partial[blockIdx.x] + tot;
 }
 
+constexpr int kSumBlocks = 2 * kSMs;
+
+// stage 1 of sum_f64: block b sums the grid-stride slice b of a[0..na) ++ c[0..*nc)
+__global__ void k_sum_partial(const double* __restrict__ a, int64_t na, const double* __restrict__ c,
+                              const uint32_t* __restrict__ nc, double* __restrict__ partial)
+{
+    __shared__ double ws[32];
+    const int64_t ncv = nc ? (int64_t)*nc : 0;
+    const int64_t tot = na + ncv;
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x)
+        s += i < na ? a[i] : c[i - na];
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : 0.0;
+        v = warp_sum(v);
+        if (threadIdx.x == 0) partial[blockIdx.x] = v;
+    }
+}
+
+__global__ void k_sum_final(const double* __restrict__ partial, int np, double* __restrict__ out, int accumulate)
+{
+    __shared__ double ws[32];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) s += partial[i];
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : 0.0;
+        v = warp_sum(v);
+        if (threadIdx.x == 0) *out = accumulate ? *out + v : v;
+    }
+}
+
 }  // namespace
+
+int64_t sum_tmp_doubles() { return kSumBlocks; }
+
+int sum_f64(const double* a, int64_t na, const double* c, const uint32_t* nc, double* out, int accumulate,
+            double* tmp, cudaStream_t s)
+{
+    k_sum_partial<<<kSumBlocks, 256, 0, s>>>(a, na, c, nc, tmp);
+    k_sum_final<<<1, 256, 0, s>>>(tmp, kSumBlocks, out, accumulate);
+    TC_CUDA_TRY(cudaGetLastError());
+    return TC_OK;
+}
 
 int64_t scan_tmp_words(int64_t n) { return (n + kScanChunk - 1) / kScanChunk + 1; }
 

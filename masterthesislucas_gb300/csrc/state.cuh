@@ -49,12 +49,12 @@ struct Handle {
     // particles
     Buf codes, perm, alt_keys, alt_vals, pos_in, pos64, prel, grad_acc;
     // nodes
-    Buf count, first, com64, m0, m2, bbc, bblen, comrel, m0r, m2t, loc, locfin, chunk, zwork, zloc;
+    Buf count, first, com64, m0, m2, bbc, bblen, comrel, m0r, m2t, loc, locfin, chunk, zwork, zloc, mu;
     // lists
     Buf ptr_pool, idx_pool, cnt_tmp;
     Lists lists;
     // scratch
-    Buf tmp, err, zpart, dtotal, host_stage;
+    Buf tmp, err, zpart, dtotal, host_stage, sumtmp;
     // stage timing (CUDA events on the handle's stream) and interaction counters
     cudaEvent_t ev[TC_NSTAGES + 2] = {};
     bool ev_ready = false;
@@ -80,6 +80,8 @@ int build_tree(Handle& h, const double* d_pos, int64_t n, double minx, double mi
 int build_lists(Handle& h);
 // fmm.cu
 int solve_fmm(Handle& h, double* d_grad, double* d_total, int accumulate, int scatter);
+// fmm_p.cu (tc_config.order != 0)
+int solve_fmm_order(Handle& h, double* d_grad, double* d_total, int accumulate, int scatter);
 
 }  // namespace tc
 

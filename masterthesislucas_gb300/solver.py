@@ -65,7 +65,7 @@ class NBodySolverFMM_SYM_MORTON:
 
     def __init__(self, kernel: str = "tsne", max_children: int = 16, tree_depth: int | None = None,
                  theta: float = 0.5, softening: float = 1e-3, precision: str = "fp32", device: int = 0,
-                 stream=None):
+                 stream=None, order: int = 0):
         cfg = _lib.TcConfig()
         check(lib().tc_config_init(ctypes.byref(cfg)))
         cfg.kernel = KERNELS[kernel]
@@ -76,6 +76,8 @@ class NBodySolverFMM_SYM_MORTON:
         cfg.precision = PRECISIONS[precision]
         cfg.device = device
         cfg.stream = stream
+        cfg.order = order
+        self.order = order
         self._h = ctypes.c_void_p()
         check(lib().tc_create(ctypes.byref(cfg), ctypes.byref(self._h)))
         self.maxChildren = max_children

@@ -1,0 +1,60 @@
+"""Order-p FMM: the error against FP64 direct sums falls with the expansion
+order at a fixed opening angle, for both kernels (the only oracle at
+arbitrary order is the direct sum; order 3 is the reference's truncation)."""
+import numpy as np
+import pytest
+
+from masterthesislucas_gb300 import NBodySolverFMM_SYM_MORTON, Points, datasets, direct
+
+pytestmark = pytest.mark.gpu
+
+
+def errors(pos, kernel, theta, orders, depth, rows, fd, leaf=16):
+    out = {}
+    for p in orders:
+        s = NBodySolverFMM_SYM_MORTON(kernel, max_children=leaf, tree_depth=depth, theta=theta, softening=1e-3,
+                                      order=p)
+        pts = Points.from_positions(pos)
+        s.updateTree(pts, pos.min(0), pos.max(0))
+        total = s.solveNbody(0.0, pts)
+        g = np.zeros_like(pos)
+        g[pts.ID] = pts.derivative
+        e = np.linalg.norm(g[rows] - fd, axis=1) / np.linalg.norm(fd, axis=1)
+        out[p] = (float(np.median(e)), total)
+    return out
+
+
+@pytest.mark.parametrize("kernel", ["gravity", "tsne"])
+def test_error_falls_with_order(kernel):
+    n = 65536
+    if kernel == "gravity":
+        pos = datasets.two_disks(n, seed=11).astype(np.float64)
+    else:
+        pos = np.random.default_rng(12).normal(0.0, 10.0, (n, 2))
+    rows = np.random.default_rng(0).choice(n, 1024, replace=False)
+    fd, _ = direct(pos, kernel=kernel, softening=1e-3, precision="fp64", rows=rows)
+    _, ztot = direct(pos, kernel=kernel, softening=1e-3, precision="fp64")
+    e = errors(pos, kernel, 0.6, (3, 4, 6, 8, 10, 12), 8, rows, fd)
+    meds = [e[p][0] for p in (3, 4, 6, 8, 10, 12)]
+    print(kernel, meds)
+    assert meds[0] > meds[2] > meds[3] > meds[5]
+    assert meds[5] < 1e-5
+    # the pair sum converges to the direct one
+    assert e[12][1] == pytest.approx(ztot, rel=1e-4)
+
+
+def test_tsne_repulsion_order_p_normalised_gradient():
+    n = 30000
+    pos = np.random.default_rng(3).normal(0.0, 5.0, (n, 2))
+    rows = np.arange(0, n, 37)
+    fd, zd = direct(pos, kernel="tsne", precision="fp64", rows=rows)
+    _, z_all = direct(pos, kernel="tsne", precision="fp64")
+    s = NBodySolverFMM_SYM_MORTON("tsne", max_children=16, theta=0.5, order=8)
+    pts = Points.from_positions(pos)
+    s.updateTree(pts, pos.min(0), pos.max(0))
+    z = s.solveNbody(0.0, pts)
+    assert z == pytest.approx(z_all, rel=1e-5)
+    g = np.zeros_like(pos)
+    g[pts.ID] = pts.derivative
+    e = np.linalg.norm(g[rows] - fd, axis=1) / np.linalg.norm(fd, axis=1)
+    assert np.median(e) < 1e-5
