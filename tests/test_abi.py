@@ -60,3 +60,15 @@ def test_invalid_config_rejected_without_gpu(L):
     h = ctypes.c_void_p()
     assert L.tc_create(ctypes.byref(cfg), ctypes.byref(h)) == _lib.TC_ERR_INVALID
     assert b"invalid" in L.tc_last_error()
+
+
+def test_dropin_adaptor_builds_against_reference_interface(L):
+    """GpuTreeSolver<TsnePoint2D> compiles and links as an NBodySolver<TsnePoint2D>
+    next to the reference's own solver headers (runs only where a GPU exists)."""
+    import subprocess
+    if not os.path.isdir("/root/reference/src"):
+        pytest.skip("reference sources not present")
+    r = subprocess.run(["make", "-s", "-B", "-f", "oracle/Makefile.ref", "dropin"], cwd=ROOT, capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    assert os.path.exists(os.path.join(ROOT, "oracle", "_ref", "dropin_check"))
