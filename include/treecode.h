@@ -143,6 +143,21 @@ int tc_direct(int kernel, double softening, int precision, const double* pos_xy,
 int tc_direct_device(int kernel, double softening, int precision, const double* d_pos_xy, int64_t n,
                      const int64_t* d_rows, int64_t m, double* d_grad_rows, double* d_total, void* stream);
 
+/* Same result as tc_direct_device, but allocates no device memory at all.
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc (a stream under CUDA-graph capture, a host framework that owns
+ * all device memory, a loop that must not block in the allocator).  Its
+ * partial sums use one static device array of TC_DIRECT_NOALLOC_SCRATCH
+ * doubles (4 MiB) that every GPU loading this library keeps until exit.
+ * Limits: m <= TC_DIRECT_NOALLOC_SCRATCH / 4 rows (larger m returns
+ * TC_ERR_INVALID); d_rows NULL selects rows 0..m-1.  The first call
+ * on a device looks up the array's device address (cudaGetSymbolAddress),
+ * so make that first call before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU race and must be serialised.        */
+#define TC_DIRECT_NOALLOC_SCRATCH (1 << 19)
+int tc_direct_device_noalloc(int kernel, double softening, int precision, const double* d_pos_xy, int64_t n,
+                             const int64_t* d_rows, int64_t m, double* d_grad_rows, double* d_total, void* stream);
+
 /* ---------------------------------------------------------------- t-SNE step
  * The TSNE class around the solver (src/nBodyInstances/tsne.h:42-563),
  * device resident.  P is the symmetric affinity matrix as CSR (rows and

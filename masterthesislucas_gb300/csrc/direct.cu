@@ -8,6 +8,8 @@
 // fixed order by a second kernel, so results are deterministic.  In FP64 this
 // is the oracle the force error of every tree result is measured against
 // (median over sampled sinks of |F - F_direct| / |F_direct|).
+#include <mutex>
+
 #include "kernels.cuh"
 #include "state.cuh"
 
@@ -176,4 +178,112 @@ extern "C" int tc_direct(int kernel, double softening, int precision, const doub
     if (e != cudaSuccess) return tc_cuda_fail(e, "tc_direct");
     if (e2 != cudaSuccess) return tc_cuda_fail(e2, "tc_direct sync");
     return TC_OK;
+}
+
+// ----------------------------------------------------------------------------
+// Allocation-free variant of tc_direct_device.
+//
+// Some callers cannot call cudaMalloc: code running while a CUDA graph is being
+// captured on the stream they hand us, allocators that forbid stray device
+// allocations (for example a host framework that owns and pools all device
+// memory), or real-time loops where an allocation may block on the driver.
+// This entry point therefore allocates nothing: its per-slice partial sums
+// live in one file-scope device array of TC_DIRECT_NOALLOC_SCRATCH doubles
+// (4 MiB), which every GPU that loads this library holds until the process
+// exits.  The caller still provides positions, rows and outputs.
+//
+// The array is shared by every call on a device and keeps the previous call's
+// contents; each call overwrites every entry it later reads, so nothing needs
+// clearing.  Calls that overlap on the GPU (two streams, or two host threads)
+// race on the array and give wrong results: serialise them.
+namespace tc {
+namespace {
+
+constexpr int64_t kNoAllocScratch = TC_DIRECT_NOALLOC_SCRATCH;
+static __device__ __align__(256) double g_direct_scratch[kNoAllocScratch];
+
+// device address of g_direct_scratch per device ordinal, looked up once per
+// device with that device current (the host-side symbol is only a stand-in)
+constexpr int kMaxDevices = 64;
+double* g_scratch_addr[kMaxDevices] = {};
+std::mutex g_scratch_mu;
+
+int scratch_for_current_device(double** out)
+{
+    int dev = 0;
+    TC_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) {
+        tc_set_error("tc_direct_device_noalloc: device ordinal %d out of range", dev);
+        return TC_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_direct_scratch);
+        if (e != cudaSuccess) return tc_cuda_fail(e, "cudaGetSymbolAddress(g_direct_scratch)");
+        g_scratch_addr[dev] = (double*)p;
+    }
+    *out = g_scratch_addr[dev];
+    return TC_OK;
+}
+
+template <typename real, typename K>
+int direct_noalloc_t(K ker, const double* d_pos, int64_t n, const int64_t* d_rows, int64_t m, double* d_grad,
+                     double* d_total, double* scratch, cudaStream_t s)
+{
+    const int64_t rb = (m + DT - 1) / DT;
+    // as many source slices as fill the GPU and fit beside the m row sums
+    int64_t fit = (kNoAllocScratch - m) / (3 * m);
+    int64_t nslice = (kSMs * 8 + rb - 1) / rb;
+    if (nslice > fit) nslice = fit;
+    if (nslice < 1) nslice = 1;
+    int64_t slice = (n + nslice - 1) / nslice;
+    slice = ((slice + DT - 1) / DT) * DT;
+    nslice = (n + slice - 1) / slice;
+    if (nslice * m * 3 + m > kNoAllocScratch || nslice > 65535) {
+        tc_set_error("tc_direct_device_noalloc: %lld rows x %lld points need more than the %lld-double scratch",
+                     (long long)m, (long long)n, (long long)kNoAllocScratch);
+        return TC_ERR_INVALID;
+    }
+    double* part = scratch;
+    double* zrow = scratch + nslice * m * 3;
+    dim3 grid((unsigned)rb, (unsigned)nslice);
+    k_direct<real, K><<<grid, DT, 0, s>>>(ker, (const double2*)d_pos, n, d_rows, m, slice, part);
+    k_direct_reduce<<<grid_for(m, 256), 256, 0, s>>>(part, m, (int)nslice, d_grad, zrow);
+    if (d_total) k_sum_rows<<<1, 1024, 0, s>>>(zrow, m, d_total);
+    TC_CUDA_TRY(cudaGetLastError());
+    return TC_OK;
+}
+
+}  // namespace
+}  // namespace tc
+
+extern "C" int tc_direct_device_noalloc(int kernel, double softening, int precision, const double* d_pos, int64_t n,
+                                        const int64_t* d_rows, int64_t m, double* d_grad_rows, double* d_total,
+                                        void* stream)
+{
+    if (!d_pos || !d_grad_rows || n <= 0 || m <= 0 || (kernel != TC_KERNEL_TSNE && kernel != TC_KERNEL_GRAVITY) ||
+        (precision != TC_PREC_FP32 && precision != TC_PREC_FP64) || (!d_rows && m > n)) {
+        tc_set_error("tc_direct_device_noalloc: invalid arguments");
+        return TC_ERR_INVALID;
+    }
+    // at least one source slice of 3 partials per row plus the row sums
+    if (4 * m > tc::kNoAllocScratch) {
+        tc_set_error("tc_direct_device_noalloc: m = %lld rows exceeds the maximum of %lld", (long long)m,
+                     (long long)(tc::kNoAllocScratch / 4));
+        return TC_ERR_INVALID;
+    }
+    double* scratch = nullptr;
+    int rc = tc::scratch_for_current_device(&scratch);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    const double e2 = softening * softening;
+    if (precision == TC_PREC_FP64) {
+        if (kernel == TC_KERNEL_GRAVITY)
+            return direct_noalloc_t<double>(KGrav<double>{e2}, d_pos, n, d_rows, m, d_grad_rows, d_total, scratch, s);
+        return direct_noalloc_t<double>(KTsne<double>{}, d_pos, n, d_rows, m, d_grad_rows, d_total, scratch, s);
+    }
+    if (kernel == TC_KERNEL_GRAVITY)
+        return direct_noalloc_t<float>(KGrav<float>{(float)e2}, d_pos, n, d_rows, m, d_grad_rows, d_total, scratch, s);
+    return direct_noalloc_t<float>(KTsne<float>{}, d_pos, n, d_rows, m, d_grad_rows, d_total, scratch, s);
 }
