@@ -46,7 +46,8 @@ THETAS = (0.4, 0.35, 0.3, 0.25, 0.2, 0.15, 0.1)
 WORKLOADS = {
     "nbody_two_disks_4m": dict(n=4194304, dist="two_disks", kernel="gravity", softening=1e-3, max_children=64),
     "nbody_two_disks_1m": dict(n=1048576, dist="two_disks", kernel="gravity", softening=1e-3, max_children=64),
-    "bh_mixture_65k": dict(n=65536, dist="mixture", kernel="gravity", softening=1e-3, max_children=16),
+    "bh_mixture_65k": dict(n=65536, dist="mixture", kernel="gravity", softening=1e-3, max_children=16,
+                           method="bh", theta=0.5),
 }
 
 
@@ -297,6 +298,81 @@ def cpu_baseline(w, theta, n_sample, threads=1, seeds=None):
     return len(jobs) * n_sample / dt, dt, depth
 
 
+def run_bh(args, w):
+    """Barnes-Hut force step (the reference's QuadTree and MAC) on the GPU."""
+    import ctypes
+    import torch
+
+    from masterthesislucas_gb300._lib import check, lib, ptr
+
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    n = w["n"]
+    pos_h = positions(w, seed=1000)
+    pos_d = torch.from_numpy(pos_h).to(dev)
+    grad_d = torch.zeros((n, 2), dtype=torch.float64, device=dev)
+    tot_d = torch.zeros(1, dtype=torch.float64, device=dev)
+    rows = np.sort(np.random.default_rng(7).choice(n, N_SAMPLES, replace=False)).astype(np.int64)
+    rows_d = torch.from_numpy(rows).to(dev)
+    ref_d = torch.zeros((N_SAMPLES, 2), dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    check(lib().tc_direct_device(1, w["softening"], 1, ptr(pos_d), n, ptr(rows_d), N_SAMPLES, ptr(ref_d), None, None))
+    torch.cuda.synchronize()
+    ref = ref_d.cpu().numpy()
+    cs = ctypes.c_void_p(stream.cuda_stream)
+
+    def step():
+        check(lib().tc_bh_solve_device(1, w["softening"], w["max_children"], w["theta"], 0, ptr(pos_d), n,
+                                       ptr(grad_d), ptr(tot_d), cs))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    with ClockSampler(0) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(k))
+            ev0[k].record(stream)
+            step()
+            ev1[k].record(stream)
+        torch.cuda.synchronize()
+    ms = [ev0[k].elapsed_time(ev1[k]) for k in range(args.steps)]
+    err = median_error(grad_d[rows_d].cpu().numpy(), ref)
+    # e2e through the host entry point
+    import time as _t
+    g_h = np.zeros((n, 2))
+    tot = ctypes.c_double(0.0)
+    e2e = []
+    for k in range(3):
+        t0 = _t.perf_counter()
+        check(lib().tc_bh_solve(1, w["softening"], w["max_children"], w["theta"], 0, ptr(pos_h), n, ptr(g_h),
+                                ctypes.byref(tot)))
+        e2e.append(_t.perf_counter() - t0)
+    import oracle
+    t0 = _t.perf_counter()
+    oracle.bh(pos_h, kernel=oracle.KERNEL_GRAVITY, eps=w["softening"], max_children=w["max_children"],
+              theta=w["theta"])
+    cpu_t = _t.perf_counter() - t0
+    t_total = sum(ms) / 1e3
+    line = {"metric": "particles/s per Barnes-Hut force step (C1, single evaluation)", "value": n * args.steps / t_total,
+            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded 8-cluster Gaussian mixture)",
+            "config": {"workload": args.workload, "n": n, "theta": w["theta"], "leaf_size": w["max_children"],
+                       "softening": w["softening"], "method": "Barnes-Hut, the reference's QuadTree and MAC",
+                       "l2": "256 MB buffer written between timed steps"},
+            "error": {"median": err[0], "p90": err[1], "max": err[2], "vs": "fp64 direct sum", "samples": N_SAMPLES},
+            "e2e": {"value": n / float(np.median(e2e)), "unit": UNIT, "h2d_bytes_per_step": n * 16,
+                    "d2h_bytes_per_step": n * 16 + 8},
+            "clocks": clk.summary(),
+            "cpu_baseline": {"value": n / cpu_t, "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": f"the full {n}-particle system, reference BH (C port), {cpu_t:.2f} s"}}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -351,6 +427,9 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         dist.init_process_group("nccl")
+    if w.get("method") == "bh":
+        run_bh(args, w)
+        return
     r = run_ours(args, w, rank, world)
     if rank != 0:
         return

@@ -158,6 +158,18 @@ int tc_direct_device(int kernel, double softening, int precision, const double* 
 int tc_direct_device_noalloc(int kernel, double softening, int precision, const double* d_pos_xy, int64_t n,
                              const int64_t* d_rows, int64_t m, double* d_grad_rows, double* d_total, void* stream);
 
+/* ---------------------------------------------------------------- Barnes-Hut
+ * NBodySolverBH::updateTree + solveNbody with the reference's QuadTree
+ * (src/nbodysolvers/cpu/nBodySolverBH.h:33-116, src/trees/cpu/quadtree.h:29-172):
+ * same root box, split rule, children order, float masses and monopole MAC
+ * l/|x - com| < theta.  Forces (input order) and the pair sum are written,
+ * not accumulated.  FP64 reproduces the reference's interaction set and
+ * values to rounding; FP32 evaluates the same interactions in FP32.        */
+int tc_bh_solve(int kernel, double softening, int max_children, double theta, int precision,
+                const double* pos_xy, int64_t n, double* grad_xy, double* total);
+int tc_bh_solve_device(int kernel, double softening, int max_children, double theta, int precision,
+                       const double* d_pos_xy, int64_t n, double* d_grad_xy, double* d_total, void* stream);
+
 /* ---------------------------------------------------------------- t-SNE step
  * The TSNE class around the solver (src/nBodyInstances/tsne.h:42-563),
  * device resident.  P is the symmetric affinity matrix as CSR (rows and

@@ -63,6 +63,8 @@ SIGNATURES = {
     "tc_direct": (_I, [_I, _D, _I, _P, _I64, _P, _I64, _P, _P]),
     "tc_direct_device": (_I, [_I, _D, _I, _P, _I64, _P, _I64, _P, _P, _P]),
     "tc_direct_device_noalloc": (_I, [_I, _D, _I, _P, _I64, _P, _I64, _P, _P, _P]),
+    "tc_bh_solve": (_I, [_I, _D, _I, _D, _I, _P, _I64, _P, _P]),
+    "tc_bh_solve_device": (_I, [_I, _D, _I, _D, _I, _P, _I64, _P, _P, _P]),
     "tc_tsne_create": (_I, [_P, _I64, _P, _P, _P, _P, _P]),
     "tc_tsne_destroy": (_I, [_P]),
     "tc_tsne_set_theta": (_I, [_P, _D]),

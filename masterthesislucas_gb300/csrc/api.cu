@@ -143,6 +143,14 @@ __global__ void k_prel(const double2* __restrict__ pos64, const uint32_t* __rest
 
 }  // namespace
 
+int bbox_keys(const double* d_pos, int64_t n, double* d_keys4, uint32_t* d_err, cudaStream_t s)
+{
+    k_bbox_init<<<1, 1, 0, s>>>(d_keys4);
+    k_bbox<<<grid_for(n, 256, kSMs * 4), 256, 0, s>>>((const double2*)d_pos, n, d_keys4, d_err);
+    TC_CUDA_TRY(cudaGetLastError());
+    return TC_OK;
+}
+
 int device_bbox(Handle& h, const double* d_pos, int64_t n, double mn[2], double mx[2])
 {
     int rc;

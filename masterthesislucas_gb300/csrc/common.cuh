@@ -104,6 +104,20 @@ int64_t sum_tmp_doubles();
 int sum_f64(const double* a, int64_t na, const double* c, const uint32_t* nc, double* out, int accumulate,
             double* tmp, cudaStream_t s);
 
+// Exact bounding box of n device points (x, y doubles) as four order-preserving
+// 64-bit keys (min x, min y, max x, max y) in d_keys4; NaN/inf sets *d_err.
+int bbox_keys(const double* d_pos, int64_t n, double* d_keys4, uint32_t* d_err, cudaStream_t s);
+__host__ __device__ inline double bbox_unkey(unsigned long long k)
+{
+    unsigned long long u = (k & 0x8000000000000000ull) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
+    union {
+        unsigned long long i;
+        double d;
+    } c;
+    c.i = u;
+    return c.d;
+}
+
 // ---------------------------------------------------------------- sort
 // Stable LSD radix sort of 32-bit keys with 32-bit values (4 passes of 8 bits).
 // keys/vals are sorted in place; alt_* are scratch of n entries each.

@@ -306,6 +306,36 @@ __global__ void k_chunks(int dep, const uint32_t* __restrict__ count, uint32_t* 
         nchunk[i] = (count[li + i] + 31u) / 32u;
 }
 
+// direct interaction of one sink (base offset bx, by) with a staged tile of
+// sources; FULL > 0 unrolls a full tile of FULL sources
+template <int FULL, typename KN>
+__device__ __forceinline__ void p2p_tile(const KN& ker, const float2* src, int m, float bx, float by, float& gx,
+                                         float& gy, float& zs)
+{
+    if (FULL > 0) {
+#pragma unroll
+        for (int j = 0; j < FULL; j++) {
+            const float2 t2 = src[j];
+            const float Rx = bx - t2.x, Ry = by - t2.y;
+            float D1, t;
+            ker.near(Rx * Rx + Ry * Ry, D1, t);
+            gx += D1 * Rx;
+            gy += D1 * Ry;
+            zs += t;
+        }
+    } else {
+        for (int j = 0; j < m; j++) {
+            const float2 t2 = src[j];
+            const float Rx = bx - t2.x, Ry = by - t2.y;
+            float D1, t;
+            ker.near(Rx * Rx + Ry * Ry, D1, t);
+            gx += D1 * Rx;
+            gy += D1 * Ry;
+            zs += t;
+        }
+    }
+}
+
 // one warp per work item (leaf S, chunk of up to 32 sinks): L2P of the final
 // local expansion of S plus direct P2P with every particle of near(S)
 template <int P, typename KN>
@@ -371,32 +401,21 @@ __global__ void __launch_bounds__(32 * kNearWarps)
                 __syncwarp();
                 const uint32_t m = min(32u, cT - q0);
                 if (act) {
-                    if (self) {
-                        n_pp += m - ((sl >= q0 && sl < q0 + m) ? 1u : 0u);
-                        for (uint32_t j = 0; j < m; j++) {
-                            if (q0 + j == sl) continue;
-                            const float2 t2 = s_src[w][j];
-                            const float Rx = bx - t2.x, Ry = by - t2.y;
-                            float D1, t;
-                            ker.near(Rx * Rx + Ry * Ry, D1, t);
-                            gx += D1 * Rx;
-                            gy += D1 * Ry;
-                            zs += t;
-                        }
-                    } else {
-                        n_pp += m;
-                        for (uint32_t j = 0; j < m; j++) {
-                            const float2 t2 = s_src[w][j];
-                            const float Rx = bx - t2.x, Ry = by - t2.y;
-                            float D1, t;
-                            ker.near(Rx * Rx + Ry * Ry, D1, t);
-                            gx += D1 * Rx;
-                            gy += D1 * Ry;
-                            zs += t;
-                        }
-                    }
+                    n_pp += m;
+                    if (m == 32u)
+                        p2p_tile<32>(ker, s_src[w], 32, bx, by, gx, gy, zs);
+                    else
+                        p2p_tile<0>(ker, s_src[w], (int)m, bx, by, gx, gy, zs);
                 }
                 __syncwarp();
+            }
+            if (self && act) {
+                // the tile loop included the sink itself: R = 0 adds no force
+                // but adds the kernel's pair term at r = 0, which is removed here
+                float D1, t0;
+                ker.near(0.0f, D1, t0);
+                zs -= t0;
+                n_pp--;
             }
         }
         if (act) {

@@ -30,8 +30,29 @@ __device__ inline bool mac_accept(double2 a, double2 b, double len, double inv_t
     return dist > thr * thr;
 }
 
+// The same decision, decided in FP32 from cell-relative COMs whenever the FP32
+// squared distance is farther than a relative 1e-5 from the threshold (the
+// FP32 distance is accurate to ~1e-7 relative for the offsets that occur);
+// inside that band the exact FP64 test decides.  FP64 throughput on GB300 is
+// 1/64 of FP32, and the band holds a vanishing fraction of candidates.
+template <typename real>
+__device__ inline bool mac_accept_fast(int dix, int diy, real hl, real thr2, const real* cra, const real* crb,
+                                       double2 a, double2 b, double len, double inv_theta)
+{
+    if (sizeof(real) == 4) {
+        const real dx = (real)dix * hl + (cra[0] - crb[0]);
+        const real dy = (real)diy * hl + (cra[1] - crb[1]);
+        const real d2 = dx * dx + dy * dy;
+        if (d2 > thr2 * (real)(1.0 + 1e-5)) return true;
+        if (d2 < thr2 * (real)(1.0 - 1e-5)) return false;
+    }
+    return mac_accept(a, b, len, inv_theta);
+}
+
 // one thread per node of level l; fill == 0 counts, fill == 1 writes
-__global__ void k_lists(int l, double inv_theta, const uint32_t* __restrict__ count, const double2* __restrict__ com64,
+template <typename real>
+__global__ void k_lists(int l, double inv_theta, real hl, const uint32_t* __restrict__ count,
+                        const double2* __restrict__ com64, const real* __restrict__ comrel,
                         const double* __restrict__ bblen, const uint32_t* __restrict__ pnear_ptr,
                         const uint32_t* __restrict__ pnear_idx, uint32_t* __restrict__ nn_cnt,
                         uint32_t* __restrict__ near_cnt, const uint32_t* __restrict__ nn_ptr,
@@ -49,6 +70,10 @@ __global__ void k_lists(int l, double inv_theta, const uint32_t* __restrict__ co
             } else {
                 const double2 ca = com64[li + a];
                 const double len = bblen[li + a];
+                const real thr = (real)((len + len) * inv_theta);
+                const real thr2 = thr * thr;
+                const int iax = (int)compact16((uint32_t)a), iay = (int)compact16((uint32_t)a >> 1);
+                const real cra[2] = {comrel[2 * (li + a)], comrel[2 * (li + a) + 1]};
                 const uint32_t p = (uint32_t)(a >> 2);
                 const uint32_t nb = fill ? nn_ptr[a] : 0, rb = fill ? near_ptr[a] : 0;
                 for (uint32_t e = pnear_ptr[p]; e < pnear_ptr[p + 1]; e++) {
@@ -56,7 +81,8 @@ __global__ void k_lists(int l, double inv_theta, const uint32_t* __restrict__ co
                     for (uint32_t j = 0; j < 4; j++) {
                         const uint32_t b = 4 * bp + j;
                         if (count[li + b] == 0) continue;
-                        if (mac_accept(ca, com64[li + b], len, inv_theta)) {
+                        if (mac_accept_fast<real>(iax - (int)compact16(b), iay - (int)compact16(b >> 1), hl, thr2, cra,
+                                                  comrel + 2 * (li + b), ca, com64[li + b], len, inv_theta)) {
                             if (fill) nn_idx[nb + nn] = b;
                             nn++;
                         } else {
@@ -108,15 +134,28 @@ int build_lists(Handle& h)
     int64_t idx_words = 0;
     std::vector<int64_t> idx_cap;
     const double inv_theta = 1.0 / h.cfg.theta;
+    auto launch = [&](int l, const uint32_t* pnp, const uint32_t* pni, uint32_t* nnc, uint32_t* nrc,
+                      const uint32_t* nnp, uint32_t* nni, const uint32_t* nrp, uint32_t* nri, int fill) {
+        const int64_t nl = (int64_t)1 << (2 * l);
+        const double hl = h.L / (double)(1u << l);
+        if (h.cfg.precision == TC_PREC_FP64)
+            k_lists<double><<<grid_for(nl, 128), 128, 0, s>>>(l, inv_theta, hl, P<uint32_t>(h.count),
+                                                             P<double2>(h.com64), P<double>(h.comrel),
+                                                             P<double>(h.bblen), pnp, pni, nnc, nrc, nnp, nni, nrp,
+                                                             nri, fill);
+        else
+            k_lists<float><<<grid_for(nl, 128), 128, 0, s>>>(l, inv_theta, (float)hl, P<uint32_t>(h.count),
+                                                            P<double2>(h.com64), P<float>(h.comrel),
+                                                            P<double>(h.bblen), pnp, pni, nnc, nrc, nnp, nni, nrp,
+                                                            nri, fill);
+    };
     // first pass over all levels needs the previous level's near lists
     // resident, so the index pool grows level by level (host reads totals).
     for (int l = 0; l <= depth; l++) {
         const int64_t nl = (int64_t)1 << (2 * l);
         const uint32_t* pnp = l ? ptr + L.near_ptr_off[l - 1] : nullptr;
         const uint32_t* pni = l ? P<uint32_t>(h.idx_pool) + L.near_idx_off[l - 1] : nullptr;
-        k_lists<<<grid_for(nl, 128), 128, 0, s>>>(l, inv_theta, P<uint32_t>(h.count), P<double2>(h.com64),
-                                                 P<double>(h.bblen), pnp, pni, nn_cnt, near_cnt, nullptr, nullptr,
-                                                 nullptr, nullptr, 0);
+        launch(l, pnp, pni, nn_cnt, near_cnt, nullptr, nullptr, nullptr, nullptr, 0);
         uint32_t* nnp = ptr + L.nn_ptr_off[l];
         uint32_t* nrp = ptr + L.near_ptr_off[l];
         if ((rc = exclusive_scan_u32(nn_cnt, nnp, nl, P<uint32_t>(h.tmp), s))) return rc;
@@ -141,10 +180,8 @@ int build_lists(Handle& h)
             h.idx_pool = nb;
         }
         pni = l ? P<uint32_t>(h.idx_pool) + L.near_idx_off[l - 1] : nullptr;
-        k_lists<<<grid_for(nl, 128), 128, 0, s>>>(l, inv_theta, P<uint32_t>(h.count), P<double2>(h.com64),
-                                                 P<double>(h.bblen), pnp, pni, nullptr, nullptr, nnp,
-                                                 P<uint32_t>(h.idx_pool) + L.nn_idx_off[l], nrp,
-                                                 P<uint32_t>(h.idx_pool) + L.near_idx_off[l], 1);
+        launch(l, pnp, pni, nullptr, nullptr, nnp, P<uint32_t>(h.idx_pool) + L.nn_idx_off[l], nrp,
+               P<uint32_t>(h.idx_pool) + L.near_idx_off[l], 1);
         h.launches += 8;
     }
     TC_CUDA_TRY(cudaGetLastError());

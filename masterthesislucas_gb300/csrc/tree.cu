@@ -17,22 +17,33 @@
 namespace tc {
 namespace {
 
+// one coordinate of createMortonCode (:545-549): (uint32)clamp(((p - min)/L) * 65536, 0, 65535).
+// FP64 division runs at 1/64 of the FP32 rate on GB300, so the quotient is
+// first formed as (p - min) * (65536/L), within 2 ulp of the exact product;
+// only when that lands within 1e-9 of an integer can the floor differ from
+// the reference's, and then the reference's own division decides.
+__device__ inline uint32_t morton_coord(double p, double nm, double L, double s65536)
+{
+    const double a = p + nm;
+    double v = a * s65536;
+    const double f = v - floor(v);
+    if (f < 1e-9 || f > 1.0 - 1e-9) v = (a / (L)) * 65536.0;
+    v = (v < 0.0) ? 0.0 : v;             // glm::max(v, 0)
+    v = (65535.0 < v) ? 65535.0 : v;     // glm::min(v, 65535)
+    return (uint32_t)v;
+}
+
 __global__ void k_morton(const double2* __restrict__ pos, int64_t n, double minx, double miny, double maxx,
                          double maxy, double L, uint32_t* __restrict__ codes, uint32_t* __restrict__ err)
 {
     const double nmx = -minx, nmy = -miny;
+    const double s65536 = 65536.0 / L;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         double2 p = pos[i];
         if (!(p.x >= minx && p.x <= maxx && p.y >= miny && p.y <= maxy)) atomicOr(err, 1u);
-        double px = (p.x + nmx) / (L);
-        double py = (p.y + nmy) / (L);
-        px = px * 65536.0;
-        py = py * 65536.0;
-        px = (px < 0.0) ? 0.0 : px;     // glm::max(v, 0)
-        py = (py < 0.0) ? 0.0 : py;
-        px = (65535.0 < px) ? 65535.0 : px;  // glm::min(v, 65535)
-        py = (65535.0 < py) ? 65535.0 : py;
-        codes[i] = (spread16((uint32_t)py) << 1) | spread16((uint32_t)px);
+        const uint32_t qx = morton_coord(p.x, nmx, L, s65536);
+        const uint32_t qy = morton_coord(p.y, nmy, L, s65536);
+        codes[i] = (spread16(qy) << 1) | spread16(qx);
     }
 }
 

@@ -205,3 +205,13 @@ def direct(pos, *, kernel="tsne", softening=1e-3, precision="fp64", rows=None):
     check(lib().tc_direct(KERNELS[kernel], softening, PRECISIONS[precision], ptr(pos), n, ptr(r), m, ptr(g),
                           ctypes.byref(tot)))
     return g, float(tot.value)
+
+
+def barnes_hut(pos, *, kernel="tsne", softening=1e-3, max_children=16, theta=0.5, precision="fp32"):
+    """NBodySolverBH on the GPU: forces in input order and the pair sum."""
+    pos = np.ascontiguousarray(pos, np.float64)
+    g = np.zeros_like(pos)
+    tot = ctypes.c_double(0.0)
+    check(lib().tc_bh_solve(KERNELS[kernel], softening, max_children, theta, PRECISIONS[precision], ptr(pos),
+                            len(pos), ptr(g), ctypes.byref(tot)))
+    return g, float(tot.value)

@@ -13,7 +13,7 @@ sources (tests/golden/make_golden.py).  Contract:
 import numpy as np
 import pytest
 
-from masterthesislucas_gb300 import NBodySolverFMM_SYM_MORTON, Points, direct
+from masterthesislucas_gb300 import NBodySolverFMM_SYM_MORTON, Points, datasets, direct
 from masterthesislucas_gb300._lib import TreecodeError
 
 pytestmark = pytest.mark.gpu
@@ -132,3 +132,29 @@ def test_repeated_solves_are_deterministic():
         outs.append((pts.derivative.copy(), t))
     np.testing.assert_array_equal(outs[0][0], outs[1][0])
     assert outs[0][1] == outs[1][1]
+
+
+@pytest.mark.parametrize("tag", ["tsne", "grav"])
+def test_barnes_hut_matches_reference(golden, tag):
+    from masterthesislucas_gb300.solver import barnes_hut
+    g = golden(f"bh_{tag}_3000")
+    kernel = "tsne" if tag == "tsne" else "gravity"
+    kw = dict(kernel=kernel, softening=float(g["eps"]) or 1e-3, max_children=int(g["max_children"]),
+              theta=float(g["theta"]))
+    grad, total = barnes_hut(g["pos"], precision="fp64", **kw)
+    assert rel_err(grad, g["grad"]).max() < 1e-12
+    assert total == pytest.approx(float(g["total"]), rel=1e-12)
+    grad32, total32 = barnes_hut(g["pos"], precision="fp32", **kw)
+    err = rel_err(grad32, g["grad"])
+    assert np.median(err) < 1e-5 and err.max() < 1e-3
+    assert total32 == pytest.approx(float(g["total"]), rel=1e-5)
+
+
+def test_barnes_hut_large_matches_oracle():
+    import oracle
+    from masterthesislucas_gb300.solver import barnes_hut
+    pos = datasets.gaussian_mixture(65536, seed=77).astype(np.float64)
+    gref, tref = oracle.bh(pos, kernel=oracle.KERNEL_GRAVITY, eps=1e-3, max_children=16, theta=0.5)
+    g, t = barnes_hut(pos, kernel="gravity", softening=1e-3, max_children=16, theta=0.5, precision="fp64")
+    assert rel_err(g, gref).max() < 1e-11
+    assert t == pytest.approx(tref, rel=1e-11)
