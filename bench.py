@@ -46,6 +46,8 @@ THETAS = (0.4, 0.35, 0.3, 0.25, 0.2, 0.15, 0.1)
 WORKLOADS = {
     "nbody_two_disks_4m": dict(n=4194304, dist="two_disks", kernel="gravity", softening=1e-3, max_children=64),
     "nbody_two_disks_1m": dict(n=1048576, dist="two_disks", kernel="gravity", softening=1e-3, max_children=64),
+    "tsne_70k": dict(n=70000, dist="tsne", dim=784, clusters=10, perplexity=30.0, kernel="tsne", order=8,
+                     theta=0.5, max_children=16, early_exaggeration=12.0, method="tsne", softening=0.0),
     "bh_mixture_65k": dict(n=65536, dist="mixture", kernel="gravity", softening=1e-3, max_children=16,
                            method="bh", theta=0.5),
 }
@@ -373,6 +375,96 @@ def run_bh(args, w):
     print(json.dumps(line))
 
 
+def run_tsne(args, w):
+    """t-SNE gradient steps (tree repulsion at order p + CSR attractive + Z + momentum), device resident."""
+    import torch
+
+    from masterthesislucas_gb300 import datasets
+    from masterthesislucas_gb300._lib import check, lib, ptr
+    from masterthesislucas_gb300.affinity import build_p_csr
+    from masterthesislucas_gb300.tsne import TSNE
+
+    n = w["n"]
+    x, _ = datasets.cluster_data(n, w["dim"], k=w["clusters"], seed=3)
+    t0 = time.perf_counter()
+    row_ptr, col, val = build_p_csr(x, perplexity=w["perplexity"], device="cuda")
+    t_p = time.perf_counter() - t0
+    y0 = datasets.tsne_init(n, seed=4, sigma=0.01)
+    t = TSNE(row_ptr, col, val, y0, early_exaggeration=w["early_exaggeration"], min_theta=w["theta"],
+             max_theta=w["theta"], max_children=w["max_children"], order=args.order or w["order"])
+    dev = torch.device("cuda", 0)
+
+    def exact_grad(y, rows):
+        """FP64 gradient on sampled rows: 4/Z * direct repulsion + attractive term."""
+        yd = torch.from_numpy(np.ascontiguousarray(y)).to(dev)
+        rd = torch.from_numpy(rows.astype(np.int64)).to(dev)
+        rep = torch.zeros((len(rows), 2), dtype=torch.float64, device=dev)
+        z = torch.zeros(1, dtype=torch.float64, device=dev)
+        check(lib().tc_direct_device(0, 0.0, 1, ptr(yd), n, ptr(rd), len(rows), ptr(rep), None, None))
+        check(lib().tc_direct_device(0, 0.0, 1, ptr(yd), n, None, n, ptr(torch.zeros((n, 2), dtype=torch.float64,
+                                                                                   device=dev)), ptr(z), None))
+        torch.cuda.synchronize()
+        zz = float(z.item())
+        g = rep.cpu().numpy() * (4.0 / zz)
+        it = t.iteration_counter - 1
+        exag = 4.0 * (w["early_exaggeration"] if it < 250 else 1.0)
+        for k, i in enumerate(rows):
+            js = col[row_ptr[i]:row_ptr[i + 1]]
+            d = y[js] - y[i]
+            q = 1.0 / (1.0 + (d * d).sum(1))
+            g[k] += exag * ((val[row_ptr[i]:row_ptr[i + 1]] * q)[:, None] * d).sum(0)
+        return g, zz
+
+    rows = np.sort(np.random.default_rng(9).choice(n, 1024, replace=False))
+    errs = []
+    steps = args.steps
+    for _ in range(args.warmup):
+        t.time_step()
+    # the warm-up iterations count as t-SNE iterations; the timed ones continue the schedule
+    torch.cuda.synchronize()
+    st = torch.cuda.Event(enable_timing=True)
+    en = torch.cuda.Event(enable_timing=True)
+    launches = 0
+    ms_total = 0.0
+    check_every = max(1, steps // 5)
+    with ClockSampler(0) as clk:
+        for k in range(steps):
+            st.record()
+            t.time_step()
+            en.record()
+            launches += t.launches()
+            torch.cuda.synchronize()
+            ms_total += st.elapsed_time(en)
+            if (k + 1) % check_every == 0:
+                y, yp, g = t.embedding()
+                ge, zz = exact_grad(yp, rows)   # g was evaluated at the previous embedding
+                e = np.linalg.norm(g[rows] - ge, axis=1) / np.linalg.norm(ge, axis=1)
+                errs.append({"iteration": t.iteration_counter, "median": float(np.median(e)),
+                             "p90": float(np.percentile(e, 90))})
+    # final KL(P || Q) with an exact FP64 Z
+    y, _, _ = t.embedding()
+    yd = torch.from_numpy(y).to(dev)
+    z = torch.zeros(1, dtype=torch.float64, device=dev)
+    check(lib().tc_direct_device(0, 0.0, 1, ptr(yd), n, None, n,
+                                 ptr(torch.zeros((n, 2), dtype=torch.float64, device=dev)), ptr(z), None))
+    torch.cuda.synchronize()
+    rr = np.repeat(np.arange(n), np.diff(row_ptr).astype(np.int64))
+    d2 = ((y[rr] - y[col]) ** 2).sum(1)
+    qv = 1.0 / (1.0 + d2) / float(z.item())
+    kl = float(np.sum(val * np.log(val / qv)))
+    s_per_step = ms_total / 1e3 / steps
+    line = {"metric": "t-SNE gradient steps/s (C2: 70k x 784, perplexity 30, order-p FMM repulsion)",
+            "value": 1.0 / s_per_step, "unit": "steps/s", "n_gpus": 1, "steps": steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * s_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (10 Gaussian clusters in 784-D clipped to [0,1]; P built here)",
+            "config": {"workload": args.workload, "n": n, "perplexity": w["perplexity"], "k": 90,
+                       "nnz": int(len(col)), "order": args.order or w["order"], "theta": w["theta"],
+                       "early_exaggeration": w["early_exaggeration"], "p_build_s": t_p},
+            "particles_per_s": n / s_per_step, "gradient_error_vs_fp64": errs, "final_kl": kl,
+            "gpu_launches": launches, "clocks": clk.summary()}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -429,6 +521,9 @@ def main():
         dist.init_process_group("nccl")
     if w.get("method") == "bh":
         run_bh(args, w)
+        return
+    if w.get("method") == "tsne":
+        run_tsne(args, w)
         return
     r = run_ours(args, w, rank, world)
     if rank != 0:

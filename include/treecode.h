@@ -170,6 +170,30 @@ int tc_bh_solve(int kernel, double softening, int max_children, double theta, in
 int tc_bh_solve_device(int kernel, double softening, int max_children, double theta, int precision,
                        const double* d_pos_xy, int64_t n, double* d_grad_xy, double* d_total, void* stream);
 
+/* ---------------------------------------------------------------- order controller
+ * No counterpart in the reference (its expansion order is fixed).  A 3-layer
+ * MLP (16 pair features -> 64 -> 64 -> 5, ReLU; BF16 weights, FP32
+ * accumulation) predicts log10 of the relative far-field force error of a
+ * node pair at orders 4, 6, 8, 10, 12; training and inference run in this
+ * library's own kernels.  Parameter layout: W1[64][16] b1[64] W2[64][64]
+ * b2[64] W3[5][64] b3[5].  Device pointers: d_x (n x 16), d_t / d_y (n x 5). */
+#define TC_MLP_IN 16
+#define TC_MLP_HIDDEN 64
+#define TC_MLP_OUT 5
+#define TC_MLP_NPARAM 5573
+typedef struct tc_mlp tc_mlp;
+int tc_mlp_create(uint64_t seed, tc_mlp** out);
+int tc_mlp_destroy(tc_mlp* m);
+int tc_mlp_set_normalization(tc_mlp* m, const float* mean, const float* stdv);
+int tc_mlp_get_params(tc_mlp* m, float* params, float* mean, float* stdv);
+int tc_mlp_set_params(tc_mlp* m, const float* params);
+/* mean-squared-error gradient of the whole set d_x/d_t (n <= 2^20), host out */
+int tc_mlp_gradient(tc_mlp* m, const float* d_x, const float* d_t, int64_t n, float* grad, float* loss);
+/* Adam on seeded random mini-batches of the set */
+int tc_mlp_train(tc_mlp* m, const float* d_x, const float* d_t, int64_t n, int steps, int batch, float lr,
+                 uint64_t seed, float* last_loss);
+int tc_mlp_forward(tc_mlp* m, const float* d_x, int64_t n, float* d_y);
+
 /* ---------------------------------------------------------------- t-SNE step
  * The TSNE class around the solver (src/nBodyInstances/tsne.h:42-563),
  * device resident.  P is the symmetric affinity matrix as CSR (rows and

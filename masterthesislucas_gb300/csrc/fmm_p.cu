@@ -24,6 +24,15 @@ namespace {
 
 __host__ __device__ constexpr int ncoef(int p) { return (p + 1) * (p + 2) / 2; }
 __host__ __device__ constexpr int cidx(int a, int b) { return (a + b) * (a + b + 1) / 2 + b; }
+// coefficient arrays are padded to 16 bytes per node for vector loads
+__host__ __device__ constexpr int kstride(int p) { return (ncoef(p) + 3) & ~3; }
+// total degree of the coefficient with linear index i
+__host__ __device__ constexpr int cdeg(int i)
+{
+    int k = 0;
+    while ((k + 1) * (k + 2) / 2 <= i) k++;
+    return k;
+}
 
 struct PotParams {
     float nu;    // phi = pref * u^-nu
@@ -156,7 +165,7 @@ __global__ void __launch_bounds__(128) k_p2m(int dep, float h, const uint32_t* _
 #pragma unroll
         for (int k = 0; k < K; k++) {
             const float v = warp_sum(acc[k]);
-            if (lane == 0) mu[node * K + k] = v;
+            if (lane == 0) mu[node * kstride(P) + k] = v;
         }
     }
 }
@@ -190,13 +199,13 @@ __global__ void __launch_bounds__(128) k_m2m(int l, float hl, const uint32_t* __
             for (int ka = 0; ka <= P; ka++) {
                 const float sc = 1.0f / (float)(1 << ka);  // child scale -> parent scale
 #pragma unroll
-                for (int b = 0; b <= ka; b++) in[cidx(ka - b, b)] = mu[ch * K + cidx(ka - b, b)] * sc;
+                for (int b = 0; b <= ka; b++) in[cidx(ka - b, b)] = mu[ch * kstride(P) + cidx(ka - b, b)] * sc;
             }
             monomials<P>(dx, dy, w);
             shift_up<P>(in, w, acc);
         }
 #pragma unroll
-        for (int k = 0; k < K; k++) mu[node * K + k] = acc[k];
+        for (int k = 0; k < K; k++) mu[node * kstride(P) + k] = acc[k];
     }
 }
 
@@ -210,11 +219,13 @@ __global__ void __launch_bounds__(128) k_m2l_p(int l, float hl, PotParams pp, co
                                                float* __restrict__ loc, double* __restrict__ zpart)
 {
     constexpr int K = ncoef(P);
+    constexpr int KS = kstride(P);
     const uint32_t li = level_index(l);
     const int64_t nl = (int64_t)1 << (2 * l);
     const float ih = 1.0f / hl;
     for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < nl; a += (int64_t)gridDim.x * blockDim.x) {
         const int64_t na = li + a;
+        if (count[na] == 0) continue;  // empty nodes are never read
         const uint32_t b0 = nn_ptr[a], b1 = nn_ptr[a + 1];
         float L[K];
 #pragma unroll
@@ -229,13 +240,18 @@ __global__ void __launch_bounds__(128) k_m2l_p(int l, float hl, PotParams pp, co
                 const float Ry = (float)(iay - (int)compact16(b >> 1)) + (cay - comrel[2 * nb + 1]) * ih;
                 float D[K];
                 derivs<P>(Rx, Ry, hl, pp, D);
-                const float* m = mu + nb * K;
+                const float4* m4 = reinterpret_cast<const float4*>(mu + nb * KS);
 #pragma unroll
-                for (int ka = 0; ka <= P; ka++) {
-                    if (ka == 1) continue;  // dipole vanishes about the COM
+                for (int c = 0; c < KS / 4; c++) {
+                    const float4 q = __ldg(m4 + c);
+                    const float mv[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
-                    for (int ba = 0; ba <= ka; ba++) {
-                        const float ma = (ka & 1) ? -m[cidx(ka - ba, ba)] : m[cidx(ka - ba, ba)];
+                    for (int j = 0; j < 4; j++) {
+                        const int ia = 4 * c + j;
+                        if (ia >= K) continue;
+                        const int ka = cdeg(ia), ba = ia - ka * (ka + 1) / 2;
+                        if (ka == 1) continue;  // dipole vanishes about the COM
+                        const float ma = (ka & 1) ? -mv[j] : mv[j];
 #pragma unroll
                         for (int kb = 0; kb + ka <= P; kb++)
 #pragma unroll
@@ -246,16 +262,24 @@ __global__ void __launch_bounds__(128) k_m2l_p(int l, float hl, PotParams pp, co
             }
         }
         double z = 0.0;
-        if (count[na] != 0 && b0 != b1) {
-            const float* m = mu + na * K;
+        if (b0 != b1) {
+            const float* m = mu + na * KS;
             float zs = 0.f;
 #pragma unroll
             for (int k = 0; k < K; k++) zs += L[k] * m[k];
             z = (double)pp.kappa * (double)zs;
         }
         zpart[na] = z;
+        float4* o4 = reinterpret_cast<float4*>(loc + na * KS);
 #pragma unroll
-        for (int k = 0; k < K; k++) loc[na * K + k] = L[k];
+        for (int c = 0; c < KS / 4; c++) {
+            float4 v;
+            v.x = 4 * c + 0 < K ? L[4 * c + 0] : 0.f;
+            v.y = 4 * c + 1 < K ? L[4 * c + 1] : 0.f;
+            v.z = 4 * c + 2 < K ? L[4 * c + 2] : 0.f;
+            v.w = 4 * c + 3 < K ? L[4 * c + 3] : 0.f;
+            o4[c] = v;
+        }
     }
 }
 
@@ -284,14 +308,14 @@ __global__ void __launch_bounds__(128) k_l2l(int l, float hl, const uint32_t* __
         for (int kb = 0; kb <= P; kb++) {
             const float sc = 1.0f / (float)(1 << kb);  // parent scale 2h -> child scale h
 #pragma unroll
-            for (int b = 0; b <= kb; b++) in[cidx(kb - b, b)] = loc[par * K + cidx(kb - b, b)] * sc;
+            for (int b = 0; b <= kb; b++) in[cidx(kb - b, b)] = loc[par * kstride(P) + cidx(kb - b, b)] * sc;
         }
 #pragma unroll
-        for (int k = 0; k < K; k++) acc[k] = loc[node * K + k];
+        for (int k = 0; k < K; k++) acc[k] = loc[node * kstride(P) + k];
         monomials<P>(ddx, ddy, w);
         shift_down<P>(in, w, acc);
 #pragma unroll
-        for (int k = 0; k < K; k++) loc[node * K + k] = acc[k];
+        for (int k = 0; k < K; k++) loc[node * kstride(P) + k] = acc[k];
     }
 }
 
@@ -375,7 +399,7 @@ __global__ void __launch_bounds__(32 * kNearWarps)
             // L2P: F = (1/h) sum_b L_b d^(b - e) / (b - e)!
             float wv[KW];
             monomials<P - 1>((px - comrel[2 * S]) * ih, (py - comrel[2 * S + 1]) * ih, wv);
-            const float* L = loc + S * K;
+            const float* L = loc + S * kstride(P);
 #pragma unroll
             for (int k = 0; k < P; k++)
 #pragma unroll
@@ -463,7 +487,8 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
     const int64_t nleaf = (int64_t)1 << (2 * dep);
     const int64_t wmax = h.n / 32 + (h.n < nleaf ? h.n : nleaf) + 1;
     int rc;
-    if ((rc = ensure(h.mu, nn * K * 4)) || (rc = ensure(h.loc, nn * K * 4)) || (rc = ensure(h.zpart, nn * 8 + 64)) ||
+    if ((rc = ensure(h.mu, nn * kstride(ORD) * 4)) || (rc = ensure(h.loc, nn * kstride(ORD) * 4)) ||
+        (rc = ensure(h.zpart, nn * 8 + 64)) ||
         (rc = ensure(h.counters, 64)) || (rc = ensure(h.chunk, (nleaf + 1) * 4)) ||
         (rc = ensure(h.zwork, wmax * 8)) || (rc = ensure(h.cnt_tmp, nleaf * 4 + 64)) ||
         (rc = ensure(h.tmp, scan_tmp_words(nleaf) * 4)) || (rc = record(h, 4)))
@@ -481,7 +506,8 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
         const int64_t nl = (int64_t)1 << (2 * l);
         k_m2m<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, mu);
     }
-    TC_CUDA_TRY(cudaMemsetAsync(loc, 0, K * 4, s));
+    TC_CUDA_TRY(cudaMemsetAsync(loc, 0, kstride(ORD) * 4, s));
+    TC_CUDA_TRY(cudaMemsetAsync(zp, 0, nn * 8, s));
     TC_CUDA_TRY(cudaMemsetAsync(zp, 0, 8, s));
     const uint32_t* ptr = P<uint32_t>(h.ptr_pool);
     const uint32_t* idx = P<uint32_t>(h.idx_pool);

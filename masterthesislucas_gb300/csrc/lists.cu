@@ -54,11 +54,12 @@ template <typename real>
 __global__ void k_lists(int l, double inv_theta, real hl, const uint32_t* __restrict__ count,
                         const double2* __restrict__ com64, const real* __restrict__ comrel,
                         const double* __restrict__ bblen, const uint32_t* __restrict__ pnear_ptr,
-                        const uint32_t* __restrict__ pnear_idx, uint32_t* __restrict__ nn_cnt,
+                        const uint32_t* __restrict__ pnear_idx, uint32_t pcap, uint32_t* __restrict__ nn_cnt,
                         uint32_t* __restrict__ near_cnt, const uint32_t* __restrict__ nn_ptr,
-                        uint32_t* __restrict__ nn_idx, const uint32_t* __restrict__ near_ptr,
-                        uint32_t* __restrict__ near_idx, int fill)
+                        uint32_t* __restrict__ nn_idx, uint32_t nn_cap, const uint32_t* __restrict__ near_ptr,
+                        uint32_t* __restrict__ near_idx, uint32_t near_cap, uint32_t* __restrict__ ovf, int fill)
 {
+    const uint32_t np = l ? (1u << (2 * (l - 1))) : 0u;
     const uint32_t li = level_index(l);
     const int64_t nl = (int64_t)1 << (2 * l);
     for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < nl; a += (int64_t)gridDim.x * blockDim.x) {
@@ -66,7 +67,10 @@ __global__ void k_lists(int l, double inv_theta, real hl, const uint32_t* __rest
         if (count[li + a] != 0) {
             if (l == 0) {
                 nr = 1;
-                if (fill) near_idx[near_ptr[a]] = 0;
+                if (fill) {
+                    if (near_ptr[a] < near_cap) near_idx[near_ptr[a]] = 0;
+                    else atomicOr(ovf, 1u);
+                }
             } else {
                 const double2 ca = com64[li + a];
                 const double len = bblen[li + a];
@@ -76,17 +80,25 @@ __global__ void k_lists(int l, double inv_theta, real hl, const uint32_t* __rest
                 const real cra[2] = {comrel[2 * (li + a)], comrel[2 * (li + a) + 1]};
                 const uint32_t p = (uint32_t)(a >> 2);
                 const uint32_t nb = fill ? nn_ptr[a] : 0, rb = fill ? near_ptr[a] : 0;
-                for (uint32_t e = pnear_ptr[p]; e < pnear_ptr[p + 1]; e++) {
+                const uint32_t pe1 = pnear_ptr[p + 1] < pcap ? pnear_ptr[p + 1] : pcap;
+                for (uint32_t e = pnear_ptr[p]; e < pe1; e++) {
                     const uint32_t bp = pnear_idx[e];
+                    if (bp >= np) continue;  // only after an overflowed parent level
                     for (uint32_t j = 0; j < 4; j++) {
                         const uint32_t b = 4 * bp + j;
                         if (count[li + b] == 0) continue;
                         if (mac_accept_fast<real>(iax - (int)compact16(b), iay - (int)compact16(b >> 1), hl, thr2, cra,
                                                   comrel + 2 * (li + b), ca, com64[li + b], len, inv_theta)) {
-                            if (fill) nn_idx[nb + nn] = b;
+                            if (fill) {
+                                if (nb + nn < nn_cap) nn_idx[nb + nn] = b;
+                                else atomicOr(ovf, 1u);
+                            }
                             nn++;
                         } else {
-                            if (fill) near_idx[rb + nr] = b;
+                            if (fill) {
+                                if (rb + nr < near_cap) near_idx[rb + nr] = b;
+                                else atomicOr(ovf, 1u);
+                            }
                             nr++;
                         }
                     }
@@ -97,6 +109,16 @@ __global__ void k_lists(int l, double inv_theta, real hl, const uint32_t* __rest
             nn_cnt[a] = nn;
             near_cnt[a] = nr;
         }
+    }
+}
+
+// per-level list totals (last entries of the CSR pointer arrays)
+__global__ void k_list_totals(const uint32_t* __restrict__ ptr, const int64_t* __restrict__ offs, int nlev,
+                              uint32_t* __restrict__ out)
+{
+    for (int k = threadIdx.x; k < 2 * nlev; k += blockDim.x) {
+        const int l = k >> 1;
+        out[k] = ptr[offs[k] + ((int64_t)1 << (2 * l))];
     }
 }
 
@@ -131,31 +153,88 @@ int build_lists(Handle& h)
     uint32_t* ptr = P<uint32_t>(h.ptr_pool);
     uint32_t* nn_cnt = P<uint32_t>(h.cnt_tmp);
     uint32_t* near_cnt = nn_cnt + nleaf;
-    int64_t idx_words = 0;
-    std::vector<int64_t> idx_cap;
     const double inv_theta = 1.0 / h.cfg.theta;
-    auto launch = [&](int l, const uint32_t* pnp, const uint32_t* pni, uint32_t* nnc, uint32_t* nrc,
-                      const uint32_t* nnp, uint32_t* nni, const uint32_t* nrp, uint32_t* nri, int fill) {
+    uint32_t* ovf_flag = P<uint32_t>(h.err) + 1;
+    auto launch = [&](int l, const uint32_t* pnp, const uint32_t* pni, uint32_t pcap, uint32_t* nnc, uint32_t* nrc,
+                      const uint32_t* nnp, uint32_t* nni, uint32_t nncap, const uint32_t* nrp, uint32_t* nri,
+                      uint32_t nrcap, int fill) {
         const int64_t nl = (int64_t)1 << (2 * l);
         const double hl = h.L / (double)(1u << l);
         if (h.cfg.precision == TC_PREC_FP64)
             k_lists<double><<<grid_for(nl, 128), 128, 0, s>>>(l, inv_theta, hl, P<uint32_t>(h.count),
                                                              P<double2>(h.com64), P<double>(h.comrel),
-                                                             P<double>(h.bblen), pnp, pni, nnc, nrc, nnp, nni, nrp,
-                                                             nri, fill);
+                                                             P<double>(h.bblen), pnp, pni, pcap, nnc, nrc, nnp, nni,
+                                                             nncap, nrp, nri, nrcap, ovf_flag, fill);
         else
             k_lists<float><<<grid_for(nl, 128), 128, 0, s>>>(l, inv_theta, (float)hl, P<uint32_t>(h.count),
                                                             P<double2>(h.com64), P<float>(h.comrel),
-                                                            P<double>(h.bblen), pnp, pni, nnc, nrc, nnp, nni, nrp,
-                                                            nri, fill);
+                                                            P<double>(h.bblen), pnp, pni, pcap, nnc, nrc, nnp, nni,
+                                                            nncap, nrp, nri, nrcap, ovf_flag, fill);
     };
-    // first pass over all levels needs the previous level's near lists
-    // resident, so the index pool grows level by level (host reads totals).
+    uint32_t* ovf = P<uint32_t>(h.err) + 1;
+    TC_CUDA_TRY(cudaMemsetAsync(ovf, 0, 4, s));
+    // Fast mode: per-level regions sized from the last exact totals (x1.25),
+    // no host round trip between levels; one synchronisation at the end
+    // verifies that no level overflowed, else the exact mode reruns.
+    const bool fast = L.caps_depth == depth && (int64_t)L.nn_cap.size() == depth + 1;
+    if (fast) {
+        int64_t words = 0;
+        for (int l = 0; l <= depth; l++) {
+            L.nn_idx_off[l] = words;
+            words += L.nn_cap[l];
+            L.near_idx_off[l] = words;
+            words += L.near_cap[l];
+        }
+        if ((rc = ensure(h.idx_pool, (size_t)words * 4 + 64))) return rc;
+        for (int l = 0; l <= depth; l++) {
+            const int64_t nl = (int64_t)1 << (2 * l);
+            const uint32_t* pnp = l ? ptr + L.near_ptr_off[l - 1] : nullptr;
+            const uint32_t* pni = l ? P<uint32_t>(h.idx_pool) + L.near_idx_off[l - 1] : nullptr;
+            const uint32_t pcap = l ? L.near_cap[l - 1] : 0u;
+            launch(l, pnp, pni, pcap, nn_cnt, near_cnt, nullptr, nullptr, 0, nullptr, nullptr, 0, 0);
+            uint32_t* nnp = ptr + L.nn_ptr_off[l];
+            uint32_t* nrp = ptr + L.near_ptr_off[l];
+            if ((rc = exclusive_scan_u32(nn_cnt, nnp, nl, P<uint32_t>(h.tmp), s))) return rc;
+            if ((rc = exclusive_scan_u32(near_cnt, nrp, nl, P<uint32_t>(h.tmp), s))) return rc;
+            launch(l, pnp, pni, pcap, nullptr, nullptr, nnp, P<uint32_t>(h.idx_pool) + L.nn_idx_off[l], L.nn_cap[l],
+                   nrp, P<uint32_t>(h.idx_pool) + L.near_idx_off[l], L.near_cap[l], 1);
+            h.launches += 8;
+        }
+        // totals of every level plus the overflow flag, in one round trip
+        std::vector<int64_t> offs(2 * (depth + 1));
+        for (int l = 0; l <= depth; l++) {
+            offs[2 * l] = L.nn_ptr_off[l];
+            offs[2 * l + 1] = L.near_ptr_off[l];
+        }
+        if ((rc = ensure(h.lstat, offs.size() * 8 + 4 * 64))) return rc;
+        TC_CUDA_TRY(cudaMemcpyAsync(h.lstat.p, offs.data(), offs.size() * 8, cudaMemcpyHostToDevice, s));
+        uint32_t* dtot = (uint32_t*)((char*)h.lstat.p + offs.size() * 8);
+        k_list_totals<<<1, 64, 0, s>>>(ptr, P<int64_t>(h.lstat), depth + 1, dtot);
+        h.launches++;
+        TC_CUDA_TRY(cudaMemcpyAsync(h.h_words, dtot, 4 * 2 * (depth + 1), cudaMemcpyDeviceToHost, s));
+        TC_CUDA_TRY(cudaMemcpyAsync(h.h_words + 40, ovf, 4, cudaMemcpyDeviceToHost, s));
+        TC_CUDA_TRY(cudaStreamSynchronize(s));
+        bool over = h.h_words[40] != 0;
+        for (int l = 0; l <= depth; l++) {
+            L.nn_total[l] = h.h_words[2 * l];
+            L.near_total[l] = h.h_words[2 * l + 1];
+            over = over || L.nn_total[l] > L.nn_cap[l] || L.near_total[l] > L.near_cap[l];
+        }
+        if (!over) {
+            TC_CUDA_TRY(cudaGetLastError());
+            return record(h, 3);
+        }
+        TC_CUDA_TRY(cudaMemsetAsync(ovf, 0, 4, s));
+    }
+    // exact mode: the host reads each level's totals before the next level
+    // (the first call, and after a fast-mode overflow)
+    int64_t idx_words = 0;
     for (int l = 0; l <= depth; l++) {
         const int64_t nl = (int64_t)1 << (2 * l);
         const uint32_t* pnp = l ? ptr + L.near_ptr_off[l - 1] : nullptr;
         const uint32_t* pni = l ? P<uint32_t>(h.idx_pool) + L.near_idx_off[l - 1] : nullptr;
-        launch(l, pnp, pni, nn_cnt, near_cnt, nullptr, nullptr, nullptr, nullptr, 0);
+        const uint32_t pcap = l ? L.near_total[l - 1] : 0u;
+        launch(l, pnp, pni, pcap, nn_cnt, near_cnt, nullptr, nullptr, 0, nullptr, nullptr, 0, 0);
         uint32_t* nnp = ptr + L.nn_ptr_off[l];
         uint32_t* nrp = ptr + L.near_ptr_off[l];
         if ((rc = exclusive_scan_u32(nn_cnt, nnp, nl, P<uint32_t>(h.tmp), s))) return rc;
@@ -180,10 +259,18 @@ int build_lists(Handle& h)
             h.idx_pool = nb;
         }
         pni = l ? P<uint32_t>(h.idx_pool) + L.near_idx_off[l - 1] : nullptr;
-        launch(l, pnp, pni, nullptr, nullptr, nnp, P<uint32_t>(h.idx_pool) + L.nn_idx_off[l], nrp,
-               P<uint32_t>(h.idx_pool) + L.near_idx_off[l], 1);
+        launch(l, pnp, pni, pcap, nullptr, nullptr, nnp, P<uint32_t>(h.idx_pool) + L.nn_idx_off[l], L.nn_total[l],
+               nrp, P<uint32_t>(h.idx_pool) + L.near_idx_off[l], L.near_total[l], 1);
         h.launches += 8;
     }
+    // capacities for the next calls
+    L.nn_cap.resize(depth + 1);
+    L.near_cap.resize(depth + 1);
+    for (int l = 0; l <= depth; l++) {
+        L.nn_cap[l] = (uint32_t)(L.nn_total[l] + L.nn_total[l] / 4 + 256);
+        L.near_cap[l] = (uint32_t)(L.near_total[l] + L.near_total[l] / 4 + 256);
+    }
+    L.caps_depth = depth;
     TC_CUDA_TRY(cudaGetLastError());
     return record(h, 3);
 }

@@ -33,6 +33,8 @@ struct Lists {
     std::vector<uint32_t> nn_total, near_total;  // host copies of the totals
     std::vector<int64_t> nn_ptr_off, near_ptr_off;   // word offsets into ptr pool
     std::vector<int64_t> nn_idx_off, near_idx_off;   // word offsets into idx pool
+    std::vector<uint32_t> nn_cap, near_cap;          // region sizes of the fast build
+    int caps_depth = -1;
 };
 
 struct Handle {
@@ -51,7 +53,7 @@ struct Handle {
     // nodes
     Buf count, first, com64, m0, m2, bbc, bblen, comrel, m0r, m2t, loc, locfin, chunk, zwork, zloc, mu;
     // lists
-    Buf ptr_pool, idx_pool, cnt_tmp;
+    Buf ptr_pool, idx_pool, cnt_tmp, lstat;
     Lists lists;
     // scratch
     Buf tmp, err, zpart, dtotal, host_stage, sumtmp;

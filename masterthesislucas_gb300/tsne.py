@@ -21,7 +21,7 @@ from ._lib import check, lib, ptr
 class TSNE:
     def __init__(self, row_ptr, col, val, y0, *, early_exaggeration: float = 4.0, min_theta: float = 0.5,
                  max_theta: float = 0.5, max_children: int = 16, precision: str = "fp32", device: int = 0,
-                 learn_rate: float | None = None):
+                 learn_rate: float | None = None, order: int = 0, depth: int = -1):
         y0 = np.ascontiguousarray(y0, np.float64)
         self.n = len(y0)
         self.row_ptr = np.ascontiguousarray(row_ptr, np.uint32)
@@ -33,6 +33,8 @@ class TSNE:
         cfg.max_children = max_children
         cfg.theta = max_theta
         cfg.precision = {"fp32": _lib.TC_PREC_FP32, "fp64": _lib.TC_PREC_FP64}[precision]
+        cfg.order = order
+        cfg.depth = depth
         cfg.device = device
         self._t = ctypes.c_void_p()
         check(lib().tc_tsne_create(ctypes.byref(cfg), self.n, ptr(self.row_ptr), ptr(self.col), ptr(self.val),
