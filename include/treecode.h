@@ -193,6 +193,26 @@ int tc_mlp_gradient(tc_mlp* m, const float* d_x, const float* d_t, int64_t n, fl
 int tc_mlp_train(tc_mlp* m, const float* d_x, const float* d_t, int64_t n, int steps, int batch, float lr,
                  uint64_t seed, float* last_loss);
 int tc_mlp_forward(tc_mlp* m, const float* d_x, int64_t n, float* d_y);
+/* the same network as the list builder evaluates it: tensor-core BF16
+ * inputs and hidden activations, FP32 accumulation                         */
+int tc_mlp_forward_tc(tc_mlp* m, const float* d_x, int64_t n, float* d_y);
+
+/* Training data from a solved order-12 handle: for node pairs d_pairs (n x 3:
+ * level, sink index, source index within the level) the 16 features and
+ * log10 of the relative error of the pair's far field at orders 4..12
+ * against the direct sum over the source's particles.                    */
+int tc_lc_pair_errors(tc_handle* h, const int32_t* d_pairs, int64_t n, float* d_feat, float* d_err);
+/* Copy one level's interaction list (kind 0: accepted pairs, 1: near pairs)
+ * of the last update: CSR pointers (4^level + 1) and entries (*total).
+ * kind 2 (controller handles): the accepted pairs' order buckets 0..4
+ * (orders 4, 6, 8, 10, 12), one byte each, into idx.                      */
+int tc_get_list(tc_handle* h, int level, int kind, uint32_t* ptr, uint32_t* idx, int64_t* total);
+/* Replace the MAC of an FP32 order-12 handle by the controller m: every
+ * candidate pair is accepted at the lowest order in {4, 6, 8, 10, 12} whose
+ * predicted relative error is <= tau, else opened.  The weights are copied
+ * (later training of m does not change the handle); m == NULL switches back
+ * to the MAC.  The next update_tree rebuilds the lists.                   */
+int tc_set_controller(tc_handle* h, tc_mlp* m, double tau);
 
 /* ---------------------------------------------------------------- t-SNE step
  * The TSNE class around the solver (src/nBodyInstances/tsne.h:42-563),

@@ -65,6 +65,18 @@ SIGNATURES = {
     "tc_direct_device_noalloc": (_I, [_I, _D, _I, _P, _I64, _P, _I64, _P, _P, _P]),
     "tc_bh_solve": (_I, [_I, _D, _I, _D, _I, _P, _I64, _P, _P]),
     "tc_bh_solve_device": (_I, [_I, _D, _I, _D, _I, _P, _I64, _P, _P, _P]),
+    "tc_mlp_create": (_I, [ctypes.c_uint64, _P]),
+    "tc_mlp_destroy": (_I, [_P]),
+    "tc_mlp_set_normalization": (_I, [_P, _P, _P]),
+    "tc_mlp_get_params": (_I, [_P, _P, _P, _P]),
+    "tc_mlp_set_params": (_I, [_P, _P]),
+    "tc_mlp_gradient": (_I, [_P, _P, _P, _I64, _P, _P]),
+    "tc_mlp_train": (_I, [_P, _P, _P, _I64, _I, _I, ctypes.c_float, ctypes.c_uint64, _P]),
+    "tc_mlp_forward": (_I, [_P, _P, _I64, _P]),
+    "tc_mlp_forward_tc": (_I, [_P, _P, _I64, _P]),
+    "tc_lc_pair_errors": (_I, [_P, _P, _I64, _P, _P]),
+    "tc_get_list": (_I, [_P, _I, _I, _P, _P, _P]),
+    "tc_set_controller": (_I, [_P, _P, ctypes.c_double]),
     "tc_tsne_create": (_I, [_P, _I64, _P, _P, _P, _P, _P]),
     "tc_tsne_destroy": (_I, [_P]),
     "tc_tsne_set_theta": (_I, [_P, _D]),

@@ -16,123 +16,12 @@
 // + (2nu n_i + n_i(n_i-1)) D_(k-2e_i) + n_j(n_j-1) D_(k-2e_j)] for
 // phi = u^-nu, u = r^2 + c, n = k - e_i, obtained by differentiating
 // u grad(phi) = -2 nu R phi.
+#include "expansion.cuh"
 #include "kernels.cuh"
 #include "state.cuh"
 
 namespace tc {
 namespace {
-
-__host__ __device__ constexpr int ncoef(int p) { return (p + 1) * (p + 2) / 2; }
-__host__ __device__ constexpr int cidx(int a, int b) { return (a + b) * (a + b + 1) / 2 + b; }
-// coefficient arrays are padded to 16 bytes per node for vector loads
-__host__ __device__ constexpr int kstride(int p) { return (ncoef(p) + 3) & ~3; }
-// total degree of the coefficient with linear index i
-__host__ __device__ constexpr int cdeg(int i)
-{
-    int k = 0;
-    while ((k + 1) * (k + 2) / 2 <= i) k++;
-    return k;
-}
-
-struct PotParams {
-    float nu;    // phi = pref * u^-nu
-    float c;     // u = r^2 + c (before scaling)
-    float kappa; // pair term t = kappa * phi
-    int kind;    // TC_KERNEL_*
-};
-
-// scaled derivatives D_g, |g| <= P, at scaled offset (x, y) for a level of size h
-template <int P>
-__device__ inline void derivs(float x, float y, float h, const PotParams& pp, float* D)
-{
-    const float c = pp.c / (h * h);
-    const float u = x * x + y * y + c;
-    const float iu = __fdividef(1.0f, u);
-    // pref * h^-2nu * u^-nu (scaled potential)
-    if (pp.kind == TC_KERNEL_GRAVITY)
-        D[0] = rsqrtf(u) / h;
-    else
-        D[0] = -0.5f * iu / (h * h);
-    const float nu2 = 2.0f * pp.nu;
-#pragma unroll
-    for (int k = 1; k <= P; k++) {
-#pragma unroll
-        for (int b = 0; b <= k; b++) {
-            const int a = k - b;
-            float t;
-            if (a >= 1) {
-                t = (nu2 + 2.0f * (a - 1)) * x * D[cidx(a - 1, b)];
-                if (b >= 1) t += 2.0f * b * y * D[cidx(a, b - 1)];
-                if (a >= 2) t += (nu2 * (a - 1) + (float)((a - 1) * (a - 2))) * D[cidx(a - 2, b)];
-                if (b >= 2) t += (float)(b * (b - 1)) * D[cidx(a, b - 2)];
-            } else {
-                t = (nu2 + 2.0f * (b - 1)) * y * D[cidx(0, b - 1)];
-                if (b >= 2) t += (nu2 * (b - 1) + (float)((b - 1) * (b - 2))) * D[cidx(0, b - 2)];
-            }
-            D[cidx(a, b)] = -t * iu;
-        }
-    }
-}
-
-// monomials w_g = d^g / g! for |g| <= Q
-template <int Q>
-__device__ inline void monomials(float dx, float dy, float* w)
-{
-    w[0] = 1.0f;
-#pragma unroll
-    for (int k = 1; k <= Q; k++) {
-#pragma unroll
-        for (int b = 0; b <= k; b++) {
-            const int a = k - b;
-            if (a >= 1)
-                w[cidx(a, b)] = w[cidx(a - 1, b)] * dx * (1.0f / a);
-            else
-                w[cidx(a, b)] = w[cidx(a, b - 1)] * dy * (1.0f / b);
-        }
-    }
-}
-
-// acc_a += sum_{b <= a} in_b * w_(a-b)       (M2M: mu(parent) from mu(child))
-template <int P>
-__device__ inline void shift_up(const float* in, const float* w, float* acc)
-{
-#pragma unroll
-    for (int ka = 0; ka <= P; ka++)
-#pragma unroll
-        for (int ba = 0; ba <= ka; ba++) {
-            const int aa = ka - ba;
-            float s = 0.f;
-#pragma unroll
-            for (int kb = 0; kb <= ka; kb++)
-#pragma unroll
-                for (int bb = 0; bb <= kb; bb++) {
-                    const int ab = kb - bb;
-                    if (ab <= aa && bb <= ba) s += in[cidx(ab, bb)] * w[cidx(aa - ab, ba - bb)];
-                }
-            acc[cidx(aa, ba)] += s;
-        }
-}
-
-// acc_b += sum_{g >= b} in_g * w_(g-b)       (L2L: local at d from local at 0)
-template <int P>
-__device__ inline void shift_down(const float* in, const float* w, float* acc)
-{
-#pragma unroll
-    for (int kb = 0; kb <= P; kb++)
-#pragma unroll
-        for (int bb = 0; bb <= kb; bb++) {
-            const int ab = kb - bb;
-            float s = 0.f;
-#pragma unroll
-            for (int kg = kb; kg <= P; kg++)
-#pragma unroll
-                for (int bg = 0; bg <= kg; bg++) {
-                    const int ag = kg - bg;
-                    if (ag >= ab && bg >= bb) s += in[cidx(ag, bg)] * w[cidx(ag - ab, bg - bb)];
-                }
-            acc[cidx(ab, bb)] += s;
-        }
-}
 
 // ------------------------------------------------------------------ P2M
 // one warp per leaf: mu_a = sum (r/h)^a / a! about the COM
@@ -212,14 +101,20 @@ __global__ void __launch_bounds__(128) k_m2m(int l, float hl, const uint32_t* __
 // ------------------------------------------------------------------ M2L
 // one thread per sink node A of level l: L(A) = sum over nn(A) of M2L; also
 // the far-field pair sum kappa * sum_b L_b mu_b(A)
-template <int P>
+// P: order of this launch; PS: storage order of mu/loc (the solve order).
+// ord/bucket select the entries of one controller order bucket (ord NULL: all);
+// write != 0 stores every coefficient of the node (zeros above order P),
+// otherwise the launch adds its contribution.
+template <int P, int PS>
 __global__ void __launch_bounds__(128) k_m2l_p(int l, float hl, PotParams pp, const uint32_t* __restrict__ nn_ptr,
-                                               const uint32_t* __restrict__ nn_idx, const uint32_t* __restrict__ count,
+                                               const uint32_t* __restrict__ nn_idx, const uint8_t* __restrict__ ord,
+                                               int bucket, int write, const uint32_t* __restrict__ count,
                                                const float* __restrict__ comrel, const float* __restrict__ mu,
                                                float* __restrict__ loc, double* __restrict__ zpart)
 {
     constexpr int K = ncoef(P);
     constexpr int KS = kstride(P);
+    constexpr int KSS = kstride(PS);
     const uint32_t li = level_index(l);
     const int64_t nl = (int64_t)1 << (2 * l);
     const float ih = 1.0f / hl;
@@ -234,13 +129,14 @@ __global__ void __launch_bounds__(128) k_m2l_p(int l, float hl, PotParams pp, co
             const int iax = (int)compact16((uint32_t)a), iay = (int)compact16((uint32_t)a >> 1);
             const float cax = comrel[2 * na], cay = comrel[2 * na + 1];
             for (uint32_t e = b0; e < b1; e++) {
+                if (ord && ord[e] != bucket) continue;
                 const uint32_t b = nn_idx[e];
                 const int64_t nb = li + b;
                 const float Rx = (float)(iax - (int)compact16(b)) + (cax - comrel[2 * nb]) * ih;
                 const float Ry = (float)(iay - (int)compact16(b >> 1)) + (cay - comrel[2 * nb + 1]) * ih;
                 float D[K];
                 derivs<P>(Rx, Ry, hl, pp, D);
-                const float4* m4 = reinterpret_cast<const float4*>(mu + nb * KS);
+                const float4* m4 = reinterpret_cast<const float4*>(mu + nb * KSS);
 #pragma unroll
                 for (int c = 0; c < KS / 4; c++) {
                     const float4 q = __ldg(m4 + c);
@@ -263,22 +159,35 @@ __global__ void __launch_bounds__(128) k_m2l_p(int l, float hl, PotParams pp, co
         }
         double z = 0.0;
         if (b0 != b1) {
-            const float* m = mu + na * KS;
+            const float* m = mu + na * KSS;
             float zs = 0.f;
 #pragma unroll
             for (int k = 0; k < K; k++) zs += L[k] * m[k];
             z = (double)pp.kappa * (double)zs;
         }
-        zpart[na] = z;
-        float4* o4 = reinterpret_cast<float4*>(loc + na * KS);
+        float4* o4 = reinterpret_cast<float4*>(loc + na * KSS);
+        if (write) {
+            zpart[na] = z;
 #pragma unroll
-        for (int c = 0; c < KS / 4; c++) {
-            float4 v;
-            v.x = 4 * c + 0 < K ? L[4 * c + 0] : 0.f;
-            v.y = 4 * c + 1 < K ? L[4 * c + 1] : 0.f;
-            v.z = 4 * c + 2 < K ? L[4 * c + 2] : 0.f;
-            v.w = 4 * c + 3 < K ? L[4 * c + 3] : 0.f;
-            o4[c] = v;
+            for (int c = 0; c < KSS / 4; c++) {
+                float4 v;
+                v.x = 4 * c + 0 < K ? L[4 * c + 0] : 0.f;
+                v.y = 4 * c + 1 < K ? L[4 * c + 1] : 0.f;
+                v.z = 4 * c + 2 < K ? L[4 * c + 2] : 0.f;
+                v.w = 4 * c + 3 < K ? L[4 * c + 3] : 0.f;
+                o4[c] = v;
+            }
+        } else if (b0 != b1) {
+            zpart[na] += z;
+#pragma unroll
+            for (int c = 0; c < KS / 4; c++) {
+                float4 v = o4[c];
+                v.x += 4 * c + 0 < K ? L[4 * c + 0] : 0.f;
+                v.y += 4 * c + 1 < K ? L[4 * c + 1] : 0.f;
+                v.z += 4 * c + 2 < K ? L[4 * c + 2] : 0.f;
+                v.w += 4 * c + 3 < K ? L[4 * c + 3] : 0.f;
+                o4[c] = v;
+            }
         }
     }
 }
@@ -500,11 +409,9 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
     const float* comrel = P<float>(h.comrel);
     const uint32_t* count = P<uint32_t>(h.count);
     auto hl = [&](int l) { return (float)(h.L / (double)(1u << l)); };
-    k_p2m<ORD><<<grid_for(nleaf * 32, 128, kSMs * 64), 128, 0, s>>>(dep, hl(dep), count, P<uint32_t>(h.first), comrel,
-                                                                 P<float>(h.prel), mu);
-    for (int l = dep - 1; l >= 0; l--) {
-        const int64_t nl = (int64_t)1 << (2 * l);
-        k_m2m<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, mu);
+    if (h.mu_stride != kstride(ORD)) {
+        tc_set_error("order-p solve: multipoles of another order (update the tree first)");
+        return TC_ERR_STATE;
     }
     TC_CUDA_TRY(cudaMemsetAsync(loc, 0, kstride(ORD) * 4, s));
     TC_CUDA_TRY(cudaMemsetAsync(zp, 0, nn * 8, s));
@@ -513,8 +420,26 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
     const uint32_t* idx = P<uint32_t>(h.idx_pool);
     for (int l = 1; l <= dep; l++) {
         const int64_t nl = (int64_t)1 << (2 * l);
-        k_m2l_p<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, ptr + h.lists.nn_ptr_off[l],
-                                                     idx + h.lists.nn_idx_off[l], count, comrel, mu, loc, zp);
+        const uint32_t* np_ = ptr + h.lists.nn_ptr_off[l];
+        const uint32_t* ni_ = idx + h.lists.nn_idx_off[l];
+        bool bucketed = false;
+        if constexpr (ORD == 12) {
+            // controller lists: one launch per order bucket, the first writes every node
+            if (h.ctrl_on) {
+                const uint8_t* od = P<uint8_t>(h.ord_pool) + h.lists.nn_idx_off[l];
+                const int g = grid_for(nl, 128);
+                k_m2l_p<4, 12><<<g, 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, 0, 1, count, comrel, mu, loc, zp);
+                k_m2l_p<6, 12><<<g, 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, 1, 0, count, comrel, mu, loc, zp);
+                k_m2l_p<8, 12><<<g, 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, 2, 0, count, comrel, mu, loc, zp);
+                k_m2l_p<10, 12><<<g, 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, 3, 0, count, comrel, mu, loc, zp);
+                k_m2l_p<12, 12><<<g, 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, 4, 0, count, comrel, mu, loc, zp);
+                h.launches += 4;
+                bucketed = true;
+            }
+        }
+        if (!bucketed)
+            k_m2l_p<ORD, ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, nullptr, 0, 1, count, comrel,
+                                                               mu, loc, zp);
     }
     for (int l = 1; l <= dep; l++) {
         const int64_t nl = (int64_t)1 << (2 * l);
@@ -534,9 +459,34 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
     if ((rc = ensure(h.sumtmp, sum_tmp_doubles() * 8)) ||
         (rc = sum_f64(zp, nn, P<double>(h.zwork), chunk_ptr + nleaf, d_total, 1, P<double>(h.sumtmp), s)))
         return rc;
-    h.launches += 4 + 3 * dep + 5;
+    h.launches += 3 + 2 * dep + 5;
     TC_CUDA_TRY(cudaGetLastError());
     return record(h, 7);
+}
+
+template <int ORD>
+int multipoles_p(Handle& h)
+{
+    cudaStream_t s = h.stream;
+    const int dep = h.depth;
+    const int64_t nn = h.nnodes;
+    const int64_t nleaf = (int64_t)1 << (2 * dep);
+    int rc;
+    if ((rc = ensure(h.mu, nn * kstride(ORD) * 4))) return rc;
+    float* mu = P<float>(h.mu);
+    const float* comrel = P<float>(h.comrel);
+    const uint32_t* count = P<uint32_t>(h.count);
+    auto hl = [&](int l) { return (float)(h.L / (double)(1u << l)); };
+    k_p2m<ORD><<<grid_for(nleaf * 32, 128, kSMs * 64), 128, 0, s>>>(dep, hl(dep), count, P<uint32_t>(h.first), comrel,
+                                                                 P<float>(h.prel), mu);
+    for (int l = dep - 1; l >= 0; l--) {
+        const int64_t nl = (int64_t)1 << (2 * l);
+        k_m2m<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, mu);
+    }
+    h.launches += 1 + dep;
+    h.mu_stride = kstride(ORD);
+    TC_CUDA_TRY(cudaGetLastError());
+    return TC_OK;
 }
 
 template <int P>
@@ -557,6 +507,21 @@ int dispatch_kernel(Handle& h, double* d_grad, int accumulate, int scatter, doub
 }
 
 }  // namespace
+
+int build_multipoles(Handle& h)
+{
+    switch (h.cfg.order) {
+    case 3: return multipoles_p<3>(h);
+    case 4: return multipoles_p<4>(h);
+    case 6: return multipoles_p<6>(h);
+    case 8: return multipoles_p<8>(h);
+    case 10: return multipoles_p<10>(h);
+    case 12: return multipoles_p<12>(h);
+    default:
+        tc_set_error("unsupported expansion order %d (3, 4, 6, 8, 10, 12)", h.cfg.order);
+        return TC_ERR_INVALID;
+    }
+}
 
 int solve_fmm_order(Handle& h, double* d_grad, double* d_total, int accumulate, int scatter)
 {

@@ -17,6 +17,8 @@
 // near(parent), the lists hold exactly the reference's visited pairs.  The
 // MAC is evaluated in FP64 from the bit-exact COMs, so the decisions are the
 // reference's decisions.
+#include "controller.cuh"
+#include "ctrl_mma.cuh"
 #include "state.cuh"
 
 namespace tc {
@@ -112,6 +114,167 @@ __global__ void k_lists(int l, double inv_theta, real hl, const uint32_t* __rest
     }
 }
 
+// ---------------------------------------------------------------- controller
+// The learned order controller replaces the MAC: every candidate pair (the
+// non-empty children of a near pair of the parent level) is given to the MLP,
+// which predicts log10 of the pair's relative far-field error at orders
+// 4, 6, 8, 10, 12; the pair is accepted at the lowest order whose prediction
+// is below log10(tau), and opened (near list) when none is.  Self pairs and
+// pairs whose RMS spreads overlap ((s_A + s_B)/|R| >= 0.9) are opened without
+// evaluating the network.
+//
+// The network runs on the tensor cores (ctrl_mma.cuh), one warp per 32
+// candidates.  The count pass stores each candidate's decision (one byte per
+// (parent near entry, child slot, sibling)); the fill pass only reads them.
+
+// per-node features for the controller (all levels; empty nodes skipped)
+__global__ void k_node_feat(int depth, double L, const uint32_t* __restrict__ count, const float* __restrict__ comrel,
+                            const float* __restrict__ mu, int mu_stride, float4* __restrict__ nfeat, int64_t nnodes)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nnodes; i += (int64_t)gridDim.x * blockDim.x) {
+        if (count[i] == 0) continue;
+        int l = 0;
+        while (l < depth && i >= (int64_t)level_index(l + 1)) l++;
+        const float ih = (float)((double)(1u << l) / L);
+        float nf[kNodeFeat];
+        node_features(mu + i * (int64_t)mu_stride, comrel[2 * i] * ih, comrel[2 * i + 1] * ih, nf);
+        nfeat[2 * i] = make_float4(nf[0], nf[1], nf[2], nf[3]);
+        nfeat[2 * i + 1] = make_float4(nf[4], nf[5], nf[6], nf[7]);
+    }
+}
+
+// Count pass: one lane per node of level l >= 1 (warps of 32 consecutive
+// nodes); lanes step through their candidates together and the warp runs the
+// network whenever one of its lanes needs it.  dec[16 e + 4 j + (a & 3)] holds
+// the decision for child j of parent near entry e: order bucket or kOpen.
+__global__ void __launch_bounds__(32 * ctrl::kWarps) k_lists_ctrl_count(
+    int l, float hl, float c_over_h2, const uint32_t* __restrict__ count, const float* __restrict__ comrel,
+    const float4* __restrict__ nfeat, const uint32_t* __restrict__ pnear_ptr, const uint32_t* __restrict__ pnear_idx,
+    uint32_t pcap, uint32_t* __restrict__ nn_cnt, uint32_t* __restrict__ near_cnt, uint8_t* __restrict__ dec,
+    const float* __restrict__ wctrl, float log_tau)
+{
+    __shared__ __align__(16) ctrl::Smem S;
+    ctrl::load_weights(S, wctrl, wctrl + TC_MLP_NPARAM, wctrl + TC_MLP_NPARAM + TC_MLP_IN);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t np = 1u << (2 * (l - 1));
+    const uint32_t li = level_index(l);
+    const int64_t nl = (int64_t)1 << (2 * l);
+    const float ih = 1.0f / hl;
+    const int64_t nwarps = (int64_t)gridDim.x * ctrl::kWarps;
+    for (int64_t base = ((int64_t)blockIdx.x * ctrl::kWarps + wid) * 32; base < nl; base += nwarps * 32) {
+        const int64_t a = base + lane;
+        bool active = a < nl && count[li + a] != 0;
+        uint32_t e = 0, e1 = 0, j = 0, nn = 0, nr = 0;
+        int iax = 0, iay = 0;
+        float cax = 0.f, cay = 0.f;
+        float nfA[kNodeFeat];
+        if (active) {
+            const uint32_t p = (uint32_t)(a >> 2);
+            e = pnear_ptr[p];
+            e1 = pnear_ptr[p + 1] < pcap ? pnear_ptr[p + 1] : pcap;
+            iax = (int)compact16((uint32_t)a);
+            iay = (int)compact16((uint32_t)a >> 1);
+            cax = comrel[2 * (li + a)] * ih;
+            cay = comrel[2 * (li + a) + 1] * ih;
+            const float4 n0 = nfeat[2 * (li + a)], n1 = nfeat[2 * (li + a) + 1];
+            nfA[0] = n0.x, nfA[1] = n0.y, nfA[2] = n0.z, nfA[3] = n0.w;
+            nfA[4] = n1.x, nfA[5] = n1.y, nfA[6] = n1.z, nfA[7] = n1.w;
+        }
+        while (__any_sync(0xffffffffu, active)) {
+            // this lane's next non-empty candidate
+            bool have = false;
+            uint32_t b = 0, slot = 0;
+            while (active) {
+                if (e >= e1) {
+                    active = false;
+                    break;
+                }
+                const uint32_t bp = pnear_idx[e];
+                const uint32_t jj = j, ee = e;
+                if (++j == 4) {
+                    j = 0;
+                    e++;
+                }
+                if (bp >= np) continue;  // only after an overflowed parent level
+                b = 4 * bp + jj;
+                if (count[li + b] == 0) continue;
+                slot = 16u * ee + 4u * jj + (uint32_t)(a & 3);
+                have = true;
+                break;
+            }
+            float f[TC_MLP_IN];
+            bool use = false;
+            if (have && b != (uint32_t)a) {
+                const float cbx = comrel[2 * (li + b)] * ih, cby = comrel[2 * (li + b) + 1] * ih;
+                const float Rx = (float)(iax - (int)compact16(b)) + (cax - cbx);
+                const float Ry = (float)(iay - (int)compact16(b >> 1)) + (cay - cby);
+                const float4 n0 = nfeat[2 * (li + b)], n1 = nfeat[2 * (li + b) + 1];
+                const float nfB[kNodeFeat] = {n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, n1.z, n1.w};
+                pair_features_nf(Rx, Ry, nfA, nfB, c_over_h2, l, f);
+                use = f[4] < 0.9f;
+            }
+            int d = -1;
+            if (__any_sync(0xffffffffu, use)) {
+                float y[TC_MLP_OUT];
+                ctrl::warp_mlp(S, wid, lane, f, use, y);
+                if (use)
+                    for (int o = TC_MLP_OUT - 1; o >= 0; o--)
+                        if (y[o] <= log_tau) d = o;
+            }
+            if (have) {
+                dec[slot] = d >= 0 ? (uint8_t)d : ctrl::kOpen;
+                if (d >= 0) nn++;
+                else nr++;
+            }
+        }
+        if (a < nl) {
+            nn_cnt[a] = nn;
+            near_cnt[a] = nr;
+        }
+    }
+}
+
+// Fill pass: one thread per node; the decisions of the count pass.
+__global__ void k_lists_ctrl_fill(int l, const uint32_t* __restrict__ count, const uint32_t* __restrict__ pnear_ptr,
+                                  const uint32_t* __restrict__ pnear_idx, uint32_t pcap, const uint8_t* __restrict__ dec,
+                                  const uint32_t* __restrict__ nn_ptr, uint32_t* __restrict__ nn_idx,
+                                  uint8_t* __restrict__ nn_ord, uint32_t nn_cap, const uint32_t* __restrict__ near_ptr,
+                                  uint32_t* __restrict__ near_idx, uint32_t near_cap, uint32_t* __restrict__ ovf)
+{
+    const uint32_t np = 1u << (2 * (l - 1));
+    const uint32_t li = level_index(l);
+    const int64_t nl = (int64_t)1 << (2 * l);
+    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < nl; a += (int64_t)gridDim.x * blockDim.x) {
+        if (count[li + a] == 0) continue;
+        const uint32_t p = (uint32_t)(a >> 2);
+        uint32_t nn = nn_ptr[a], nr = near_ptr[a];
+        const uint32_t pe1 = pnear_ptr[p + 1] < pcap ? pnear_ptr[p + 1] : pcap;
+        for (uint32_t e = pnear_ptr[p]; e < pe1; e++) {
+            const uint32_t bp = pnear_idx[e];
+            if (bp >= np) continue;
+            for (uint32_t j = 0; j < 4; j++) {
+                const uint32_t b = 4 * bp + j;
+                if (count[li + b] == 0) continue;
+                const uint8_t d = dec[16u * e + 4u * j + (uint32_t)(a & 3)];
+                if (d != ctrl::kOpen) {
+                    if (nn < nn_cap) {
+                        nn_idx[nn] = b;
+                        nn_ord[nn] = d;
+                    } else {
+                        atomicOr(ovf, 1u);
+                    }
+                    nn++;
+                } else {
+                    if (nr < near_cap) near_idx[nr] = b;
+                    else atomicOr(ovf, 1u);
+                    nr++;
+                }
+            }
+        }
+    }
+}
+
 // per-level list totals (last entries of the CSR pointer arrays)
 __global__ void k_list_totals(const uint32_t* __restrict__ ptr, const int64_t* __restrict__ offs, int nlev,
                               uint32_t* __restrict__ out)
@@ -157,10 +320,25 @@ int build_lists(Handle& h)
     uint32_t* ovf_flag = P<uint32_t>(h.err) + 1;
     auto launch = [&](int l, const uint32_t* pnp, const uint32_t* pni, uint32_t pcap, uint32_t* nnc, uint32_t* nrc,
                       const uint32_t* nnp, uint32_t* nni, uint32_t nncap, const uint32_t* nrp, uint32_t* nri,
-                      uint32_t nrcap, int fill) {
+                      uint32_t nrcap, int fill) -> int {
         const int64_t nl = (int64_t)1 << (2 * l);
         const double hl = h.L / (double)(1u << l);
-        if (h.cfg.precision == TC_PREC_FP64)
+        if (h.ctrl_on && l > 0) {
+            if (!fill) {
+                int rc2 = ensure(h.dec, (size_t)pcap * 16 + 64);
+                if (rc2) return rc2;
+                k_lists_ctrl_count<<<grid_for(nl, 32 * ctrl::kWarps, kSMs * 16), 32 * ctrl::kWarps, 0, s>>>(
+                    l, (float)hl, (float)(h.ctrl_c / (hl * hl)), P<uint32_t>(h.count), P<float>(h.comrel),
+                    P<float4>(h.nfeat), pnp, pni, pcap, nnc, nrc, P<uint8_t>(h.dec), P<float>(h.ctrl_w),
+                    h.ctrl_log_tau);
+            } else {
+                // nni points into the index pool; the order of entry i sits at byte i of the order pool
+                uint8_t* ordp = P<uint8_t>(h.ord_pool) + (nni - P<uint32_t>(h.idx_pool));
+                k_lists_ctrl_fill<<<grid_for(nl, 128), 128, 0, s>>>(l, P<uint32_t>(h.count), pnp, pni, pcap,
+                                                                    P<uint8_t>(h.dec), nnp, nni, ordp, nncap, nrp,
+                                                                    nri, nrcap, ovf_flag);
+            }
+        } else if (h.cfg.precision == TC_PREC_FP64)
             k_lists<double><<<grid_for(nl, 128), 128, 0, s>>>(l, inv_theta, hl, P<uint32_t>(h.count),
                                                              P<double2>(h.com64), P<double>(h.comrel),
                                                              P<double>(h.bblen), pnp, pni, pcap, nnc, nrc, nnp, nni,
@@ -170,7 +348,19 @@ int build_lists(Handle& h)
                                                             P<double2>(h.com64), P<float>(h.comrel),
                                                             P<double>(h.bblen), pnp, pni, pcap, nnc, nrc, nnp, nni,
                                                             nncap, nrp, nri, nrcap, ovf_flag, fill);
+        return 0;
     };
+    if (h.ctrl_on) {
+        if (h.mu_stride < 45) {  // the features read multipoles up to order 8
+            tc_set_error("controller: the handle's multipoles are below order 8");
+            return TC_ERR_STATE;
+        }
+        if ((rc = ensure(h.nfeat, (size_t)h.nnodes * 32))) return rc;
+        k_node_feat<<<grid_for(h.nnodes, 256), 256, 0, s>>>(depth, h.L, P<uint32_t>(h.count), P<float>(h.comrel),
+                                                             P<float>(h.mu), h.mu_stride, P<float4>(h.nfeat),
+                                                             h.nnodes);
+        h.launches++;
+    }
     uint32_t* ovf = P<uint32_t>(h.err) + 1;
     TC_CUDA_TRY(cudaMemsetAsync(ovf, 0, 4, s));
     // Fast mode: per-level regions sized from the last exact totals (x1.25),
@@ -186,18 +376,21 @@ int build_lists(Handle& h)
             words += L.near_cap[l];
         }
         if ((rc = ensure(h.idx_pool, (size_t)words * 4 + 64))) return rc;
+        if (h.ctrl_on && (rc = ensure(h.ord_pool, h.idx_pool.bytes / 4 + 64))) return rc;
         for (int l = 0; l <= depth; l++) {
             const int64_t nl = (int64_t)1 << (2 * l);
             const uint32_t* pnp = l ? ptr + L.near_ptr_off[l - 1] : nullptr;
             const uint32_t* pni = l ? P<uint32_t>(h.idx_pool) + L.near_idx_off[l - 1] : nullptr;
             const uint32_t pcap = l ? L.near_cap[l - 1] : 0u;
-            launch(l, pnp, pni, pcap, nn_cnt, near_cnt, nullptr, nullptr, 0, nullptr, nullptr, 0, 0);
+            if ((rc = launch(l, pnp, pni, pcap, nn_cnt, near_cnt, nullptr, nullptr, 0, nullptr, nullptr, 0, 0)))
+                return rc;
             uint32_t* nnp = ptr + L.nn_ptr_off[l];
             uint32_t* nrp = ptr + L.near_ptr_off[l];
             if ((rc = exclusive_scan_u32(nn_cnt, nnp, nl, P<uint32_t>(h.tmp), s))) return rc;
             if ((rc = exclusive_scan_u32(near_cnt, nrp, nl, P<uint32_t>(h.tmp), s))) return rc;
-            launch(l, pnp, pni, pcap, nullptr, nullptr, nnp, P<uint32_t>(h.idx_pool) + L.nn_idx_off[l], L.nn_cap[l],
-                   nrp, P<uint32_t>(h.idx_pool) + L.near_idx_off[l], L.near_cap[l], 1);
+            if ((rc = launch(l, pnp, pni, pcap, nullptr, nullptr, nnp, P<uint32_t>(h.idx_pool) + L.nn_idx_off[l],
+                             L.nn_cap[l], nrp, P<uint32_t>(h.idx_pool) + L.near_idx_off[l], L.near_cap[l], 1)))
+                return rc;
             h.launches += 8;
         }
         // totals of every level plus the overflow flag, in one round trip
@@ -234,7 +427,7 @@ int build_lists(Handle& h)
         const uint32_t* pnp = l ? ptr + L.near_ptr_off[l - 1] : nullptr;
         const uint32_t* pni = l ? P<uint32_t>(h.idx_pool) + L.near_idx_off[l - 1] : nullptr;
         const uint32_t pcap = l ? L.near_total[l - 1] : 0u;
-        launch(l, pnp, pni, pcap, nn_cnt, near_cnt, nullptr, nullptr, 0, nullptr, nullptr, 0, 0);
+        if ((rc = launch(l, pnp, pni, pcap, nn_cnt, near_cnt, nullptr, nullptr, 0, nullptr, nullptr, 0, 0))) return rc;
         uint32_t* nnp = ptr + L.nn_ptr_off[l];
         uint32_t* nrp = ptr + L.near_ptr_off[l];
         if ((rc = exclusive_scan_u32(nn_cnt, nnp, nl, P<uint32_t>(h.tmp), s))) return rc;
@@ -258,9 +451,19 @@ int build_lists(Handle& h)
             release(h.idx_pool);
             h.idx_pool = nb;
         }
+        if (h.ctrl_on && h.ord_pool.bytes < h.idx_pool.bytes / 4 + 64) {
+            Buf nb;
+            if ((rc = ensure(nb, h.idx_pool.bytes / 4 + 64))) return rc;
+            if (h.ord_pool.p && L.nn_idx_off[l] > 0)
+                TC_CUDA_TRY(cudaMemcpyAsync(nb.p, h.ord_pool.p, L.nn_idx_off[l], cudaMemcpyDeviceToDevice, s));
+            TC_CUDA_TRY(cudaStreamSynchronize(s));
+            release(h.ord_pool);
+            h.ord_pool = nb;
+        }
         pni = l ? P<uint32_t>(h.idx_pool) + L.near_idx_off[l - 1] : nullptr;
-        launch(l, pnp, pni, pcap, nullptr, nullptr, nnp, P<uint32_t>(h.idx_pool) + L.nn_idx_off[l], L.nn_total[l],
-               nrp, P<uint32_t>(h.idx_pool) + L.near_idx_off[l], L.near_total[l], 1);
+        if ((rc = launch(l, pnp, pni, pcap, nullptr, nullptr, nnp, P<uint32_t>(h.idx_pool) + L.nn_idx_off[l],
+                         L.nn_total[l], nrp, P<uint32_t>(h.idx_pool) + L.near_idx_off[l], L.near_total[l], 1)))
+            return rc;
         h.launches += 8;
     }
     // capacities for the next calls

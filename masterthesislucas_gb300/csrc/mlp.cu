@@ -14,6 +14,7 @@
 #include <cmath>
 #include <vector>
 
+#include "ctrl_mma.cuh"
 #include "state.cuh"
 
 namespace tc {
@@ -212,6 +213,29 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const float* __restrict__ w
     }
 }
 
+// the list builder's tensor-core forward (BF16 inputs and activations), for tests
+__global__ void __launch_bounds__(32 * ctrl::kWarps) k_mlp_forward_tc(const float* __restrict__ wr,
+                                                                     const float* __restrict__ mean,
+                                                                     const float* __restrict__ stdv,
+                                                                     const float* __restrict__ X, int64_t n,
+                                                                     float* __restrict__ Y)
+{
+    __shared__ __align__(16) ctrl::Smem S;
+    ctrl::load_weights(S, wr, mean, stdv);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t nwarps = (int64_t)gridDim.x * ctrl::kWarps;
+    for (int64_t base = ((int64_t)blockIdx.x * ctrl::kWarps + wid) * 32; base < n; base += nwarps * 32) {
+        const int64_t r = base + lane;
+        float f[NI], y[NO];
+        const bool use = r < n;
+        for (int k = 0; k < NI; k++) f[k] = use ? X[r * NI + k] : 0.f;
+        ctrl::warp_mlp(S, wid, lane, f, use, y);
+        if (use)
+            for (int k = 0; k < NO; k++) Y[r * NO + k] = y[k];
+    }
+}
+
 }  // namespace
 }  // namespace tc
 
@@ -303,6 +327,50 @@ int tc_mlp_set_params(tc_mlp* m, const float* params)
     TC_CUDA_TRY(cudaMemcpy(m->master.p, params, NP * 4, cudaMemcpyHostToDevice));
     k_round_params<<<grid_for(NP, 256), 256>>>(P<float>(m->master), P<float>(m->rounded));
     TC_CUDA_TRY(cudaDeviceSynchronize());
+    return TC_OK;
+}
+
+int tc_mlp_forward_tc(tc_mlp* m, const float* d_x, int64_t n, float* d_y)
+{
+    if (!m || !d_x || !d_y || n <= 0) return TC_ERR_INVALID;
+    const int64_t blocks = (n + 32 * ctrl::kWarps - 1) / (32 * ctrl::kWarps);
+    k_mlp_forward_tc<<<(unsigned)(blocks < kSMs * 16 ? blocks : kSMs * 16), 32 * ctrl::kWarps>>>(
+        P<float>(m->rounded), P<float>(m->mean), P<float>(m->stdv), d_x, n, d_y);
+    TC_CUDA_TRY(cudaGetLastError());
+    TC_CUDA_TRY(cudaDeviceSynchronize());
+    return TC_OK;
+}
+
+int tc_set_controller(tc_handle* t, tc_mlp* m, double tau)
+{
+    if (!t) return TC_ERR_INVALID;
+    Handle& h = t->h;
+    TC_CUDA_TRY(cudaSetDevice(h.cfg.device));
+    if (!m) {  // back to the MAC
+        h.ctrl_on = false;
+        h.tree_ready = false;
+        return TC_OK;
+    }
+    if (!(tau > 0.0) || !(tau < 1.0)) {
+        tc_set_error("tc_set_controller: tau must lie in (0, 1)");
+        return TC_ERR_INVALID;
+    }
+    if (h.cfg.order != 12 || h.cfg.precision != TC_PREC_FP32) {
+        tc_set_error("tc_set_controller: needs an FP32 order-12 handle");
+        return TC_ERR_INVALID;
+    }
+    int rc;
+    if ((rc = ensure(h.ctrl_w, (NP + 2 * NI) * 4 + 64))) return rc;
+    TC_CUDA_TRY(cudaMemcpyAsync(h.ctrl_w.p, m->rounded.p, NP * 4, cudaMemcpyDeviceToDevice, h.stream));
+    TC_CUDA_TRY(cudaMemcpyAsync(P<float>(h.ctrl_w) + NP, m->mean.p, NI * 4, cudaMemcpyDeviceToDevice, h.stream));
+    TC_CUDA_TRY(cudaMemcpyAsync(P<float>(h.ctrl_w) + NP + NI, m->stdv.p, NI * 4, cudaMemcpyDeviceToDevice, h.stream));
+    TC_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    h.ctrl_on = true;
+    h.ctrl_log_tau = (float)std::log10(tau);
+    h.ctrl_c = h.cfg.kernel == TC_KERNEL_GRAVITY ? h.cfg.softening * h.cfg.softening : 1.0;
+    // the lists (and their capacities) change with the acceptance rule
+    h.tree_ready = false;
+    h.lists.caps_depth = -1;
     return TC_OK;
 }
 

@@ -53,7 +53,13 @@ struct Handle {
     // nodes
     Buf count, first, com64, m0, m2, bbc, bblen, comrel, m0r, m2t, loc, locfin, chunk, zwork, zloc, mu;
     // lists
-    Buf ptr_pool, idx_pool, cnt_tmp, lstat;
+    Buf ptr_pool, idx_pool, cnt_tmp, lstat, ord_pool, nfeat, dec;
+    // learned order controller (order-p mode): weights + normalisation copy
+    bool ctrl_on = false;
+    float ctrl_log_tau = -4.f;
+    double ctrl_c = 0.0;      // kernel constant c of u = r^2 + c
+    Buf ctrl_w;
+    int mu_stride = 0;        // floats per node of mu (kstride of the solve order)
     Lists lists;
     // scratch
     Buf tmp, err, zpart, dtotal, host_stage, sumtmp;
@@ -84,6 +90,7 @@ int build_lists(Handle& h);
 int solve_fmm(Handle& h, double* d_grad, double* d_total, int accumulate, int scatter);
 // fmm_p.cu (tc_config.order != 0)
 int solve_fmm_order(Handle& h, double* d_grad, double* d_total, int accumulate, int scatter);
+int build_multipoles(Handle& h);
 
 }  // namespace tc
 

@@ -305,6 +305,8 @@ int build_tree(Handle& h, const double* d_pos, int64_t n, double minx, double mi
         h.launches++;
     }
     TC_CUDA_TRY(cudaGetLastError());
+    // order-p multipoles belong to the tree: the list builder's controller reads them
+    if (h.cfg.order && (rc = build_multipoles(h))) return rc;
     if ((rc = record(h, 2))) return rc;
     h.tree_ready = true;
     return TC_OK;

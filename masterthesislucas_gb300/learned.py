@@ -1,0 +1,227 @@
+"""Learned expansion-order controller: data generation and training (host side).
+
+The network and its training run in libtreecode's own kernels (csrc/mlp.cu);
+the error samples come from the method itself (csrc/learned.cu): for node
+pairs drawn from the candidate lists of order-12 solves on independently
+seeded systems, the pair's far-field force error at orders 4, 6, 8, 10, 12 is
+measured against the direct sum over the source node's particles.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib, datasets
+from ._lib import check, lib, ptr
+from .solver import NBodySolverFMM_SYM_MORTON
+
+ORDERS = (4, 6, 8, 10, 12)
+NPARAM = 5573
+
+
+class OrderController:
+    """The 16 -> 64 -> 64 -> 5 MLP (BF16 weights, FP32 accumulation) on the GPU."""
+
+    def __init__(self, seed: int = 0):
+        self._m = ctypes.c_void_p()
+        check(lib().tc_mlp_create(ctypes.c_uint64(seed), ctypes.byref(self._m)))
+        self.mean = np.zeros(16, np.float32)
+        self.std = np.ones(16, np.float32)
+
+    def close(self):
+        if self._m:
+            lib().tc_mlp_destroy(self._m)
+            self._m = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_normalization(self, mean, std):
+        self.mean = np.ascontiguousarray(mean, np.float32)
+        self.std = np.ascontiguousarray(np.maximum(std, 1e-6), np.float32)
+        check(lib().tc_mlp_set_normalization(self._m, ptr(self.mean), ptr(self.std)))
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(NPARAM, np.float32)
+        check(lib().tc_mlp_get_params(self._m, ptr(p), None, None))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        check(lib().tc_mlp_set_params(self._m, ptr(p)))
+
+    def gradient(self, X_d, T_d):
+        g = np.zeros(NPARAM, np.float32)
+        loss = ctypes.c_float(0)
+        check(lib().tc_mlp_gradient(self._m, ptr(X_d), ptr(T_d), X_d.shape[0], ptr(g), ctypes.byref(loss)))
+        return g, float(loss.value)
+
+    def train(self, X_d, T_d, steps: int, batch: int = 4096, lr: float = 2e-3, seed: int = 0) -> float:
+        loss = ctypes.c_float(0)
+        check(lib().tc_mlp_train(self._m, ptr(X_d), ptr(T_d), X_d.shape[0], steps, batch, ctypes.c_float(lr),
+                                 ctypes.c_uint64(seed), ctypes.byref(loss)))
+        return float(loss.value) / (batch * len(ORDERS))
+
+    def predict_tc(self, X_d):
+        """The list builder's tensor-core evaluation (BF16 inputs and activations)."""
+        import torch
+        Y = torch.empty((X_d.shape[0], len(ORDERS)), dtype=torch.float32, device=X_d.device)
+        check(lib().tc_mlp_forward_tc(self._m, ptr(X_d), X_d.shape[0], ptr(Y)))
+        return Y
+
+    def predict(self, X_d):
+        import torch
+        Y = torch.empty((X_d.shape[0], len(ORDERS)), dtype=torch.float32, device=X_d.device)
+        check(lib().tc_mlp_forward(self._m, ptr(X_d), X_d.shape[0], ptr(Y)))
+        return Y
+
+    def save(self, path):
+        np.savez(path, params=self.params(), mean=self.mean, std=self.std, orders=np.array(ORDERS))
+
+    @classmethod
+    def load(cls, path):
+        z = np.load(path)
+        c = cls()
+        c.set_params(z["params"])
+        c.set_normalization(z["mean"], z["std"])
+        return c
+
+
+def sample_pairs(solver: NBodySolverFMM_SYM_MORTON, per_level: int, rng, min_level: int = 2):
+    """Candidate pairs (level, sink, source) drawn from the accepted and near lists."""
+    out = []
+    d = solver.depth()
+    for level in range(min_level, d + 1):
+        nl = 4 ** level
+        for kind in (0, 1):
+            ptr_h = np.zeros(nl + 1, np.uint32)
+            tot = ctypes.c_int64(0)
+            check(lib().tc_get_list(solver._h, level, kind, ptr(ptr_h), None, ctypes.byref(tot)))
+            if tot.value == 0:
+                continue
+            idx_h = np.zeros(tot.value, np.uint32)
+            check(lib().tc_get_list(solver._h, level, kind, ptr(ptr_h), ptr(idx_h), ctypes.byref(tot)))
+            k = min(per_level, tot.value)
+            e = rng.choice(tot.value, k, replace=False)
+            sink = np.searchsorted(ptr_h, e, side="right") - 1
+            src = idx_h[e]
+            keep = sink != src
+            out.append(np.stack([np.full(keep.sum(), level), sink[keep], src[keep]], 1))
+    return np.concatenate(out).astype(np.int32) if out else np.zeros((0, 3), np.int32)
+
+
+def generate(n_systems: int = 4, n_particles: int = 1 << 20, kernel: str = "gravity", per_level: int = 20000,
+             theta_gen: float = 1.6, seed: int = 0, depth_offset: int = 2, leaf: int = 64):
+    """Features and log10 errors from independently seeded systems (GPU)."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    feats, errs = [], []
+    for k in range(n_systems):
+        sd = int(rng.integers(1 << 30))
+        if kernel == "gravity":
+            pos = (datasets.two_disks(n_particles, seed=sd) if k % 2 == 0 else
+                   datasets.gaussian_mixture(n_particles, seed=sd)).astype(np.float64)
+        else:
+            pos = np.random.default_rng(sd).normal(0.0, 10.0 * (1 + k), (n_particles, 2))
+        from .solver import get_depth
+        depth = min(14, get_depth(leaf, n_particles) + depth_offset)
+        s = NBodySolverFMM_SYM_MORTON(kernel, max_children=leaf, tree_depth=depth, theta=theta_gen,
+                                      softening=1e-3, order=12)
+        pos_d = torch.from_numpy(pos).cuda()
+        g = torch.zeros_like(pos_d)
+        t = torch.zeros(1, dtype=torch.float64, device="cuda")
+        s.update_tree_device(pos_d)
+        s.solve_device(g, t)
+        pairs = sample_pairs(s, per_level, rng)
+        pd = torch.from_numpy(pairs).cuda()
+        F = torch.zeros((len(pairs), 16), dtype=torch.float32, device="cuda")
+        E = torch.zeros((len(pairs), 5), dtype=torch.float32, device="cuda")
+        check(lib().tc_lc_pair_errors(s._h, ptr(pd), len(pairs), ptr(F), ptr(E)))
+        feats.append(F.cpu().numpy())
+        errs.append(E.cpu().numpy())
+        s.close()
+    return np.concatenate(feats), np.concatenate(errs)
+
+
+def fit(X, T, *, steps=3000, batch=4096, lr=2e-3, seed=0, holdout=0.1):
+    """Trains an OrderController; returns it with train/holdout mean-squared errors."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    n = len(X)
+    perm = rng.permutation(n)
+    nh = int(n * holdout)
+    hold, tr = perm[:nh], perm[nh:]
+    c = OrderController(seed)
+    c.set_normalization(X[tr].mean(0), X[tr].std(0))
+    Xd = torch.from_numpy(np.ascontiguousarray(X[tr])).cuda()
+    Td = torch.from_numpy(np.ascontiguousarray(T[tr])).cuda()
+    c.train(Xd, Td, steps=steps, batch=batch, lr=lr, seed=seed)
+    ph = c.predict(torch.from_numpy(np.ascontiguousarray(X[hold])).cuda()).cpu().numpy()
+    pt = c.predict(Xd[:200000]).cpu().numpy()
+    mse_h = float(((ph - T[hold]) ** 2).mean()) if nh else float("nan")
+    mse_t = float(((pt - T[tr][:200000]) ** 2).mean())
+    return c, {"train_mse": mse_t, "holdout_mse": mse_h, "n_train": len(tr), "n_holdout": nh}
+
+
+# ---------------------------------------------------------------- CPU reference
+def bf16(x):
+    """Round-to-nearest-even to bfloat16, kept in float32 (the kernels' rounding)."""
+    u = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    lsb = (u >> 16) & 1
+    u = (u + 0x7FFF + lsb) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def unpack(p):
+    o = 0
+    W1 = p[o:o + 1024].reshape(64, 16); o += 1024
+    b1 = p[o:o + 64]; o += 64
+    W2 = p[o:o + 4096].reshape(64, 64); o += 4096
+    b2 = p[o:o + 64]; o += 64
+    W3 = p[o:o + 320].reshape(5, 64); o += 320
+    b3 = p[o:o + 5]
+    return W1, b1, W2, b2, W3, b3
+
+
+def reference_forward(p, X, mean, std, round_activations=False):
+    """Forward pass with BF16-rounded weights (FP64 arithmetic); with
+    round_activations the normalised inputs and the hidden activations are
+    rounded to BF16 too, as the list builder's tensor-core evaluation does."""
+    r = bf16 if round_activations else (lambda a: a)
+    W1, b1, W2, b2, W3, b3 = [a.astype(np.float64) for a in unpack(bf16(p))]
+    x = r(((X - mean) * (1.0 / std).astype(np.float32)).astype(np.float32)).astype(np.float64)
+    h1 = r(np.maximum(x @ W1.T + b1, 0).astype(np.float32)).astype(np.float64)
+    h2 = r(np.maximum(h1 @ W2.T + b2, 0).astype(np.float32)).astype(np.float64)
+    return h2 @ W3.T + b3
+
+
+def reference_loss_grad(p, X, T, mean, std, round_weights=True, dtype=np.float64):
+    """Mean-squared-error loss and its gradient w.r.t. the (rounded) parameters."""
+    q = bf16(p) if round_weights else p
+    W1, b1, W2, b2, W3, b3 = [a.astype(dtype) for a in unpack(q.astype(dtype))]
+    x = ((X - mean) / std).astype(dtype)
+    z1 = x @ W1.T + b1
+    h1 = np.maximum(z1, 0)
+    z2 = h1 @ W2.T + b2
+    h2 = np.maximum(z2, 0)
+    y = h2 @ W3.T + b3
+    e = y - T
+    n = e.size
+    loss = float((e ** 2).sum() / n)
+    dy = 2 * e / n
+    gW3 = dy.T @ h2
+    gb3 = dy.sum(0)
+    d2 = (dy @ W3) * (z2 > 0)
+    gW2 = d2.T @ h1
+    gb2 = d2.sum(0)
+    d1 = (d2 @ W2) * (z1 > 0)
+    gW1 = d1.T @ x
+    gb1 = d1.sum(0)
+    g = np.concatenate([gW1.ravel(), gb1, gW2.ravel(), gb2, gW3.ravel(), gb3])
+    return loss, g

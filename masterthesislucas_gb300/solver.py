@@ -182,6 +182,19 @@ class NBodySolverFMM_SYM_MORTON:
         check(lib().tc_get_counters(self._h, ptr(c)))
         return dict(p2p_pairs=int(c[0]), m2p=int(c[1]), p2l=int(c[2]), m2l=int(c[3]))
 
+    def set_controller(self, controller, tau: float = 1e-4):
+        """Accept pairs by a learned order controller (FP32, order 12 handles);
+        None restores the MAC.  Takes effect at the next updateTree."""
+        check(lib().tc_set_controller(self._h, None if controller is None else controller._m, float(tau)))
+
+    def list_orders(self, level: int) -> np.ndarray:
+        """Order bucket (0..4 for orders 4, 6, 8, 10, 12) of each accepted pair of a level."""
+        tot = ctypes.c_int64(0)
+        check(lib().tc_get_list(self._h, level, 0, None, None, ctypes.byref(tot)))
+        out = np.zeros(max(tot.value, 1), np.uint8)
+        check(lib().tc_get_list(self._h, level, 2, None, ptr(out), ctypes.byref(tot)))
+        return out[:tot.value]
+
     # device-resident entry points (torch tensors on the handle's device)
     def update_tree_device(self, pos, minPos=None, maxPos=None):
         mn = None if minPos is None else np.asarray(minPos, np.float64)

@@ -1,0 +1,159 @@
+"""The controller's GPU kernels: gradients against the CPU oracle, training
+convergence, and the self-measured pair errors (falling with order)."""
+import numpy as np
+import pytest
+
+from masterthesislucas_gb300 import learned
+
+pytestmark = pytest.mark.gpu
+
+
+def test_gpu_gradient_matches_cpu_oracle():
+    import torch
+    rng = np.random.default_rng(1)
+    c = learned.OrderController(seed=3)
+    mean = rng.normal(0, 0.1, 16).astype(np.float32)
+    std = rng.uniform(0.5, 2.0, 16).astype(np.float32)
+    c.set_normalization(mean, std)
+    X = rng.normal(0, 1, (777, 16)).astype(np.float32)
+    T = rng.normal(-3, 1, (777, 5)).astype(np.float32)
+    g_gpu, loss_sum = c.gradient(torch.from_numpy(X).cuda(), torch.from_numpy(T).cuda())
+    loss, g_ref = learned.reference_loss_grad(c.params(), X.astype(np.float64), T.astype(np.float64),
+                                             mean.astype(np.float64), std.astype(np.float64), round_weights=True)
+    assert loss_sum / T.size == pytest.approx(loss, rel=1e-4)
+    scale = np.abs(g_ref).max()
+    assert np.abs(g_gpu - g_ref).max() < 1e-4 * scale
+
+
+def test_tensor_core_forward_matches_bf16_oracle():
+    """The list builder's mma.sync evaluation against the CPU oracle that rounds
+    inputs and activations to BF16 the same way (odd n: a partial warp)."""
+    import torch
+    rng = np.random.default_rng(5)
+    c = learned.OrderController(seed=9)
+    mean = rng.normal(0, 0.5, 16).astype(np.float32)
+    std = rng.uniform(0.5, 2.0, 16).astype(np.float32)
+    c.set_normalization(mean, std)
+    X = rng.normal(0, 1.5, (4133, 16)).astype(np.float32)
+    Xd = torch.from_numpy(X).cuda()
+    y_tc = c.predict_tc(Xd).cpu().numpy()
+    y32 = c.predict(Xd).cpu().numpy()
+    ref_bf = learned.reference_forward(c.params(), X, mean, std, round_activations=True)
+    ref_32 = learned.reference_forward(c.params(), X, mean, std, round_activations=False)
+    scale = np.abs(ref_32).max()
+    d = np.abs(y_tc - ref_bf)
+    # an activation that lands on a BF16 rounding boundary may round the other way
+    assert np.median(d) < 1e-4 * scale and d.max() < 2e-2 * scale, (np.median(d), d.max(), scale)
+    assert np.abs(y32 - ref_32).max() < 1e-4 * scale
+    assert np.abs(y_tc - ref_32).max() < 5e-2 * scale
+
+
+def test_training_fits_a_smooth_target():
+    import torch
+    rng = np.random.default_rng(2)
+    X = rng.normal(0, 1, (60000, 16)).astype(np.float32)
+    T = np.stack([np.sin(X[:, 0]) + 0.5 * X[:, 1] * X[:, 2] - k * X[:, 3] ** 2 for k in range(5)], 1)
+    T = T.astype(np.float32)
+    c, stats = learned.fit(X, T, steps=1500, batch=2048, lr=3e-3, seed=5)
+    assert stats["holdout_mse"] < 0.1 * T.var(), stats
+
+
+def test_pair_errors_fall_with_order():
+    X, E = learned.generate(n_systems=1, n_particles=200000, per_level=2000, seed=4)
+    assert X.shape[1] == 16 and E.shape[1] == 5 and len(X) > 1000
+    assert np.isfinite(X).all() and np.isfinite(E).all()
+    # well-separated pairs: error decreases with order
+    far = X[:, 4] < 0.4
+    med = np.median(E[far], axis=0)
+    assert med[0] > med[2] > med[4], med
+
+
+# ---------------------------------------------------------------- controller in the solver
+def _analytic_controller(b3, slope):
+    """y_o = b3[o] - slope[o] * relu(log2|R|): a distance rule written as an MLP."""
+    p = np.zeros(learned.NPARAM, np.float32)
+    p[0] = 1.0                      # W1[0][0]: h1_0 = relu(feature 0 = log2|R|)
+    p[1088] = 1.0                   # W2[0][0]: h2_0 = h1_0
+    for o in range(5):
+        p[5248 + 64 * o] = -slope[o]  # W3[o][0]
+        p[5568 + o] = b3[o]
+    c = learned.OrderController()
+    c.set_params(p)
+    c.set_normalization(np.zeros(16, np.float32), np.ones(16, np.float32))
+    return c
+
+
+def _solve(pos, ctrl, tau=1e-4, depth=None):
+    import torch
+    from masterthesislucas_gb300 import NBodySolverFMM_SYM_MORTON
+    s = NBodySolverFMM_SYM_MORTON("gravity", max_children=32, tree_depth=depth, theta=1.0, softening=1e-3, order=12)
+    s.set_controller(ctrl, tau)
+    pd = torch.from_numpy(pos).cuda()
+    g = torch.zeros_like(pd)
+    t = torch.zeros(1, dtype=torch.float64, device="cuda")
+    s.update_tree_device(pd)
+    s.solve_device(g, t)
+    torch.cuda.synchronize()  # the handle runs on its own stream
+    return s, g.cpu().numpy(), float(t.item())
+
+
+def _rel_err(g, ref):
+    return np.linalg.norm(g - ref, axis=1) / np.linalg.norm(ref, axis=1)
+
+
+def test_never_accepting_controller_is_the_direct_sum():
+    from masterthesislucas_gb300 import datasets, solver
+    pos = datasets.two_disks(12000, seed=3).astype(np.float64)
+    c = _analytic_controller([10.0] * 5, [0.0] * 5)
+    s, g, _ = _solve(pos, c)
+    nn, nr = s.list_stats()
+    assert int(nn.sum()) == 0 and s.counters()["m2l"] == 0
+    ref, _ = solver.direct(pos, kernel="gravity", softening=1e-3, precision="fp64")
+    # the solver returns forces in input order on the device path's scatter
+    err = _rel_err(g, ref)
+    assert np.median(err) < 2e-6 and err.max() < 1e-3, (np.median(err), err.max())  # FP32 P2P
+    s.close()
+
+
+def test_order_buckets_agree_with_uniform_order12():
+    """Same accepted pairs (|R| >= 3 cells), orders by distance vs all at order 12.
+
+    Candidates are children of near pairs of the parent level, so |R| stays
+    below about 8 cells; the buckets split that range."""
+    from masterthesislucas_gb300 import datasets, solver
+    pos = datasets.two_disks(60000, seed=7).astype(np.float64)
+    lg = np.log2
+    thr = [lg(7.5), lg(6.5), lg(5.5), lg(4.5), lg(3.0)]   # order 4 beyond 7.5 cells, ..., order 12 beyond 3
+    mixed = _analytic_controller([-4.0 + t for t in thr], [1.0] * 5)
+    uni = _analytic_controller([10.0, 10.0, 10.0, 10.0, -4.0 + thr[4]], [0.0, 0.0, 0.0, 0.0, 1.0])
+    sm, gm, zm = _solve(pos, mixed)
+    su, gu, zu = _solve(pos, uni)
+    assert np.array_equal(np.asarray(sm.list_stats()[0]), np.asarray(su.list_stats()[0]))
+    used = np.bincount(np.concatenate([sm.list_orders(l) for l in range(1, sm.depth() + 1)]), minlength=5)
+    assert (used[:5] > 0).all(), used
+    uo = np.concatenate([su.list_orders(l) for l in range(1, su.depth() + 1)])
+    assert (uo == 4).all()
+    ref, _ = solver.direct(pos, kernel="gravity", softening=1e-3, precision="fp64")
+    em, eu = _rel_err(gm, ref), _rel_err(gu, ref)
+    d = _rel_err(gm, gu)
+    assert np.median(eu) < 1e-4 and np.median(em) < 1e-4, (np.median(eu), np.median(em))
+    assert np.median(d) < 5e-5, np.median(d)
+    assert zm == pytest.approx(zu, rel=1e-5)
+    sm.close()
+    su.close()
+
+
+def test_trained_controller_meets_tolerance_with_mixed_orders():
+    from masterthesislucas_gb300 import datasets, solver
+    X, E = learned.generate(n_systems=2, n_particles=150000, per_level=6000, seed=11)
+    c, stats = learned.fit(X, E, steps=2000, batch=4096, lr=2e-3, seed=1)
+    assert stats["holdout_mse"] < 0.25, stats
+    pos = datasets.two_disks(100000, seed=99).astype(np.float64)
+    s, g, _ = _solve(pos, c, tau=1e-4)
+    rows = np.random.default_rng(0).choice(len(pos), 2048, replace=False)
+    ref, _ = solver.direct(pos, kernel="gravity", softening=1e-3, precision="fp64", rows=rows)
+    err = _rel_err(g[rows], ref)
+    assert np.median(err) < 3e-4, np.median(err)
+    orders = np.concatenate([s.list_orders(l) for l in range(1, s.depth() + 1)])
+    assert len(orders) > 0 and np.bincount(orders, minlength=5)[:4].sum() > 0  # not everything at order 12
+    s.close()
