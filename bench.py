@@ -8,10 +8,16 @@ F_direct an FP64 direct sum on the GPU).
 Default workload (the metric's configuration): the 2D N-body force step on
 N = 4,194,304 particles in two exponential disks (scale lengths 0.1 and 0.05,
 centres 0.6 apart, masses 1/N), Plummer-softened gravity eps = 1e-3, leaf size
-64 (tree depth 9), FP32 expansions and P2P.  A step is one updateTree +
-solveNbody of the symmetric Morton FMM at the reference's fixed expansion
-order; the opening angle is the largest of a candidate list whose measured
-median error is <= 1e-4 (calibrated before timing, untimed).
+64, FP32 expansions and P2P.  A step is one updateTree + solveNbody.  Three
+methods are calibrated (untimed) and timed on the same positions:
+  learned     the learned-order controller (trained first on independently
+              seeded 1M-particle systems; depth and tolerance tau tuned);
+  plain_best  the plain order-p FMM autotuned over depth, theta and order;
+  plain_p12   the plain FMM at fixed order 12 (fastest depth/theta meeting
+              the error target).
+Every arm meets the error target on the 4,096 sampled particles; the value is
+the faster of learned and plain_best, and "comparison" holds all three with
+the learned method's speed-up over each plain one.
 
 Arms:
   --impl ours       (default) the CUDA library on 1..N GPUs (replicas: each
@@ -42,6 +48,10 @@ UNIT = "particles/s"
 TARGET_ERR = 1e-4
 N_SAMPLES = 4096
 THETAS = (0.4, 0.35, 0.3, 0.25, 0.2, 0.15, 0.1)
+# learned-order controller training: systems x pairs sampled per level x Adam steps
+CTRL_SYSTEMS = 8
+CTRL_PER_LEVEL = 200000
+CTRL_STEPS = 6000
 
 WORKLOADS = {
     "nbody_two_disks_4m": dict(n=4194304, dist="two_disks", kernel="gravity", softening=1e-3, max_children=64),
@@ -129,11 +139,28 @@ def median_error(grad, ref):
     return float(np.median(e)), float(np.percentile(e, 90)), float(e.max())
 
 
+def train_controller(w, seed=0):
+    """The learned-order controller: pair-error samples measured by the method
+    on independently seeded 1M-particle systems of the workload's distribution,
+    then the MLP trained by the library's own kernels (untimed)."""
+    from masterthesislucas_gb300 import learned
+    t0 = time.perf_counter()
+    X, E = learned.generate(n_systems=CTRL_SYSTEMS, n_particles=1 << 20, kernel=w["kernel"],
+                            per_level=CTRL_PER_LEVEL, seed=seed, leaf=w["max_children"])
+    t1 = time.perf_counter()
+    ctrl, stats = learned.fit(X, E, steps=CTRL_STEPS, batch=8192, lr=2e-3, seed=seed)
+    stats.update({"samples": int(len(X)), "systems": CTRL_SYSTEMS, "system_n": 1 << 20,
+                  "generate_s": round(t1 - t0, 2), "train_s": round(time.perf_counter() - t1, 2),
+                  "steps": CTRL_STEPS, "orders": list(learned.ORDERS)})
+    return ctrl, stats
+
+
 def run_ours(args, w, rank, world):
     import torch
 
     from masterthesislucas_gb300 import NBodySolverFMM_SYM_MORTON
     from masterthesislucas_gb300._lib import check, lib, ptr
+    from masterthesislucas_gb300.autotune import tune, tune_learned
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
@@ -153,10 +180,13 @@ def run_ours(args, w, rank, world):
     torch.cuda.synchronize()
     ref = ref_d.cpu().numpy()
 
-    def make(theta, order=0, depth=None):
-        return NBodySolverFMM_SYM_MORTON(w["kernel"], max_children=w["max_children"], tree_depth=depth, theta=theta,
-                                         softening=w["softening"], precision="fp32", order=order,
-                                         device=dev.index, stream=stream.cuda_stream)
+    def make(theta, order=0, depth=None, controller=None, tau=None):
+        s = NBodySolverFMM_SYM_MORTON(w["kernel"], max_children=w["max_children"], tree_depth=depth, theta=theta,
+                                      softening=w["softening"], precision="fp32", order=order,
+                                      device=dev.index, stream=stream.cuda_stream)
+        if controller is not None:
+            s.set_controller(controller, tau)
+        return s
 
     def step(s):
         s.update_tree_device(pos_d)
@@ -185,57 +215,85 @@ def run_ours(args, w, rank, world):
                 break
             s0.close()
 
-    # autotuned order-p method (depth, theta, order)
-    from masterthesislucas_gb300.autotune import tune
+    # plain order-p FMM, autotuned over (depth, theta, order); its order-12 line is the fixed-p=12 baseline
+    target = TARGET_ERR * 0.9
     if args.order:
-        best = {"depth": args.depth or None, "theta": args.theta or 0.5, "order": args.order}
+        plain = {"depth": args.depth or None, "theta": args.theta or 0.5, "order": args.order}
         trials = []
     else:
-        best, trials = tune(pos_d, ref, rows_d, kernel=w["kernel"], softening=w["softening"],
-                            leaf=w["max_children"], target=TARGET_ERR * 0.9, stream=stream, device=dev.index)
-        if best is None:
+        plain, trials = tune(pos_d, ref, rows_d, kernel=w["kernel"], softening=w["softening"],
+                             leaf=w["max_children"], target=target, stream=stream, device=dev.index)
+        if plain is None:
             raise SystemExit("autotuner found no configuration meeting the error target")
-    theta = best["theta"]
-    s = make(theta, order=best["order"], depth=best["depth"])
-    step(s)
-    torch.cuda.synchronize()
-    calib = {"best": best, "trials": trials, "reference_order": ref_order}
+    p12 = min((t for t in trials if t["order"] == 12 and t["err"] <= target), key=lambda t: t["ms"], default=None)
+
+    # learned-order controller
+    learned_cfg, ltrials, ctrl_stats, ctrl = None, [], None, None
+    if not args.no_learned:
+        ctrl, ctrl_stats = train_controller(w, seed=rank)
+        learned_cfg, ltrials = tune_learned(pos_d, ref, rows_d, ctrl, kernel=w["kernel"], softening=w["softening"],
+                                            leaf=w["max_children"], target=target, stream=stream, device=dev.index)
+    calib = {"plain_best": plain, "plain_p12": p12, "learned_best": learned_cfg, "plain_trials": trials,
+             "learned_trials": ltrials, "controller": ctrl_stats, "reference_order": ref_order}
 
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > L2 (129 MB)
-    for _ in range(args.warmup):
-        step(s)
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    stage_sum = None
-    launches = 0
-    with ClockSampler(dev.index) as clk:
-        for k in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.fill_(float(k))
-            ev0[k].record(stream)
-            s.update_tree_device(pos_d)
-            launches += s.launches()
-            s.solve_device(grad_d, tot_d, accumulate=False, scatter=True)
-            launches += s.launches()
-            ev1[k].record(stream)
-            st = s.stage_times()
-            stage_sum = st if stage_sum is None else {a: stage_sum[a] + st[a] for a in st}
-        torch.cuda.synchronize()
-    ms = [ev0[k].elapsed_time(ev1[k]) for k in range(args.steps)]
-    t_total = sum(ms) / 1e3
-    if world > 1:
-        t = torch.tensor([t_total], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_total = float(t.item())
-    counters = s.counters()
-    stages = {a: v / args.steps for a, v in stage_sum.items()}
-    g = grad_d[rows_d].cpu().numpy()
-    err = median_error(g, ref)
 
-    # end to end through the C ABI with pinned host buffers
+    def timed(s, steps, sample_clocks):
+        for _ in range(args.warmup):
+            step(s)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        stage_sum, launches = None, 0
+        with ClockSampler(dev.index) as clk:
+            for k in range(steps):
+                with torch.cuda.stream(stream):
+                    flush.fill_(float(k))
+                ev0[k].record(stream)
+                s.update_tree_device(pos_d)
+                launches += s.launches()
+                s.solve_device(grad_d, tot_d, accumulate=False, scatter=True)
+                launches += s.launches()
+                ev1[k].record(stream)
+                st = s.stage_times()
+                stage_sum = st if stage_sum is None else {a: stage_sum[a] + st[a] for a in st}
+            torch.cuda.synchronize()
+        ms = [ev0[k].elapsed_time(ev1[k]) for k in range(steps)]
+        t_total = sum(ms) / 1e3
+        if world > 1:
+            t = torch.tensor([t_total], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            t_total = float(t.item())
+        err = median_error(grad_d[rows_d].cpu().numpy(), ref)
+        return dict(ms=ms, t_total=t_total, stages={a: v / steps for a, v in stage_sum.items()},
+                    counters=s.counters(), err=err, clocks=clk.summary() if sample_clocks else None,
+                    launches=launches, depth=s.depth())
+
+    # the arms: the learned-order method (headline, when it meets the target) and the plain ones beside it
+    arms = {}
+    s_plain = make(plain["theta"], order=plain["order"], depth=plain["depth"])
+    arms["plain_best"] = timed(s_plain, args.steps, sample_clocks=True)
+    arms["plain_best"].update(theta=plain["theta"], order=plain["order"])
+    if p12 is not None:
+        if plain["order"] == 12 and (p12["depth"], p12["theta"]) == (plain["depth"], plain["theta"]):
+            arms["plain_p12"] = arms["plain_best"]
+        else:
+            s12 = make(p12["theta"], order=12, depth=p12["depth"])
+            arms["plain_p12"] = timed(s12, args.steps, sample_clocks=False)
+            arms["plain_p12"].update(theta=p12["theta"], order=12)
+            s12.close()
+    s_head, head, s_l = s_plain, "plain_best", None
+    if learned_cfg is not None:
+        s_l = make(1.0, order=12, depth=learned_cfg["depth"], controller=ctrl, tau=learned_cfg["tau"])
+        arms["learned"] = timed(s_l, args.steps, sample_clocks=True)
+        arms["learned"].update(tau=learned_cfg["tau"], order=12)
+        # the headline is the faster of the two methods (both meet the error target)
+        if arms["learned"]["t_total"] < arms["plain_best"]["t_total"]:
+            s_head, head = s_l, "learned"
+
+    # end to end through the C ABI with pinned host buffers, on the headline arm
     from masterthesislucas_gb300._lib import check as chk
     import ctypes
     pos_pin = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
@@ -250,13 +308,15 @@ def run_ours(args, w, rank, world):
         grad_np[:] = 0.0
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        chk(lib().tc_update_tree(s._h, ptr(pos_np), ptr(ids_np), n, ptr(mn), ptr(mx)))
+        chk(lib().tc_update_tree(s_head._h, ptr(pos_np), ptr(ids_np), n, ptr(mn), ptr(mx)))
         tot = ctypes.c_double(0.0)
-        chk(lib().tc_solve(s._h, ctypes.byref(tot), None, ptr(grad_np), n))
+        chk(lib().tc_solve(s_head._h, ctypes.byref(tot), None, ptr(grad_np), n))
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e_ms = e2e_ms[2:]
-    return dict(theta=theta, order=best["order"], calib=calib, ms=ms, t_total=t_total, stages=stages,
-                counters=counters, err=err, clocks=clk.summary(), launches=launches, e2e_ms=e2e_ms, depth=s.depth())
+    s_plain.close()
+    if s_l is not None:
+        s_l.close()
+    return dict(head=head, arms=arms, calib=calib, e2e_ms=e2e_ms)
 
 
 def cpu_baseline(w, theta, n_sample, threads=1, seeds=None):
@@ -478,6 +538,7 @@ def main():
     ap.add_argument("--skip-reference-order", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=262144)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-order controller arm")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]
@@ -529,38 +590,56 @@ def main():
     if rank != 0:
         return
     n = w["n"]
-    value = n * world * args.steps / r["t_total"]
+    head = r["arms"][r["head"]]
+    value = n * world * args.steps / head["t_total"]
     e2e_s = float(np.mean(r["e2e_ms"])) / 1e3
     peaks, peak_src = load_peaks()
     sm_mhz = peaks.get("sm_max_mhz", 2070.0)
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12  # TFLOP/s, nominal at the max SM clock
-    t_near = r["stages"]["near"] / 1e3
-    flops = 20.0 * r["counters"]["p2p_pairs"]
+    t_near = head["stages"]["near"] / 1e3
+    flops = 20.0 * head["counters"]["p2p_pairs"]
     achieved = flops / t_near / 1e12 if t_near > 0 else None
-    config.update({"theta": r["theta"], "depth": r["depth"], "order": r["order"],
-                   "expansion": f"total order {r['order']} Cartesian Taylor about the COM",
+
+    def arm_summary(a):
+        return {"particles_per_s": n * args.steps / a["t_total"], "ms_per_step": 1e3 * a["t_total"] / args.steps,
+                "depth": a["depth"], "order": a.get("order"), "theta": a.get("theta"), "tau": a.get("tau"),
+                "median_err": a["err"][0], "stages_ms": a["stages"], "counters": a["counters"]}
+
+    comparison = {k: arm_summary(a) for k, a in r["arms"].items()}
+    if "learned" in comparison:
+        lv = comparison["learned"]["particles_per_s"]
+        for k in ("plain_p12", "plain_best"):
+            if k in comparison:
+                comparison[f"learned_speedup_vs_{k}"] = lv / comparison[k]["particles_per_s"]
+    method = {"learned": "learned-order symmetric Morton FMM: MLP controller (16-64-64-5, BF16 tensor-core "
+                         "inference in the list build) picks accept/open and the order in {4,6,8,10,12} per pair",
+              "plain_best": "plain fixed-order symmetric Morton FMM (autotuned depth/theta/order)"}[r["head"]]
+    config.update({"theta": head.get("theta"), "tau": head.get("tau"), "depth": head["depth"],
+                   "order": head.get("order"), "method": r["head"],
+                   "expansion": "total-order Cartesian Taylor about the COM",
                    "autotune": r["calib"],
                    "l2": "256 MB buffer written between timed steps (inputs also exceed L2)"})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * r["t_total"] / args.steps, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": 1e3 * head["t_total"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded two-disk positions; no published dataset for this workload)",
         "config": config,
-        "method": "plain fixed-order symmetric Morton FMM (autotuned depth/theta/order); learned-order controller not built",
-        "error": {"median": r["err"][0], "p90": r["err"][1], "max": r["err"][2], "vs": "fp64 direct sum",
+        "method": method,
+        "comparison": comparison,
+        "error": {"median": head["err"][0], "p90": head["err"][1], "max": head["err"][2], "vs": "fp64 direct sum",
                   "samples": N_SAMPLES},
-        "stages_ms": r["stages"],
-        "counters": r["counters"],
-        "roofline": {"kernel": "k_leaf_near (P2P + M2P + L2P)", "bound": "fp32",
+        "stages_ms": head["stages"],
+        "counters": head["counters"],
+        "roofline": {"kernel": "k_near_p (P2P + L2P)", "bound": "fp32",
                      "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": (achieved / fp32_peak) if achieved else None, "traffic": None,
                      "flops_per_pair": 20, "peak_source": f"nominal: 152 SMs x 128 FP32 lanes x 2 x {sm_mhz:.0f} MHz "
                                                           f"(MEASURED_PEAKS.json holds no FP32 figure; {peak_src})"},
         "e2e": {"value": n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * 16,
                 "d2h_bytes_per_step": n * 16 + n * 4 + n * 16 + 8},
-        "gpu_launches": r["launches"],
-        "clocks": r["clocks"],
+        "gpu_launches": head["launches"],
+        "clocks": head["clocks"],
     }
     if not args.no_cpu_baseline:
         ref_th = (r["calib"]["reference_order"] or {}).get("theta", 0.15)

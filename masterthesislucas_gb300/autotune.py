@@ -1,4 +1,5 @@
-"""Autotuner for the order-p FMM: tree depth, opening angle and expansion order.
+"""Autotuner for the order-p FMM: tree depth, opening angle and expansion order
+(and, for the learned-order controller, tree depth and tolerance tau).
 
 For a given particle set (device-resident) it measures, for each candidate
 (depth, theta, order), the device time of one updateTree + solveNbody (CUDA
@@ -14,8 +15,9 @@ import numpy as np
 
 from .solver import NBodySolverFMM_SYM_MORTON, get_depth
 
-ORDERS = (4, 6, 8, 10)
-THETAS = (1.2, 1.0, 0.9, 0.8, 0.7, 0.6, 0.5, 0.4)
+ORDERS = (4, 6, 8, 10, 12)
+THETAS = (1.6, 1.4, 1.3, 1.2, 1.1, 1.0, 0.9, 0.8, 0.7, 0.6, 0.5, 0.4)
+TAUS = (3e-3, 2e-3, 1e-3, 7e-4, 5e-4, 3e-4, 2e-4, 1e-4, 5e-5)
 
 
 def median_error(grad_rows: np.ndarray, ref_rows: np.ndarray) -> float:
@@ -66,4 +68,56 @@ def tune(pos_d, ref_rows, rows_d, *, kernel: str, softening: float, leaf: int, t
                     if best is None or ms < best["ms"]:
                         best = t
                     break  # smaller theta at this order only costs more
+    return best, trials
+
+
+def _time_step(s, pos_d, grad_d, tot_d, s_torch):
+    import torch
+    s.update_tree_device(pos_d)
+    s.solve_device(grad_d, tot_d)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s_torch)
+    s.update_tree_device(pos_d)
+    s.solve_device(grad_d, tot_d)
+    e1.record(s_torch)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def tune_learned(pos_d, ref_rows, rows_d, controller, *, kernel: str, softening: float, leaf: int, target: float,
+                 stream=None, depths=None, taus=TAUS, device: int = 0, log=None):
+    """The learned-order controller's knobs: for each depth the largest tau
+    (loosest tolerance) whose measured median error meets the target.
+    Returns (best, trials); best = dict(depth, tau, ms, err) or None."""
+    import torch
+
+    n = pos_d.shape[0]
+    d0 = get_depth(leaf, n)
+    depths = depths or (d0 + 1, d0 + 2)
+    grad_d = torch.zeros((n, 2), dtype=torch.float64, device=pos_d.device)
+    tot_d = torch.zeros(1, dtype=torch.float64, device=pos_d.device)
+    s_torch = torch.cuda.Stream(device=pos_d.device) if stream is None else stream
+    trials, best = [], None
+    for depth in depths:
+        if depth > 15:
+            continue
+        for tau in taus:
+            s = NBodySolverFMM_SYM_MORTON(kernel, max_children=leaf, tree_depth=depth, theta=1.0,
+                                          softening=softening, precision="fp32", order=12, device=device,
+                                          stream=s_torch.cuda_stream)
+            try:
+                s.set_controller(controller, tau)
+                ms = _time_step(s, pos_d, grad_d, tot_d, s_torch)
+                err = median_error(grad_d[rows_d].cpu().numpy(), ref_rows)
+            finally:
+                s.close()
+            t = dict(depth=depth, tau=tau, ms=ms, err=err)
+            trials.append(t)
+            if log:
+                log(t)
+            if err <= target:
+                if best is None or ms < best["ms"]:
+                    best = t
+                break  # smaller tau at this depth only costs more
     return best, trials

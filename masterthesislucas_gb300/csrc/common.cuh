@@ -18,6 +18,8 @@ void tc_set_error(const char* fmt, ...);
 namespace tc {
 
 constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs
+// leaves above this many particles take a warp (leaf moments, P2M) in the order-p path
+constexpr uint32_t kLeafSmall = 32;
 
 __host__ __device__ inline uint32_t spread16(uint32_t x)
 {

@@ -16,6 +16,8 @@
 // + (2nu n_i + n_i(n_i-1)) D_(k-2e_i) + n_j(n_j-1) D_(k-2e_j)] for
 // phi = u^-nu, u = r^2 + c, n = k - e_i, obtained by differentiating
 // u grad(phi) = -2 nu R phi.
+#include <type_traits>
+
 #include "expansion.cuh"
 #include "kernels.cuh"
 #include "state.cuh"
@@ -24,22 +26,68 @@ namespace tc {
 namespace {
 
 // ------------------------------------------------------------------ P2M
-// one warp per leaf: mu_a = sum (r/h)^a / a! about the COM
+// mu_a = sum (r/h)^a / a! about the COM.  Leaves of up to kLeafSmall
+// particles take one thread each (monomials built degree by degree, two rows
+// live); the larger leaves, listed by the leaf build, one warp each.
+
+template <int P>
+__global__ void __launch_bounds__(128) k_p2m_small(int dep, float h, const uint32_t* __restrict__ count,
+                                                   const uint32_t* __restrict__ first,
+                                                   const float* __restrict__ comrel, const float* __restrict__ prel,
+                                                   float* __restrict__ mu)
+{
+    constexpr int K = ncoef(P);
+    const uint32_t li = level_index(dep);
+    const int64_t nl = (int64_t)1 << (2 * dep);
+    const float ih = 1.0f / h;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t node = li + i;
+        const uint32_t c = count[node];
+        if (c == 0 || c > kLeafSmall) continue;
+        const uint32_t f = first[node];
+        const float cx = comrel[2 * node], cy = comrel[2 * node + 1];
+        float acc[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) acc[k] = 0.f;
+        for (uint32_t q = 0; q < c; q++) {
+            const float dx = (prel[2 * (f + q)] - cx) * ih, dy = (prel[2 * (f + q) + 1] - cy) * ih;
+            float row[P + 1];
+            row[0] = 1.0f;
+            acc[0] += 1.0f;
+#pragma unroll
+            for (int k = 1; k <= P; k++) {
+                // degree k from degree k-1: w_(a,b) = w_(a-1,b) dx / a, w_(0,k) = w_(0,k-1) dy / k
+                const float last = row[k - 1];
+#pragma unroll
+                for (int b = 0; b < k; b++) row[b] = row[b] * dx * (1.0f / (k - b));
+                row[k] = last * dy * (1.0f / k);
+#pragma unroll
+                for (int b = 0; b <= k; b++) acc[cidx(k - b, b)] += row[b];
+            }
+        }
+        float4* o4 = reinterpret_cast<float4*>(mu + node * kstride(P));
+#pragma unroll
+        for (int c4 = 0; c4 < kstride(P) / 4; c4++)
+            o4[c4] = make_float4(4 * c4 < K ? acc[4 * c4] : 0.f, 4 * c4 + 1 < K ? acc[4 * c4 + 1] : 0.f,
+                                 4 * c4 + 2 < K ? acc[4 * c4 + 2] : 0.f, 4 * c4 + 3 < K ? acc[4 * c4 + 3] : 0.f);
+    }
+}
+
 template <int P>
 __global__ void __launch_bounds__(128) k_p2m(int dep, float h, const uint32_t* __restrict__ count,
                                              const uint32_t* __restrict__ first, const float* __restrict__ comrel,
-                                             const float* __restrict__ prel, float* __restrict__ mu)
+                                             const float* __restrict__ prel, const uint32_t* __restrict__ big,
+                                             float* __restrict__ mu)
 {
     constexpr int K = ncoef(P);
     const int lane = threadIdx.x & 31;
     const uint32_t li = level_index(dep);
-    const int64_t nl = (int64_t)1 << (2 * dep);
+    const int64_t nbig = big[0];
     const float ih = 1.0f / h;
     const int64_t wstride = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t i = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); i < nl; i += wstride) {
-        const int64_t node = li + i;
+    for (int64_t w = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); w < nbig; w += wstride) {
+        const int64_t node = li + big[1 + w];
         const uint32_t c = count[node];
-        if (c == 0) continue;
         const uint32_t f = first[node];
         const float cx = comrel[2 * node], cy = comrel[2 * node + 1];
         float acc[K];
@@ -98,23 +146,179 @@ __global__ void __launch_bounds__(128) k_m2m(int l, float hl, const uint32_t* __
     }
 }
 
+// ------------------------------------------------------------------ shifts at orders >= 10
+// Streaming shifts: one thread per node, the shift's monomials and the
+// accumulators in registers, the input expansion read coefficient by
+// coefficient (no third register array).
+// input degree KA and up, one degree per instantiation (a single nest over
+// all degrees exceeds the unroller's limit at order 12)
+template <int P, int KA>
+__device__ __forceinline__ void m2m_deg(const float* __restrict__ in, const float* w, float* acc)
+{
+    if constexpr (KA <= P) {
+        constexpr float sc = 1.0f / (float)(1 << KA);  // child -> parent scale
+#pragma unroll
+        for (int ba = 0; ba <= KA; ba++) {
+            const float v = __ldg(in + cidx(KA - ba, ba)) * sc;
+#pragma unroll
+            for (int kg = 0; kg + KA <= P; kg++)
+#pragma unroll
+                for (int bg = 0; bg <= kg; bg++) acc[cidx(KA - ba + kg - bg, ba + bg)] += v * w[cidx(kg - bg, bg)];
+        }
+        m2m_deg<P, KA + 1>(in, w, acc);
+    }
+}
+
+template <int P>
+__device__ __forceinline__ void m2m_child(float dx, float dy, const float* __restrict__ in, float* acc)
+{
+    float w[ncoef(P)];
+    monomials<P>(dx, dy, w);
+    m2m_deg<P, 0>(in, w, acc);
+}
+
+template <int P>
+__global__ void __launch_bounds__(128) k_m2m_stream(int l, float hl, const uint32_t* __restrict__ count,
+                                                    const float* __restrict__ comrel, float* __restrict__ mu)
+{
+    constexpr int K = ncoef(P), KS = kstride(P);
+    const uint32_t li = level_index(l), lc = level_index(l + 1);
+    const int64_t nl = (int64_t)1 << (2 * l);
+    const float ih = 1.0f / hl;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t node = li + i;
+        if (count[node] == 0) continue;
+        const float px = comrel[2 * node], py = comrel[2 * node + 1];
+        float acc[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) acc[k] = 0.f;
+#pragma unroll 1
+        for (int j = 0; j < 4; j++) {
+            const int64_t ch = lc + 4 * i + j;
+            if (count[ch] == 0) continue;
+            // child COM - parent COM: child cell centre sits at (+-1/4, +-1/4) h of the parent's
+            const float ox = (j & 1) ? 0.25f : -0.25f, oy = (j & 2) ? 0.25f : -0.25f;
+            m2m_child<P>(ox + (comrel[2 * ch] - px) * ih, oy + (comrel[2 * ch + 1] - py) * ih, mu + ch * KS, acc);
+        }
+        float4* o4 = reinterpret_cast<float4*>(mu + node * KS);
+#pragma unroll
+        for (int c = 0; c < KS / 4; c++)
+            o4[c] = make_float4(4 * c < K ? acc[4 * c] : 0.f, 4 * c + 1 < K ? acc[4 * c + 1] : 0.f,
+                                4 * c + 2 < K ? acc[4 * c + 2] : 0.f, 4 * c + 3 < K ? acc[4 * c + 3] : 0.f);
+    }
+}
+
+template <int P>
+__global__ void __launch_bounds__(128) k_l2l_stream(int l, float hl, const uint32_t* __restrict__ count,
+                                                    const float* __restrict__ comrel, float* __restrict__ loc)
+{
+    constexpr int K = ncoef(P), KS = kstride(P);
+    const uint32_t li = level_index(l), lp = level_index(l - 1);
+    const int64_t nl = (int64_t)1 << (2 * l);
+    const float ih = 1.0f / hl;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t node = li + i;
+        if (count[node] == 0) continue;
+        const int64_t par = lp + (i >> 2);
+        const int j = (int)(i & 3);
+        const float ox = ((j & 1) ? 0.5f : -0.5f), oy = ((j & 2) ? 0.5f : -0.5f);
+        const float ddx = ox + (comrel[2 * node] - comrel[2 * par]) * ih;
+        const float ddy = oy + (comrel[2 * node + 1] - comrel[2 * par + 1]) * ih;
+        float w[K], acc[K];
+        monomials<P>(ddx, ddy, w);
+        const float4* a4 = reinterpret_cast<const float4*>(loc + node * KS);
+#pragma unroll
+        for (int c = 0; c < KS / 4; c++) {
+            const float4 v = a4[c];
+            if (4 * c < K) acc[4 * c] = v.x;
+            if (4 * c + 1 < K) acc[4 * c + 1] = v.y;
+            if (4 * c + 2 < K) acc[4 * c + 2] = v.z;
+            if (4 * c + 3 < K) acc[4 * c + 3] = v.w;
+        }
+        const float* in = loc + par * KS;
+#pragma unroll
+        for (int kg = 0; kg <= P; kg++) {
+            const float sc = 1.0f / (float)(1 << kg);  // parent scale 2h -> h
+#pragma unroll
+            for (int bg = 0; bg <= kg; bg++) {
+                const int ag = kg - bg;
+                const float v = in[cidx(ag, bg)] * sc;
+#pragma unroll
+                for (int ab = 0; ab <= ag; ab++)
+#pragma unroll
+                    for (int bb = 0; bb <= bg; bb++) acc[cidx(ab, bb)] += v * w[cidx(ag - ab, bg - bb)];
+            }
+        }
+        float4* o4 = reinterpret_cast<float4*>(loc + node * KS);
+#pragma unroll
+        for (int c = 0; c < KS / 4; c++)
+            o4[c] = make_float4(4 * c < K ? acc[4 * c] : 0.f, 4 * c + 1 < K ? acc[4 * c + 1] : 0.f,
+                                4 * c + 2 < K ? acc[4 * c + 2] : 0.f, 4 * c + 3 < K ? acc[4 * c + 3] : 0.f);
+    }
+}
+
 // ------------------------------------------------------------------ M2L
-// one thread per sink node A of level l: L(A) = sum over nn(A) of M2L; also
-// the far-field pair sum kappa * sum_b L_b mu_b(A)
-// P: order of this launch; PS: storage order of mu/loc (the solve order).
-// ord/bucket select the entries of one controller order bucket (ord NULL: all);
-// write != 0 stores every coefficient of the node (zeros above order P),
-// otherwise the launch adds its contribution.
-template <int P, int PS>
-__global__ void __launch_bounds__(128) k_m2l_p(int l, float hl, PotParams pp, const uint32_t* __restrict__ nn_ptr,
-                                               const uint32_t* __restrict__ nn_idx, const uint8_t* __restrict__ ord,
-                                               int bucket, int write, const uint32_t* __restrict__ count,
-                                               const float* __restrict__ comrel, const float* __restrict__ mu,
-                                               float* __restrict__ loc, double* __restrict__ zpart)
+// L_b += sum_a (-1)^|a| mu_a D_(a+b) at order P for one source (multipoles
+// stored with stride KSS); L holds at least ncoef(P) coefficients.
+template <int P, int KSS>
+__device__ __forceinline__ void m2l_acc(float Rx, float Ry, float hl, const PotParams& pp, const float* __restrict__ m,
+                                        float* L)
 {
     constexpr int K = ncoef(P);
     constexpr int KS = kstride(P);
-    constexpr int KSS = kstride(PS);
+    static_assert(KS <= KSS, "storage order below the launch order");
+    float D[K];
+    derivs<P>(Rx, Ry, hl, pp, D);
+    const float4* m4 = reinterpret_cast<const float4*>(m);
+#pragma unroll
+    for (int c = 0; c < KS / 4; c++) {
+        const float4 q = __ldg(m4 + c);
+        const float mv[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int ia = 4 * c + j;
+            if (ia >= K) continue;
+            const int ka = cdeg(ia), ba = ia - ka * (ka + 1) / 2;
+            if (ka == 1) continue;  // dipole vanishes about the COM
+            const float ma = (ka & 1) ? -mv[j] : mv[j];
+#pragma unroll
+            for (int kb = 0; kb + ka <= P; kb++)
+#pragma unroll
+                for (int bb = 0; bb <= kb; bb++) L[cidx(kb - bb, bb)] += ma * D[cidx(ka - ba + kb - bb, ba + bb)];
+        }
+    }
+}
+
+// the node's local expansion, the far-field pair sum kappa * sum_b L_b mu_b(A)
+template <int K, int KS>
+__device__ __forceinline__ void m2l_store(int64_t na, bool any, float kappa, const float* L,
+                                          const float* __restrict__ mu, float* __restrict__ loc,
+                                          double* __restrict__ zpart)
+{
+    double z = 0.0;
+    if (any) {
+        const float* m = mu + na * KS;
+        float zs = 0.f;
+#pragma unroll
+        for (int k = 0; k < K; k++) zs += L[k] * m[k];
+        z = (double)kappa * (double)zs;
+    }
+    zpart[na] = z;
+    float4* o4 = reinterpret_cast<float4*>(loc + na * KS);
+#pragma unroll
+    for (int c = 0; c < KS / 4; c++)
+        o4[c] = make_float4(4 * c < K ? L[4 * c] : 0.f, 4 * c + 1 < K ? L[4 * c + 1] : 0.f,
+                            4 * c + 2 < K ? L[4 * c + 2] : 0.f, 4 * c + 3 < K ? L[4 * c + 3] : 0.f);
+}
+
+// one thread per sink node A of level l: L(A) = sum over nn(A) of M2L
+template <int P>
+__global__ void __launch_bounds__(128) k_m2l_p(int l, float hl, PotParams pp, const uint32_t* __restrict__ nn_ptr,
+                                               const uint32_t* __restrict__ nn_idx, const uint32_t* __restrict__ count,
+                                               const float* __restrict__ comrel, const float* __restrict__ mu,
+                                               float* __restrict__ loc, double* __restrict__ zpart)
+{
+    constexpr int K = ncoef(P), KS = kstride(P);
     const uint32_t li = level_index(l);
     const int64_t nl = (int64_t)1 << (2 * l);
     const float ih = 1.0f / hl;
@@ -125,64 +329,80 @@ __global__ void __launch_bounds__(128) k_m2l_p(int l, float hl, PotParams pp, co
         float L[K];
 #pragma unroll
         for (int k = 0; k < K; k++) L[k] = 0.f;
-        if (b0 != b1) {
-            const int iax = (int)compact16((uint32_t)a), iay = (int)compact16((uint32_t)a >> 1);
-            const float cax = comrel[2 * na], cay = comrel[2 * na + 1];
-            for (uint32_t e = b0; e < b1; e++) {
-                if (ord && ord[e] != bucket) continue;
+        const int iax = (int)compact16((uint32_t)a), iay = (int)compact16((uint32_t)a >> 1);
+        const float cax = comrel[2 * na], cay = comrel[2 * na + 1];
+        for (uint32_t e = b0; e < b1; e++) {
+            const uint32_t b = nn_idx[e];
+            const int64_t nb = li + b;
+            const float Rx = (float)(iax - (int)compact16(b)) + (cax - comrel[2 * nb]) * ih;
+            const float Ry = (float)(iay - (int)compact16(b >> 1)) + (cay - comrel[2 * nb + 1]) * ih;
+            m2l_acc<P, KS>(Rx, Ry, hl, pp, mu + nb * KS, L);
+        }
+        m2l_store<K, KS>(na, b0 != b1, pp.kappa, L, mu, loc, zpart);
+    }
+}
+
+// Controller lists: a node's accepted entries come sorted by order bucket
+// (orders 4, 6, 8, 10, 12).  Two launches per level: buckets 4..8 with an
+// order-8 accumulator (half the registers, twice the resident warps), which
+// writes the node's local expansion (zeros above order 8), then buckets 10
+// and 12 with an order-12 accumulator, which adds.  (A lower-order
+// contribution has no coefficients above its order, so the pair sum over the
+// stored coefficients equals the sum of the per-order sums.)
+template <int PACC, int OLO, int OHI>
+__global__ void __launch_bounds__(128) k_m2l_mixed(int l, float hl, PotParams pp, const uint32_t* __restrict__ nn_ptr,
+                                                   const uint32_t* __restrict__ nn_idx,
+                                                   const uint8_t* __restrict__ ord,
+                                                   const uint32_t* __restrict__ count,
+                                                   const float* __restrict__ comrel, const float* __restrict__ mu,
+                                                   float* __restrict__ loc, double* __restrict__ zpart)
+{
+    constexpr int K = ncoef(PACC), KS = kstride(12);
+    constexpr bool first = OLO == 0;
+    const uint32_t li = level_index(l);
+    const int64_t nl = (int64_t)1 << (2 * l);
+    const float ih = 1.0f / hl;
+    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < nl; a += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t na = li + a;
+        if (count[na] == 0) continue;
+        const uint32_t p0 = nn_ptr[a], b1 = nn_ptr[a + 1];
+        uint32_t e = p0;
+        while (e < b1 && ord[e] < OLO) e++;
+        const uint32_t b0 = e;
+        float L[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) L[k] = 0.f;
+        const int iax = (int)compact16((uint32_t)a), iay = (int)compact16((uint32_t)a >> 1);
+        const float cax = comrel[2 * na], cay = comrel[2 * na + 1];
+        auto bucket = [&](auto order_tag, int o) {
+            constexpr int PO = decltype(order_tag)::value;
+            for (; e < b1 && ord[e] == o; e++) {
                 const uint32_t b = nn_idx[e];
                 const int64_t nb = li + b;
                 const float Rx = (float)(iax - (int)compact16(b)) + (cax - comrel[2 * nb]) * ih;
                 const float Ry = (float)(iay - (int)compact16(b >> 1)) + (cay - comrel[2 * nb + 1]) * ih;
-                float D[K];
-                derivs<P>(Rx, Ry, hl, pp, D);
-                const float4* m4 = reinterpret_cast<const float4*>(mu + nb * KSS);
-#pragma unroll
-                for (int c = 0; c < KS / 4; c++) {
-                    const float4 q = __ldg(m4 + c);
-                    const float mv[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-                    for (int j = 0; j < 4; j++) {
-                        const int ia = 4 * c + j;
-                        if (ia >= K) continue;
-                        const int ka = cdeg(ia), ba = ia - ka * (ka + 1) / 2;
-                        if (ka == 1) continue;  // dipole vanishes about the COM
-                        const float ma = (ka & 1) ? -mv[j] : mv[j];
-#pragma unroll
-                        for (int kb = 0; kb + ka <= P; kb++)
-#pragma unroll
-                            for (int bb = 0; bb <= kb; bb++)
-                                L[cidx(kb - bb, bb)] += ma * D[cidx(ka - ba + kb - bb, ba + bb)];
-                    }
-                }
+                if constexpr (PO <= PACC) m2l_acc<PO, KS>(Rx, Ry, hl, pp, mu + nb * KS, L);
             }
-        }
-        double z = 0.0;
-        if (b0 != b1) {
-            const float* m = mu + na * KSS;
+        };
+        if constexpr (OLO <= 0 && 0 <= OHI) bucket(std::integral_constant<int, 4>{}, 0);
+        if constexpr (OLO <= 1 && 1 <= OHI) bucket(std::integral_constant<int, 6>{}, 1);
+        if constexpr (OLO <= 2 && 2 <= OHI) bucket(std::integral_constant<int, 8>{}, 2);
+        if constexpr (OLO <= 3 && 3 <= OHI) bucket(std::integral_constant<int, 10>{}, 3);
+        if constexpr (OLO <= 4 && 4 <= OHI) bucket(std::integral_constant<int, 12>{}, 4);
+        const bool any = e != b0;
+        if (first) {
+            m2l_store<K, KS>(na, any, pp.kappa, L, mu, loc, zpart);
+        } else if (any) {
+            const float* m = mu + na * KS;
             float zs = 0.f;
 #pragma unroll
             for (int k = 0; k < K; k++) zs += L[k] * m[k];
-            z = (double)pp.kappa * (double)zs;
-        }
-        float4* o4 = reinterpret_cast<float4*>(loc + na * KSS);
-        if (write) {
-            zpart[na] = z;
-#pragma unroll
-            for (int c = 0; c < KSS / 4; c++) {
-                float4 v;
-                v.x = 4 * c + 0 < K ? L[4 * c + 0] : 0.f;
-                v.y = 4 * c + 1 < K ? L[4 * c + 1] : 0.f;
-                v.z = 4 * c + 2 < K ? L[4 * c + 2] : 0.f;
-                v.w = 4 * c + 3 < K ? L[4 * c + 3] : 0.f;
-                o4[c] = v;
-            }
-        } else if (b0 != b1) {
-            zpart[na] += z;
+            zpart[na] += (double)pp.kappa * (double)zs;
+            float4* o4 = reinterpret_cast<float4*>(loc + na * KS);
 #pragma unroll
             for (int c = 0; c < KS / 4; c++) {
                 float4 v = o4[c];
-                v.x += 4 * c + 0 < K ? L[4 * c + 0] : 0.f;
+                v.x += 4 * c < K ? L[4 * c] : 0.f;
                 v.y += 4 * c + 1 < K ? L[4 * c + 1] : 0.f;
                 v.z += 4 * c + 2 < K ? L[4 * c + 2] : 0.f;
                 v.w += 4 * c + 3 < K ? L[4 * c + 3] : 0.f;
@@ -422,28 +642,27 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
         const int64_t nl = (int64_t)1 << (2 * l);
         const uint32_t* np_ = ptr + h.lists.nn_ptr_off[l];
         const uint32_t* ni_ = idx + h.lists.nn_idx_off[l];
-        bool bucketed = false;
+        bool mixed = false;
         if constexpr (ORD == 12) {
-            // controller lists: one launch per order bucket, the first writes every node
             if (h.ctrl_on) {
                 const uint8_t* od = P<uint8_t>(h.ord_pool) + h.lists.nn_idx_off[l];
-                const int g = grid_for(nl, 128);
-                k_m2l_p<4, 12><<<g, 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, 0, 1, count, comrel, mu, loc, zp);
-                k_m2l_p<6, 12><<<g, 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, 1, 0, count, comrel, mu, loc, zp);
-                k_m2l_p<8, 12><<<g, 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, 2, 0, count, comrel, mu, loc, zp);
-                k_m2l_p<10, 12><<<g, 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, 3, 0, count, comrel, mu, loc, zp);
-                k_m2l_p<12, 12><<<g, 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, 4, 0, count, comrel, mu, loc, zp);
-                h.launches += 4;
-                bucketed = true;
+                k_m2l_mixed<8, 0, 2><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, count, comrel, mu,
+                                                                       loc, zp);
+                k_m2l_mixed<12, 3, 4><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, count, comrel, mu,
+                                                                        loc, zp);
+                h.launches++;
+                mixed = true;
             }
         }
-        if (!bucketed)
-            k_m2l_p<ORD, ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, nullptr, 0, 1, count, comrel,
-                                                               mu, loc, zp);
+        if (!mixed)
+            k_m2l_p<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, count, comrel, mu, loc, zp);
     }
     for (int l = 1; l <= dep; l++) {
         const int64_t nl = (int64_t)1 << (2 * l);
-        k_l2l<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, loc);
+        if constexpr (ORD >= 10)
+            k_l2l_stream<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, loc);
+        else
+            k_l2l<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, loc);
     }
     uint32_t* nchunk = P<uint32_t>(h.cnt_tmp);
     uint32_t* chunk_ptr = P<uint32_t>(h.chunk);
@@ -477,13 +696,18 @@ int multipoles_p(Handle& h)
     const float* comrel = P<float>(h.comrel);
     const uint32_t* count = P<uint32_t>(h.count);
     auto hl = [&](int l) { return (float)(h.L / (double)(1u << l)); };
-    k_p2m<ORD><<<grid_for(nleaf * 32, 128, kSMs * 64), 128, 0, s>>>(dep, hl(dep), count, P<uint32_t>(h.first), comrel,
-                                                                 P<float>(h.prel), mu);
+    k_p2m_small<ORD><<<grid_for(nleaf, 128), 128, 0, s>>>(dep, hl(dep), count, P<uint32_t>(h.first), comrel,
+                                                         P<float>(h.prel), mu);
+    k_p2m<ORD><<<grid_for((h.n / (kLeafSmall + 1) + 1) * 32, 128), 128, 0, s>>>(
+        dep, hl(dep), count, P<uint32_t>(h.first), comrel, P<float>(h.prel), P<uint32_t>(h.bigleaf), mu);
     for (int l = dep - 1; l >= 0; l--) {
         const int64_t nl = (int64_t)1 << (2 * l);
-        k_m2m<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, mu);
+        if constexpr (ORD >= 10)
+            k_m2m_stream<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, mu);
+        else
+            k_m2m<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, mu);
     }
-    h.launches += 1 + dep;
+    h.launches += 2 + dep;
     h.mu_stride = kstride(ORD);
     TC_CUDA_TRY(cudaGetLastError());
     return TC_OK;

@@ -235,7 +235,9 @@ __global__ void __launch_bounds__(32 * ctrl::kWarps) k_lists_ctrl_count(
     }
 }
 
-// Fill pass: one thread per node; the decisions of the count pass.
+// Fill pass: one thread per node; the decisions of the count pass.  Each
+// node's accepted entries are written grouped by order bucket (ascending), so
+// that the M2L launch of one bucket reads one contiguous range per node.
 __global__ void k_lists_ctrl_fill(int l, const uint32_t* __restrict__ count, const uint32_t* __restrict__ pnear_ptr,
                                   const uint32_t* __restrict__ pnear_idx, uint32_t pcap, const uint8_t* __restrict__ dec,
                                   const uint32_t* __restrict__ nn_ptr, uint32_t* __restrict__ nn_idx,
@@ -248,23 +250,40 @@ __global__ void k_lists_ctrl_fill(int l, const uint32_t* __restrict__ count, con
     for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < nl; a += (int64_t)gridDim.x * blockDim.x) {
         if (count[li + a] == 0) continue;
         const uint32_t p = (uint32_t)(a >> 2);
-        uint32_t nn = nn_ptr[a], nr = near_ptr[a];
+        const uint32_t pe0 = pnear_ptr[p];
         const uint32_t pe1 = pnear_ptr[p + 1] < pcap ? pnear_ptr[p + 1] : pcap;
-        for (uint32_t e = pnear_ptr[p]; e < pe1; e++) {
+        uint32_t start[TC_MLP_OUT] = {0, 0, 0, 0, 0};
+        for (uint32_t e = pe0; e < pe1; e++) {
+            const uint32_t bp = pnear_idx[e];
+            if (bp >= np) continue;
+            for (uint32_t j = 0; j < 4; j++) {
+                if (count[li + 4 * bp + j] == 0) continue;
+                const uint8_t d = dec[16u * e + 4u * j + (uint32_t)(a & 3)];
+                if (d < TC_MLP_OUT) start[d]++;
+            }
+        }
+        uint32_t run = nn_ptr[a];
+        for (int o = 0; o < TC_MLP_OUT; o++) {
+            const uint32_t c = start[o];
+            start[o] = run;
+            run += c;
+        }
+        uint32_t nr = near_ptr[a];
+        for (uint32_t e = pe0; e < pe1; e++) {
             const uint32_t bp = pnear_idx[e];
             if (bp >= np) continue;
             for (uint32_t j = 0; j < 4; j++) {
                 const uint32_t b = 4 * bp + j;
                 if (count[li + b] == 0) continue;
                 const uint8_t d = dec[16u * e + 4u * j + (uint32_t)(a & 3)];
-                if (d != ctrl::kOpen) {
-                    if (nn < nn_cap) {
-                        nn_idx[nn] = b;
-                        nn_ord[nn] = d;
+                if (d < TC_MLP_OUT) {
+                    const uint32_t pos = start[d]++;
+                    if (pos < nn_cap) {
+                        nn_idx[pos] = b;
+                        nn_ord[pos] = d;
                     } else {
                         atomicOr(ovf, 1u);
                     }
-                    nn++;
                 } else {
                     if (nr < near_cap) near_idx[nr] = b;
                     else atomicOr(ovf, 1u);

@@ -54,6 +54,8 @@ struct Handle {
     Buf count, first, com64, m0, m2, bbc, bblen, comrel, m0r, m2t, loc, locfin, chunk, zwork, zloc, mu;
     // lists
     Buf ptr_pool, idx_pool, cnt_tmp, lstat, ord_pool, nfeat, dec;
+    // order-p path: leaves above kLeafSmall particles ([0] count, then indices)
+    Buf bigleaf;
     // learned order controller (order-p mode): weights + normalisation copy
     bool ctrl_on = false;
     float ctrl_log_tau = -4.f;
