@@ -58,6 +58,8 @@ WORKLOADS = {
     "nbody_two_disks_1m": dict(n=1048576, dist="two_disks", kernel="gravity", softening=1e-3, max_children=64),
     "tsne_70k": dict(n=70000, dist="tsne", dim=784, clusters=10, perplexity=30.0, kernel="tsne", order=8,
                      theta=0.5, max_children=16, early_exaggeration=12.0, method="tsne", softening=0.0),
+    "leapfrog_two_disks_4m": dict(n=4194304, dist="two_disks", kernel="gravity", softening=1e-3, max_children=64,
+                                  method="leapfrog", dt=1e-4),
     "bh_mixture_65k": dict(n=65536, dist="mixture", kernel="gravity", softening=1e-3, max_children=16,
                            method="bh", theta=0.5),
 }
@@ -360,6 +362,77 @@ def cpu_baseline(w, theta, n_sample, threads=1, seeds=None):
     return len(jobs) * n_sample / dt, dt, depth
 
 
+def run_leapfrog(args, w):
+    """N-body time stepping: kick-drift-kick leapfrog (dt = 1e-4) over the
+    FMM force on the two rotating disks; the FMM configuration is autotuned on
+    the initial positions (untimed).  Reports particles/s per force step,
+    steps/s and the FP64 energy drift and momentum over the timed steps."""
+    import torch
+
+    from masterthesislucas_gb300._lib import check, lib, ptr
+    from masterthesislucas_gb300.autotune import tune
+    from masterthesislucas_gb300.nbody import LeapfrogNBody, circular_velocities
+
+    dev = torch.device("cuda", 0)
+    n = w["n"]
+    m = 1.0 / n
+    pos_h = positions(w, seed=1000)
+    vel_h = circular_velocities(pos_h, m, w["softening"], centres=[[-0.3, 0.0], [0.3, 0.0]])
+    pos_d = torch.from_numpy(pos_h).to(dev)
+    rows = np.sort(np.random.default_rng(7).choice(n, N_SAMPLES, replace=False)).astype(np.int64)
+    rows_d = torch.from_numpy(rows).to(dev)
+    ref_d = torch.zeros((N_SAMPLES, 2), dtype=torch.float64, device=dev)
+    check(lib().tc_direct_device(1, w["softening"], 1, ptr(pos_d), n, ptr(rows_d), N_SAMPLES, ptr(ref_d), None, None))
+    torch.cuda.synchronize()
+    best, _ = tune(pos_d, ref_d.cpu().numpy(), rows_d, kernel="gravity", softening=w["softening"],
+                   leaf=w["max_children"], target=TARGET_ERR * 0.9, device=0)
+    sim = LeapfrogNBody(pos_h, vel_h, mass=m, dt=w["dt"], softening=w["softening"], max_children=w["max_children"],
+                        tree_depth=best["depth"], theta=best["theta"], order=best["order"])
+    sim.step(args.warmup)
+    d0 = sim.diagnostics()
+    torch.cuda.synchronize()
+    launches = 0
+    with ClockSampler(0) as clk:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t0.record()
+        for _ in range(args.steps):
+            sim.step(1)
+            launches += sim.solver.launches()
+        torch.cuda.synchronize()
+        t1.record()
+        torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1)
+    d1 = sim.diagnostics()
+    # force error at the final positions
+    x_d = sim.x
+    check(lib().tc_direct_device(1, w["softening"], 1, ptr(x_d), n, ptr(rows_d), N_SAMPLES, ptr(ref_d), None, None))
+    torch.cuda.synchronize()
+    ref_end = ref_d.cpu().numpy() * m
+    acc_end = sim.a[rows_d].cpu().numpy()
+    err = median_error(acc_end, ref_end)
+    sim.close()
+    value = n * args.steps / (ms / 1e3)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded two rotating exponential disks, circular velocities from the enclosed mass)",
+            "config": {"workload": args.workload, "n": n, "dt": w["dt"], "integrator": "kick-drift-kick leapfrog",
+                       "depth": best["depth"], "theta": best["theta"], "order": best["order"],
+                       "l2": "inputs exceed L2 (4M particles: 64 MB positions + tree)"},
+            "steps_per_s": 1e3 * args.steps / ms,
+            "diagnostics": {"energy_start": d0["energy"], "energy_end": d1["energy"],
+                            "energy_drift_rel": abs(d1["energy"] - d0["energy"]) / abs(d0["energy"]),
+                            "momentum_start": [d0["px"], d0["py"]], "momentum_end": [d1["px"], d1["py"]],
+                            "kinetic_end": d1["kinetic"],
+                            "potential_end": d1["potential"], "sum": "fp64, fixed order"},
+            "error": {"median": err[0], "p90": err[1], "max": err[2], "vs": "fp64 direct sum at the final positions",
+                      "samples": N_SAMPLES},
+            "gpu_launches": launches, "clocks": clk.summary()}
+    print(json.dumps(line))
+
+
 def run_bh(args, w):
     """Barnes-Hut force step (the reference's QuadTree and MAC) on the GPU."""
     import ctypes
@@ -580,6 +653,9 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         dist.init_process_group("nccl")
+    if w.get("method") == "leapfrog":
+        run_leapfrog(args, w)
+        return
     if w.get("method") == "bh":
         run_bh(args, w)
         return

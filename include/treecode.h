@@ -170,6 +170,20 @@ int tc_bh_solve(int kernel, double softening, int max_children, double theta, in
 int tc_bh_solve_device(int kernel, double softening, int max_children, double theta, int precision,
                        const double* d_pos_xy, int64_t n, double* d_grad_xy, double* d_total, void* stream);
 
+/* ---------------------------------------------------------------- N-body time step
+ * Kick-drift-kick leapfrog on a gravity handle.  The reference's N-body
+ * scenes step kick-then-drift around their solver call (2D, commented out:
+ * src/nBodyInstances/gravitysim.h:99-127; 3D: nbodySim.h:215-240); this is
+ * the time-centred leapfrog form of that loop with the project's softened
+ * 2D kernel and FP64 energy/momentum diagnostics.  Device arrays in
+ * input order: positions, velocities and accelerations (n x 2 FP64, G = 1,
+ * equal masses `mass`).  init != 0 first computes the acceleration at the
+ * current positions (the first call); dt == 0 with init only evaluates.
+ * d_diag (device, 4 doubles) receives {kinetic, potential, Px, Py} after the
+ * step, summed in FP64 in a fixed order.  Asynchronous on the handle's stream. */
+int tc_leapfrog_step(tc_handle* h, double* d_pos_xy, double* d_vel_xy, double* d_acc_xy, int64_t n, double dt,
+                     double mass, int init, double* d_diag);
+
 /* ---------------------------------------------------------------- order controller
  * No counterpart in the reference (its expansion order is fixed).  A 3-layer
  * MLP (16 pair features -> 64 -> 64 -> 5, ReLU; BF16 weights, FP32

@@ -77,6 +77,7 @@ SIGNATURES = {
     "tc_lc_pair_errors": (_I, [_P, _P, _I64, _P, _P]),
     "tc_get_list": (_I, [_P, _I, _I, _P, _P, _P]),
     "tc_set_controller": (_I, [_P, _P, ctypes.c_double]),
+    "tc_leapfrog_step": (_I, [_P, _P, _P, _P, _I64, _D, _D, _I, _P]),
     "tc_tsne_create": (_I, [_P, _I64, _P, _P, _P, _P, _P]),
     "tc_tsne_destroy": (_I, [_P]),
     "tc_tsne_set_theta": (_I, [_P, _D]),

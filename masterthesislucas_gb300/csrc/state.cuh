@@ -56,6 +56,7 @@ struct Handle {
     Buf ptr_pool, idx_pool, cnt_tmp, lstat, ord_pool, nfeat, dec;
     // order-p path: leaves above kLeafSmall particles ([0] count, then indices)
     Buf bigleaf;
+    Buf diagpart;  // leapfrog diagnostics: per-block partial sums
     // learned order controller (order-p mode): weights + normalisation copy
     bool ctrl_on = false;
     float ctrl_log_tau = -4.f;
