@@ -239,6 +239,8 @@ int tc_tsne_create(const tc_config* cfg, int64_t n, const uint32_t* row_ptr, con
                    const double* val, const double* y0, tc_tsne** out);
 int tc_tsne_destroy(tc_tsne* t);
 int tc_tsne_set_theta(tc_tsne* t, double theta);
+/* tree depth of the next steps (0..15); the reference derives it from N */
+int tc_tsne_set_depth(tc_tsne* t, int depth);
 /* One TSNE_buffers::timeStep (tsne_buffers.h:125-168): updateTree on the
  * current embedding, updateRepulsive (tsne.h:287-301), updateAttractive
  * (:356-381) with factor exag_code (the reference uses 16 for the first 250
@@ -248,6 +250,32 @@ int tc_tsne_step(tc_tsne* t, double exag_code, double momentum, double lr, doubl
 /* Current embedding, previous embedding and last gradient, in ID order.    */
 int tc_tsne_get(tc_tsne* t, double* y, double* y_prev, double* grad);
 int tc_tsne_last_launch_count(tc_tsne* t);
+
+/* Batches: many independent embeddings (each its own tc_tsne, FP32, order
+ * p > 0, created on one device and stepped only through the batch) advance
+ * in lockstep, one CUDA graph launch per step.  Inside the graph every
+ * system's tree is built over a fixed square box (its extent enlarged by
+ * `margin` plus a look-ahead of its last displacement, refreshed when a
+ * point leaves it) with the list capacities of its last exact build; after
+ * each launch a system that left its box or overflowed a list is stepped
+ * again uncaptured and its graphs are re-captured.  No counterpart in the
+ * reference (one embedding per TSNE object).                              */
+typedef struct tc_tsne_batch tc_tsne_batch;
+int tc_tsne_batch_create(tc_tsne* const* systems, int count, double margin, tc_tsne_batch** out);
+int tc_tsne_batch_destroy(tc_tsne_batch* b);
+/* exag_code and momentum as tc_tsne_step; each system's learning rate is
+ * lr_per_point * its n (the reference's N/15 at 1/15)                      */
+int tc_tsne_batch_step(tc_tsne_batch* b, double exag_code, double momentum, double lr_per_point);
+/* stats (8 values): {graph launches, captures, uncaptured re-steps, nodes
+ * in the systems' phase-0 graphs, particles in the batch, kernels per step,
+ * host microseconds in graph launches, host microseconds in re-steps}.     */
+int tc_tsne_batch_stats(tc_tsne_batch* b, int64_t* stats);
+/* enable == 0: the same steps (same boxes, same refresh rule) enqueued
+ * uncaptured, one system after another; for checking the graph path.     */
+int tc_tsne_batch_set_capture(tc_tsne_batch* b, int enable);
+/* After the stream of a no-sync (captured) update has been synchronised:
+ * bit 0 a position lay outside the box, bit 1 a list level overflowed.    */
+int tc_async_status(tc_handle* h);
 
 const char* tc_last_error(void);
 

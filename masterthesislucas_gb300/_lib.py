@@ -81,9 +81,16 @@ SIGNATURES = {
     "tc_tsne_create": (_I, [_P, _I64, _P, _P, _P, _P, _P]),
     "tc_tsne_destroy": (_I, [_P]),
     "tc_tsne_set_theta": (_I, [_P, _D]),
+    "tc_tsne_set_depth": (_I, [_P, _I]),
     "tc_tsne_step": (_I, [_P, _D, _D, _D, _P]),
     "tc_tsne_get": (_I, [_P, _P, _P, _P]),
     "tc_tsne_last_launch_count": (_I, [_P]),
+    "tc_tsne_batch_create": (_I, [_P, _I, _D, _P]),
+    "tc_tsne_batch_destroy": (_I, [_P]),
+    "tc_tsne_batch_step": (_I, [_P, _D, _D, _D]),
+    "tc_tsne_batch_stats": (_I, [_P, _P]),
+    "tc_tsne_batch_set_capture": (_I, [_P, _I]),
+    "tc_async_status": (_I, [_P]),
 }
 
 _lib = None

@@ -70,15 +70,21 @@ def build_p_csr(x, perplexity: float = 30.0, k: int | None = None, device=None):
     n = xt.shape[0]
     k = min(k, n - 1)
     d2, idx = knn(xt, k)
-    p = perplexity_rows(d2, perplexity).cpu().numpy()
-    idx = idx.cpu().numpy()
+    if xt.is_cuda:
+        return _symmetrize_device(perplexity_rows(d2, perplexity), idx, n)
+    return _symmetrize_host(perplexity_rows(d2, perplexity).cpu().numpy(), idx.cpu().numpy(), n)
+
+
+def _symmetrize_host(p: np.ndarray, idx: np.ndarray, n: int):
+    """(P + P^T) / (2N) as CSR (rows and columns sorted), on the host."""
+    k = idx.shape[1]
     rows = np.repeat(np.arange(n, dtype=np.int64), k)
     cols = idx.reshape(-1)
     vals = p.reshape(-1)
     # symmetrise: (P + P^T) / (2N)
     r2 = np.concatenate([rows, cols])
     c2 = np.concatenate([cols, rows])
-    v2 = np.concatenate([vals, vals]) / (2.0 * n)
+    v2 = np.concatenate([vals, vals]) * (1.0 / (2.0 * n))  # as the device path scales
     key = r2 * n + c2
     order = np.argsort(key, kind="stable")
     key = key[order]
@@ -91,3 +97,26 @@ def build_p_csr(x, perplexity: float = 30.0, k: int | None = None, device=None):
     np.add.at(row_ptr, r + 1, 1)
     row_ptr = np.cumsum(row_ptr).astype(np.uint32)
     return row_ptr, c, vsum.astype(np.float64)
+
+
+def _symmetrize_device(p: torch.Tensor, idx: torch.Tensor, n: int):
+    """(P + P^T) / (2N) as CSR, on the GPU (each entry sums at most two
+    values, so the result does not depend on the summation order)."""
+    k = idx.shape[1]
+    dev = idx.device
+    rows = torch.arange(n, device=dev, dtype=torch.int64).repeat_interleave(k)
+    cols = idx.reshape(-1).to(torch.int64)
+    vals = p.reshape(-1).to(torch.float64)
+    key = torch.cat([rows * n + cols, cols * n + rows])
+    v2 = torch.cat([vals, vals]) * (1.0 / (2.0 * n))
+    key, order = torch.sort(key, stable=True)
+    v2 = v2[order]
+    uniq, counts = torch.unique_consecutive(key, return_counts=True)
+    seg = torch.repeat_interleave(torch.arange(len(uniq), device=dev), counts)
+    vsum = torch.zeros(len(uniq), dtype=torch.float64, device=dev).index_add_(0, seg, v2)
+    r = uniq // n
+    c = (uniq % n).to(torch.int32)
+    row_ptr = torch.zeros(n + 1, dtype=torch.int64, device=dev)
+    row_ptr[1:] = torch.cumsum(torch.bincount(r, minlength=n), 0)
+    return (row_ptr.cpu().numpy().astype(np.uint32), c.cpu().numpy().astype(np.uint32),
+            vsum.cpu().numpy().astype(np.float64))

@@ -53,6 +53,7 @@ void release(Buf& b)
 
 int record(Handle& h, int i)
 {
+    if (h.nosync) return TC_OK;  // stage timing events stay out of captured graphs
     if (!h.ev_ready) {
         for (auto& e : h.ev) TC_CUDA_TRY(cudaEventCreate(&e));
         h.ev_ready = true;
@@ -325,9 +326,10 @@ static int update_common(Handle& h, const double* d_pos, int64_t n, const double
     }
     int rc = build_tree(h, d_pos, n, mn[0], mn[1], mx[0], mx[1]);
     if (rc) return rc;
-    rc = build_lists(h);  // synchronises the stream (list sizes)
+    rc = build_lists(h);  // synchronises the stream (list sizes), except in no-sync mode
     if (rc) return rc;
     TC_CUDA_TRY(cudaMemcpyAsync(h.h_words + 8, h.err.p, 4, cudaMemcpyDeviceToHost, h.stream));
+    if (h.nosync) return TC_OK;  // the caller reads the flags after its own synchronisation
     TC_CUDA_TRY(cudaStreamSynchronize(h.stream));
     if (h.h_words[8]) {
         h.tree_ready = false;
@@ -582,3 +584,10 @@ int tc_get_counters(tc_handle* t, uint64_t* counts)
 }
 
 }  // extern "C"
+
+extern "C" int tc_async_status(tc_handle* t)
+{
+    if (!t) return TC_ERR_INVALID;
+    const Handle& h = t->h;
+    return (h.h_words[8] ? 1 : 0) | (h.h_words[40] ? 2 : 0);
+}

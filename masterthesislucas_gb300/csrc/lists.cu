@@ -294,6 +294,16 @@ __global__ void k_lists_ctrl_fill(int l, const uint32_t* __restrict__ count, con
     }
 }
 
+// No-sync builds cannot check the capacities before the lists are read: the
+// CSR pointers are clamped to the capacity so that every reader stays inside
+// the level's region (an overflowed level then yields truncated lists, and
+// the overflow flag tells the caller to redo the step).
+__global__ void k_clamp_ptr(uint32_t* __restrict__ ptr, int64_t n, uint32_t cap)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (ptr[i] > cap) ptr[i] = cap;
+}
+
 // per-level list totals (last entries of the CSR pointer arrays)
 __global__ void k_list_totals(const uint32_t* __restrict__ ptr, const int64_t* __restrict__ offs, int nlev,
                               uint32_t* __restrict__ out)
@@ -305,6 +315,23 @@ __global__ void k_list_totals(const uint32_t* __restrict__ ptr, const int64_t* _
 }
 
 }  // namespace
+
+// Sizes the list pools for a fast (capacity-based) build ahead of a stream
+// capture, where no allocation may happen.  The pools' contents are not kept.
+int prepare_nosync(Handle& h)
+{
+    const Lists& L = h.lists;
+    if (L.caps_depth != h.depth || (int64_t)L.nn_cap.size() != h.depth + 1) {
+        tc_set_error("no-sync list build needs the capacities of an earlier build at this depth");
+        return TC_ERR_STATE;
+    }
+    int64_t words = 0;
+    for (int l = 0; l <= h.depth; l++) words += (int64_t)L.nn_cap[l] + L.near_cap[l];
+    int rc;
+    if ((rc = ensure(h.idx_pool, (size_t)words * 4 + 64))) return rc;
+    if (h.ctrl_on && (rc = ensure(h.ord_pool, h.idx_pool.bytes / 4 + 64))) return rc;
+    return TC_OK;
+}
 
 int build_lists(Handle& h)
 {
@@ -386,6 +413,10 @@ int build_lists(Handle& h)
     // no host round trip between levels; one synchronisation at the end
     // verifies that no level overflowed, else the exact mode reruns.
     const bool fast = L.caps_depth == depth && (int64_t)L.nn_cap.size() == depth + 1;
+    if (h.nosync && !fast) {
+        tc_set_error("no-sync list build needs the capacities of an earlier build at this depth");
+        return TC_ERR_STATE;
+    }
     if (fast) {
         int64_t words = 0;
         for (int l = 0; l <= depth; l++) {
@@ -410,7 +441,18 @@ int build_lists(Handle& h)
             if ((rc = launch(l, pnp, pni, pcap, nullptr, nullptr, nnp, P<uint32_t>(h.idx_pool) + L.nn_idx_off[l],
                              L.nn_cap[l], nrp, P<uint32_t>(h.idx_pool) + L.near_idx_off[l], L.near_cap[l], 1)))
                 return rc;
+            if (h.nosync) {
+                k_clamp_ptr<<<grid_for(nl + 1, 256), 256, 0, s>>>(nnp, nl + 1, L.nn_cap[l]);
+                k_clamp_ptr<<<grid_for(nl + 1, 256), 256, 0, s>>>(nrp, nl + 1, L.near_cap[l]);
+                h.launches += 2;
+            }
             h.launches += 8;
+        }
+        if (h.nosync) {
+            // captured step: the overflow flag lands in pinned memory for the caller to check
+            TC_CUDA_TRY(cudaMemcpyAsync(h.h_words + 40, ovf, 4, cudaMemcpyDeviceToHost, s));
+            TC_CUDA_TRY(cudaGetLastError());
+            return TC_OK;
         }
         // totals of every level plus the overflow flag, in one round trip
         std::vector<int64_t> offs(2 * (depth + 1));
@@ -489,8 +531,8 @@ int build_lists(Handle& h)
     L.nn_cap.resize(depth + 1);
     L.near_cap.resize(depth + 1);
     for (int l = 0; l <= depth; l++) {
-        L.nn_cap[l] = (uint32_t)(L.nn_total[l] + L.nn_total[l] / 4 + 256);
-        L.near_cap[l] = (uint32_t)(L.near_total[l] + L.near_total[l] / 4 + 256);
+        L.nn_cap[l] = (uint32_t)(L.nn_total[l] + (int64_t)(L.nn_total[l] * h.cap_slack) + 256);
+        L.near_cap[l] = (uint32_t)(L.near_total[l] + (int64_t)(L.near_total[l] * h.cap_slack) + 256);
     }
     L.caps_depth = depth;
     TC_CUDA_TRY(cudaGetLastError());

@@ -58,6 +58,10 @@ struct Handle {
     Buf bigleaf;
     Buf diagpart;  // leapfrog diagnostics: per-block partial sums
     // learned order controller (order-p mode): weights + normalisation copy
+    // no-sync mode (stream capture): no host round trips or stage events; the
+    // outside-box and list-overflow flags are copied to pinned h_words[8], [40]
+    bool nosync = false;
+    double cap_slack = 0.25;  // fast-mode list capacity: exact total * (1 + slack) + 256
     bool ctrl_on = false;
     float ctrl_log_tau = -4.f;
     double ctrl_c = 0.0;      // kernel constant c of u = r^2 + c
@@ -94,6 +98,7 @@ int solve_fmm(Handle& h, double* d_grad, double* d_total, int accumulate, int sc
 // fmm_p.cu (tc_config.order != 0)
 int solve_fmm_order(Handle& h, double* d_grad, double* d_total, int accumulate, int scatter);
 int build_multipoles(Handle& h);
+int prepare_nosync(Handle& h);
 
 }  // namespace tc
 

@@ -85,3 +85,88 @@ class TSNE:
 
     def launches(self) -> int:
         return int(lib().tc_tsne_last_launch_count(self._t))
+
+    def set_depth(self, depth: int):
+        check(lib().tc_tsne_set_depth(self._t, int(depth)))
+        self.depth = int(depth)
+
+
+def tune_depth(system: TSNE, offsets=(0, 1, 2, 3), order: int = 8, theta: float = 0.5, leaf: int = 16,
+               reps: int = 2) -> dict:
+    """Autotunes one embedding's tree depth on its current positions: the
+    device time of updateTree + solveNbody (CUDA events) at getDepth + each
+    offset, with a separate solver on a copy of the embedding; the fastest
+    depth is set on the system."""
+    import torch
+    from .solver import NBodySolverFMM_SYM_MORTON, get_depth
+    y = torch.from_numpy(np.ascontiguousarray(system.embedding()[0])).cuda()
+    g = torch.zeros_like(y)
+    tot = torch.zeros(1, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.Stream()
+    d0 = get_depth(leaf, system.n)
+    trials = []
+    for off in offsets:
+        d = d0 + off
+        if d > 15:
+            continue
+        s = NBodySolverFMM_SYM_MORTON("tsne", max_children=leaf, tree_depth=d, theta=theta, order=order,
+                                      stream=stream.cuda_stream)
+        s.update_tree_device(y)
+        s.solve_device(g, tot)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            s.update_tree_device(y)
+            s.solve_device(g, tot)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        trials.append((e0.elapsed_time(e1) / reps, d))
+        s.close()
+    ms, best = min(trials)
+    system.set_depth(best)
+    return {"depth": best, "ms": ms, "trials": trials}
+
+
+class TSNEBatch:
+    """Independent embeddings advanced in lockstep, one CUDA graph launch per
+    step (``tc_tsne_batch_*``).  ``systems`` are ``TSNE`` objects (FP32,
+    order > 0, not stepped on their own afterwards); they share the
+    schedule: exaggeration for the first 250 iterations, momentum 0.5 then
+    0.8, learning rate n/15 per system."""
+
+    def __init__(self, systems, margin: float = 0.5, capture: bool = True):
+        self.systems = list(systems)
+        arr = (ctypes.c_void_p * len(self.systems))(*[s._t.value for s in self.systems])
+        self._b = ctypes.c_void_p()
+        check(lib().tc_tsne_batch_create(arr, len(self.systems), float(margin), ctypes.byref(self._b)))
+        if not capture:
+            check(lib().tc_tsne_batch_set_capture(self._b, 0))
+        self.early_exaggeration = self.systems[0].early_exaggeration
+        self.iteration_counter = self.systems[0].iteration_counter
+
+    def time_step(self):
+        it = self.iteration_counter
+        exag = 4.0 * (self.early_exaggeration if it < 250 else 1.0)
+        mom = 0.5 if it < 250 else 0.8
+        check(lib().tc_tsne_batch_step(self._b, exag, mom, 1.0 / 15.0))
+        self.iteration_counter += 1
+        for s in self.systems:
+            s.iteration_counter = self.iteration_counter
+
+    def stats(self) -> dict:
+        out = np.zeros(8, np.int64)
+        check(lib().tc_tsne_batch_stats(self._b, ptr(out)))
+        return dict(graph_launches=int(out[0]), captures=int(out[1]), restepped=int(out[2]),
+                    graph_nodes=int(out[3]), particles=int(out[4]), kernels_per_launch=int(out[5]),
+                    graph_ms=out[6] / 1e3, restep_ms=out[7] / 1e3)
+
+    def close(self):
+        if self._b:
+            lib().tc_tsne_batch_destroy(self._b)
+            self._b = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
