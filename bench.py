@@ -60,6 +60,9 @@ WORKLOADS = {
                      theta=0.5, max_children=16, early_exaggeration=12.0, method="tsne", softening=0.0),
     "leapfrog_two_disks_4m": dict(n=4194304, dist="two_disks", kernel="gravity", softening=1e-3, max_children=64,
                                   method="leapfrog", dt=1e-4),
+    "tsne_batch_256": dict(n=0, systems=256, n_min=2000, n_max=200000, dim=64, clusters=(5, 20), perplexity=30.0,
+                           kernel="tsne", max_children=16, theta=0.5, method="tsne_batch", softening=0.0, dist="tsne",
+                           presteps=5),
     "bh_mixture_65k": dict(n=65536, dist="mixture", kernel="gravity", softening=1e-3, max_children=16,
                            method="bh", theta=0.5),
 }
@@ -433,6 +436,85 @@ def run_leapfrog(args, w):
     print(json.dumps(line))
 
 
+def batch_order(n):
+    """Expansion order per system size for the batched t-SNE, from {4, 8, 12}:
+    a fixed size rule (p = 4 below 20k particles, p = 8 above)."""
+    return 4 if n < 20000 else 8
+
+
+def run_tsne_batch(args, w):
+    """Batched uneven t-SNE: independent embeddings (N log-uniform in
+    [2k, 200k], 64-dim Gaussian-cluster data, perplexity 30, k = 90 CSR P)
+    advance one gradient step per CUDA graph launch.  Setup (untimed): P per
+    system, a few uncaptured steps so that the embeddings leave their initial
+    blob, then each system's tree depth autotuned on its embedding."""
+    import torch
+
+    from masterthesislucas_gb300 import affinity, datasets
+    from masterthesislucas_gb300.tsne import TSNE, TSNEBatch, tune_depth
+
+    rng = np.random.default_rng(2024)
+    ns = np.exp(rng.uniform(np.log(w["n_min"]), np.log(w["n_max"]), w["systems"])).astype(np.int64)
+    t0 = time.perf_counter()
+    systems = []
+    for i, n in enumerate(ns):
+        k = int(rng.integers(w["clusters"][0], w["clusters"][1] + 1))
+        x, _ = datasets.cluster_data(int(n), w["dim"], k=k, seed=10_000 + i)
+        rp, col, val = affinity.build_p_csr(x, perplexity=w["perplexity"], device="cuda")
+        y0 = np.random.default_rng(20_000 + i).normal(0.0, 1e-2, (int(n), 2))  # N(0, 1e-4)
+        systems.append(TSNE(rp, col, val, y0, early_exaggeration=12.0, max_children=w["max_children"],
+                            order=batch_order(int(n))))
+    t_p = time.perf_counter() - t0
+    for s in systems:
+        for _ in range(w["presteps"]):
+            s.time_step()
+    depths = [tune_depth(s, theta=w["theta"])["depth"] for s in systems]
+    t_setup = time.perf_counter() - t0
+    batch = TSNEBatch(systems, margin=0.5)
+    for _ in range(args.warmup):
+        batch.time_step()
+    st0 = batch.stats()
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        t1 = time.perf_counter()
+        for _ in range(args.steps):
+            batch.time_step()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t1
+    st1 = batch.stats()
+    total = int(ns.sum())
+    value = total * args.steps / dt
+    from masterthesislucas_gb300.solver import get_depth
+    line = {"metric": "t-SNE gradient steps of a batch of embeddings (particles/s over all systems)",
+            "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (64-dim Gaussian clusters per system, P built by the project's kNN/perplexity code)",
+            "config": {"workload": args.workload, "systems": int(w["systems"]), "particles": total,
+                       "n_min": int(ns.min()), "n_max": int(ns.max()), "perplexity": w["perplexity"], "k": 90,
+                       "leaf_size": w["max_children"], "theta": w["theta"],
+                       "orders": {"4": int((ns < 20000).sum()), "8": int((ns >= 20000).sum())},
+                       "depth_offsets": np.bincount([d - get_depth(w["max_children"], int(n))
+                                                     for d, n in zip(depths, ns)]).tolist(),
+                       "iterations_before_timing": w["presteps"] + args.warmup,
+                       "timing": "host clock around K batch steps (each one graph launch plus the flag check)",
+                       "l2": "inputs exceed L2 (the batch holds %d particles)" % total},
+            "steps_per_s": args.steps / dt,
+            "graph": {"launches_timed": st1["graph_launches"] - st0["graph_launches"],
+                      "captures_timed": st1["captures"] - st0["captures"],
+                      "restepped_timed": st1["restepped"] - st0["restepped"],
+                      "graph_ms_timed": st1["graph_ms"] - st0["graph_ms"],
+                      "restep_ms_timed": st1["restep_ms"] - st0["restep_ms"],
+                      "nodes": st1["graph_nodes"], "latency_ms": 1e3 * dt / args.steps},
+            "setup_s": {"affinities": round(t_p, 1), "total": round(t_setup, 1)},
+            "gpu_launches": st1["kernels_per_launch"] * args.steps,
+            "clocks": clk.summary()}
+    batch.close()
+    for s in systems:
+        s.close()
+    print(json.dumps(line))
+
+
 def run_bh(args, w):
     """Barnes-Hut force step (the reference's QuadTree and MAC) on the GPU."""
     import ctypes
@@ -653,6 +735,9 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         dist.init_process_group("nccl")
+    if w.get("method") == "tsne_batch":
+        run_tsne_batch(args, w)
+        return
     if w.get("method") == "leapfrog":
         run_leapfrog(args, w)
         return

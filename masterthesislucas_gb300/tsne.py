@@ -39,6 +39,8 @@ class TSNE:
         self._t = ctypes.c_void_p()
         check(lib().tc_tsne_create(ctypes.byref(cfg), self.n, ptr(self.row_ptr), ptr(self.col), ptr(self.val),
                                    ptr(y0), ctypes.byref(self._t)))
+        self.order = order
+        self.max_children = max_children
         self.learnRate = self.n / 15.0 if learn_rate is None else learn_rate
         self.early_exaggeration = early_exaggeration
         self.min_theta = min_theta
@@ -91,8 +93,7 @@ class TSNE:
         self.depth = int(depth)
 
 
-def tune_depth(system: TSNE, offsets=(0, 1, 2, 3), order: int = 8, theta: float = 0.5, leaf: int = 16,
-               reps: int = 2) -> dict:
+def tune_depth(system: TSNE, offsets=(0, 1, 2, 3), theta: float = 0.5, reps: int = 2) -> dict:
     """Autotunes one embedding's tree depth on its current positions: the
     device time of updateTree + solveNbody (CUDA events) at getDepth + each
     offset, with a separate solver on a copy of the embedding; the fastest
@@ -103,6 +104,7 @@ def tune_depth(system: TSNE, offsets=(0, 1, 2, 3), order: int = 8, theta: float 
     g = torch.zeros_like(y)
     tot = torch.zeros(1, dtype=torch.float64, device="cuda")
     stream = torch.cuda.Stream()
+    leaf, order = system.max_children, system.order
     d0 = get_depth(leaf, system.n)
     trials = []
     for off in offsets:
