@@ -144,7 +144,7 @@ def median_error(grad, ref):
     return float(np.median(e)), float(np.percentile(e, 90)), float(e.max())
 
 
-def train_controller(w, seed=0):
+def train_controller(w, seed=0, steps=CTRL_STEPS):
     """The learned-order controller: pair-error samples measured by the method
     on independently seeded 1M-particle systems of the workload's distribution,
     then the MLP trained by the library's own kernels (untimed)."""
@@ -153,10 +153,10 @@ def train_controller(w, seed=0):
     X, E = learned.generate(n_systems=CTRL_SYSTEMS, n_particles=1 << 20, kernel=w["kernel"],
                             per_level=CTRL_PER_LEVEL, seed=seed, leaf=w["max_children"])
     t1 = time.perf_counter()
-    ctrl, stats = learned.fit(X, E, steps=CTRL_STEPS, batch=8192, lr=2e-3, seed=seed)
+    ctrl, stats = learned.fit(X, E, steps=steps, batch=8192, lr=2e-3, seed=seed)
     stats.update({"samples": int(len(X)), "systems": CTRL_SYSTEMS, "system_n": 1 << 20,
                   "generate_s": round(t1 - t0, 2), "train_s": round(time.perf_counter() - t1, 2),
-                  "steps": CTRL_STEPS, "orders": list(learned.ORDERS)})
+                  "steps": steps, "orders": list(learned.ORDERS)})
     return ctrl, stats
 
 
@@ -235,7 +235,11 @@ def run_ours(args, w, rank, world):
     # learned-order controller
     learned_cfg, ltrials, ctrl_stats, ctrl = None, [], None, None
     if not args.no_learned:
-        ctrl, ctrl_stats = train_controller(w, seed=rank)
+        ctrl, ctrl_stats = train_controller(w, seed=rank, steps=args.ctrl_steps)
+    if ctrl is not None and args.tau:
+        from masterthesislucas_gb300.solver import get_depth
+        learned_cfg = {"depth": args.learned_depth or get_depth(w["max_children"], n) + 1, "tau": args.tau}
+    elif ctrl is not None:
         learned_cfg, ltrials = tune_learned(pos_d, ref, rows_d, ctrl, kernel=w["kernel"], softening=w["softening"],
                                             leaf=w["max_children"], target=target, stream=stream, device=dev.index)
     calib = {"plain_best": plain, "plain_p12": p12, "learned_best": learned_cfg, "plain_trials": trials,
@@ -694,6 +698,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=262144)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-order controller arm")
+    ap.add_argument("--tau", type=float, default=0.0, help="fix the controller tolerance instead of tuning it")
+    ap.add_argument("--learned-depth", type=int, default=0)
+    ap.add_argument("--ctrl-steps", type=int, default=CTRL_STEPS, help="controller training steps")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]
