@@ -76,6 +76,8 @@ def lib():
         L.orc_build_tree.argtypes = [ctypes.c_uint32, I64, P, P, P, P]
         L.orc_sym_fmm_solve.argtypes = [I, D, ctypes.c_uint32, D, I64, P, P, P, P]
         L.orc_sym_fmm.argtypes = [I, D, I, I, D, I64, P, P, P, P, P, P, P, P, P]
+        L.orc_fmm_morton_solve.argtypes = [I, D, D, P, P, P, P]
+        L.orc_fmm_morton.argtypes = [I, D, I, I, D, I64, P, P, P, P, P, P, P, P, P]
         L.orc_naive.argtypes = [I, D, I64, P, P, P, I]
         L.orc_direct_rows.argtypes = [I, D, I64, P, I64, P, P, I]
         L.orc_bh.argtypes = [I, D, I, D, I64, P, P, P]
@@ -128,8 +130,9 @@ def sort_perm(codes):
 
 
 def sym_fmm(pos, *, kernel=KERNEL_TSNE, eps=0.0, max_children=16, depth=-1, theta=0.5,
-            mn=None, mx=None, want_nodes=True):
-    """updateTree + solveNbody of the symmetric Morton FMM (sorted-order outputs)."""
+            mn=None, mx=None, want_nodes=True, symmetric=True):
+    """updateTree + solveNbody of the symmetric Morton FMM (sorted-order
+    outputs); symmetric=False runs the non-symmetric FMM_MORTON instead."""
     pos = np.ascontiguousarray(pos, np.float64)
     n = len(pos)
     if mn is None:
@@ -141,9 +144,9 @@ def sym_fmm(pos, *, kernel=KERNEL_TSNE, eps=0.0, max_children=16, depth=-1, thet
     g = np.zeros((n, 2))
     tot = np.zeros(1)
     nodes = np.zeros(node_count(d), NODE_DTYPE) if want_nodes else None
-    lib().orc_sym_fmm(kernel, eps, max_children, d, theta, n, _p(pos),
-                      _p(np.asarray(mn, np.float64)), _p(np.asarray(mx, np.float64)),
-                      _p(codes), _p(ids), _p(ps), _p(g), _p(tot), _p(nodes))
+    fn = lib().orc_sym_fmm if symmetric else lib().orc_fmm_morton
+    fn(kernel, eps, max_children, d, theta, n, _p(pos), _p(np.asarray(mn, np.float64)),
+       _p(np.asarray(mx, np.float64)), _p(codes), _p(ids), _p(ps), _p(g), _p(tot), _p(nodes))
     return dict(codes=codes, ids=ids, pos=ps, grad=g, total=float(tot[0]), nodes=nodes, depth=d)
 
 

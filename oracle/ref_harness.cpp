@@ -117,6 +117,56 @@ void GRAV_SYM_PP(double& total, TsnePoint2D& a, TsnePoint2D& b)
     total += 2.0 * t;
 }
 
+// gravity in the non-symmetric solver's slots (TSNEFMM_MORTON*Kernel layout,
+// nBodySolverFMM_MORTON.h:513-683): sink side only, C2/C3 with the source mass
+void GRAV_M_NN(double& total, NodeFMM_MORTON_2D& A, NodeFMM_MORTON_2D& B)
+{
+    glm::dvec2 R = A.centreOfMass - B.centreOfMass;
+    double D1, D2, D3, t;
+    grav_derivs(R.x * R.x + R.y * R.y, D1, D2, D3, t);
+    total += (A.M0 * B.M0) * t;
+    double c1[2];
+    Fastor::Tensor<double, 2, 2> C2;
+    Fastor::Tensor<double, 2, 2, 2> C3;
+    far_c1(R, B.M0, B.M2, D1, D2, D3, c1);
+    c2c3(R, B.M0, D1, D2, D3, C2, C3);
+    A.C1(0) += c1[0]; A.C1(1) += c1[1];
+    A.C2 += C2; A.C3 += C3;
+}
+
+void GRAV_M_PN(double& total, TsnePoint2D& p, NodeFMM_MORTON_2D& B)
+{
+    glm::dvec2 R = p.position - B.centreOfMass;
+    double D1, D2, D3, t;
+    grav_derivs(R.x * R.x + R.y * R.y, D1, D2, D3, t);
+    total += B.M0 * t;
+    double c1[2];
+    far_c1(R, B.M0, B.M2, D1, D2, D3, c1);
+    p.derivative += glm::dvec2(c1[0], c1[1]);
+}
+
+void GRAV_M_NP(double& total, NodeFMM_MORTON_2D& A, TsnePoint2D& p)
+{
+    glm::dvec2 R = A.centreOfMass - p.position;
+    double D1, D2, D3, t;
+    grav_derivs(R.x * R.x + R.y * R.y, D1, D2, D3, t);
+    total += A.M0 * t;
+    Fastor::Tensor<double, 2, 2> C2;
+    Fastor::Tensor<double, 2, 2, 2> C3;
+    c2c3(R, 1.0, D1, D2, D3, C2, C3);
+    A.C1(0) += R.x * D1; A.C1(1) += R.y * D1;
+    A.C2 += C2; A.C3 += C3;
+}
+
+void GRAV_M_PP(double& total, TsnePoint2D& a, TsnePoint2D& b)
+{
+    glm::dvec2 R = a.position - b.position;
+    double D1, D2, D3, t;
+    grav_derivs(R.x * R.x + R.y * R.y, D1, D2, D3, t);
+    total += t;
+    a.derivative += D1 * R;
+}
+
 void GRAV_NAIVE(double& total, TsnePoint2D& a, TsnePoint2D& b)
 {
     glm::dvec2 R = a.position - b.position;
@@ -188,9 +238,13 @@ int ref_sym_fmm(int kernel, double eps, int max_children, int depth, double thet
         t_solve = std::chrono::duration<double>(t2 - t1).count();
         nv = &sym->nodes;
     } else {
-        if (kernel != 0) return -1;
-        asym = new NBodySolverFMM_MORTON<TsnePoint2D>(&TSNEFMM_MORTONNNKernel, &TSNEFMM_MORTONPNKernel, &TSNEFMM_MORTONNPKernel,
-                                                       &TSNEFMM_MORTONPPKernel, max_children, depth, theta);
+        if (kernel == 0)
+            asym = new NBodySolverFMM_MORTON<TsnePoint2D>(&TSNEFMM_MORTONNNKernel, &TSNEFMM_MORTONPNKernel,
+                                                           &TSNEFMM_MORTONNPKernel, &TSNEFMM_MORTONPPKernel,
+                                                           max_children, depth, theta);
+        else
+            asym = new NBodySolverFMM_MORTON<TsnePoint2D>(&GRAV_M_NN, &GRAV_M_PN, &GRAV_M_NP, &GRAV_M_PP,
+                                                           max_children, depth, theta);
         auto t0 = std::chrono::steady_clock::now();
         asym->updateTree(pts, mn, mx);
         auto t1 = std::chrono::steady_clock::now();

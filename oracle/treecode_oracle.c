@@ -485,6 +485,235 @@ void orc_sym_fmm_solve(int kernel, double eps, uint32_t depth, double theta, int
     *total = c.total;
 }
 
+/* ------------------------------------------------------------------ */
+/* non-symmetric FMM_MORTON (nBodySolverFMM_MORTON.h)                  */
+/* ------------------------------------------------------------------ */
+
+/* the non-symmetric kernels' radial factors (:517-522): D1 = 1/(rS rS),
+ * D2 = -4/(rS rS rS), D3 = 24/(rS rS rS rS) -- divided directly, which
+ * rounds differently from the symmetric kernels' reciprocal powers          */
+static inline derivs tsne_derivs_m(double sq_r)
+{
+    derivs d;
+    double rS = 1.0 + sq_r;
+    d.D1 = 1.0 / (rS * rS);
+    d.D2 = -4.0 / (rS * rS * rS);
+    d.D3 = 24.0 / (rS * rS * rS * rS);
+    d.t = rS;
+    return d;
+}
+
+/* TSNEFMM_MORTONNNKernel (:513-582) / gravity counterpart: the sink only;
+ * C2 and C3 carry the source mass alone (no MA0).                          */
+static void m_kernel_nn(sym_ctx* c, orc_node* A, orc_node* B)
+{
+    double Rx = A->com[0] - B->com[0];
+    double Ry = A->com[1] - B->com[1];
+    double sq = Rx * Rx + Ry * Ry;
+    double C1[2], C2[4], C3[8];
+    derivs d = (c->kernel == ORC_KERNEL_TSNE) ? tsne_derivs_m(sq) : grav_derivs(sq, c->eps2);
+    if (c->kernel == ORC_KERNEL_TSNE)
+        c->total += (A->m0 * B->m0) / d.t;
+    else
+        c->total += (A->m0 * B->m0) * d.t;
+    far_c1(Rx, Ry, B->m0, B->m2, d.D1, d.D2, d.D3, C1);
+    if (c->kernel == ORC_KERNEL_TSNE)
+        c2c3(Rx, Ry, B->m0, 1.0, 0, d.D1, d.D2, d.D3, C2, C3);
+    else
+        c2c3_grav(Rx, Ry, B->m0, d.D1, d.D2, d.D3, C2, C3);
+    A->c1[0] += C1[0]; A->c1[1] += C1[1];
+    for (int i = 0; i < 4; i++) A->c2[i] += C2[i];
+    for (int i = 0; i < 8; i++) A->c3[i] += C3[i];
+}
+
+/* TSNEFMM_MORTONPNKernel (:584-613): M2P into the sink point              */
+static void m_kernel_pn(sym_ctx* c, int64_t p, orc_node* B)
+{
+    const double* x = c->pos + 2 * p;
+    double Rx = x[0] - B->com[0];
+    double Ry = x[1] - B->com[1];
+    double sq = Rx * Rx + Ry * Ry;
+    double C1[2];
+    derivs d = (c->kernel == ORC_KERNEL_TSNE) ? tsne_derivs_m(sq) : grav_derivs(sq, c->eps2);
+    if (c->kernel == ORC_KERNEL_TSNE)
+        c->total += B->m0 / d.t;
+    else
+        c->total += B->m0 * d.t;
+    far_c1(Rx, Ry, B->m0, B->m2, d.D1, d.D2, d.D3, C1);
+    c->grad[2 * p] += C1[0];
+    c->grad[2 * p + 1] += C1[1];
+}
+
+/* TSNEFMM_MORTONNPKernel (:615-673): P2L into the sink node (unit mass)   */
+static void m_kernel_np(sym_ctx* c, orc_node* A, int64_t p)
+{
+    const double* x = c->pos + 2 * p;
+    double Rx = A->com[0] - x[0];
+    double Ry = A->com[1] - x[1];
+    double sq = Rx * Rx + Ry * Ry;
+    double C2[4], C3[8];
+    derivs d = (c->kernel == ORC_KERNEL_TSNE) ? tsne_derivs_m(sq) : grav_derivs(sq, c->eps2);
+    if (c->kernel == ORC_KERNEL_TSNE) {
+        c->total += A->m0 / d.t;
+        c2c3(Rx, Ry, 1.0, 1.0, 0, d.D1, d.D2, d.D3, C2, C3);
+    } else {
+        c->total += A->m0 * d.t;
+        c2c3_grav(Rx, Ry, 1.0, d.D1, d.D2, d.D3, C2, C3);
+    }
+    A->c1[0] += (Rx * d.D1);
+    A->c1[1] += (Ry * d.D1);
+    for (int i = 0; i < 4; i++) A->c2[i] += C2[i];
+    for (int i = 0; i < 8; i++) A->c3[i] += C3[i];
+}
+
+/* TSNEFMM_MORTONPPKernel (:675-683): the sink point only                  */
+static void m_kernel_pp(sym_ctx* c, int64_t a, int64_t b)
+{
+    const double* xa = c->pos + 2 * a;
+    const double* xb = c->pos + 2 * b;
+    double Rx = xa[0] - xb[0];
+    double Ry = xa[1] - xb[1];
+    double sq = Rx * Rx + Ry * Ry;
+    if (c->kernel == ORC_KERNEL_TSNE) {
+        double fd = 1.0 / (1.0 + sq);
+        c->total += fd;
+        c->grad[2 * a] += fd * fd * Rx;
+        c->grad[2 * a + 1] += fd * fd * Ry;
+    } else {
+        derivs d = grav_derivs(sq, c->eps2);
+        c->total += d.t;
+        c->grad[2 * a] += d.D1 * Rx;
+        c->grad[2 * a + 1] += d.D1 * Ry;
+    }
+}
+
+/* traverseBHMP (:199-232): point-node MAC L_B / |x - com_B| < theta        */
+static void m_trav_bhmp(sym_ctx* c, int64_t p, orc_node* B)
+{
+    const double* x = c->pos + 2 * p;
+    double dx = x[0] - B->com[0], dy = x[1] - B->com[1];
+    double dist = sqrt(dx * dx + dy * dy);
+    if (B->bb_len / dist < c->theta) {
+        m_kernel_pn(c, p, B);
+    } else if (B->first_child == 0) {
+        for (int64_t q = B->first_part; q < (int64_t)B->first_part + B->count; q++)
+            if (q != p) m_kernel_pp(c, p, q);
+    } else {
+        for (uint32_t k = B->first_child; k < B->first_child + 4; k++)
+            if (c->nodes[k].count != 0) m_trav_bhmp(c, p, &c->nodes[k]);
+    }
+}
+
+/* traverseBHRMP (:234-268): node-point MAC L_A / |com_A - x| < theta       */
+static void m_trav_bhrmp(sym_ctx* c, orc_node* A, int64_t p)
+{
+    const double* x = c->pos + 2 * p;
+    double dx = A->com[0] - x[0], dy = A->com[1] - x[1];
+    double dist = sqrt(dx * dx + dy * dy);
+    if (A->bb_len / dist < c->theta) {
+        m_kernel_np(c, A, p);
+    } else if (A->first_child == 0) {
+        for (int64_t q = A->first_part; q < (int64_t)A->first_part + A->count; q++)
+            if (q != p) m_kernel_pp(c, q, p);
+    } else {
+        for (uint32_t k = A->first_child; k < A->first_child + 4; k++)
+            if (c->nodes[k].count != 0) m_trav_bhrmp(c, &c->nodes[k], p);
+    }
+}
+
+/* traverseFMM (:148-197): ordered (sink, source) pairs, MAC
+ * (L_A + L_B) / |com_A - com_B| < theta.                                   */
+static void m_trav(sym_ctx* c, orc_node* A, orc_node* B)
+{
+    double dx = A->com[0] - B->com[0], dy = A->com[1] - B->com[1];
+    double dist = sqrt(dx * dx + dy * dy);
+    if ((A->bb_len + B->bb_len) / dist < c->theta) {
+        if (A->count != 0 && B->count != 0) m_kernel_nn(c, A, B);
+    } else if (A->first_child == 0) {
+        for (int64_t i = A->first_part; i < (int64_t)A->first_part + A->count; i++)
+            if (B->count != 0) m_trav_bhmp(c, i, B);
+    } else if (B->first_child == 0) {
+        for (int64_t j = B->first_part; j < (int64_t)B->first_part + B->count; j++)
+            if (A->count != 0) m_trav_bhrmp(c, A, j);
+    } else {
+        for (uint32_t a = A->first_child; a < A->first_child + 4; a++)
+            for (uint32_t b = B->first_child; b < B->first_child + 4; b++)
+                if (c->nodes[a].count != 0 && c->nodes[b].count != 0) m_trav(c, &c->nodes[a], &c->nodes[b]);
+    }
+}
+
+/* applyForces (:382-430): as the symmetric solver's, without the M0
+ * normalisation (the kernels never applied the sink mass).                */
+static void m_apply_forces(sym_ctx* c, orc_node* q)
+{
+    if (q->first_child != 0) {
+        for (uint32_t k = q->first_child; k < q->first_child + 4; k++) {
+            orc_node* ch = &c->nodes[k];
+            if (ch->count == 0) continue;
+            double d[2] = {ch->com[0] - q->com[0], ch->com[1] - q->com[1]};
+            double e1[2], e3[4], e31[2], e2[4];
+            contract2(d, q->c2, e1);
+            contract3(d, q->c3, e3);
+            contract2(d, e3, e31);
+            for (int i = 0; i < 2; i++) ch->c1[i] += q->c1[i] + e1[i] + 0.5 * e31[i];
+            for (int i = 0; i < 4; i++) e2[i] = q->c2[i] + e3[i];
+            for (int i = 0; i < 4; i++) ch->c2[i] += e2[i];
+            for (int i = 0; i < 8; i++) ch->c3[i] += q->c3[i];
+            m_apply_forces(c, ch);
+        }
+    } else {
+        for (int64_t p = q->first_part; p < (int64_t)q->first_part + q->count; p++) {
+            double d[2] = {c->pos[2 * p] - q->com[0], c->pos[2 * p + 1] - q->com[1]};
+            double e1[2], e3[4], e31[2];
+            contract2(d, q->c2, e1);
+            contract3(d, q->c3, e3);
+            contract2(d, e3, e31);
+            c->grad[2 * p] += q->c1[0] + e1[0] + 0.5 * e31[0];
+            c->grad[2 * p + 1] += q->c1[1] + e1[1] + 0.5 * e31[1];
+        }
+    }
+}
+
+void orc_fmm_morton_solve(int kernel, double eps, double theta, const double* pos, orc_node* nodes,
+                          double* grad, double* total)
+{
+    sym_ctx c;
+    c.kernel = kernel;
+    c.eps2 = eps * eps;
+    c.theta = theta;
+    c.pos = pos;
+    c.grad = grad;
+    c.nodes = nodes;
+    c.total = *total;
+    m_trav(&c, &nodes[0], &nodes[0]);
+    m_apply_forces(&c, &nodes[0]);
+    *total = c.total;
+}
+
+void orc_fmm_morton(int kernel, double eps, int max_children, int depth, double theta, int64_t n,
+                    const double* pos, const double min_xy[2], const double max_xy[2],
+                    uint32_t* codes_sorted, int32_t* ids_sorted, double* pos_sorted,
+                    double* grad_sorted, double* total, orc_node* nodes)
+{
+    uint32_t d = depth >= 0 ? (uint32_t)depth : orc_get_depth(max_children, n);
+    uint32_t* codes = (uint32_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(uint32_t));
+    orc_morton_codes(n, pos, min_xy, max_xy, codes);
+    orc_sort_perm(n, codes, ids_sorted);
+    for (int64_t k = 0; k < n; k++) {
+        int32_t i = ids_sorted[k];
+        codes_sorted[k] = codes[i];
+        pos_sorted[2 * k] = pos[2 * i];
+        pos_sorted[2 * k + 1] = pos[2 * i + 1];
+    }
+    free(codes);
+    int64_t nn = orc_node_count(d);
+    orc_node* own = NULL;
+    if (!nodes) nodes = own = (orc_node*)malloc((size_t)nn * sizeof(orc_node));
+    orc_build_tree(d, n, pos_sorted, min_xy, max_xy, nodes);
+    if (n > 0) orc_fmm_morton_solve(kernel, eps, theta, pos_sorted, nodes, grad_sorted, total);
+    free(own);
+}
+
 void orc_sym_fmm(int kernel, double eps, int max_children, int depth, double theta, int64_t n,
                  const double* pos, const double min_xy[2], const double max_xy[2],
                  uint32_t* codes_sorted, int32_t* ids_sorted, double* pos_sorted,

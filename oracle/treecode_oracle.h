@@ -69,6 +69,19 @@ void orc_sym_fmm(int kernel, double eps, int max_children, int depth, double the
                  uint32_t* codes_sorted, int32_t* ids_sorted, double* pos_sorted,
                  double* grad_sorted, double* total, orc_node* nodes /* may be NULL */);
 
+/* NBodySolverFMM_MORTON (nBodySolverFMM_MORTON.h), the non-symmetric
+ * variant: traverseFMM (:148-197) over ordered (sink, source) pairs with
+ * the MAC (L_A + L_B)/|com_A - com_B| < theta, traverseBHMP/BHRMP
+ * (:199-268), kernels NN/PN/NP/PP (:513-683; gravity as in the symmetric
+ * solver), applyForces (:382-430).  Same tree build; arguments as
+ * orc_sym_fmm / orc_sym_fmm_solve.                                         */
+void orc_fmm_morton_solve(int kernel, double eps, double theta, const double* pos_sorted, orc_node* nodes,
+                          double* grad, double* total);
+void orc_fmm_morton(int kernel, double eps, int max_children, int depth, double theta,
+                    int64_t n, const double* pos, const double min_xy[2], const double max_xy[2],
+                    uint32_t* codes_sorted, int32_t* ids_sorted, double* pos_sorted,
+                    double* grad_sorted, double* total, orc_node* nodes /* may be NULL */);
+
 /* NBodySolverNaive::solveNbody + TSNEnaiveKernel (nBodySolverNaive.h:53-141):
  * FP64 O(N^2), input order, nthreads row partitions.  grad is overwritten. */
 void orc_naive(int kernel, double eps, int64_t n, const double* pos, double* grad,

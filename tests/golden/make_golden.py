@@ -75,6 +75,15 @@ def tsne_step_case(name, n=600, dim=16, steps=3, seed=21, theta=0.5, exag_code=1
          perplexity=perplexity)
 
 
+def asym_cases():
+    """The non-symmetric NBodySolverFMM_MORTON (gravity put in its kernel slots)."""
+    sym_case("asym_grav_mixture_4096", datasets.gaussian_mixture(4096, seed=6), kernel=1, eps=1e-3,
+             symmetric=False)
+    sym_case("asym_tsne_deep_2000_theta1", np.random.default_rng(15).uniform(-5, 5, (2000, 2)), depth=5,
+             theta=1.0, symmetric=False)
+    sym_case("asym_tsne_tiny_17", np.random.default_rng(117).normal(0, 1, (17, 2)), symmetric=False)
+
+
 def main():
     if oracle.build_ref() is None:
         raise SystemExit("reference sources not found; fixtures cannot be regenerated")
@@ -91,6 +100,7 @@ def main():
     for n in (2, 3, 17, 64):
         sym_case(f"sym_tsne_tiny_{n}", np.random.default_rng(100 + n).normal(0, 1, (n, 2)))
     sym_case("asym_tsne_gauss_3000", rng.normal(0, 3, (3000, 2)), symmetric=False)
+    asym_cases()
     for kernel, eps, tag in ((0, 0.0, "tsne"), (1, 1e-3, "grav")):
         pos = datasets.gaussian_mixture(1500, seed=31).astype(np.float64)
         g, t = oracle.ref_naive(pos, kernel=kernel, eps=eps)

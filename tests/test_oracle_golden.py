@@ -13,13 +13,18 @@ SYM_CASES = ["sym_tsne_gauss_3000", "sym_grav_mixture_4096", "sym_tsne_ties_1000
              "sym_tsne_tiny_3", "sym_tsne_tiny_17", "sym_tsne_tiny_64"]
 
 
-@pytest.mark.parametrize("case", SYM_CASES)
+# the non-symmetric NBodySolverFMM_MORTON (nBodySolverFMM_MORTON.h)
+ASYM_CASES = ["asym_tsne_gauss_3000", "asym_grav_mixture_4096", "asym_tsne_deep_2000_theta1",
+              "asym_tsne_tiny_17"]
+
+
+@pytest.mark.parametrize("case", SYM_CASES + ASYM_CASES)
 def test_sym_fmm_bit_exact(golden, case):
     g = golden(case)
     mn, mx = g["minmax"][:2], g["minmax"][2:]
     r = oracle.sym_fmm(g["pos"], kernel=int(g["kernel"]), eps=float(g["eps"]),
                        max_children=int(g["max_children"]), depth=int(g["depth"]),
-                       theta=float(g["theta"]), mn=mn, mx=mx)
+                       theta=float(g["theta"]), mn=mn, mx=mx, symmetric=not case.startswith("asym"))
     assert r["depth"] == int(g["depth"])
     np.testing.assert_array_equal(r["codes"], g["codes"])
     np.testing.assert_array_equal(r["ids"], g["ids"])
