@@ -72,6 +72,19 @@ int tc_destroy(tc_handle* h);
  * (TSNE::setThetaForAll, src/nBodyInstances/tsne.h:245-252).               */
 int tc_set_theta(tc_handle* h, double theta);
 
+/* Solver variant at the reference's expansion order (tc_config.order 0):
+ * TC_VARIANT_SYM       NBodySolverFMM_SYM_MORTON (the default),
+ * TC_VARIANT_MORTON    NBodySolverFMM_MORTON (src/nbodysolvers/cpu/
+ *                      nBodySolverFMM_MORTON.h:28-505): ordered (sink,
+ *                      source) traversal with the MAC (L_A + L_B)/|dcom| <
+ *                      theta, node-node kernels into the sink only, and at
+ *                      the leaves M2P (L_T/|x - com_T| < theta) or P2P for
+ *                      every sink point (traverseBHMP, :199-232).
+ * Takes effect at the next tc_update_tree.                                 */
+#define TC_VARIANT_SYM 0
+#define TC_VARIANT_MORTON 1
+int tc_set_variant(tc_handle* h, int variant);
+
 /* getDepth (nBodySolverFMM_SYM_MORTON.h:106-115), clamped at 0 for n < leaf. */
 int tc_get_depth(int max_children, int64_t n, uint32_t* depth);
 /* node count of the level-dense tree, initNodesSize (:117-151).             */

@@ -23,6 +23,8 @@ TC_KERNEL_TSNE = 0
 TC_KERNEL_GRAVITY = 1
 TC_PREC_FP32 = 0
 TC_PREC_FP64 = 1
+TC_VARIANT_SYM = 0
+TC_VARIANT_MORTON = 1
 
 
 class TcConfig(ctypes.Structure):
@@ -47,6 +49,7 @@ SIGNATURES = {
     "tc_create": (_I, [_P, _P]),
     "tc_destroy": (_I, [_P]),
     "tc_set_theta": (_I, [_P, _D]),
+    "tc_set_variant": (_I, [_P, _I]),
     "tc_get_depth": (_I, [_I, _I64, _P]),
     "tc_node_count": (_I, [ctypes.c_uint32, _P]),
     "tc_update_tree": (_I, [_P, _P, _P, _I64, _P, _P]),

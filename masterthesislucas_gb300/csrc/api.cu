@@ -591,3 +591,18 @@ extern "C" int tc_async_status(tc_handle* t)
     const Handle& h = t->h;
     return (h.h_words[8] ? 1 : 0) | (h.h_words[40] ? 2 : 0);
 }
+
+extern "C" int tc_set_variant(tc_handle* t, int variant)
+{
+    if (!t || (variant != TC_VARIANT_SYM && variant != TC_VARIANT_MORTON)) {
+        tc_set_error("tc_set_variant: unknown variant");
+        return TC_ERR_INVALID;
+    }
+    if (variant == TC_VARIANT_MORTON && t->h.cfg.order != 0) {
+        tc_set_error("tc_set_variant: the non-symmetric solver runs at the reference's expansion order (order 0)");
+        return TC_ERR_INVALID;
+    }
+    t->h.variant = variant;
+    t->h.tree_ready = false;  // the interaction lists depend on the MAC
+    return TC_OK;
+}

@@ -89,7 +89,9 @@ __device__ inline void add_shifted(const real* C, real dx, real dy, real* acc)
 struct Geo {
     int depth;
     double inv_theta;
+    double theta;
     double h_leaf;     // leaf cell size
+    int variant;       // 1: the non-symmetric FMM_MORTON leaf stage
 };
 
 template <typename real, typename K>
@@ -141,6 +143,14 @@ __global__ void __launch_bounds__(128) k_m2l(K ker, int l, real hl, const uint32
             zpart[na] = zz;
         }
     }
+}
+
+// point-node MAC of the non-symmetric solver's traverseBHMP
+// (nBodySolverFMM_MORTON.h:201-204): L_B / |x - com_B| < theta
+__device__ inline bool pn_pass_m(double2 x, double2 com, double len, double theta)
+{
+    double dx = x.x - com.x, dy = x.y - com.y;
+    return len / sqrt(dx * dx + dy * dy) < theta;
 }
 
 // point-node MAC of traverse_SYM_PN, exactly as the reference evaluates it
@@ -207,7 +217,7 @@ __global__ void __launch_bounds__(32 * kLeafWarps)
             const real dy = h * (((real)isy + real(0.5)) - (iay + real(0.5)) * scale) + (csy - comrel[2 * A + 1]);
             add_shifted(CA, dx, dy, C);
         }
-        for (uint32_t e = e0; e < e1; e++) {
+        for (uint32_t e = e0; e < e1 && !geo.variant; e++) {  // the non-symmetric solver has no P2L here
             const uint32_t ti = near_idx[e];
             if (ti >= (uint32_t)si) continue;
             const int64_t T = li + ti;
@@ -297,7 +307,50 @@ __global__ void __launch_bounds__(32 * kLeafWarps)
             const real ox = real(isx - (int)compact16(ti)) * h, oy = real(isy - (int)compact16(ti >> 1)) * h;
             // base = x_s - (cell centre of T); each source subtracts its prel
             const real bx = ox + px, by = oy + py;
-            if (ti == (uint32_t)si) {
+            if (geo.variant) {
+                // non-symmetric: every sink tests every partner T (S itself
+                // included): M2P when L_T / |x - com_T| < theta, else P2P over
+                // T without the sink itself (traverseBHMP, :199-232)
+                const bool pass = act && pn_pass_m(x64, com64[T], bblen[T], geo.theta);
+                if (pass) {
+                    const real Rx = bx - comrel[2 * T], Ry = by - comrel[2 * T + 1];
+                    real D1, D2, D3, t;
+                    ker.far(Rx * Rx + Ry * Ry, D1, D2, D3, t);
+                    const real mT = m0r[T];
+                    real c1x, c1y;
+                    far_c1(Rx, Ry, mT, m2t[3 * T], m2t[3 * T + 1], m2t[3 * T + 2], D1, D2, D3, c1x, c1y);
+                    gx += c1x;
+                    gy += c1y;
+                    zs += mT * t;
+                    n_m2p++;
+                }
+                const bool direct = act && !pass;
+                if (__any_sync(0xffffffffu, direct)) {
+                    for (uint32_t q0 = 0; q0 < cT; q0 += 32) {
+                        const uint32_t q = q0 + lane;
+                        if (q < cT) {
+                            s_src[w][lane][0] = prel[2 * (fT + q)];
+                            s_src[w][lane][1] = prel[2 * (fT + q) + 1];
+                        }
+                        __syncwarp();
+                        const uint32_t m = min(32u, cT - q0);
+                        if (direct) {
+                            const bool self = ti == (uint32_t)si && sl >= q0 && sl < q0 + m;
+                            n_pp += m - (self ? 1u : 0u);
+                            for (uint32_t j = 0; j < m; j++) {
+                                if (self && q0 + j == sl) continue;
+                                const real Rx = bx - s_src[w][j][0], Ry = by - s_src[w][j][1];
+                                real D1, t;
+                                ker.near(Rx * Rx + Ry * Ry, D1, t);
+                                gx += D1 * Rx;
+                                gy += D1 * Ry;
+                                zs += t;
+                            }
+                        }
+                        __syncwarp();
+                    }
+                }
+            } else if (ti == (uint32_t)si) {
                 for (uint32_t q0 = 0; q0 < cT; q0 += 32) {
                     const uint32_t q = q0 + lane;
                     if (q < cT) {
@@ -507,7 +560,9 @@ int solve_t(Handle& h, K ker, double* d_grad, int accumulate, int scatter, doubl
     Geo geo;
     geo.depth = dep;
     geo.inv_theta = 1.0 / h.cfg.theta;
+    geo.theta = h.cfg.theta;
     geo.h_leaf = h.L / (double)(1u << dep);
+    geo.variant = h.variant;
     // work items of the near field: 32-sink chunks of the non-empty leaves
     const int64_t wmax = h.n / 32 + (h.n < nleaf ? h.n : nleaf) + 1;
     if ((rc = ensure(h.chunk, (nleaf + 1) * 4)) || (rc = ensure(h.zwork, wmax * 8)) ||

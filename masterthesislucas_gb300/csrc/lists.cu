@@ -32,6 +32,15 @@ __device__ inline bool mac_accept(double2 a, double2 b, double len, double inv_t
     return dist > thr * thr;
 }
 
+// the non-symmetric solver's MAC (nBodySolverFMM_MORTON.h:150-153):
+// (L_A + L_B) / |com_A - com_B| < theta, in the reference's operation order
+__device__ inline bool mac_accept_m(double2 a, double2 b, double len, double theta)
+{
+    double dx = a.x - b.x, dy = a.y - b.y;
+    double dist = sqrt(dx * dx + dy * dy);
+    return (len + len) / dist < theta;
+}
+
 // The same decision, decided in FP32 from cell-relative COMs whenever the FP32
 // squared distance is farther than a relative 1e-5 from the threshold (the
 // FP32 distance is accurate to ~1e-7 relative for the offsets that occur);
@@ -39,7 +48,7 @@ __device__ inline bool mac_accept(double2 a, double2 b, double len, double inv_t
 // 1/64 of FP32, and the band holds a vanishing fraction of candidates.
 template <typename real>
 __device__ inline bool mac_accept_fast(int dix, int diy, real hl, real thr2, const real* cra, const real* crb,
-                                       double2 a, double2 b, double len, double inv_theta)
+                                       double2 a, double2 b, double len, double inv_theta, double theta, int variant)
 {
     if (sizeof(real) == 4) {
         const real dx = (real)dix * hl + (cra[0] - crb[0]);
@@ -48,12 +57,12 @@ __device__ inline bool mac_accept_fast(int dix, int diy, real hl, real thr2, con
         if (d2 > thr2 * (real)(1.0 + 1e-5)) return true;
         if (d2 < thr2 * (real)(1.0 - 1e-5)) return false;
     }
-    return mac_accept(a, b, len, inv_theta);
+    return variant ? mac_accept_m(a, b, len, theta) : mac_accept(a, b, len, inv_theta);
 }
 
 // one thread per node of level l; fill == 0 counts, fill == 1 writes
 template <typename real>
-__global__ void k_lists(int l, double inv_theta, real hl, const uint32_t* __restrict__ count,
+__global__ void k_lists(int l, double inv_theta, double theta, int variant, real hl, const uint32_t* __restrict__ count,
                         const double2* __restrict__ com64, const real* __restrict__ comrel,
                         const double* __restrict__ bblen, const uint32_t* __restrict__ pnear_ptr,
                         const uint32_t* __restrict__ pnear_idx, uint32_t pcap, uint32_t* __restrict__ nn_cnt,
@@ -90,7 +99,8 @@ __global__ void k_lists(int l, double inv_theta, real hl, const uint32_t* __rest
                         const uint32_t b = 4 * bp + j;
                         if (count[li + b] == 0) continue;
                         if (mac_accept_fast<real>(iax - (int)compact16(b), iay - (int)compact16(b >> 1), hl, thr2, cra,
-                                                  comrel + 2 * (li + b), ca, com64[li + b], len, inv_theta)) {
+                                                  comrel + 2 * (li + b), ca, com64[li + b], len, inv_theta, theta,
+                                                  variant)) {
                             if (fill) {
                                 if (nb + nn < nn_cap) nn_idx[nb + nn] = b;
                                 else atomicOr(ovf, 1u);
@@ -385,12 +395,14 @@ int build_lists(Handle& h)
                                                                     nri, nrcap, ovf_flag);
             }
         } else if (h.cfg.precision == TC_PREC_FP64)
-            k_lists<double><<<grid_for(nl, 128), 128, 0, s>>>(l, inv_theta, hl, P<uint32_t>(h.count),
+            k_lists<double><<<grid_for(nl, 128), 128, 0, s>>>(l, inv_theta, h.cfg.theta, h.variant, hl,
+                                                             P<uint32_t>(h.count),
                                                              P<double2>(h.com64), P<double>(h.comrel),
                                                              P<double>(h.bblen), pnp, pni, pcap, nnc, nrc, nnp, nni,
                                                              nncap, nrp, nri, nrcap, ovf_flag, fill);
         else
-            k_lists<float><<<grid_for(nl, 128), 128, 0, s>>>(l, inv_theta, (float)hl, P<uint32_t>(h.count),
+            k_lists<float><<<grid_for(nl, 128), 128, 0, s>>>(l, inv_theta, h.cfg.theta, h.variant, (float)hl,
+                                                            P<uint32_t>(h.count),
                                                             P<double2>(h.com64), P<float>(h.comrel),
                                                             P<double>(h.bblen), pnp, pni, pcap, nnc, nrc, nnp, nni,
                                                             nncap, nrp, nri, nrcap, ovf_flag, fill);

@@ -60,6 +60,8 @@ struct Handle {
     // learned order controller (order-p mode): weights + normalisation copy
     // no-sync mode (stream capture): no host round trips or stage events; the
     // outside-box and list-overflow flags are copied to pinned h_words[8], [40]
+    // reference-order solver: 0 the symmetric FMM_SYM_MORTON, 1 the non-symmetric FMM_MORTON
+    int variant = 0;
     bool nosync = false;
     double cap_slack = 0.25;  // fast-mode list capacity: exact total * (1 + slack) + 256
     bool ctrl_on = false;

@@ -207,6 +207,20 @@ class NBodySolverFMM_SYM_MORTON:
         check(lib().tc_solve_device(self._h, ptr(grad), ptr(total), int(accumulate), int(scatter)))
 
 
+class NBodySolverFMM_MORTON(NBodySolverFMM_SYM_MORTON):
+    """The reference's non-symmetric Morton FMM (src/nbodysolvers/cpu/
+    nBodySolverFMM_MORTON.h): the same tree, ordered (sink, source) pairs,
+    kernels applied to the sink only, M2P/P2P per sink point at the leaves.
+    Runs at the reference's expansion order."""
+
+    def __init__(self, kernel: str = "tsne", max_children: int = 16, tree_depth: int | None = None,
+                 theta: float = 0.5, **kw):
+        if kw.get("order", 0):
+            raise ValueError("NBodySolverFMM_MORTON runs at the reference's expansion order (order 0)")
+        super().__init__(kernel, max_children=max_children, tree_depth=tree_depth, theta=theta, **kw)
+        check(lib().tc_set_variant(self._h, _lib.TC_VARIANT_MORTON))
+
+
 def direct(pos, *, kernel="tsne", softening=1e-3, precision="fp64", rows=None):
     """O(N^2) force on `rows` (all points when None) on the GPU."""
     pos = np.ascontiguousarray(pos, np.float64)

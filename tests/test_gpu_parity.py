@@ -1,4 +1,5 @@
-"""GPU parity of the symmetric Morton FMM against the reference's own outputs.
+"""GPU parity of the symmetric Morton FMM (and of the non-symmetric
+FMM_MORTON variant) against the reference's own outputs.
 
 Golden fixtures come from the reference's CPU solvers compiled from their
 sources (tests/golden/make_golden.py).  Contract:
@@ -13,7 +14,7 @@ sources (tests/golden/make_golden.py).  Contract:
 import numpy as np
 import pytest
 
-from masterthesislucas_gb300 import NBodySolverFMM_SYM_MORTON, Points, datasets, direct
+from masterthesislucas_gb300 import NBodySolverFMM_MORTON, NBodySolverFMM_SYM_MORTON, Points, datasets, direct
 from masterthesislucas_gb300._lib import TreecodeError
 
 pytestmark = pytest.mark.gpu
@@ -22,13 +23,19 @@ SYM_CASES = ["sym_tsne_gauss_3000", "sym_grav_mixture_4096", "sym_tsne_ties_1000
              "sym_tsne_deep_2000_theta1", "sym_grav_disks_3000_theta03", "sym_tsne_tiny_2",
              "sym_tsne_tiny_3", "sym_tsne_tiny_17", "sym_tsne_tiny_64"]
 
+# the non-symmetric NBodySolverFMM_MORTON
+ASYM_CASES = ["asym_tsne_gauss_3000", "asym_grav_mixture_4096", "asym_tsne_deep_2000_theta1",
+              "asym_tsne_tiny_17"]
+ALL_CASES = SYM_CASES + ASYM_CASES
+
 FP32_MEDIAN = 2e-6
 FP32_MAX = 1e-3
 
 
-def run_case(g, precision):
+def run_case(g, precision, case=""):
     kernel = "tsne" if int(g["kernel"]) == 0 else "gravity"
-    s = NBodySolverFMM_SYM_MORTON(kernel, max_children=int(g["max_children"]), tree_depth=int(g["depth"]),
+    cls = NBodySolverFMM_MORTON if case.startswith("asym") else NBodySolverFMM_SYM_MORTON
+    s = cls(kernel, max_children=int(g["max_children"]), tree_depth=int(g["depth"]),
                                   theta=float(g["theta"]), softening=float(g["eps"]) or 1e-3,
                                   precision=precision)
     pts = Points.from_positions(g["pos"])
@@ -45,10 +52,10 @@ def rel_err(a, b):
 
 
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
-@pytest.mark.parametrize("case", SYM_CASES)
+@pytest.mark.parametrize("case", ALL_CASES)
 def test_tree_bit_exact(golden, case, precision):
     g = golden(case)
-    s, pts, dump, _, _ = run_case(g, precision)
+    s, pts, dump, _, _ = run_case(g, precision, case)
     np.testing.assert_array_equal(dump["codes"], g["codes"])
     np.testing.assert_array_equal(dump["perm"], g["ids"])
     np.testing.assert_array_equal(pts.ID, g["ids"])
@@ -58,10 +65,10 @@ def test_tree_bit_exact(golden, case, precision):
     np.testing.assert_array_equal(dump["nodes"][:, :13], g["nodes"][:, :13])
 
 
-@pytest.mark.parametrize("case", SYM_CASES)
+@pytest.mark.parametrize("case", ALL_CASES)
 def test_forces_fp64_match_reference(golden, case):
     g = golden(case)
-    s, pts, _, nodes, total = run_case(g, "fp64")
+    s, pts, _, nodes, total = run_case(g, "fp64", case)
     err = rel_err(pts.derivative, g["grad"])
     assert err.max() < 1e-10, err.max()
     assert total == pytest.approx(float(g["total"]), rel=1e-10)
@@ -73,10 +80,10 @@ def test_forces_fp64_match_reference(golden, case):
     assert np.abs(c_gpu - c_ref).max() <= 1e-9 * scale.max() or np.all(np.abs(c_gpu - c_ref) <= 1e-9 * scale)
 
 
-@pytest.mark.parametrize("case", SYM_CASES)
+@pytest.mark.parametrize("case", ALL_CASES)
 def test_forces_fp32_match_reference(golden, case):
     g = golden(case)
-    s, pts, _, _, total = run_case(g, "fp32")
+    s, pts, _, _, total = run_case(g, "fp32", case)
     if len(pts) < 3:
         np.testing.assert_allclose(pts.derivative, g["grad"], rtol=1e-5)
     err = rel_err(pts.derivative, g["grad"])
