@@ -286,6 +286,19 @@ int tc_tsne_batch_stats(tc_tsne_batch* b, int64_t* stats);
 /* enable == 0: the same steps (same boxes, same refresh rule) enqueued
  * uncaptured, one system after another; for checking the graph path.     */
 int tc_tsne_batch_set_capture(tc_tsne_batch* b, int enable);
+/* A whole force step (tc_update_tree_device over a fixed box + a fresh pair
+ * sum + tc_solve_device) captured once as a CUDA graph on the handle's stream
+ * and replayed by tc_step_launch with one launch and no host round trip.  No
+ * counterpart in the reference.  The capture needs an earlier synchronous
+ * tc_update_tree_device of the same n (its list sizes bound the captured
+ * lists) and runs one ordinary solve first.  box: min x, min y, max x, max y
+ * (host).  After a replay has been synchronised, tc_async_status(h) != 0
+ * means the step is invalid (a point left the box or a list outgrew its
+ * capacity): redo it with tc_update_tree_device + tc_solve_device and capture
+ * again.  The graph keeps the pointers it was captured with.                */
+int tc_step_capture(tc_handle* h, const double* d_pos_xy, int64_t n, const double* box, double* d_grad_xy,
+                    double* d_total, int scatter);
+int tc_step_launch(tc_handle* h);
 /* After the stream of a no-sync (captured) update has been synchronised:
  * bit 0 a position lay outside the box, bit 1 a list level overflowed.    */
 int tc_async_status(tc_handle* h);

@@ -94,6 +94,8 @@ SIGNATURES = {
     "tc_tsne_batch_stats": (_I, [_P, _P]),
     "tc_tsne_batch_set_capture": (_I, [_P, _I]),
     "tc_async_status": (_I, [_P]),
+    "tc_step_capture": (_I, [_P, _P, _I64, _P, _P, _P, _I]),
+    "tc_step_launch": (_I, [_P]),
 }
 
 _lib = None

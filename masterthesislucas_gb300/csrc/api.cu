@@ -298,6 +298,7 @@ int tc_destroy(tc_handle* t)
                    &h.loc, &h.locfin, &h.mu, &h.chunk, &h.zwork, &h.zloc, &h.counters, &h.ptr_pool, &h.idx_pool, &h.cnt_tmp, &h.lstat, &h.ord_pool, &h.nfeat, &h.dec, &h.bigleaf, &h.diagpart, &h.ctrl_w, &h.tmp, &h.err, &h.zpart, &h.dtotal, &h.sumtmp,
                    &h.host_stage};
     for (Buf* b : bufs) release(*b);
+    if (h.step_graph) cudaGraphExecDestroy(h.step_graph);
     if (h.h_total) cudaFreeHost(h.h_total);
     if (h.h_words) cudaFreeHost(h.h_words);
     if (h.own_stream && h.stream) cudaStreamDestroy(h.stream);
@@ -604,5 +605,67 @@ extern "C" int tc_set_variant(tc_handle* t, int variant)
     }
     t->h.variant = variant;
     t->h.tree_ready = false;  // the interaction lists depend on the MAC
+    return TC_OK;
+}
+
+extern "C" int tc_step_capture(tc_handle* t, const double* d_pos_xy, int64_t n, const double* box, double* d_grad_xy,
+                               double* d_total, int scatter)
+{
+    if (!t || !d_pos_xy || !box || !d_grad_xy || !d_total) {
+        tc_set_error("tc_step_capture: null argument");
+        return TC_ERR_INVALID;
+    }
+    Handle& h = t->h;
+    TC_CUDA_TRY(cudaSetDevice(h.cfg.device));
+    if (!h.tree_ready || h.n != n) {
+        tc_set_error("tc_step_capture: needs a synchronous update of the same n first (it sizes the lists)");
+        return TC_ERR_STATE;
+    }
+    // one ordinary solve sizes the solver's buffers; then nothing may allocate
+    int rc = tc_solve_device(t, d_grad_xy, d_total, 0, scatter);
+    if (rc) return rc;
+    TC_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    if ((rc = prepare_nosync(h))) return rc;
+    if (h.step_graph) {
+        cudaGraphExecDestroy(h.step_graph);
+        h.step_graph = nullptr;
+    }
+    TC_CUDA_TRY(cudaStreamBeginCapture(h.stream, cudaStreamCaptureModeThreadLocal));
+    h.nosync = true;
+    rc = tc_update_tree_device(t, d_pos_xy, n, box, box + 2);
+    int launches = h.launches;
+    if (!rc) {
+        const cudaError_t e = cudaMemsetAsync(d_total, 0, 8, h.stream);
+        rc = e == cudaSuccess ? tc_solve_device(t, d_grad_xy, d_total, 0, scatter) : tc_cuda_fail(e, "memset");
+        launches += h.launches;
+    }
+    h.nosync = false;
+    cudaGraph_t g = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(h.stream, &g);
+    if (rc || ee != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return rc ? rc : tc_cuda_fail(ee, "cudaStreamEndCapture");
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&h.step_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+        h.step_graph = nullptr;
+        return tc_cuda_fail(ei, "cudaGraphInstantiate");
+    }
+    h.graph_launches = launches;
+    return TC_OK;
+}
+
+extern "C" int tc_step_launch(tc_handle* t)
+{
+    if (!t) return TC_ERR_INVALID;
+    Handle& h = t->h;
+    if (!h.step_graph) {
+        tc_set_error("tc_step_launch: no captured step");
+        return TC_ERR_STATE;
+    }
+    TC_CUDA_TRY(cudaSetDevice(h.cfg.device));
+    TC_CUDA_TRY(cudaGraphLaunch(h.step_graph, h.stream));
+    h.launches = h.graph_launches;
     return TC_OK;
 }

@@ -339,7 +339,12 @@ int prepare_nosync(Handle& h)
     for (int l = 0; l <= h.depth; l++) words += (int64_t)L.nn_cap[l] + L.near_cap[l];
     int rc;
     if ((rc = ensure(h.idx_pool, (size_t)words * 4 + 64))) return rc;
-    if (h.ctrl_on && (rc = ensure(h.ord_pool, h.idx_pool.bytes / 4 + 64))) return rc;
+    if (h.ctrl_on) {
+        if ((rc = ensure(h.ord_pool, h.idx_pool.bytes / 4 + 64))) return rc;
+        uint32_t pmax = 0;  // the controller's per-candidate decisions, sized for the widest parent level
+        for (int l = 0; l < h.depth; l++) pmax = L.near_cap[l] > pmax ? L.near_cap[l] : pmax;
+        if ((rc = ensure(h.dec, (size_t)pmax * 16 + 64))) return rc;
+    }
     return TC_OK;
 }
 

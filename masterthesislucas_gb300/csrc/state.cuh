@@ -73,6 +73,8 @@ struct Handle {
     // scratch
     Buf tmp, err, zpart, dtotal, host_stage, sumtmp;
     // stage timing (CUDA events on the handle's stream) and interaction counters
+    cudaGraphExec_t step_graph = nullptr;  // a captured update + solve (tc_step_capture)
+    int graph_launches = 0;
     cudaEvent_t ev[TC_NSTAGES + 2] = {};
     bool ev_ready = false;
     Buf counters;  // u64: p2p pairs, m2p, p2l (device)

@@ -182,6 +182,26 @@ class NBodySolverFMM_SYM_MORTON:
         check(lib().tc_get_counters(self._h, ptr(c)))
         return dict(p2p_pairs=int(c[0]), m2p=int(c[1]), p2l=int(c[2]), m2l=int(c[3]))
 
+    def capture_step(self, pos, grad, total, box=None, scatter: bool = True):
+        """Captures updateTree + solveNbody on device tensors as one CUDA graph
+        (after an ordinary update_tree_device of the same positions' size)."""
+        import numpy as _np
+        if box is None:
+            mn = pos.min(0).values.cpu().numpy()
+            mx = pos.max(0).values.cpu().numpy()
+            box = _np.concatenate([mn, mx])
+        self._box = _np.ascontiguousarray(box, _np.float64)
+        check(lib().tc_step_capture(self._h, ptr(pos), pos.shape[0], ptr(self._box), ptr(grad), ptr(total),
+                                    int(scatter)))
+
+    def launch_step(self):
+        """Replays the captured step (asynchronous on the handle's stream)."""
+        check(lib().tc_step_launch(self._h))
+
+    def async_status(self) -> int:
+        """After synchronising a replay: 0 valid, bit 0 a point left the box, bit 1 a list overflowed."""
+        return int(lib().tc_async_status(self._h))
+
     def set_controller(self, controller, tau: float = 1e-4):
         """Accept pairs by a learned order controller (FP32, order 12 handles);
         None restores the MAC.  Takes effect at the next updateTree."""
