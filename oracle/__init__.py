@@ -81,6 +81,7 @@ def lib():
         L.orc_naive.argtypes = [I, D, I64, P, P, P, I]
         L.orc_direct_rows.argtypes = [I, D, I64, P, I64, P, P, I]
         L.orc_bh.argtypes = [I, D, I, D, I64, P, P, P]
+        L.orc_bhmp.argtypes = [I, D, I, D, I64, P, P, P]
         L.orc_bh.restype = I
         L.orc_tsne_attractive.argtypes = [I64, P, P, P, P, D, P]
         L.orc_tsne_step.argtypes = [I64, P, P, P, P, P, I, I, D, D, D, D, P, P, P]
@@ -98,6 +99,7 @@ def ref_lib():
         R.ref_sym_fmm.argtypes = [I, D, I, I, D, I64] + [P] * 9 + [I]
         R.ref_naive.argtypes = [I, D, I64, P, P, P]
         R.ref_bh.argtypes = [I, D, I, D, I64, P, P, P, P]
+        R.ref_bhmp.argtypes = [I, D, I, D, I64, P, P, P]
         _ref = R
     return _ref
 
@@ -148,6 +150,15 @@ def sym_fmm(pos, *, kernel=KERNEL_TSNE, eps=0.0, max_children=16, depth=-1, thet
     fn(kernel, eps, max_children, d, theta, n, _p(pos), _p(np.asarray(mn, np.float64)),
        _p(np.asarray(mx, np.float64)), _p(codes), _p(ids), _p(ps), _p(g), _p(tot), _p(nodes))
     return dict(codes=codes, ids=ids, pos=ps, grad=g, total=float(tot[0]), nodes=nodes, depth=d)
+
+
+def bhmp(pos, *, kernel=KERNEL_TSNE, eps=0.0, max_children=16, theta=0.5):
+    """NBodySolverBHMP (Barnes-Hut with quadrupoles), input order."""
+    pos = np.ascontiguousarray(pos, np.float64)
+    g = np.zeros_like(pos)
+    tot = np.zeros(1)
+    lib().orc_bhmp(kernel, eps, max_children, theta, len(pos), _p(pos), _p(g), _p(tot))
+    return g, float(tot[0])
 
 
 def naive(pos, *, kernel=KERNEL_TSNE, eps=0.0, nthreads=None):
@@ -241,6 +252,17 @@ def ref_bh(pos, *, kernel=KERNEL_TSNE, eps=0.0, max_children=16, theta=0.5):
     tot = np.zeros(1)
     tm = np.zeros(2)
     R.ref_bh(kernel, eps, max_children, theta, len(pos), _p(pos), _p(g), _p(tot), _p(tm))
+    return g, float(tot[0])
+
+
+def ref_bhmp(pos, *, kernel=KERNEL_TSNE, eps=0.0, max_children=16, theta=0.5):
+    R = ref_lib()
+    if R is None:
+        return None
+    pos = np.ascontiguousarray(pos, np.float64)
+    g = np.zeros_like(pos)
+    tot = np.zeros(1)
+    R.ref_bhmp(kernel, eps, max_children, theta, len(pos), _p(pos), _p(g), _p(tot))
     return g, float(tot[0])
 
 

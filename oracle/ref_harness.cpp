@@ -9,6 +9,7 @@
 //   NBodySolverNaive            src/nbodysolvers/cpu/nBodySolverNaive.h:18-112
 //   NBodySolverBH               src/nbodysolvers/cpu/nBodySolverBH.h:14-89
 //   NBodySolverFMM_MORTON       src/nbodysolvers/cpu/nBodySolverFMM_MORTON.h:28-505
+//   NBodySolverBHMP             src/nbodysolvers/cpu/nBodySolverBHMP.h:17-135
 // The t-SNE kernels are the reference's own (TSNE_FMM_SYM_MORTON_*_Kernel,
 // TSNEnaiveKernel, TSNEBH*Kernel, TSNEFMM_MORTON*Kernel).  The reference has no
 // live gravity kernel; the gravity kernels below are this project's
@@ -26,6 +27,7 @@
 #include "nbodysolvers/cpu/nBodySolverFMM_MORTON.h"
 #include "nbodysolvers/cpu/nBodySolverNaive.h"
 #include "nbodysolvers/cpu/nBodySolverBH.h"
+#include "nbodysolvers/cpu/nBodySolverBHMP.h"
 
 namespace {
 
@@ -165,6 +167,18 @@ void GRAV_M_PP(double& total, TsnePoint2D& a, TsnePoint2D& b)
     grav_derivs(R.x * R.x + R.y * R.y, D1, D2, D3, t);
     total += t;
     a.derivative += D1 * R;
+}
+
+// gravity in NBodySolverBHMP's point-node slot: C1 with the node's quadrupole
+void GRAV_BHMP_PN(double& total, TsnePoint2D& p, QuadTreeMultiPole<TsnePoint2D>* node)
+{
+    glm::dvec2 R = p.position - node->centreOfMass;
+    double D1, D2, D3, t;
+    grav_derivs(R.x * R.x + R.y * R.y, D1, D2, D3, t);
+    total += node->totalMass * t;
+    double c1[2];
+    far_c1(R, node->totalMass, node->quadrupole, D1, D2, D3, c1);
+    p.derivative += glm::dvec2(c1[0], c1[1]);
 }
 
 void GRAV_NAIVE(double& total, TsnePoint2D& a, TsnePoint2D& b)
@@ -315,6 +329,22 @@ int ref_bh(int kernel, double eps, int max_children, double theta, int64_t n, co
         times[0] = std::chrono::duration<double>(t1 - t0).count();
         times[1] = std::chrono::duration<double>(t2 - t1).count();
     }
+    return 0;
+}
+
+// NBodySolverBHMP (kernel 0 = t-SNE, 1 = softened gravity), input order.
+int ref_bhmp(int kernel, double eps, int max_children, double theta, int64_t n, const double* pos_xy,
+             double* grad, double* total)
+{
+    g_eps2 = eps * eps;
+    std::vector<TsnePoint2D> pts = make_points(n, pos_xy);
+    NBodySolverBHMP<TsnePoint2D> s(kernel == 0 ? &TSNEBHMPPNKernel : &GRAV_BHMP_PN,
+                                   kernel == 0 ? &TSNEBHMPPPKernel : &GRAV_NAIVE, max_children, theta);
+    double tot = 0.0;
+    s.updateTree(pts, glm::dvec2(0.0), glm::dvec2(0.0));
+    s.solveNbody(tot, pts);
+    for (int64_t i = 0; i < n; i++) { grad[2 * i] = pts[i].derivative.x; grad[2 * i + 1] = pts[i].derivative.y; }
+    if (total) *total = tot;
     return 0;
 }
 

@@ -1001,6 +1001,185 @@ int orc_bh(int kernel, double eps, int max_children, double theta, int64_t n,
 }
 
 /* ------------------------------------------------------------------ */
+/* Barnes-Hut with quadrupoles: NBodySolverBHMP + QuadTreeMultiPole    */
+/* ------------------------------------------------------------------ */
+
+typedef struct bhmp_node {
+    double mass;             /* QuadTreeMultiPole::totalMass (double)          */
+    double com[2];
+    double quad[4];          /* quadrupole (row-major 2x2)                     */
+    double lo[2], hi[2];
+    int32_t* occ;
+    int64_t nocc;
+    struct bhmp_node* ch[4];
+    int nch;
+} bhmp_node;
+
+/* QuadTreeMultiPole::createTree (quadtreemultipole.h:174-289): the same split
+ * as QuadTree, FP64 masses and COMs, quadrupole sum_c [M_c (dc dc^T) + Q_c]. */
+static void bhmp_create(bhmp_node* q, const double* pos, int maxc)
+{
+    if (q->nocc > maxc) {
+        int32_t* part[4];
+        int64_t cnt[4] = {0, 0, 0, 0};
+        for (int k = 0; k < 4; k++) part[k] = (int32_t*)malloc((size_t)q->nocc * sizeof(int32_t));
+        double l = (q->hi[0] - q->lo[0]) / 2.0;
+        double mx = q->lo[0] + l, my = q->lo[1] + l;
+        for (int64_t i = 0; i < q->nocc; i++) {
+            int32_t id = q->occ[i];
+            double x = pos[2 * id], y = pos[2 * id + 1];
+            int k;
+            if (x >= mx && y >= my) k = 0;          /* HH */
+            else if (x >= mx && y < my) k = 1;      /* HL */
+            else if (x < mx && y >= my) k = 2;      /* LH */
+            else k = 3;                             /* LL */
+            part[k][cnt[k]++] = id;
+        }
+        double blo[4][2] = {{mx, my}, {mx, q->lo[1]}, {q->lo[0], my}, {q->lo[0], q->lo[1]}};
+        double bhi[4][2] = {{q->hi[0], q->hi[1]}, {q->hi[0], my}, {mx, q->hi[1]}, {mx, my}};
+        q->nch = 0;
+        for (int k = 0; k < 4; k++) {
+            if (cnt[k] == 0) {
+                free(part[k]);
+                continue;
+            }
+            bhmp_node* c = (bhmp_node*)calloc(1, sizeof(bhmp_node));
+            c->occ = part[k];
+            c->nocc = cnt[k];
+            c->lo[0] = blo[k][0]; c->lo[1] = blo[k][1];
+            c->hi[0] = bhi[k][0]; c->hi[1] = bhi[k][1];
+            q->ch[q->nch++] = c;
+        }
+        q->mass = 0.0;
+        q->com[0] = q->com[1] = 0.0;
+        for (int k = 0; k < q->nch; k++) {
+            bhmp_create(q->ch[k], pos, maxc);
+            q->mass += q->ch[k]->mass;
+            q->com[0] += q->ch[k]->mass * q->ch[k]->com[0];
+            q->com[1] += q->ch[k]->mass * q->ch[k]->com[1];
+        }
+        q->com[0] /= q->mass;
+        q->com[1] /= q->mass;
+        for (int i = 0; i < 4; i++) q->quad[i] = 0.0;
+        for (int k = 0; k < q->nch; k++) {
+            const bhmp_node* c = q->ch[k];
+            double rx = c->com[0] - q->com[0], ry = c->com[1] - q->com[1];
+            double o[4] = {rx * rx, rx * ry, ry * rx, ry * ry};
+            for (int i = 0; i < 4; i++) q->quad[i] += c->mass * o[i];
+            for (int i = 0; i < 4; i++) q->quad[i] += c->quad[i];
+        }
+    } else {
+        q->mass = 0.0;
+        q->com[0] = q->com[1] = 0.0;
+        for (int64_t i = 0; i < q->nocc; i++) {
+            q->mass += 1.0;
+            q->com[0] += 1.0 * pos[2 * q->occ[i]];
+            q->com[1] += 1.0 * pos[2 * q->occ[i] + 1];
+        }
+        q->com[0] /= q->mass;
+        q->com[1] /= q->mass;
+        for (int i = 0; i < 4; i++) q->quad[i] = 0.0;
+        for (int64_t i = 0; i < q->nocc; i++) {
+            double rx = pos[2 * q->occ[i]] - q->com[0], ry = pos[2 * q->occ[i] + 1] - q->com[1];
+            double o[4] = {rx * rx, rx * ry, ry * rx, ry * ry};
+            for (int j = 0; j < 4; j++) q->quad[j] += o[j];
+        }
+    }
+}
+
+static void bhmp_free(bhmp_node* q)
+{
+    for (int k = 0; k < q->nch; k++) {
+        bhmp_free(q->ch[k]);
+        free(q->ch[k]);
+    }
+    free(q->occ);
+}
+
+/* NBodySolverBHMP::traverseBHMP (nBodySolverBHMP.h:59-93) + TSNEBHMPPNKernel
+ * / TSNEBHMPPPKernel (:97-135); gravity puts the softened kernel in the same
+ * slots (C1 with the source quadrupole).                                   */
+static void bhmp_trav(bh_ctx* c, int64_t p, const bhmp_node* q, double* g)
+{
+    double l = q->hi[0] - q->lo[0];
+    double dx = c->pos[2 * p] - q->com[0], dy = c->pos[2 * p + 1] - q->com[1];
+    double len = sqrt(dx * dx + dy * dy);
+    if (l / len < c->theta) {
+        double sq = dx * dx + dy * dy;
+        double C1[2];
+        derivs d;
+        if (c->kernel == ORC_KERNEL_TSNE) {
+            double rS = 1.0 + sq;
+            d.D1 = 1.0 / (rS * rS);
+            d.D2 = -4.0 / (rS * rS * rS);
+            d.D3 = 24.0 / (rS * rS * rS * rS);
+            c->total += q->mass / rS;
+        } else {
+            d = grav_derivs(sq, c->eps2);
+            c->total += q->mass * d.t;
+        }
+        far_c1(dx, dy, q->mass, q->quad, d.D1, d.D2, d.D3, C1);
+        g[0] += C1[0];
+        g[1] += C1[1];
+    } else if (q->nch <= 1) {
+        for (int64_t i = 0; i < q->nocc; i++) {
+            int64_t o = q->occ[i];
+            if (o == p) continue;
+            double ex = c->pos[2 * p] - c->pos[2 * o], ey = c->pos[2 * p + 1] - c->pos[2 * o + 1];
+            double sq = ex * ex + ey * ey;
+            if (c->kernel == ORC_KERNEL_TSNE) {
+                double fd = 1.0 / (1.0 + sq);
+                c->total += fd;
+                g[0] += fd * fd * ex;
+                g[1] += fd * fd * ey;
+            } else {
+                derivs d = grav_derivs(sq, c->eps2);
+                c->total += d.t;
+                g[0] += d.D1 * ex;
+                g[1] += d.D1 * ey;
+            }
+        }
+    } else {
+        for (int k = 0; k < q->nch; k++) bhmp_trav(c, p, q->ch[k], g);
+    }
+}
+
+int orc_bhmp(int kernel, double eps, int max_children, double theta, int64_t n,
+             const double* pos, double* grad, double* total)
+{
+    if (n <= 0) {
+        if (total) *total = 0.0;
+        return 0;
+    }
+    bhmp_node root;
+    memset(&root, 0, sizeof(root));
+    root.occ = (int32_t*)malloc((size_t)n * sizeof(int32_t));
+    root.nocc = n;
+    double lo[2] = {INFINITY, INFINITY}, hi[2] = {-INFINITY, -INFINITY};
+    for (int64_t i = 0; i < n; i++) {
+        root.occ[i] = (int32_t)i;
+        for (int a = 0; a < 2; a++) {
+            lo[a] = dmin(lo[a], pos[2 * i + a]);
+            hi[a] = dmax(hi[a], pos[2 * i + a]);
+        }
+    }
+    double ld = dmax(hi[0] - lo[0], hi[1] - lo[1]);
+    root.lo[0] = lo[0];
+    root.lo[1] = lo[1];
+    root.hi[0] = lo[0] + ld + 0.0001;
+    root.hi[1] = lo[1] + ld + 0.0001;
+    bhmp_create(&root, pos, max_children);
+    bh_ctx c = {kernel, eps * eps, theta, pos, 0.0};
+    for (int64_t i = 0; i < n; i++) {
+        grad[2 * i] = grad[2 * i + 1] = 0.0;
+        bhmp_trav(&c, i, &root, grad + 2 * i);
+    }
+    if (total) *total = c.total;
+    bhmp_free(&root);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
 /* t-SNE composition                                                   */
 /* ------------------------------------------------------------------ */
 

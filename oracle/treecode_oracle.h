@@ -95,6 +95,11 @@ void orc_direct_rows(int kernel, double eps, int64_t n, const double* pos, int64
  * grad is overwritten (input order), total overwritten.                    */
 int orc_bh(int kernel, double eps, int max_children, double theta, int64_t n,
            const double* pos, double* grad, double* total);
+/* NBodySolverBHMP + QuadTreeMultiPole (nBodySolverBHMP.h:17-135,
+ * quadtreemultipole.h:31-289): Barnes-Hut with FP64 masses and a quadrupole
+ * correction (the C1 of the FMM kernels) at accepted nodes.                 */
+int orc_bhmp(int kernel, double eps, int max_children, double theta, int64_t n,
+             const double* pos, double* grad, double* total);
 
 /* TSNE::updateAttractive (tsne.h:356-381): grad[i] += exag * sum_j P_ij q_ij (y_j - y_i) */
 void orc_tsne_attractive(int64_t n, const uint32_t* row_ptr, const uint32_t* col,

@@ -84,6 +84,14 @@ def asym_cases():
     sym_case("asym_tsne_tiny_17", np.random.default_rng(117).normal(0, 1, (17, 2)), symmetric=False)
 
 
+def bhmp_cases():
+    """NBodySolverBHMP: Barnes-Hut with quadrupoles (gravity put in its slots)."""
+    for kernel, eps, tag in ((0, 0.0, "tsne"), (1, 1e-3, "grav")):
+        pos = datasets.gaussian_mixture(3000, seed=33).astype(np.float64)
+        g, t = oracle.ref_bhmp(pos, kernel=kernel, eps=eps, max_children=16, theta=0.5)
+        save(f"bhmp_{tag}_3000", pos=pos, grad=g, total=t, kernel=kernel, eps=eps, max_children=16, theta=0.5)
+
+
 def main():
     if oracle.build_ref() is None:
         raise SystemExit("reference sources not found; fixtures cannot be regenerated")
@@ -109,6 +117,7 @@ def main():
         g, t = oracle.ref_bh(pos, kernel=kernel, eps=eps, max_children=16, theta=0.5)
         save(f"bh_{tag}_3000", pos=pos, grad=g, total=t, kernel=kernel, eps=eps, max_children=16,
              theta=0.5)
+    bhmp_cases()
     tsne_step_case("tsne_step_600")
 
 

@@ -63,6 +63,15 @@ def test_bh_bit_exact(golden, tag):
     assert total == float(g["total"])
 
 
+@pytest.mark.parametrize("tag", ["tsne", "grav"])
+def test_bhmp_bit_exact(golden, tag):
+    g = golden(f"bhmp_{tag}_3000")
+    grad, total = oracle.bhmp(g["pos"], kernel=int(g["kernel"]), eps=float(g["eps"]),
+                              max_children=int(g["max_children"]), theta=float(g["theta"]))
+    np.testing.assert_array_equal(grad, g["grad"])
+    assert total == float(g["total"])
+
+
 def test_tsne_step_matches_reference_composition(golden):
     g = golden("tsne_step_600")
     ys = [g["y0"], g["y0"]]
