@@ -182,6 +182,14 @@ int tc_bh_solve(int kernel, double softening, int max_children, double theta, in
                 const double* pos_xy, int64_t n, double* grad_xy, double* total);
 int tc_bh_solve_device(int kernel, double softening, int max_children, double theta, int precision,
                        const double* d_pos_xy, int64_t n, double* d_grad_xy, double* d_total, void* stream);
+/* NBodySolverBHMP + QuadTreeMultiPole (src/nbodysolvers/cpu/nBodySolverBHMP.h:
+ * 17-135, src/trees/cpu/quadtreemultipole.h:31-289): the same tree with FP64
+ * masses and a quadrupole per node; accepted nodes contribute monopole +
+ * quadrupole (TSNEBHMPPNKernel, :97-126).  Arguments as tc_bh_solve.        */
+int tc_bhmp_solve(int kernel, double softening, int max_children, double theta, int precision,
+                  const double* pos_xy, int64_t n, double* grad_xy, double* total);
+int tc_bhmp_solve_device(int kernel, double softening, int max_children, double theta, int precision,
+                         const double* d_pos_xy, int64_t n, double* d_grad_xy, double* d_total, void* stream);
 
 /* ---------------------------------------------------------------- N-body time step
  * Kick-drift-kick leapfrog on a gravity handle.  The reference's N-body

@@ -68,6 +68,8 @@ SIGNATURES = {
     "tc_direct_device_noalloc": (_I, [_I, _D, _I, _P, _I64, _P, _I64, _P, _P, _P]),
     "tc_bh_solve": (_I, [_I, _D, _I, _D, _I, _P, _I64, _P, _P]),
     "tc_bh_solve_device": (_I, [_I, _D, _I, _D, _I, _P, _I64, _P, _P, _P]),
+    "tc_bhmp_solve": (_I, [_I, _D, _I, _D, _I, _P, _I64, _P, _P]),
+    "tc_bhmp_solve_device": (_I, [_I, _D, _I, _D, _I, _P, _I64, _P, _P, _P]),
     "tc_mlp_create": (_I, [ctypes.c_uint64, _P]),
     "tc_mlp_destroy": (_I, [_P]),
     "tc_mlp_set_normalization": (_I, [_P, _P, _P]),

@@ -15,6 +15,12 @@
 // children order with the MAC l/|x - com| < theta; a node with at most one
 // child is treated as a leaf (PP over all its occupants).  In FP64 the
 // result is the reference's, bit for bit (same operations, same order).
+//
+// The multipole variant (NBodySolverBHMP + QuadTreeMultiPole,
+// src/nbodysolvers/cpu/nBodySolverBHMP.h:17-135,
+// src/trees/cpu/quadtreemultipole.h:31-289) uses the same tree with FP64
+// masses and COMs and a quadrupole sum_c [M_c (dc dc^T) + Q_c]; an accepted
+// node contributes the FMM kernels' C1 (monopole + quadrupole).
 #include <vector>
 
 #include "kernels.cuh"
@@ -22,6 +28,10 @@
 
 namespace tc {
 namespace {
+
+struct Quad {
+    double x, y, z, w;  // xx, xy, yx, yy
+};
 
 struct BHNodes {
     double2* lo;
@@ -33,7 +43,81 @@ struct BHNodes {
     float* mass;
     double2* com;   // full-precision COM (the node's own member)
     float2* comf;   // the COM its parent sees (float)
+    double* m64;    // multipole variant: FP64 mass
+    Quad* quad;     // multipole variant: quadrupole
 };
+
+// QuadTreeMultiPole::createTree's moments for one level (children done)
+__global__ void k_bhmp_moments(uint32_t lvl_begin, uint32_t lvl_end, BHNodes t, const double2* __restrict__ pos,
+                               const uint32_t* __restrict__ order)
+{
+    for (uint32_t k = lvl_begin + blockIdx.x * blockDim.x + threadIdx.x; k < lvl_end; k += gridDim.x * blockDim.x) {
+        double m = 0.0, cx = 0.0, cy = 0.0;
+        Quad q = {0.0, 0.0, 0.0, 0.0};
+        if (t.nchild[k] == 0) {
+            for (uint32_t i = t.start[k]; i < t.start[k] + t.count[k]; i++) {
+                const double2 p = pos[order[i]];
+                m += 1.0;
+                cx += 1.0 * p.x;
+                cy += 1.0 * p.y;
+            }
+            cx /= m;
+            cy /= m;
+            for (uint32_t i = t.start[k]; i < t.start[k] + t.count[k]; i++) {
+                const double2 p = pos[order[i]];
+                const double rx = p.x - cx, ry = p.y - cy;
+                q.x += rx * rx;
+                q.y += rx * ry;
+                q.z += ry * rx;
+                q.w += ry * ry;
+            }
+        } else {
+            const uint32_t f = t.first_child[k], e = f + t.nchild[k];
+            for (uint32_t c = f; c < e; c++) {
+                const double mc = t.m64[c];
+                const double2 cc = t.com[c];
+                m += mc;
+                cx += mc * cc.x;
+                cy += mc * cc.y;
+            }
+            cx /= m;
+            cy /= m;
+            for (uint32_t c = f; c < e; c++) {
+                const double mc = t.m64[c];
+                const double2 cc = t.com[c];
+                const double rx = cc.x - cx, ry = cc.y - cy;
+                const Quad qc = t.quad[c];
+                q.x += mc * (rx * rx);
+                q.y += mc * (rx * ry);
+                q.z += mc * (ry * rx);
+                q.w += mc * (ry * ry);
+                q.x += qc.x;
+                q.y += qc.y;
+                q.z += qc.z;
+                q.w += qc.w;
+            }
+        }
+        t.m64[k] = m;
+        t.com[k] = make_double2(cx, cy);
+        t.quad[k] = q;
+    }
+}
+
+// C1 of a source of mass m and quadrupole Q at offset R (the FMM kernels' far
+// field, nBodySolverBHMP.h:111-126)
+template <typename real>
+__device__ inline void bh_far_c1(real Rx, real Ry, real m, Quad Q, real D1, real D2, real D3, real& ox, real& oy)
+{
+    const double inv = 1.0 / (double)m;
+    const real Txx = (real)(inv * Q.x), Txy = (real)(inv * Q.y), Tyx = (real)(inv * Q.z), Tyy = (real)(inv * Q.w);
+    const real S1 = Txx + Tyy;
+    const real S2 = (Rx * Rx * Txx) + (Rx * Ry * Txy) + (Ry * Rx * Tyx) + (Ry * Ry * Tyy);
+    const real S3x = Rx * Txx + Ry * Txy;
+    const real S3y = Rx * Tyx + Ry * Tyy;
+    const real base = D1 + real(0.5) * S1 * D2 + real(0.5) * S2 * D3;
+    ox = m * (Rx * base + S3x * D2);
+    oy = m * (Ry * base + S3y * D2);
+}
 
 __global__ void k_bh_root(const double* __restrict__ keys, uint32_t n, BHNodes t)
 {
@@ -189,7 +273,7 @@ __global__ void k_bh_mass(uint32_t lvl_begin, uint32_t lvl_end, BHNodes t, const
 constexpr int kBHStack = 128;
 
 // traverseBH (nBodySolverBH.h:56-89) per point, depth first in children order
-template <typename real, typename K>
+template <typename real, typename K, bool MP>
 __global__ void __launch_bounds__(128) k_bh_traverse(K ker, const double2* __restrict__ pos, uint32_t n, BHNodes t,
                                                      const uint32_t* __restrict__ order, double theta,
                                                      double* __restrict__ grad, double* __restrict__ zrow,
@@ -208,12 +292,23 @@ __global__ void __launch_bounds__(128) k_bh_traverse(K ker, const double2* __res
             const double dx = x.x - c.x, dy = x.y - c.y;
             const double len = sqrt(dx * dx + dy * dy);
             if (l / len < theta) {
-                const real tm = (real)t.mass[nd];
-                real D1, tt;
-                ker.near((real)(dx * dx + dy * dy), D1, tt);
-                z += tm * tt;
-                gx += tm * D1 * (real)dx;
-                gy += tm * D1 * (real)dy;
+                if constexpr (MP) {
+                    const real tm = (real)t.m64[nd];
+                    real D1, D2, D3, tt;
+                    ker.far((real)(dx * dx + dy * dy), D1, D2, D3, tt);
+                    real cx1, cy1;
+                    bh_far_c1<real>((real)dx, (real)dy, tm, t.quad[nd], D1, D2, D3, cx1, cy1);
+                    z += tm * tt;
+                    gx += cx1;
+                    gy += cy1;
+                } else {
+                    const real tm = (real)t.mass[nd];
+                    real D1, tt;
+                    ker.near((real)(dx * dx + dy * dy), D1, tt);
+                    z += tm * tt;
+                    gx += tm * D1 * (real)dx;
+                    gy += tm * D1 * (real)dy;
+                }
             } else if (t.nchild[nd] <= 1) {
                 for (uint32_t i = t.start[nd]; i < t.start[nd] + t.count[nd]; i++) {
                     const uint32_t o = order[i];
@@ -261,9 +356,11 @@ int dalloc(DevBuf& b, size_t count)
 
 using namespace tc;
 
-extern "C" int tc_bh_solve_device(int kernel, double softening, int max_children, double theta, int precision,
-                                  const double* d_pos_xy, int64_t n64, double* d_grad_xy, double* d_total,
-                                  void* stream)
+namespace tc {
+namespace {
+
+int bh_solve_impl(int kernel, double softening, int max_children, double theta, int precision,
+                  const double* d_pos_xy, int64_t n64, double* d_grad_xy, double* d_total, void* stream, bool mp)
 {
     if (!d_pos_xy || !d_grad_xy || n64 <= 0 || n64 > (1 << 30) || max_children <= 0 || !(theta > 0.0) ||
         (kernel != TC_KERNEL_TSNE && kernel != TC_KERNEL_GRAVITY)) {
@@ -288,8 +385,11 @@ extern "C" int tc_bh_solve_device(int kernel, double softening, int max_children
         (rc = dalloc<uint32_t>(b_tmp, (size_t)scan_tmp_words((int64_t)cap + n) + 16)) ||
         (rc = dalloc<double>(b_bbox, 4)) || (rc = dalloc<double>(b_zrow, n)) || (rc = dalloc<uint32_t>(b_err, 4)))
         return rc;
+    DevBuf b_m64, b_quad;
+    if (mp && ((rc = dalloc<double>(b_m64, cap)) || (rc = dalloc<Quad>(b_quad, cap)))) return rc;
     BHNodes t{(double2*)b_lo.p, (double2*)b_hi.p, (uint32_t*)b_start.p, (uint32_t*)b_count.p, (uint32_t*)b_fc.p,
-              (uint32_t*)b_nc.p, (float*)b_mass.p, (double2*)b_com.p, (float2*)b_comf.p};
+              (uint32_t*)b_nc.p, (float*)b_mass.p, (double2*)b_com.p, (float2*)b_comf.p, (double*)b_m64.p,
+              (Quad*)b_quad.p};
     uint32_t* order = (uint32_t*)b_order.p;
     uint32_t* order2 = (uint32_t*)b_order2.p;
     uint32_t* node_of = (uint32_t*)b_nodeof.p;
@@ -339,28 +439,51 @@ extern "C" int tc_bh_solve_device(int kernel, double softening, int max_children
             return TC_ERR_INVALID;
         }
     }
-    for (int l = (int)level_begin.size() - 1; l >= 0; l--)
-        k_bh_mass<<<grid_for(level_end[l] - level_begin[l], 128), 128, 0, s>>>(level_begin[l], level_end[l], t,
-                                                                               (const double2*)d_pos_xy, order);
+    for (int l = (int)level_begin.size() - 1; l >= 0; l--) {
+        if (mp)
+            k_bhmp_moments<<<grid_for(level_end[l] - level_begin[l], 128), 128, 0, s>>>(
+                level_begin[l], level_end[l], t, (const double2*)d_pos_xy, order);
+        else
+            k_bh_mass<<<grid_for(level_end[l] - level_begin[l], 128), 128, 0, s>>>(level_begin[l], level_end[l], t,
+                                                                                   (const double2*)d_pos_xy, order);
+    }
     const double e2 = softening * softening;
+    const double2* P2 = (const double2*)d_pos_xy;
+    double* zr = (double*)b_zrow.p;
+    uint32_t* er = (uint32_t*)b_err.p;
+    const int gt = grid_for(n, 128);
     if (precision == TC_PREC_FP64) {
-        if (kernel == TC_KERNEL_GRAVITY)
-            k_bh_traverse<double><<<grid_for(n, 128), 128, 0, s>>>(KGrav<double>{e2}, (const double2*)d_pos_xy, n, t,
-                                                                   order, theta, d_grad_xy, (double*)b_zrow.p,
-                                                                   (uint32_t*)b_err.p);
-        else
-            k_bh_traverse<double><<<grid_for(n, 128), 128, 0, s>>>(KTsne<double>{}, (const double2*)d_pos_xy, n, t,
-                                                                   order, theta, d_grad_xy, (double*)b_zrow.p,
-                                                                   (uint32_t*)b_err.p);
+        if (kernel == TC_KERNEL_GRAVITY) {
+            if (mp)
+                k_bh_traverse<double, KGrav<double>, true>
+                    <<<gt, 128, 0, s>>>(KGrav<double>{e2}, P2, n, t, order, theta, d_grad_xy, zr, er);
+            else
+                k_bh_traverse<double, KGrav<double>, false>
+                    <<<gt, 128, 0, s>>>(KGrav<double>{e2}, P2, n, t, order, theta, d_grad_xy, zr, er);
+        } else {
+            if (mp)
+                k_bh_traverse<double, KTsne<double>, true>
+                    <<<gt, 128, 0, s>>>(KTsne<double>{}, P2, n, t, order, theta, d_grad_xy, zr, er);
+            else
+                k_bh_traverse<double, KTsne<double>, false>
+                    <<<gt, 128, 0, s>>>(KTsne<double>{}, P2, n, t, order, theta, d_grad_xy, zr, er);
+        }
     } else {
-        if (kernel == TC_KERNEL_GRAVITY)
-            k_bh_traverse<float><<<grid_for(n, 128), 128, 0, s>>>(KGrav<float>{(float)e2}, (const double2*)d_pos_xy, n,
-                                                                  t, order, theta, d_grad_xy, (double*)b_zrow.p,
-                                                                  (uint32_t*)b_err.p);
-        else
-            k_bh_traverse<float><<<grid_for(n, 128), 128, 0, s>>>(KTsne<float>{}, (const double2*)d_pos_xy, n, t,
-                                                                  order, theta, d_grad_xy, (double*)b_zrow.p,
-                                                                  (uint32_t*)b_err.p);
+        if (kernel == TC_KERNEL_GRAVITY) {
+            if (mp)
+                k_bh_traverse<float, KGrav<float>, true>
+                    <<<gt, 128, 0, s>>>(KGrav<float>{(float)e2}, P2, n, t, order, theta, d_grad_xy, zr, er);
+            else
+                k_bh_traverse<float, KGrav<float>, false>
+                    <<<gt, 128, 0, s>>>(KGrav<float>{(float)e2}, P2, n, t, order, theta, d_grad_xy, zr, er);
+        } else {
+            if (mp)
+                k_bh_traverse<float, KTsne<float>, true>
+                    <<<gt, 128, 0, s>>>(KTsne<float>{}, P2, n, t, order, theta, d_grad_xy, zr, er);
+            else
+                k_bh_traverse<float, KTsne<float>, false>
+                    <<<gt, 128, 0, s>>>(KTsne<float>{}, P2, n, t, order, theta, d_grad_xy, zr, er);
+        }
     }
     DevBuf b_sum;
     if ((rc = dalloc<double>(b_sum, sum_tmp_doubles()))) return rc;
@@ -376,8 +499,27 @@ extern "C" int tc_bh_solve_device(int kernel, double softening, int max_children
     return TC_OK;
 }
 
-extern "C" int tc_bh_solve(int kernel, double softening, int max_children, double theta, int precision,
-                           const double* pos_xy, int64_t n, double* grad_xy, double* total)
+}  // namespace
+}  // namespace tc
+
+extern "C" int tc_bh_solve_device(int kernel, double softening, int max_children, double theta, int precision,
+                                  const double* d_pos_xy, int64_t n64, double* d_grad_xy, double* d_total,
+                                  void* stream)
+{
+    return bh_solve_impl(kernel, softening, max_children, theta, precision, d_pos_xy, n64, d_grad_xy, d_total, stream,
+                         false);
+}
+
+extern "C" int tc_bhmp_solve_device(int kernel, double softening, int max_children, double theta, int precision,
+                                    const double* d_pos_xy, int64_t n64, double* d_grad_xy, double* d_total,
+                                    void* stream)
+{
+    return bh_solve_impl(kernel, softening, max_children, theta, precision, d_pos_xy, n64, d_grad_xy, d_total, stream,
+                         true);
+}
+
+static int bh_solve_host(int kernel, double softening, int max_children, double theta, int precision,
+                         const double* pos_xy, int64_t n, double* grad_xy, double* total, bool mp)
 {
     if (!pos_xy || !grad_xy || n <= 0) {
         tc_set_error("tc_bh_solve: invalid arguments");
@@ -392,8 +534,8 @@ extern "C" int tc_bh_solve(int kernel, double softening, int max_children, doubl
     if (e == cudaSuccess) e = cudaMalloc(&dt.p, 8);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dp.p, pos_xy, (size_t)n * 16, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) {
-        rc = tc_bh_solve_device(kernel, softening, max_children, theta, precision, (const double*)dp.p, n,
-                                (double*)dg.p, (double*)dt.p, s);
+        rc = tc::bh_solve_impl(kernel, softening, max_children, theta, precision, (const double*)dp.p, n,
+                               (double*)dg.p, (double*)dt.p, s, mp);
         if (rc == TC_OK) e = cudaMemcpyAsync(grad_xy, dg.p, (size_t)n * 16, cudaMemcpyDeviceToHost, s);
         if (rc == TC_OK && e == cudaSuccess && total) e = cudaMemcpyAsync(total, dt.p, 8, cudaMemcpyDeviceToHost, s);
     }
@@ -403,4 +545,16 @@ extern "C" int tc_bh_solve(int kernel, double softening, int max_children, doubl
     if (e != cudaSuccess) return tc_cuda_fail(e, "tc_bh_solve");
     if (e2 != cudaSuccess) return tc_cuda_fail(e2, "tc_bh_solve sync");
     return TC_OK;
+}
+
+extern "C" int tc_bh_solve(int kernel, double softening, int max_children, double theta, int precision,
+                           const double* pos_xy, int64_t n, double* grad_xy, double* total)
+{
+    return bh_solve_host(kernel, softening, max_children, theta, precision, pos_xy, n, grad_xy, total, false);
+}
+
+extern "C" int tc_bhmp_solve(int kernel, double softening, int max_children, double theta, int precision,
+                             const double* pos_xy, int64_t n, double* grad_xy, double* total)
+{
+    return bh_solve_host(kernel, softening, max_children, theta, precision, pos_xy, n, grad_xy, total, true);
 }

@@ -254,11 +254,14 @@ def direct(pos, *, kernel="tsne", softening=1e-3, precision="fp64", rows=None):
     return g, float(tot.value)
 
 
-def barnes_hut(pos, *, kernel="tsne", softening=1e-3, max_children=16, theta=0.5, precision="fp32"):
-    """NBodySolverBH on the GPU: forces in input order and the pair sum."""
+def barnes_hut(pos, *, kernel="tsne", softening=1e-3, max_children=16, theta=0.5, precision="fp32",
+               multipole=False):
+    """NBodySolverBH on the GPU (NBodySolverBHMP with multipole=True): forces
+    in input order and the pair sum."""
     pos = np.ascontiguousarray(pos, np.float64)
     g = np.zeros_like(pos)
     tot = ctypes.c_double(0.0)
-    check(lib().tc_bh_solve(KERNELS[kernel], softening, max_children, theta, PRECISIONS[precision], ptr(pos),
-                            len(pos), ptr(g), ctypes.byref(tot)))
+    fn = lib().tc_bhmp_solve if multipole else lib().tc_bh_solve
+    check(fn(KERNELS[kernel], softening, max_children, theta, PRECISIONS[precision], ptr(pos), len(pos), ptr(g),
+             ctypes.byref(tot)))
     return g, float(tot.value)

@@ -157,6 +157,27 @@ def test_barnes_hut_matches_reference(golden, tag):
     assert total32 == pytest.approx(float(g["total"]), rel=1e-5)
 
 
+@pytest.mark.parametrize("tag", ["tsne", "grav"])
+def test_barnes_hut_multipole_matches_reference(golden, tag):
+    from masterthesislucas_gb300.solver import barnes_hut
+    g = golden(f"bhmp_{tag}_3000")
+    kernel = "tsne" if tag == "tsne" else "gravity"
+    kw = dict(kernel=kernel, softening=float(g["eps"]) or 1e-3, max_children=int(g["max_children"]),
+              theta=float(g["theta"]), multipole=True)
+    grad, total = barnes_hut(g["pos"], precision="fp64", **kw)
+    assert rel_err(grad, g["grad"]).max() < 1e-12
+    assert total == pytest.approx(float(g["total"]), rel=1e-12)
+    grad32, total32 = barnes_hut(g["pos"], precision="fp32", **kw)
+    err = rel_err(grad32, g["grad"])
+    assert np.median(err) < 1e-5 and err.max() < 1e-3
+    assert total32 == pytest.approx(float(g["total"]), rel=1e-5)
+    # the quadrupole makes it more accurate than the monopole BH on the same tree
+    bh, _ = barnes_hut(g["pos"], precision="fp64", **{**kw, "multipole": False})
+    from masterthesislucas_gb300 import direct
+    ref, _ = direct(g["pos"], kernel=kernel, softening=kw["softening"], precision="fp64")
+    assert np.median(rel_err(grad, ref)) < np.median(rel_err(bh, ref))
+
+
 def test_barnes_hut_large_matches_oracle():
     import oracle
     from masterthesislucas_gb300.solver import barnes_hut
