@@ -63,6 +63,8 @@ WORKLOADS = {
     "tsne_batch_256": dict(n=0, systems=256, n_min=2000, n_max=200000, dim=64, clusters=(5, 20), perplexity=30.0,
                            kernel="tsne", max_children=16, theta=0.5, method="tsne_batch", softening=0.0, dist="tsne",
                            presteps=5),
+    "bhmp_mixture_65k": dict(n=65536, dist="mixture", kernel="gravity", softening=1e-3, max_children=16,
+                             method="bh", theta=0.5, multipole=True),
     "bh_mixture_65k": dict(n=65536, dist="mixture", kernel="gravity", softening=1e-3, max_children=16,
                            method="bh", theta=0.5),
 }
@@ -558,9 +560,13 @@ def run_bh(args, w):
     ref = ref_d.cpu().numpy()
     cs = ctypes.c_void_p(stream.cuda_stream)
 
+    mp = bool(w.get("multipole"))
+    solve_dev = lib().tc_bhmp_solve_device if mp else lib().tc_bh_solve_device
+    solve_host = lib().tc_bhmp_solve if mp else lib().tc_bh_solve
+
     def step():
-        check(lib().tc_bh_solve_device(1, w["softening"], w["max_children"], w["theta"], 0, ptr(pos_d), n,
-                                       ptr(grad_d), ptr(tot_d), cs))
+        check(solve_dev(1, w["softening"], w["max_children"], w["theta"], 0, ptr(pos_d), n, ptr(grad_d), ptr(tot_d),
+                        cs))
 
     for _ in range(args.warmup):
         step()
@@ -585,28 +591,32 @@ def run_bh(args, w):
     e2e = []
     for k in range(3):
         t0 = _t.perf_counter()
-        check(lib().tc_bh_solve(1, w["softening"], w["max_children"], w["theta"], 0, ptr(pos_h), n, ptr(g_h),
-                                ctypes.byref(tot)))
+        check(solve_host(1, w["softening"], w["max_children"], w["theta"], 0, ptr(pos_h), n, ptr(g_h),
+                         ctypes.byref(tot)))
         e2e.append(_t.perf_counter() - t0)
     import oracle
     t0 = _t.perf_counter()
-    oracle.bh(pos_h, kernel=oracle.KERNEL_GRAVITY, eps=w["softening"], max_children=w["max_children"],
-              theta=w["theta"])
+    (oracle.bhmp if mp else oracle.bh)(pos_h, kernel=oracle.KERNEL_GRAVITY, eps=w["softening"],
+                                       max_children=w["max_children"], theta=w["theta"])
     cpu_t = _t.perf_counter() - t0
     t_total = sum(ms) / 1e3
-    line = {"metric": "particles/s per Barnes-Hut force step (C1, single evaluation)", "value": n * args.steps / t_total,
+    name = "Barnes-Hut with quadrupoles (NBodySolverBHMP)" if mp else "Barnes-Hut (C1, single evaluation)"
+    line = {"metric": f"particles/s per {name} force step", "value": n * args.steps / t_total,
             "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded 8-cluster Gaussian mixture)",
             "config": {"workload": args.workload, "n": n, "theta": w["theta"], "leaf_size": w["max_children"],
-                       "softening": w["softening"], "method": "Barnes-Hut, the reference's QuadTree and MAC",
+                       "softening": w["softening"],
+                       "method": ("Barnes-Hut + quadrupoles, the reference's QuadTreeMultiPole and MAC" if mp
+                                  else "Barnes-Hut, the reference's QuadTree and MAC"),
                        "l2": "256 MB buffer written between timed steps"},
             "error": {"median": err[0], "p90": err[1], "max": err[2], "vs": "fp64 direct sum", "samples": N_SAMPLES},
             "e2e": {"value": n / float(np.median(e2e)), "unit": UNIT, "h2d_bytes_per_step": n * 16,
                     "d2h_bytes_per_step": n * 16 + 8},
             "clocks": clk.summary(),
             "cpu_baseline": {"value": n / cpu_t, "unit": UNIT, "cores": 1, "kind": "port",
-                             "sample": f"the full {n}-particle system, reference BH (C port), {cpu_t:.2f} s"}}
+                             "sample": f"the full {n}-particle system, reference {'BHMP' if mp else 'BH'} (C port), "
+                                       f"{cpu_t:.2f} s"}}
     print(json.dumps(line))
 
 

@@ -21,6 +21,9 @@
 // src/trees/cpu/quadtreemultipole.h:31-289) uses the same tree with FP64
 // masses and COMs and a quadrupole sum_c [M_c (dc dc^T) + Q_c]; an accepted
 // node contributes the FMM kernels' C1 (monopole + quadrupole).
+#include <map>
+#include <memory>
+#include <mutex>
 #include <vector>
 
 #include "kernels.cuh"
@@ -336,15 +339,59 @@ __global__ void __launch_bounds__(128) k_bh_traverse(K ker, const double2* __res
     }
 }
 
+// Scratch of one call, carved from a per-device workspace that persists
+// between calls and only grows (calls on one device are serialised by its
+// mutex), so that repeated solves allocate nothing after the first.
+struct BHWork {
+    std::mutex mu;
+    Buf slot[32];
+    cudaEvent_t done = nullptr;  // recorded after each call's last use of the workspace
+    bool recorded = false;
+};
+
+// records the workspace's completion event on every exit of a call
+struct WorkRelease {
+    BHWork& w;
+    cudaStream_t s;
+    ~WorkRelease()
+    {
+        if (w.done && cudaEventRecord(w.done, s) == cudaSuccess) w.recorded = true;
+    }
+};
+
+__global__ void k_bh_iota(uint32_t* __restrict__ order, uint32_t n)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) order[i] = i;
+}
+
+BHWork& bh_work(int dev)
+{
+    static std::mutex m;
+    static std::map<int, std::unique_ptr<BHWork>> w;
+    std::lock_guard<std::mutex> g(m);
+    auto& p = w[dev];
+    if (!p) p.reset(new BHWork());
+    return *p;
+}
+
 struct DevBuf {
     void* p = nullptr;
-    ~DevBuf() { if (p) cudaFree(p); }
 };
+
+thread_local BHWork* g_work = nullptr;
+thread_local int g_slot = 0;
 
 template <typename T>
 int dalloc(DevBuf& b, size_t count)
 {
-    TC_CUDA_TRY(cudaMalloc(&b.p, count * sizeof(T) + 16));
+    if (!g_work || g_slot >= 32) {
+        tc_set_error("bh: workspace slots exhausted");
+        return TC_ERR_STATE;
+    }
+    Buf& w = g_work->slot[g_slot++];
+    int rc = ensure(w, count * sizeof(T) + 16);
+    if (rc) return rc;
+    b.p = w.p;
     return TC_OK;
 }
 
@@ -370,6 +417,16 @@ int bh_solve_impl(int kernel, double softening, int max_children, double theta, 
     const uint32_t n = (uint32_t)n64;
     cudaStream_t s = (cudaStream_t)stream;
     int rc = TC_OK;
+    int dev = 0;
+    TC_CUDA_TRY(cudaGetDevice(&dev));
+    BHWork& work = bh_work(dev);
+    std::lock_guard<std::mutex> work_lock(work.mu);
+    if (!work.done) TC_CUDA_TRY(cudaEventCreateWithFlags(&work.done, cudaEventDisableTiming));
+    // the previous call's kernels (possibly on another stream) finish first
+    if (work.recorded) TC_CUDA_TRY(cudaStreamWaitEvent(s, work.done, 0));
+    WorkRelease release_on_exit{work, s};
+    g_work = &work;
+    g_slot = 0;
     // node capacity (splits past it are refused, not written)
     const size_t cap = (size_t)4 * n + 64;
     DevBuf b_lo, b_hi, b_start, b_count, b_fc, b_nc, b_mass, b_com, b_comf, b_order, b_order2, b_nodeof, b_nodeof2,
@@ -399,12 +456,7 @@ int bh_solve_impl(int kernel, double softening, int max_children, double theta, 
     TC_CUDA_TRY(cudaMemsetAsync(b_err.p, 0, 16, s));
     if ((rc = bbox_keys(d_pos_xy, n64, (double*)b_bbox.p, (uint32_t*)b_err.p, s))) return rc;
     TC_CUDA_TRY(cudaMemsetAsync(node_of, 0, (size_t)n * 4, s));
-    {
-        std::vector<uint32_t> iota(n);
-        for (uint32_t i = 0; i < n; i++) iota[i] = i;
-        TC_CUDA_TRY(cudaMemcpyAsync(order, iota.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s));
-        TC_CUDA_TRY(cudaStreamSynchronize(s));
-    }
+    k_bh_iota<<<grid_for(n, 256), 256, 0, s>>>(order, n);
     k_bh_root<<<1, 1, 0, s>>>((const double*)b_bbox.p, n, t);
     std::vector<uint32_t> level_begin = {0}, level_end = {1};
     uint32_t total_nodes = 1;
@@ -518,6 +570,11 @@ extern "C" int tc_bhmp_solve_device(int kernel, double softening, int max_childr
                          true);
 }
 
+struct OwnBuf {
+    void* p = nullptr;
+    ~OwnBuf() { if (p) cudaFree(p); }
+};
+
 static int bh_solve_host(int kernel, double softening, int max_children, double theta, int precision,
                          const double* pos_xy, int64_t n, double* grad_xy, double* total, bool mp)
 {
@@ -527,7 +584,7 @@ static int bh_solve_host(int kernel, double softening, int max_children, double 
     }
     cudaStream_t s;
     TC_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-    DevBuf dp, dg, dt;
+    OwnBuf dp, dg, dt;
     int rc = TC_OK;
     cudaError_t e = cudaMalloc(&dp.p, (size_t)n * 16);
     if (e == cudaSuccess) e = cudaMalloc(&dg.p, (size_t)n * 16);
