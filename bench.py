@@ -475,12 +475,20 @@ def run_tsne_batch(args, w):
     from masterthesislucas_gb300 import affinity, datasets
     from masterthesislucas_gb300.tsne import TSNE, TSNEBatch, tune_depth
 
+    from masterthesislucas_gb300 import shard
+
+    rank, world = int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
     rng = np.random.default_rng(2024)
-    ns = np.exp(rng.uniform(np.log(w["n_min"]), np.log(w["n_max"]), w["systems"])).astype(np.int64)
+    ns_all = np.exp(rng.uniform(np.log(w["n_min"]), np.log(w["n_max"]), w["systems"])).astype(np.int64)
+    ks_all = rng.integers(w["clusters"][0], w["clusters"][1] + 1, len(ns_all))
+    # the systems are independent: each rank owns whole systems, no exchange
+    mine = shard.shard(ns_all, rank, world)
+    ns = ns_all[mine]
     t0 = time.perf_counter()
     systems = []
-    for i, n in enumerate(ns):
-        k = int(rng.integers(w["clusters"][0], w["clusters"][1] + 1))
+    for i, n in zip(mine, ns):
+        k = int(ks_all[i])
         x, _ = datasets.cluster_data(int(n), w["dim"], k=k, seed=10_000 + i)
         rp, col, val = affinity.build_p_csr(x, perplexity=w["perplexity"], device="cuda")
         y0 = np.random.default_rng(20_000 + i).normal(0.0, 1e-2, (int(n), 2))  # N(0, 1e-4)
@@ -497,23 +505,28 @@ def run_tsne_batch(args, w):
         batch.time_step()
     st0 = batch.stats()
     torch.cuda.synchronize()
-    with ClockSampler(0) as clk:
+    if world > 1:
+        torch.distributed.barrier()
+    with ClockSampler(local) as clk:
         t1 = time.perf_counter()
         for _ in range(args.steps):
             batch.time_step()
         torch.cuda.synchronize()
         dt = time.perf_counter() - t1
     st1 = batch.stats()
-    total = int(ns.sum())
+    dev = torch.device("cuda", local)
+    dt = shard.max_over_ranks(dt, device=dev)
+    total = shard.sum_over_ranks(int(ns.sum()), device=dev)
     value = total * args.steps / dt
     from masterthesislucas_gb300.solver import get_depth
     line = {"metric": "t-SNE gradient steps of a batch of embeddings (particles/s over all systems)",
-            "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (64-dim Gaussian clusters per system, P built by the project's kNN/perplexity code)",
             "config": {"workload": args.workload, "systems": int(w["systems"]), "particles": total,
-                       "n_min": int(ns.min()), "n_max": int(ns.max()), "perplexity": w["perplexity"], "k": 90,
+                       "n_min": int(ns_all.min()), "n_max": int(ns_all.max()),
+                       "parallelism": f"systems split over {world} rank(s) by particle count, no exchange", "perplexity": w["perplexity"], "k": 90,
                        "leaf_size": w["max_children"], "theta": w["theta"],
                        "orders": {"4": int((ns < 20000).sum()), "8": int((ns >= 20000).sum())},
                        "depth_offsets": np.bincount([d - get_depth(w["max_children"], int(n))
@@ -534,7 +547,8 @@ def run_tsne_batch(args, w):
     batch.close()
     for s in systems:
         s.close()
-    print(json.dumps(line))
+    if rank == 0:
+        print(json.dumps(line))
 
 
 def run_bh(args, w):
