@@ -34,14 +34,15 @@ template <int P>
 __global__ void __launch_bounds__(128) k_p2m_small(int dep, float h, const uint32_t* __restrict__ count,
                                                    const uint32_t* __restrict__ first,
                                                    const float* __restrict__ comrel, const float* __restrict__ prel,
-                                                   float* __restrict__ mu)
+                                                   float* __restrict__ mu, const uint32_t* __restrict__ act, const uint32_t* __restrict__ act_pos)
 {
     constexpr int K = ncoef(P);
     const uint32_t li = level_index(dep);
     const int64_t nl = (int64_t)1 << (2 * dep);
     const float ih = 1.0f / h;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t node = li + i;
+    const uint32_t k1 = act_pos[li + nl];
+    for (uint32_t k = act_pos[li] + blockIdx.x * blockDim.x + threadIdx.x; k < k1; k += gridDim.x * blockDim.x) {
+        const int64_t node = act[k];
         const uint32_t c = count[node];
         if (c == 0 || c > kLeafSmall) continue;
         const uint32_t f = first[node];
@@ -112,15 +113,16 @@ __global__ void __launch_bounds__(128) k_p2m(int dep, float h, const uint32_t* _
 // scale h/2) to the node's COM at scale h
 template <int P>
 __global__ void __launch_bounds__(128) k_m2m(int l, float hl, const uint32_t* __restrict__ count,
-                                             const float* __restrict__ comrel, float* __restrict__ mu)
+                                             const float* __restrict__ comrel, float* __restrict__ mu, const uint32_t* __restrict__ act, const uint32_t* __restrict__ act_pos)
 {
     constexpr int K = ncoef(P);
     const uint32_t li = level_index(l), lc = level_index(l + 1);
     const int64_t nl = (int64_t)1 << (2 * l);
     const float ih = 1.0f / hl;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t node = li + i;
-        if (count[node] == 0) continue;
+    const uint32_t k1 = act_pos[li + nl];
+    for (uint32_t k = act_pos[li] + blockIdx.x * blockDim.x + threadIdx.x; k < k1; k += gridDim.x * blockDim.x) {
+        const int64_t node = act[k];
+        const int64_t i = node - li;
         const float px = comrel[2 * node], py = comrel[2 * node + 1];
         float acc[K];
 #pragma unroll
@@ -179,15 +181,16 @@ __device__ __forceinline__ void m2m_child(float dx, float dy, const float* __res
 
 template <int P>
 __global__ void __launch_bounds__(128) k_m2m_stream(int l, float hl, const uint32_t* __restrict__ count,
-                                                    const float* __restrict__ comrel, float* __restrict__ mu)
+                                                    const float* __restrict__ comrel, float* __restrict__ mu, const uint32_t* __restrict__ act, const uint32_t* __restrict__ act_pos)
 {
     constexpr int K = ncoef(P), KS = kstride(P);
     const uint32_t li = level_index(l), lc = level_index(l + 1);
     const int64_t nl = (int64_t)1 << (2 * l);
     const float ih = 1.0f / hl;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t node = li + i;
-        if (count[node] == 0) continue;
+    const uint32_t k1 = act_pos[li + nl];
+    for (uint32_t k = act_pos[li] + blockIdx.x * blockDim.x + threadIdx.x; k < k1; k += gridDim.x * blockDim.x) {
+        const int64_t node = act[k];
+        const int64_t i = node - li;
         const float px = comrel[2 * node], py = comrel[2 * node + 1];
         float acc[K];
 #pragma unroll
@@ -210,15 +213,16 @@ __global__ void __launch_bounds__(128) k_m2m_stream(int l, float hl, const uint3
 
 template <int P>
 __global__ void __launch_bounds__(128) k_l2l_stream(int l, float hl, const uint32_t* __restrict__ count,
-                                                    const float* __restrict__ comrel, float* __restrict__ loc)
+                                                    const float* __restrict__ comrel, float* __restrict__ loc, const uint32_t* __restrict__ act, const uint32_t* __restrict__ act_pos)
 {
     constexpr int K = ncoef(P), KS = kstride(P);
     const uint32_t li = level_index(l), lp = level_index(l - 1);
     const int64_t nl = (int64_t)1 << (2 * l);
     const float ih = 1.0f / hl;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t node = li + i;
-        if (count[node] == 0) continue;
+    const uint32_t k1 = act_pos[li + nl];
+    for (uint32_t k = act_pos[li] + blockIdx.x * blockDim.x + threadIdx.x; k < k1; k += gridDim.x * blockDim.x) {
+        const int64_t node = act[k];
+        const int64_t i = node - li;
         const int64_t par = lp + (i >> 2);
         const int j = (int)(i & 3);
         const float ox = ((j & 1) ? 0.5f : -0.5f), oy = ((j & 2) ? 0.5f : -0.5f);
@@ -316,15 +320,16 @@ template <int P>
 __global__ void __launch_bounds__(128) k_m2l_p(int l, float hl, PotParams pp, const uint32_t* __restrict__ nn_ptr,
                                                const uint32_t* __restrict__ nn_idx, const uint32_t* __restrict__ count,
                                                const float* __restrict__ comrel, const float* __restrict__ mu,
-                                               float* __restrict__ loc, double* __restrict__ zpart)
+                                               float* __restrict__ loc, double* __restrict__ zpart, const uint32_t* __restrict__ act, const uint32_t* __restrict__ act_pos)
 {
     constexpr int K = ncoef(P), KS = kstride(P);
     const uint32_t li = level_index(l);
     const int64_t nl = (int64_t)1 << (2 * l);
     const float ih = 1.0f / hl;
-    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < nl; a += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t na = li + a;
-        if (count[na] == 0) continue;  // empty nodes are never read
+    const uint32_t k1 = act_pos[li + nl];  // empty nodes are never read
+    for (uint32_t k = act_pos[li] + blockIdx.x * blockDim.x + threadIdx.x; k < k1; k += gridDim.x * blockDim.x) {
+        const int64_t na = act[k];
+        const int64_t a = na - li;
         const uint32_t b0 = nn_ptr[a], b1 = nn_ptr[a + 1];
         float L[K];
 #pragma unroll
@@ -355,16 +360,17 @@ __global__ void __launch_bounds__(128) k_m2l_mixed(int l, float hl, PotParams pp
                                                    const uint8_t* __restrict__ ord,
                                                    const uint32_t* __restrict__ count,
                                                    const float* __restrict__ comrel, const float* __restrict__ mu,
-                                                   float* __restrict__ loc, double* __restrict__ zpart)
+                                                   float* __restrict__ loc, double* __restrict__ zpart, const uint32_t* __restrict__ act, const uint32_t* __restrict__ act_pos)
 {
     constexpr int K = ncoef(PACC), KS = kstride(12);
     constexpr bool first = OLO == 0;
     const uint32_t li = level_index(l);
     const int64_t nl = (int64_t)1 << (2 * l);
     const float ih = 1.0f / hl;
-    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < nl; a += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t na = li + a;
-        if (count[na] == 0) continue;
+    const uint32_t k1 = act_pos[li + nl];
+    for (uint32_t k = act_pos[li] + blockIdx.x * blockDim.x + threadIdx.x; k < k1; k += gridDim.x * blockDim.x) {
+        const int64_t na = act[k];
+        const int64_t a = na - li;
         const uint32_t p0 = nn_ptr[a], b1 = nn_ptr[a + 1];
         uint32_t e = p0;
         while (e < b1 && ord[e] < OLO) e++;
@@ -416,15 +422,16 @@ __global__ void __launch_bounds__(128) k_m2l_mixed(int l, float hl, PotParams pp
 // one thread per node of level l >= 1: L_fin = L_own + shift(L_fin(parent))
 template <int P>
 __global__ void __launch_bounds__(128) k_l2l(int l, float hl, const uint32_t* __restrict__ count,
-                                             const float* __restrict__ comrel, float* __restrict__ loc)
+                                             const float* __restrict__ comrel, float* __restrict__ loc, const uint32_t* __restrict__ act, const uint32_t* __restrict__ act_pos)
 {
     constexpr int K = ncoef(P);
     const uint32_t li = level_index(l), lp = level_index(l - 1);
     const int64_t nl = (int64_t)1 << (2 * l);
     const float ih = 1.0f / hl;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t node = li + i;
-        if (count[node] == 0) continue;
+    const uint32_t k1 = act_pos[li + nl];
+    for (uint32_t k = act_pos[li] + blockIdx.x * blockDim.x + threadIdx.x; k < k1; k += gridDim.x * blockDim.x) {
+        const int64_t node = act[k];
+        const int64_t i = node - li;
         const int64_t par = lp + (i >> 2);
         const int j = (int)(i & 3);
         // node COM - parent COM in units of the node's cell size h: the child
@@ -459,121 +466,176 @@ __global__ void k_chunks(int dep, const uint32_t* __restrict__ count, uint32_t* 
         nchunk[i] = (count[li + i] + 31u) / 32u;
 }
 
-// direct interaction of one sink (base offset bx, by) with a staged tile of
-// sources; FULL > 0 unrolls a full tile of FULL sources
-template <int FULL, typename KN>
-__device__ __forceinline__ void p2p_tile(const KN& ker, const float2* src, int m, float bx, float by, float& gx,
-                                         float& gy, float& zs)
+// work item -> leaf, from the exclusive scan of the chunk counts (items of
+// one leaf are consecutive); cap bounds the map's storage
+__global__ void k_chunk_leaf(int dep, const uint32_t* __restrict__ chunk_ptr, uint32_t* __restrict__ item_leaf,
+                             uint32_t cap)
 {
-    if (FULL > 0) {
+    const int64_t nl = (int64_t)1 << (2 * dep);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t c1 = min(chunk_ptr[i + 1], cap);
+        for (uint32_t c = chunk_ptr[i]; c < c1; c++) item_leaf[c] = (uint32_t)i;
+    }
+}
+
+// Sources staged per warp (float2, in the sink leaf's frame).  The whole near
+// list of a sink leaf is usually a few hundred particles, so one or two fills.
+constexpr int kNearBuf = 256;
+// Padding source: far enough that its force factor underflows to zero and its
+// pair term (~1e-18 gravity, ~1e-36 t-SNE) is absorbed by any real sum.
+constexpr float kFarAway = 1.0e18f;
+
+// One sink (px, py) against its share of the staged sources: g lanes share a
+// sink, lane r of the group takes float4 slots r, r + g, r + 2g, ... (two
+// sources each; consecutive lanes read consecutive 16-byte slots, so the
+// group's loads are conflict-free and the groups' identical loads broadcast).
+// n4 is a multiple of 4g, so every lane runs the same number of trips.
+template <typename KN>
+__device__ __forceinline__ void p2p_staged(const KN& ker, const float4* __restrict__ s4, uint32_t n4, uint32_t r,
+                                           uint32_t g, float px, float py, float& gx, float& gy, float& zs)
+{
+    for (uint32_t j = r; j < n4; j += 4 * g) {
 #pragma unroll
-        for (int j = 0; j < FULL; j++) {
-            const float2 t2 = src[j];
-            const float Rx = bx - t2.x, Ry = by - t2.y;
+        for (int u = 0; u < 4; u++) {
+            const float4 t4 = s4[j + u * g];
             float D1, t;
-            ker.near(Rx * Rx + Ry * Ry, D1, t);
-            gx += D1 * Rx;
-            gy += D1 * Ry;
+            float Rx = px - t4.x, Ry = py - t4.y;
+            ker.near_xy(Rx, Ry, D1, t);
+            gx = fmaf(D1, Rx, gx);
+            gy = fmaf(D1, Ry, gy);
             zs += t;
-        }
-    } else {
-        for (int j = 0; j < m; j++) {
-            const float2 t2 = src[j];
-            const float Rx = bx - t2.x, Ry = by - t2.y;
-            float D1, t;
-            ker.near(Rx * Rx + Ry * Ry, D1, t);
-            gx += D1 * Rx;
-            gy += D1 * Ry;
+            Rx = px - t4.z;
+            Ry = py - t4.w;
+            ker.near_xy(Rx, Ry, D1, t);
+            gx = fmaf(D1, Rx, gx);
+            gy = fmaf(D1, Ry, gy);
             zs += t;
         }
     }
 }
 
-// one warp per work item (leaf S, chunk of up to 32 sinks): L2P of the final
-// local expansion of S plus direct P2P with every particle of near(S)
+// One warp per work item (leaf S, chunk of m <= 32 sinks): L2P of the final
+// local expansion of S plus direct P2P with every particle of near(S).
+// * The near list is read 32 entries at a time, one per lane (index, first
+//   particle, count, frame offset), and broadcast by shuffles.
+// * Its particles are staged into shared memory shifted into S's
+//   cell-relative frame (x_T + (cell_T - cell_S) h), so the inner loop is one
+//   unrolled pass over a flat array, padded with far-away sources.
+// * A chunk of m sinks gives each sink g = 2^floor(log2(32/m)) lanes that
+//   split its sources; their partial forces are summed by shuffles.
 template <int P, typename KN>
-__global__ void __launch_bounds__(32 * kNearWarps)
+__global__ void __launch_bounds__(32 * kNearWarps, 9)
     k_near_p(KN ker, int dep, float h, const uint32_t* __restrict__ count, const uint32_t* __restrict__ first,
              const float* __restrict__ comrel, const float* __restrict__ loc, const uint32_t* __restrict__ near_ptr,
              const uint32_t* __restrict__ near_idx, const uint32_t* __restrict__ chunk_ptr,
-             const float* __restrict__ prel, const uint32_t* __restrict__ perm, double* __restrict__ grad,
-             int accumulate, int scatter, double* __restrict__ zwork, unsigned long long* __restrict__ counters)
+             const uint32_t* __restrict__ item_leaf, uint32_t cap, const float* __restrict__ prel,
+             const uint32_t* __restrict__ perm, double* __restrict__ grad, int accumulate, int scatter,
+             double* __restrict__ zwork, unsigned long long* __restrict__ counters)
 {
-    constexpr int K = ncoef(P);
     constexpr int KW = ncoef(P - 1);
-    __shared__ float2 s_src[kNearWarps][32];
+    __shared__ __align__(16) float2 s_src[kNearWarps][kNearBuf];
     uint32_t n_pp = 0;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    float2* buf = s_src[w];
+    const float4* buf4 = reinterpret_cast<const float4*>(s_src[w]);
+    const float2* prel2 = reinterpret_cast<const float2*>(prel);
     const uint32_t li = level_index(dep);
     const int64_t nl = (int64_t)1 << (2 * dep);
     const float ih = 1.0f / h;
-    const uint32_t nwork = chunk_ptr[nl];
+    const uint32_t nwork = min(chunk_ptr[nl], cap);
     const int64_t wstride = (int64_t)gridDim.x * kNearWarps;
     for (int64_t wi = blockIdx.x * (int64_t)kNearWarps + w; wi < nwork; wi += wstride) {
-        int64_t lo = 0, hi = nl;
-        while (hi - lo > 1) {
-            const int64_t mid = (lo + hi) >> 1;
-            if (chunk_ptr[mid] <= (uint32_t)wi) lo = mid; else hi = mid;
-        }
-        const int64_t si = lo;
+        const int64_t si = item_leaf[wi];
         const int64_t S = li + si;
         const uint32_t cS = count[S], fS = first[S];
-        const uint32_t sl = ((uint32_t)wi - chunk_ptr[si]) * 32u + lane;
-        const bool act = sl < cS;
-        const uint32_t s = fS + (act ? sl : 0);
+        const uint32_t c0 = ((uint32_t)wi - chunk_ptr[si]) * 32u;
+        const uint32_t m = min(32u, cS - c0);  // >= 1: a chunk exists only for sinks
+        const uint32_t lg = 5u - (32u - __clz(m - 1u));  // log2 g, g * m <= 32
+        const uint32_t g = 1u << lg, r = lane & (g - 1u), sk = lane >> lg;
+        const bool act = sk < m;
+        const uint32_t s = fS + c0 + (act ? sk : 0u);
         const int isx = (int)compact16((uint32_t)si), isy = (int)compact16((uint32_t)si >> 1);
-        const float px = prel[2 * s], py = prel[2 * s + 1];
+        const float2 p2 = prel2[s];
+        const float px = p2.x, py = p2.y;
         float gx = 0.f, gy = 0.f, zs = 0.f;
-        if (act) {
+        // warp-uniform: fill and every count
+        uint32_t fill = 0, staged = 0;
+        bool has_self = false;
+        const uint32_t e0 = near_ptr[si], e1 = near_ptr[si + 1];
+        for (uint32_t eb = e0; eb < e1; eb += 32) {
+            const uint32_t nt = min(32u, e1 - eb);
+            uint32_t mf = 0, mc = 0;
+            float mox = 0.f, moy = 0.f;
+            if (lane < nt) {
+                const uint32_t ti = near_idx[eb + lane];
+                mf = first[li + ti];
+                mc = count[li + ti];
+                mox = (float)((int)compact16(ti) - isx) * h;
+                moy = (float)((int)compact16(ti >> 1) - isy) * h;
+                has_self |= ti == (uint32_t)si;
+            }
+            for (uint32_t t = 0; t < nt; t++) {
+                const uint32_t fT = __shfl_sync(0xffffffffu, mf, t), cT = __shfl_sync(0xffffffffu, mc, t);
+                const float ox = __shfl_sync(0xffffffffu, mox, t), oy = __shfl_sync(0xffffffffu, moy, t);
+                for (uint32_t q0 = 0; q0 < cT; q0 += 32) {
+                    const uint32_t mq = min(32u, cT - q0);
+                    if (fill + mq > (uint32_t)kNearBuf) {
+                        // evaluate the staged sources (the buffer is a multiple of 8g long)
+                        const uint32_t n8 = (fill + 8u * g - 1u) & ~(8u * g - 1u);
+                        for (uint32_t q = fill + lane; q < n8; q += 32) buf[q] = make_float2(kFarAway, kFarAway);
+                        __syncwarp();
+                        if (act) p2p_staged(ker, buf4, n8 / 2, r, g, px, py, gx, gy, zs);
+                        __syncwarp();
+                        staged += fill;
+                        fill = 0;
+                    }
+                    if (lane < mq) {
+                        const float2 t2 = prel2[fT + q0 + lane];
+                        buf[fill + lane] = make_float2(t2.x + ox, t2.y + oy);
+                    }
+                    fill += mq;
+                }
+            }
+        }
+        if (fill > 0) {
+            const uint32_t n8 = (fill + 8u * g - 1u) & ~(8u * g - 1u);
+            for (uint32_t q = fill + lane; q < n8; q += 32) buf[q] = make_float2(kFarAway, kFarAway);
+            __syncwarp();
+            if (act) p2p_staged(ker, buf4, n8 / 2, r, g, px, py, gx, gy, zs);
+            __syncwarp();
+            staged += fill;
+        }
+        has_self = __any_sync(0xffffffffu, has_self);
+        // the g lanes of a sink hold partial forces: sum them into lane r = 0
+        for (uint32_t o = g >> 1; o > 0; o >>= 1) {
+            gx += __shfl_xor_sync(0xffffffffu, gx, o);
+            gy += __shfl_xor_sync(0xffffffffu, gy, o);
+        }
+        if (act && r == 0) {
             // L2P: F = (1/h) sum_b L_b d^(b - e) / (b - e)!
             float wv[KW];
             monomials<P - 1>((px - comrel[2 * S]) * ih, (py - comrel[2 * S + 1]) * ih, wv);
             const float* L = loc + S * kstride(P);
+            float lx = 0.f, ly = 0.f;
 #pragma unroll
             for (int k = 0; k < P; k++)
 #pragma unroll
                 for (int b = 0; b <= k; b++) {
                     const int a = k - b;
-                    gx += L[cidx(a + 1, b)] * wv[cidx(a, b)];
-                    gy += L[cidx(a, b + 1)] * wv[cidx(a, b)];
+                    lx += L[cidx(a + 1, b)] * wv[cidx(a, b)];
+                    ly += L[cidx(a, b + 1)] * wv[cidx(a, b)];
                 }
-            gx *= ih;
-            gy *= ih;
-        }
-        const uint32_t e0 = near_ptr[si], e1 = near_ptr[si + 1];
-        for (uint32_t e = e0; e < e1; e++) {
-            const uint32_t ti = near_idx[e];
-            const int64_t T = li + ti;
-            const uint32_t fT = first[T], cT = count[T];
-            const float bx = (float)(isx - (int)compact16(ti)) * h + px;
-            const float by = (float)(isy - (int)compact16(ti >> 1)) * h + py;
-            const bool self = ti == (uint32_t)si;
-            for (uint32_t q0 = 0; q0 < cT; q0 += 32) {
-                const uint32_t q = q0 + lane;
-                if (q < cT) s_src[w][lane] = make_float2(prel[2 * (fT + q)], prel[2 * (fT + q) + 1]);
-                __syncwarp();
-                const uint32_t m = min(32u, cT - q0);
-                if (act) {
-                    n_pp += m;
-                    if (m == 32u)
-                        p2p_tile<32>(ker, s_src[w], 32, bx, by, gx, gy, zs);
-                    else
-                        p2p_tile<0>(ker, s_src[w], (int)m, bx, by, gx, gy, zs);
-                }
-                __syncwarp();
-            }
-            if (self && act) {
-                // the tile loop included the sink itself: R = 0 adds no force
-                // but adds the kernel's pair term at r = 0, which is removed here
+            n_pp += staged;
+            if (has_self) {
+                // the staged sources included the sink itself: R = 0 adds no
+                // force but adds the kernel's pair term at r = 0, removed here
                 float D1, t0;
-                ker.near(0.0f, D1, t0);
+                ker.near_xy(0.0f, 0.0f, D1, t0);
                 zs -= t0;
                 n_pp--;
             }
-        }
-        if (act) {
             const int64_t o = scatter ? (int64_t)perm[s] : (int64_t)s;
-            double ox2 = (double)gx, oy2 = (double)gy;
+            double ox2 = (double)(lx * ih + gx), oy2 = (double)(ly * ih + gy);
             if (accumulate) {
                 ox2 += grad[2 * o];
                 oy2 += grad[2 * o + 1];
@@ -619,7 +681,8 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
     if ((rc = ensure(h.mu, nn * kstride(ORD) * 4)) || (rc = ensure(h.loc, nn * kstride(ORD) * 4)) ||
         (rc = ensure(h.zpart, nn * 8 + 64)) ||
         (rc = ensure(h.counters, 64)) || (rc = ensure(h.chunk, (nleaf + 1) * 4)) ||
-        (rc = ensure(h.zwork, wmax * 8)) || (rc = ensure(h.cnt_tmp, nleaf * 4 + 64)) ||
+        (rc = ensure(h.zwork, wmax * 8)) || (rc = ensure(h.chunk_leaf, wmax * 4)) ||
+        (rc = ensure(h.cnt_tmp, nleaf * 4 + 64)) ||
         (rc = ensure(h.tmp, scan_tmp_words(nleaf) * 4)) || (rc = record(h, 4)))
         return rc;
     TC_CUDA_TRY(cudaMemsetAsync(h.counters.p, 0, 64, s));
@@ -647,38 +710,39 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
             if (h.ctrl_on) {
                 const uint8_t* od = P<uint8_t>(h.ord_pool) + h.lists.nn_idx_off[l];
                 k_m2l_mixed<8, 0, 2><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, count, comrel, mu,
-                                                                       loc, zp);
+                                                                       loc, zp, P<uint32_t>(h.act), P<uint32_t>(h.act_pos));
                 k_m2l_mixed<12, 3, 4><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, count, comrel, mu,
-                                                                        loc, zp);
+                                                                        loc, zp, P<uint32_t>(h.act), P<uint32_t>(h.act_pos));
                 h.launches++;
                 mixed = true;
             }
         }
         if (!mixed)
-            k_m2l_p<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, count, comrel, mu, loc, zp);
+            k_m2l_p<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, count, comrel, mu, loc, zp, P<uint32_t>(h.act), P<uint32_t>(h.act_pos));
     }
     for (int l = 1; l <= dep; l++) {
         const int64_t nl = (int64_t)1 << (2 * l);
         if constexpr (ORD >= 10)
-            k_l2l_stream<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, loc);
+            k_l2l_stream<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, loc, P<uint32_t>(h.act), P<uint32_t>(h.act_pos));
         else
-            k_l2l<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, loc);
+            k_l2l<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, loc, P<uint32_t>(h.act), P<uint32_t>(h.act_pos));
     }
     uint32_t* nchunk = P<uint32_t>(h.cnt_tmp);
     uint32_t* chunk_ptr = P<uint32_t>(h.chunk);
     k_chunks<<<grid_for(nleaf, 256), 256, 0, s>>>(dep, count, nchunk);
     if ((rc = exclusive_scan_u32(nchunk, chunk_ptr, nleaf, P<uint32_t>(h.tmp), s))) return rc;
+    k_chunk_leaf<<<grid_for(nleaf, 256), 256, 0, s>>>(dep, chunk_ptr, P<uint32_t>(h.chunk_leaf), (uint32_t)wmax);
     if ((rc = record(h, 5))) return rc;
     const int64_t wblk = (wmax + kNearWarps - 1) / kNearWarps;
     k_near_p<ORD, KN><<<(unsigned)(wblk < kSMs * 256 ? wblk : kSMs * 256), 32 * kNearWarps, 0, s>>>(
         ker, dep, hl(dep), count, P<uint32_t>(h.first), comrel, loc, ptr + h.lists.near_ptr_off[dep],
-        idx + h.lists.near_idx_off[dep], chunk_ptr, P<float>(h.prel), P<uint32_t>(h.perm), d_grad, accumulate,
-        scatter, P<double>(h.zwork), P<unsigned long long>(h.counters));
+        idx + h.lists.near_idx_off[dep], chunk_ptr, P<uint32_t>(h.chunk_leaf), (uint32_t)wmax, P<float>(h.prel),
+        P<uint32_t>(h.perm), d_grad, accumulate, scatter, P<double>(h.zwork), P<unsigned long long>(h.counters));
     if ((rc = record(h, 6))) return rc;
     if ((rc = ensure(h.sumtmp, sum_tmp_doubles() * 8)) ||
         (rc = sum_f64(zp, nn, P<double>(h.zwork), chunk_ptr + nleaf, d_total, 1, P<double>(h.sumtmp), s)))
         return rc;
-    h.launches += 3 + 2 * dep + 5;
+    h.launches += 3 + 2 * dep + 6;
     TC_CUDA_TRY(cudaGetLastError());
     return record(h, 7);
 }
@@ -697,15 +761,15 @@ int multipoles_p(Handle& h)
     const uint32_t* count = P<uint32_t>(h.count);
     auto hl = [&](int l) { return (float)(h.L / (double)(1u << l)); };
     k_p2m_small<ORD><<<grid_for(nleaf, 128), 128, 0, s>>>(dep, hl(dep), count, P<uint32_t>(h.first), comrel,
-                                                         P<float>(h.prel), mu);
+                                                         P<float>(h.prel), mu, P<uint32_t>(h.act), P<uint32_t>(h.act_pos));
     k_p2m<ORD><<<grid_for((h.n / (kLeafSmall + 1) + 1) * 32, 128), 128, 0, s>>>(
         dep, hl(dep), count, P<uint32_t>(h.first), comrel, P<float>(h.prel), P<uint32_t>(h.bigleaf), mu);
     for (int l = dep - 1; l >= 0; l--) {
         const int64_t nl = (int64_t)1 << (2 * l);
         if constexpr (ORD >= 10)
-            k_m2m_stream<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, mu);
+            k_m2m_stream<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, mu, P<uint32_t>(h.act), P<uint32_t>(h.act_pos));
         else
-            k_m2m<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, mu);
+            k_m2m<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, mu, P<uint32_t>(h.act), P<uint32_t>(h.act_pos));
     }
     h.launches += 2 + dep;
     h.mu_stride = kstride(ORD);

@@ -22,6 +22,23 @@ __device__ inline float rsq<float>(float x) { return rsqrtf(x); }
 template <>
 __device__ inline double rsq<double>(double x) { return 1.0 / sqrt(x); }
 
+// Single-instruction approximations of the PTX ISA (rcp.approx.ftz.f32,
+// rsqrt.approx.ftz.f32: relative error below 2^-23 and 2^-22.9) for the
+// P2P inner loops, where every instruction of the pair is on the critical
+// issue path.
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float rsqrt_approx(float x)
+{
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // Student-t kernel of the t-SNE repulsion: F(R) = R (1+r^2)^-2, pair term (1+r^2)^-1
 template <typename real>
 struct KTsne {
@@ -37,6 +54,13 @@ struct KTsne {
     __device__ inline void near(real s, real& D1, real& t) const
     {
         real fd = rcp<real>(real(1) + s);
+        D1 = fd * fd;
+        t = fd;
+    }
+    // near() of s = Rx^2 + Ry^2 with the constant folded into the FMA chain
+    __device__ __forceinline__ void near_xy(float Rx, float Ry, float& D1, float& t) const
+    {
+        const float fd = rcp_approx(fmaf(Ry, Ry, fmaf(Rx, Rx, 1.0f)));
         D1 = fd * fd;
         t = fd;
     }
@@ -61,6 +85,12 @@ struct KGrav {
     {
         real isq = rsq<real>(s + eps2);
         D1 = -isq * isq * isq;
+        t = -isq;
+    }
+    __device__ __forceinline__ void near_xy(float Rx, float Ry, float& D1, float& t) const
+    {
+        const float isq = rsqrt_approx(fmaf(Ry, Ry, fmaf(Rx, Rx, (float)eps2)));
+        D1 = -(isq * isq) * isq;
         t = -isq;
     }
 };

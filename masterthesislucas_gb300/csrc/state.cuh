@@ -56,6 +56,11 @@ struct Handle {
     Buf ptr_pool, idx_pool, cnt_tmp, lstat, ord_pool, nfeat, dec;
     // order-p path: leaves above kLeafSmall particles ([0] count, then indices)
     Buf bigleaf;
+    Buf chunk_leaf;  // near-field work item -> its leaf (order-p solve)
+    // order p: the non-empty nodes of every level in Morton order (act) and the
+    // exclusive scan of non-emptiness over all nodes (act_pos); level l owns
+    // act[act_pos[li] .. act_pos[li + 4^l])
+    Buf act, act_pos;
     Buf diagpart;  // leapfrog diagnostics: per-block partial sums
     // learned order controller (order-p mode): weights + normalisation copy
     // no-sync mode (stream capture): no host round trips or stage events; the
