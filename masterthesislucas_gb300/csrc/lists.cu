@@ -68,12 +68,17 @@ __global__ void k_lists(int l, double inv_theta, double theta, int variant, real
                         const uint32_t* __restrict__ pnear_idx, uint32_t pcap, uint32_t* __restrict__ nn_cnt,
                         uint32_t* __restrict__ near_cnt, const uint32_t* __restrict__ nn_ptr,
                         uint32_t* __restrict__ nn_idx, uint32_t nn_cap, const uint32_t* __restrict__ near_ptr,
-                        uint32_t* __restrict__ near_idx, uint32_t near_cap, uint32_t* __restrict__ ovf, int fill)
+                        uint32_t* __restrict__ near_idx, uint32_t near_cap, uint32_t* __restrict__ ovf, int fill,
+                        const uint32_t* __restrict__ act, const uint32_t* __restrict__ act_pos)
 {
     const uint32_t np = l ? (1u << (2 * (l - 1))) : 0u;
     const uint32_t li = level_index(l);
     const int64_t nl = (int64_t)1 << (2 * l);
-    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < nl; a += (int64_t)gridDim.x * blockDim.x) {
+    // with an active-node list only the non-empty nodes are visited (the
+    // caller zeroes the counts of the others)
+    const int64_t k0 = act ? (int64_t)act_pos[li] : 0, k1 = act ? (int64_t)act_pos[li + nl] : nl;
+    for (int64_t k = k0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < k1; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t a = act ? (int64_t)act[k] - li : k;
         uint32_t nn = 0, nr = 0;
         if (count[li + a] != 0) {
             if (l == 0) {
@@ -371,12 +376,15 @@ int build_lists(Handle& h)
     const int64_t nleaf = (int64_t)1 << (2 * depth);
     int rc;
     if ((rc = ensure(h.ptr_pool, ptr_words * 4)) || (rc = ensure(h.cnt_tmp, 2 * nleaf * 4 + 64)) ||
-        (rc = ensure(h.tmp, (radix_tmp_words(h.n) > scan_tmp_words(nleaf) ? radix_tmp_words(h.n)
-                                                                           : scan_tmp_words(nleaf)) * 4)))
+        (rc = ensure(h.tmp, (radix_tmp_words(h.n) > 2 * scan_tmp_words(nleaf) ? radix_tmp_words(h.n)
+                                                                               : 2 * scan_tmp_words(nleaf)) * 4)))
         return rc;
     uint32_t* ptr = P<uint32_t>(h.ptr_pool);
     uint32_t* nn_cnt = P<uint32_t>(h.cnt_tmp);
     uint32_t* near_cnt = nn_cnt + nleaf;
+    // order p (FP32): the tree build listed the non-empty nodes
+    const uint32_t* act = h.cfg.order && h.cfg.precision != TC_PREC_FP64 ? P<uint32_t>(h.act) : nullptr;
+    const uint32_t* act_pos = act ? P<uint32_t>(h.act_pos) : nullptr;
     const double inv_theta = 1.0 / h.cfg.theta;
     uint32_t* ovf_flag = P<uint32_t>(h.err) + 1;
     auto launch = [&](int l, const uint32_t* pnp, const uint32_t* pni, uint32_t pcap, uint32_t* nnc, uint32_t* nrc,
@@ -404,13 +412,13 @@ int build_lists(Handle& h)
                                                              P<uint32_t>(h.count),
                                                              P<double2>(h.com64), P<double>(h.comrel),
                                                              P<double>(h.bblen), pnp, pni, pcap, nnc, nrc, nnp, nni,
-                                                             nncap, nrp, nri, nrcap, ovf_flag, fill);
+                                                             nncap, nrp, nri, nrcap, ovf_flag, fill, nullptr, nullptr);
         else
             k_lists<float><<<grid_for(nl, 128), 128, 0, s>>>(l, inv_theta, h.cfg.theta, h.variant, (float)hl,
                                                             P<uint32_t>(h.count),
                                                             P<double2>(h.com64), P<float>(h.comrel),
                                                             P<double>(h.bblen), pnp, pni, pcap, nnc, nrc, nnp, nni,
-                                                            nncap, nrp, nri, nrcap, ovf_flag, fill);
+                                                            nncap, nrp, nri, nrcap, ovf_flag, fill, act, act_pos);
         return 0;
     };
     if (h.ctrl_on) {
@@ -449,12 +457,15 @@ int build_lists(Handle& h)
             const uint32_t* pnp = l ? ptr + L.near_ptr_off[l - 1] : nullptr;
             const uint32_t* pni = l ? P<uint32_t>(h.idx_pool) + L.near_idx_off[l - 1] : nullptr;
             const uint32_t pcap = l ? L.near_cap[l - 1] : 0u;
+            if (act) {
+                TC_CUDA_TRY(cudaMemsetAsync(nn_cnt, 0, nl * 4, s));
+                TC_CUDA_TRY(cudaMemsetAsync(near_cnt, 0, nl * 4, s));
+            }
             if ((rc = launch(l, pnp, pni, pcap, nn_cnt, near_cnt, nullptr, nullptr, 0, nullptr, nullptr, 0, 0)))
                 return rc;
             uint32_t* nnp = ptr + L.nn_ptr_off[l];
             uint32_t* nrp = ptr + L.near_ptr_off[l];
-            if ((rc = exclusive_scan_u32(nn_cnt, nnp, nl, P<uint32_t>(h.tmp), s))) return rc;
-            if ((rc = exclusive_scan_u32(near_cnt, nrp, nl, P<uint32_t>(h.tmp), s))) return rc;
+            if ((rc = exclusive_scan2_u32(nn_cnt, nnp, near_cnt, nrp, nl, P<uint32_t>(h.tmp), s))) return rc;
             if ((rc = launch(l, pnp, pni, pcap, nullptr, nullptr, nnp, P<uint32_t>(h.idx_pool) + L.nn_idx_off[l],
                              L.nn_cap[l], nrp, P<uint32_t>(h.idx_pool) + L.near_idx_off[l], L.near_cap[l], 1)))
                 return rc;
@@ -463,7 +474,7 @@ int build_lists(Handle& h)
                 k_clamp_ptr<<<grid_for(nl + 1, 256), 256, 0, s>>>(nrp, nl + 1, L.near_cap[l]);
                 h.launches += 2;
             }
-            h.launches += 8;
+            h.launches += 2 + (nl <= 2048 ? 1 : 3);  // count, fill, scan
         }
         if (h.nosync) {
             // captured step: the overflow flag lands in pinned memory for the caller to check
@@ -505,11 +516,14 @@ int build_lists(Handle& h)
         const uint32_t* pnp = l ? ptr + L.near_ptr_off[l - 1] : nullptr;
         const uint32_t* pni = l ? P<uint32_t>(h.idx_pool) + L.near_idx_off[l - 1] : nullptr;
         const uint32_t pcap = l ? L.near_total[l - 1] : 0u;
+        if (act) {
+            TC_CUDA_TRY(cudaMemsetAsync(nn_cnt, 0, nl * 4, s));
+            TC_CUDA_TRY(cudaMemsetAsync(near_cnt, 0, nl * 4, s));
+        }
         if ((rc = launch(l, pnp, pni, pcap, nn_cnt, near_cnt, nullptr, nullptr, 0, nullptr, nullptr, 0, 0))) return rc;
         uint32_t* nnp = ptr + L.nn_ptr_off[l];
         uint32_t* nrp = ptr + L.near_ptr_off[l];
-        if ((rc = exclusive_scan_u32(nn_cnt, nnp, nl, P<uint32_t>(h.tmp), s))) return rc;
-        if ((rc = exclusive_scan_u32(near_cnt, nrp, nl, P<uint32_t>(h.tmp), s))) return rc;
+        if ((rc = exclusive_scan2_u32(nn_cnt, nnp, near_cnt, nrp, nl, P<uint32_t>(h.tmp), s))) return rc;
         TC_CUDA_TRY(cudaMemcpyAsync(h.h_words, nnp + nl, 4, cudaMemcpyDeviceToHost, s));
         TC_CUDA_TRY(cudaMemcpyAsync(h.h_words + 1, nrp + nl, 4, cudaMemcpyDeviceToHost, s));
         TC_CUDA_TRY(cudaStreamSynchronize(s));
@@ -542,7 +556,7 @@ int build_lists(Handle& h)
         if ((rc = launch(l, pnp, pni, pcap, nullptr, nullptr, nnp, P<uint32_t>(h.idx_pool) + L.nn_idx_off[l],
                          L.nn_total[l], nrp, P<uint32_t>(h.idx_pool) + L.near_idx_off[l], L.near_total[l], 1)))
             return rc;
-        h.launches += 8;
+        h.launches += 2 + (nl <= 2048 ? 1 : 3);  // count, fill, scan
     }
     // capacities for the next calls
     L.nn_cap.resize(depth + 1);

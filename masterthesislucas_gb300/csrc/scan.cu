@@ -64,6 +64,72 @@ __global__ void k_scan_final(const uint32_t* __restrict__ in, uint32_t* __restri
     if (blockIdx.x == nb - 1 && threadIdx.x == 0) out[n] = partial[blockIdx.x] + tot;
 }
 
+// two arrays at once: blockIdx.y selects (in0, out0) or (in1, out1); the
+// partials of array y sit at partial + y * nb
+__global__ void k_scan_reduce2(const uint32_t* __restrict__ in0, const uint32_t* __restrict__ in1, int64_t n,
+                               uint32_t* __restrict__ partial, int64_t nb)
+{
+    const uint32_t* in = blockIdx.y ? in1 : in0;
+    int64_t base = (int64_t)blockIdx.x * kScanChunk;
+    uint32_t s = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++) {
+        int64_t k = base + (int64_t)i * kScanThreads + threadIdx.x;
+        if (k < n) s += in[k];
+    }
+    s = warp_sum(s);
+    __shared__ uint32_t ws[kScanThreads / 32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int w = 0; w < kScanThreads / 32; w++) t += ws[w];
+        partial[blockIdx.y * nb + blockIdx.x] = t;
+    }
+}
+
+__global__ void k_scan_partials2(uint32_t* partial, int64_t nb)
+{
+    uint32_t* p = partial + blockIdx.x * nb;
+    uint32_t carry = 0;
+    for (int64_t base = 0; base < nb; base += blockDim.x) {
+        int64_t k = base + threadIdx.x;
+        uint32_t v = k < nb ? p[k] : 0u;
+        uint32_t tot;
+        uint32_t ex = block_exclusive_scan(v, tot);
+        if (k < nb) p[k] = carry + ex;
+        carry += tot;
+    }
+}
+
+// partial == nullptr: a single chunk (nb == 1), no carry
+__global__ void k_scan_final2(const uint32_t* __restrict__ in0, uint32_t* __restrict__ out0,
+                              const uint32_t* __restrict__ in1, uint32_t* __restrict__ out1, int64_t n,
+                              const uint32_t* __restrict__ partial, int64_t nb)
+{
+    const uint32_t* in = blockIdx.y ? in1 : in0;
+    uint32_t* out = blockIdx.y ? out1 : out0;
+    const uint32_t carry = partial ? partial[blockIdx.y * nb + blockIdx.x] : 0u;
+    int64_t base = (int64_t)blockIdx.x * kScanChunk + (int64_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t s = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++) {
+        int64_t k = base + i;
+        v[i] = k < n ? in[k] : 0u;
+        s += v[i];
+    }
+    uint32_t tot;
+    uint32_t ex = block_exclusive_scan(s, tot) + carry;
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++) {
+        int64_t k = base + i;
+        if (k < n) out[k] = ex;
+        ex += v[i];
+    }
+    if (blockIdx.x == nb - 1 && threadIdx.x == 0) out[n] = carry + tot;
+}
+
 constexpr int kSumBlocks = 2 * kSMs;
 
 // stage 1 of sum_f64: block b sums the grid-stride slice b of a[0..na) ++ c[0..*nc)
@@ -123,9 +189,34 @@ int exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* t
         return TC_OK;
     }
     int64_t nb = (n + kScanChunk - 1) / kScanChunk;
+    if (nb == 1) {
+        k_scan_final2<<<dim3(1, 1), kScanThreads, 0, s>>>(in, out, in, out, n, nullptr, 1);
+        TC_CUDA_TRY(cudaGetLastError());
+        return TC_OK;
+    }
     k_scan_reduce<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, tmp);
     k_scan_partials<<<1, 1024, 0, s>>>(tmp, nb);
     k_scan_final<<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, tmp, nb);
+    TC_CUDA_TRY(cudaGetLastError());
+    return TC_OK;
+}
+
+int exclusive_scan2_u32(const uint32_t* in0, uint32_t* out0, const uint32_t* in1, uint32_t* out1, int64_t n,
+                        uint32_t* tmp, cudaStream_t s)
+{
+    if (n <= 0) {
+        TC_CUDA_TRY(cudaMemsetAsync(out0, 0, sizeof(uint32_t), s));
+        TC_CUDA_TRY(cudaMemsetAsync(out1, 0, sizeof(uint32_t), s));
+        return TC_OK;
+    }
+    int64_t nb = (n + kScanChunk - 1) / kScanChunk;
+    if (nb == 1) {
+        k_scan_final2<<<dim3(1, 2), kScanThreads, 0, s>>>(in0, out0, in1, out1, n, nullptr, 1);
+    } else {
+        k_scan_reduce2<<<dim3((unsigned)nb, 2), kScanThreads, 0, s>>>(in0, in1, n, tmp, nb);
+        k_scan_partials2<<<2, 1024, 0, s>>>(tmp, nb);
+        k_scan_final2<<<dim3((unsigned)nb, 2), kScanThreads, 0, s>>>(in0, out0, in1, out1, n, tmp, nb);
+    }
     TC_CUDA_TRY(cudaGetLastError());
     return TC_OK;
 }

@@ -126,7 +126,7 @@ int radix_sort_u32(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32_t*
         int rc = exclusive_scan_u32(hist, offs, h, stmp, s);
         if (rc) return rc;
         k_radix_scatter<<<nb, RT, 0, s>>>(ki, vi, ko, vo, n, pass * 8, offs, nb, pass == 0);
-        if (launches) *launches += 5;
+        if (launches) *launches += 2 + (h <= 2048 ? 1 : 3);  // histogram, scatter, scan
         uint32_t* t = ki; ki = ko; ko = t;
         t = vi; vi = vo; vo = t;
     }
