@@ -326,6 +326,7 @@ __global__ void __launch_bounds__(128) k_m2l_p(int l, float hl, PotParams pp, co
     const uint32_t li = level_index(l);
     const int64_t nl = (int64_t)1 << (2 * l);
     const float ih = 1.0f / hl;
+    const float2* comrel2 = reinterpret_cast<const float2*>(comrel);
     const uint32_t k1 = act_pos[li + nl];  // empty nodes are never read
     for (uint32_t k = act_pos[li] + blockIdx.x * blockDim.x + threadIdx.x; k < k1; k += gridDim.x * blockDim.x) {
         const int64_t na = act[k];
@@ -335,12 +336,21 @@ __global__ void __launch_bounds__(128) k_m2l_p(int l, float hl, PotParams pp, co
 #pragma unroll
         for (int k = 0; k < K; k++) L[k] = 0.f;
         const int iax = (int)compact16((uint32_t)a), iay = (int)compact16((uint32_t)a >> 1);
-        const float cax = comrel[2 * na], cay = comrel[2 * na + 1];
+        const float2 ca = comrel2[na];
+        // the next entry's index and COM are loaded one iteration ahead, so
+        // the dependent index -> COM loads overlap the current M2L
+        uint32_t bn = b0 < b1 ? nn_idx[b0] : 0u;
+        float2 cn = comrel2[li + bn];
         for (uint32_t e = b0; e < b1; e++) {
-            const uint32_t b = nn_idx[e];
+            const uint32_t b = bn;
+            const float2 cb = cn;
+            if (e + 1 < b1) {
+                bn = nn_idx[e + 1];
+                cn = comrel2[li + bn];
+            }
             const int64_t nb = li + b;
-            const float Rx = (float)(iax - (int)compact16(b)) + (cax - comrel[2 * nb]) * ih;
-            const float Ry = (float)(iay - (int)compact16(b >> 1)) + (cay - comrel[2 * nb + 1]) * ih;
+            const float Rx = (float)(iax - (int)compact16(b)) + (ca.x - cb.x) * ih;
+            const float Ry = (float)(iay - (int)compact16(b >> 1)) + (ca.y - cb.y) * ih;
             m2l_acc<P, KS>(Rx, Ry, hl, pp, mu + nb * KS, L);
         }
         m2l_store<K, KS>(na, b0 != b1, pp.kappa, L, mu, loc, zpart);
@@ -367,6 +377,7 @@ __global__ void __launch_bounds__(128) k_m2l_mixed(int l, float hl, PotParams pp
     const uint32_t li = level_index(l);
     const int64_t nl = (int64_t)1 << (2 * l);
     const float ih = 1.0f / hl;
+    const float2* comrel2 = reinterpret_cast<const float2*>(comrel);
     const uint32_t k1 = act_pos[li + nl];
     for (uint32_t k = act_pos[li] + blockIdx.x * blockDim.x + threadIdx.x; k < k1; k += gridDim.x * blockDim.x) {
         const int64_t na = act[k];
@@ -379,14 +390,25 @@ __global__ void __launch_bounds__(128) k_m2l_mixed(int l, float hl, PotParams pp
 #pragma unroll
         for (int k = 0; k < K; k++) L[k] = 0.f;
         const int iax = (int)compact16((uint32_t)a), iay = (int)compact16((uint32_t)a >> 1);
-        const float cax = comrel[2 * na], cay = comrel[2 * na + 1];
+        const float2 ca = comrel2[na];
+        // next entry's order, index and COM one iteration ahead
+        uint8_t on = e < b1 ? ord[e] : 0xff;
+        uint32_t bn = e < b1 ? nn_idx[e] : 0u;
+        float2 cn = comrel2[li + bn];
         auto bucket = [&](auto order_tag, int o) {
             constexpr int PO = decltype(order_tag)::value;
-            for (; e < b1 && ord[e] == o; e++) {
-                const uint32_t b = nn_idx[e];
+            for (; e < b1 && on == o; e++) {
+                const uint32_t b = bn;
+                const float2 cb = cn;
+                on = 0xff;
+                if (e + 1 < b1) {
+                    on = ord[e + 1];
+                    bn = nn_idx[e + 1];
+                    cn = comrel2[li + bn];
+                }
                 const int64_t nb = li + b;
-                const float Rx = (float)(iax - (int)compact16(b)) + (cax - comrel[2 * nb]) * ih;
-                const float Ry = (float)(iay - (int)compact16(b >> 1)) + (cay - comrel[2 * nb + 1]) * ih;
+                const float Rx = (float)(iax - (int)compact16(b)) + (ca.x - cb.x) * ih;
+                const float Ry = (float)(iay - (int)compact16(b >> 1)) + (ca.y - cb.y) * ih;
                 if constexpr (PO <= PACC) m2l_acc<PO, KS>(Rx, Ry, hl, pp, mu + nb * KS, L);
             }
         };
