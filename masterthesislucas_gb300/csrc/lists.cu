@@ -144,10 +144,12 @@ __global__ void k_lists(int l, double inv_theta, double theta, int variant, real
 
 // per-node features for the controller (all levels; empty nodes skipped)
 __global__ void k_node_feat(int depth, double L, const uint32_t* __restrict__ count, const float* __restrict__ comrel,
-                            const float* __restrict__ mu, int mu_stride, float4* __restrict__ nfeat, int64_t nnodes)
+                            const float* __restrict__ mu, int mu_stride, float4* __restrict__ nfeat, int64_t nnodes,
+                            const uint32_t* __restrict__ act, const uint32_t* __restrict__ act_pos)
 {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nnodes; i += (int64_t)gridDim.x * blockDim.x) {
-        if (count[i] == 0) continue;
+    const int64_t k1 = act_pos[nnodes];
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < k1; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = act[k];
         int l = 0;
         while (l < depth && i >= (int64_t)level_index(l + 1)) l++;
         const float ih = (float)((double)(1u << l) / L);
@@ -166,7 +168,8 @@ __global__ void __launch_bounds__(32 * ctrl::kWarps) k_lists_ctrl_count(
     int l, float hl, float c_over_h2, const uint32_t* __restrict__ count, const float* __restrict__ comrel,
     const float4* __restrict__ nfeat, const uint32_t* __restrict__ pnear_ptr, const uint32_t* __restrict__ pnear_idx,
     uint32_t pcap, uint32_t* __restrict__ nn_cnt, uint32_t* __restrict__ near_cnt, uint8_t* __restrict__ dec,
-    const float* __restrict__ wctrl, float log_tau)
+    const float* __restrict__ wctrl, float log_tau, const uint32_t* __restrict__ act,
+    const uint32_t* __restrict__ act_pos)
 {
     __shared__ __align__(16) ctrl::Smem S;
     ctrl::load_weights(S, wctrl, wctrl + TC_MLP_NPARAM, wctrl + TC_MLP_NPARAM + TC_MLP_IN);
@@ -177,9 +180,13 @@ __global__ void __launch_bounds__(32 * ctrl::kWarps) k_lists_ctrl_count(
     const int64_t nl = (int64_t)1 << (2 * l);
     const float ih = 1.0f / hl;
     const int64_t nwarps = (int64_t)gridDim.x * ctrl::kWarps;
-    for (int64_t base = ((int64_t)blockIdx.x * ctrl::kWarps + wid) * 32; base < nl; base += nwarps * 32) {
-        const int64_t a = base + lane;
-        bool active = a < nl && count[li + a] != 0;
+    // lanes take consecutive non-empty nodes of the level (the counts of the
+    // empty ones are zeroed by the caller)
+    const int64_t k0 = act_pos[li], k1 = act_pos[li + nl];
+    for (int64_t base = k0 + ((int64_t)blockIdx.x * ctrl::kWarps + wid) * 32; base < k1; base += nwarps * 32) {
+        const bool valid = base + lane < k1;
+        const int64_t a = valid ? (int64_t)act[base + lane] - li : 0;
+        bool active = valid;
         uint32_t e = 0, e1 = 0, j = 0, nn = 0, nr = 0;
         int iax = 0, iay = 0;
         float cax = 0.f, cay = 0.f;
@@ -243,7 +250,7 @@ __global__ void __launch_bounds__(32 * ctrl::kWarps) k_lists_ctrl_count(
                 else nr++;
             }
         }
-        if (a < nl) {
+        if (valid) {
             nn_cnt[a] = nn;
             near_cnt[a] = nr;
         }
@@ -257,13 +264,16 @@ __global__ void k_lists_ctrl_fill(int l, const uint32_t* __restrict__ count, con
                                   const uint32_t* __restrict__ pnear_idx, uint32_t pcap, const uint8_t* __restrict__ dec,
                                   const uint32_t* __restrict__ nn_ptr, uint32_t* __restrict__ nn_idx,
                                   uint8_t* __restrict__ nn_ord, uint32_t nn_cap, const uint32_t* __restrict__ near_ptr,
-                                  uint32_t* __restrict__ near_idx, uint32_t near_cap, uint32_t* __restrict__ ovf)
+                                  uint32_t* __restrict__ near_idx, uint32_t near_cap, uint32_t* __restrict__ ovf,
+                                  const uint32_t* __restrict__ act, const uint32_t* __restrict__ act_pos)
 {
     const uint32_t np = 1u << (2 * (l - 1));
     const uint32_t li = level_index(l);
     const int64_t nl = (int64_t)1 << (2 * l);
-    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < nl; a += (int64_t)gridDim.x * blockDim.x) {
-        if (count[li + a] == 0) continue;
+    const int64_t k1 = act_pos[li + nl];
+    for (int64_t k = act_pos[li] + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < k1;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t a = (int64_t)act[k] - li;
         const uint32_t p = (uint32_t)(a >> 2);
         const uint32_t pe0 = pnear_ptr[p];
         const uint32_t pe1 = pnear_ptr[p + 1] < pcap ? pnear_ptr[p + 1] : pcap;
@@ -399,13 +409,13 @@ int build_lists(Handle& h)
                 k_lists_ctrl_count<<<grid_for(nl, 32 * ctrl::kWarps, kSMs * 16), 32 * ctrl::kWarps, 0, s>>>(
                     l, (float)hl, (float)(h.ctrl_c / (hl * hl)), P<uint32_t>(h.count), P<float>(h.comrel),
                     P<float4>(h.nfeat), pnp, pni, pcap, nnc, nrc, P<uint8_t>(h.dec), P<float>(h.ctrl_w),
-                    h.ctrl_log_tau);
+                    h.ctrl_log_tau, act, act_pos);
             } else {
                 // nni points into the index pool; the order of entry i sits at byte i of the order pool
                 uint8_t* ordp = P<uint8_t>(h.ord_pool) + (nni - P<uint32_t>(h.idx_pool));
                 k_lists_ctrl_fill<<<grid_for(nl, 128), 128, 0, s>>>(l, P<uint32_t>(h.count), pnp, pni, pcap,
                                                                     P<uint8_t>(h.dec), nnp, nni, ordp, nncap, nrp,
-                                                                    nri, nrcap, ovf_flag);
+                                                                    nri, nrcap, ovf_flag, act, act_pos);
             }
         } else if (h.cfg.precision == TC_PREC_FP64)
             k_lists<double><<<grid_for(nl, 128), 128, 0, s>>>(l, inv_theta, h.cfg.theta, h.variant, hl,
@@ -422,6 +432,10 @@ int build_lists(Handle& h)
         return 0;
     };
     if (h.ctrl_on) {
+        if (!act) {
+            tc_set_error("controller: needs the order-p FP32 tree");
+            return TC_ERR_STATE;
+        }
         if (h.mu_stride < 45) {  // the features read multipoles up to order 8
             tc_set_error("controller: the handle's multipoles are below order 8");
             return TC_ERR_STATE;
@@ -429,7 +443,7 @@ int build_lists(Handle& h)
         if ((rc = ensure(h.nfeat, (size_t)h.nnodes * 32))) return rc;
         k_node_feat<<<grid_for(h.nnodes, 256), 256, 0, s>>>(depth, h.L, P<uint32_t>(h.count), P<float>(h.comrel),
                                                              P<float>(h.mu), h.mu_stride, P<float4>(h.nfeat),
-                                                             h.nnodes);
+                                                             h.nnodes, act, act_pos);
         h.launches++;
     }
     uint32_t* ovf = P<uint32_t>(h.err) + 1;

@@ -107,6 +107,10 @@ int solve_fmm(Handle& h, double* d_grad, double* d_total, int accumulate, int sc
 // fmm_p.cu (tc_config.order != 0)
 int solve_fmm_order(Handle& h, double* d_grad, double* d_total, int accumulate, int scatter);
 int build_multipoles(Handle& h);
+// order-p FP32 tree (tree_p.cu): Morton codes, and the node records after the
+// gather of the sorted particles
+int morton_p(Handle& h, const double* d_pos, int64_t n, double maxx, double maxy);
+int build_records_p(Handle& h, double hleaf);
 int prepare_nosync(Handle& h);
 
 }  // namespace tc

@@ -6,9 +6,8 @@
 //   bottomUpNodeConstruction (:381-470) -> k_bottom_up, one launch per level
 // Leaf moments are summed sequentially in sorted order by one thread per
 // leaf and internal nodes combine children in the reference's j = 3..0 order,
-// so COM, M0 and M2 come out bit-identical to the reference's FP64 values
-// (the order-p path sums large leaves by warp reductions instead: same
-// topology and codes, moments equal to rounding).
+// so COM, M0 and M2 come out bit-identical to the reference's FP64 values.
+// The order-p path (FP32 only) builds its records in tree_p.cu instead.
 // Alongside the FP64 node record the kernels write the compute copies in
 // cell-relative coordinates (COM minus the ideal cell centre), which keep
 // FP32 differences accurate to a fraction of the cell size.
@@ -137,124 +136,6 @@ __global__ void k_leaf_moments(const double2* __restrict__ pos64, int depth, dou
         bbc[node] = make_double2(minx + h * (double)ix + 0.5 * h, miny + h * (double)iy + 0.5 * h);
         bblen[node] = h;
         write_compute<real>(node, sx, sy, M0, a, b, d, cx, cy, comrel, m0r, m2t);
-    }
-}
-
-// The same leaf records for the order-p (physics) path, where the FP64
-// moments need not round like the reference's sequential loop: leaves of up
-// to kLeafSmall particles keep one thread each; larger leaves (k_leaf_big)
-// take one warp each with shuffle reductions, instead of one thread walking
-// hundreds of particles through dependent FP64 additions.
-
-// big: [0] the number of large leaves, then their indices (any order; each
-// leaf's record depends on its own particles only)
-template <typename real>
-__global__ void k_leaf_small(const double2* __restrict__ pos64, int depth, double minx, double miny, double h,
-                             uint32_t* __restrict__ count, const uint32_t* __restrict__ first,
-                             double2* __restrict__ com64, double* __restrict__ m0, double* __restrict__ m2,
-                             double2* __restrict__ bbc, double* __restrict__ bblen, real* __restrict__ comrel,
-                             real* __restrict__ m0r, real* __restrict__ m2t, uint32_t* __restrict__ big)
-{
-    const uint32_t li = level_index(depth);
-    const int64_t nl = (int64_t)1 << (2 * depth);
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t node = li + i;
-        const uint32_t f = first[node];
-        const uint32_t c = count[node] - f;  // count holds the end index here
-        count[node] = c;
-        if (c > kLeafSmall) {
-            big[1 + atomicAdd(big, 1u)] = (uint32_t)i;
-            continue;
-        }
-        const uint32_t ix = compact16((uint32_t)i), iy = compact16((uint32_t)i >> 1);
-        const double cx = minx + ((double)ix + 0.5) * h;
-        const double cy = miny + ((double)iy + 0.5) * h;
-        if (c == 0) {
-            com64[node] = make_double2(0.0, 0.0);
-            m0[node] = 0.0;
-            m2[3 * node] = m2[3 * node + 1] = m2[3 * node + 2] = 0.0;
-            bbc[node] = make_double2(0.0, 0.0);
-            bblen[node] = 0.0;
-            write_compute<real>(node, cx, cy, 0.0, 0.0, 0.0, 0.0, cx, cy, comrel, m0r, m2t);
-            continue;
-        }
-        double sx = 0.0, sy = 0.0;
-        for (uint32_t p = f; p < f + c; p++) {
-            const double2 q = pos64[p];
-            sx += q.x;
-            sy += q.y;
-        }
-        const double M0 = (double)c;
-        sx /= M0;
-        sy /= M0;
-        double a = 0.0, b = 0.0, d = 0.0;
-        for (uint32_t p = f; p < f + c; p++) {
-            const double2 q = pos64[p];
-            const double rx = q.x - sx, ry = q.y - sy;
-            a += rx * rx;
-            b += rx * ry;
-            d += ry * ry;
-        }
-        com64[node] = make_double2(sx, sy);
-        m0[node] = M0;
-        m2[3 * node] = a;
-        m2[3 * node + 1] = b;
-        m2[3 * node + 2] = d;
-        bbc[node] = make_double2(minx + h * (double)ix + 0.5 * h, miny + h * (double)iy + 0.5 * h);
-        bblen[node] = h;
-        write_compute<real>(node, sx, sy, M0, a, b, d, cx, cy, comrel, m0r, m2t);
-    }
-}
-
-template <typename real>
-__global__ void k_leaf_big(const double2* __restrict__ pos64, int depth, double minx, double miny, double h,
-                           const uint32_t* __restrict__ count, const uint32_t* __restrict__ first,
-                           double2* __restrict__ com64, double* __restrict__ m0, double* __restrict__ m2,
-                           double2* __restrict__ bbc, double* __restrict__ bblen, real* __restrict__ comrel,
-                           real* __restrict__ m0r, real* __restrict__ m2t, const uint32_t* __restrict__ big)
-{
-    const int lane = threadIdx.x & 31;
-    const uint32_t li = level_index(depth);
-    const int64_t nbig = big[0];
-    const int64_t wstride = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t w = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); w < nbig; w += wstride) {
-        const int64_t i = big[1 + w];
-        const int64_t node = li + i;
-        const uint32_t c = count[node];
-        const uint32_t f = first[node];
-        double sx = 0.0, sy = 0.0;
-        for (uint32_t p = f + lane; p < f + c; p += 32) {
-            const double2 q = pos64[p];
-            sx += q.x;
-            sy += q.y;
-        }
-        const double M0 = (double)c;
-        sx = warp_sum(sx) / M0;
-        sy = warp_sum(sy) / M0;
-        double a = 0.0, b = 0.0, d = 0.0;
-        for (uint32_t p = f + lane; p < f + c; p += 32) {
-            const double2 q = pos64[p];
-            const double rx = q.x - sx, ry = q.y - sy;
-            a += rx * rx;
-            b += rx * ry;
-            d += ry * ry;
-        }
-        a = warp_sum(a);
-        b = warp_sum(b);
-        d = warp_sum(d);
-        if (lane == 0) {
-            const uint32_t ix = compact16((uint32_t)i), iy = compact16((uint32_t)i >> 1);
-            const double cx = minx + ((double)ix + 0.5) * h;
-            const double cy = miny + ((double)iy + 0.5) * h;
-            com64[node] = make_double2(sx, sy);
-            m0[node] = M0;
-            m2[3 * node] = a;
-            m2[3 * node + 1] = b;
-            m2[3 * node + 2] = d;
-            bbc[node] = make_double2(minx + h * (double)ix + 0.5 * h, miny + h * (double)iy + 0.5 * h);
-            bblen[node] = h;
-            write_compute<real>(node, sx, sy, M0, a, b, d, cx, cy, comrel, m0r, m2t);
-        }
     }
 }
 
@@ -413,9 +294,15 @@ int build_tree(Handle& h, const double* d_pos, int64_t n, double minx, double mi
 
     if ((rc = record(h, 0))) return rc;
     TC_CUDA_TRY(cudaMemsetAsync(h.err.p, 0, sizeof(uint32_t), s));
-    k_morton<<<grid_for(n, 256), 256, 0, s>>>((const double2*)d_pos, n, minx, miny, maxx, maxy, L,
-                                               P<uint32_t>(h.codes), P<uint32_t>(h.err));
-    h.launches++;
+    // order p in FP32: the physics-mode records of tree_p.cu (no FP64-exact codes or moments)
+    const bool physics = h.cfg.order && !f64;
+    if (physics) {
+        if ((rc = morton_p(h, d_pos, n, maxx, maxy))) return rc;
+    } else {
+        k_morton<<<grid_for(n, 256), 256, 0, s>>>((const double2*)d_pos, n, minx, miny, maxx, maxy, L,
+                                                   P<uint32_t>(h.codes), P<uint32_t>(h.err));
+        h.launches++;
+    }
     TC_CUDA_TRY(cudaGetLastError());
     rc = radix_sort_u32(P<uint32_t>(h.codes), P<uint32_t>(h.perm), P<uint32_t>(h.alt_keys), P<uint32_t>(h.alt_vals), n,
                         P<uint32_t>(h.tmp), s, &h.launches);
@@ -439,19 +326,8 @@ int build_tree(Handle& h, const double* d_pos, int64_t n, double minx, double mi
                                                                 (const double2*)d_pos, n, depth, minx, miny, hleaf,
                                                                 P<double2>(h.pos64), P<float>(h.prel),
                                                                 P<uint32_t>(h.first), P<uint32_t>(h.count));
-        if (h.cfg.order) {
-            const int64_t maxbig = n / (kLeafSmall + 1) + 1;
-            if ((rc = ensure(h.bigleaf, (maxbig + 1) * 4))) return rc;
-            TC_CUDA_TRY(cudaMemsetAsync(h.bigleaf.p, 0, 4, s));
-            k_leaf_small<float><<<grid_for(nleaf, 128), 128, 0, s>>>(
-                P<double2>(h.pos64), depth, minx, miny, hleaf, P<uint32_t>(h.count), P<uint32_t>(h.first),
-                P<double2>(h.com64), P<double>(h.m0), P<double>(h.m2), P<double2>(h.bbc), P<double>(h.bblen),
-                P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t), P<uint32_t>(h.bigleaf));
-            k_leaf_big<float><<<grid_for(maxbig * 32, 128), 128, 0, s>>>(
-                P<double2>(h.pos64), depth, minx, miny, hleaf, P<uint32_t>(h.count), P<uint32_t>(h.first),
-                P<double2>(h.com64), P<double>(h.m0), P<double>(h.m2), P<double2>(h.bbc), P<double>(h.bblen),
-                P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t), P<uint32_t>(h.bigleaf));
-            h.launches++;
+        if (physics) {
+            if ((rc = build_records_p(h, hleaf))) return rc;
         } else {
             k_leaf_moments<float><<<grid_for(nleaf, 128), 128, 0, s>>>(
                 P<double2>(h.pos64), depth, minx, miny, hleaf, P<uint32_t>(h.count), P<uint32_t>(h.first),
@@ -459,8 +335,8 @@ int build_tree(Handle& h, const double* d_pos, int64_t n, double minx, double mi
                 P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t));
         }
     }
-    h.launches += 2;
-    for (int l = depth - 1; l >= 0; l--) {
+    h.launches += physics ? 1 : 2;
+    for (int l = depth - 1; l >= 0 && !physics; l--) {
         const double hl = L / (double)(1u << l);
         const int64_t nl = (int64_t)1 << (2 * l);
         if (f64)

@@ -1,0 +1,257 @@
+// Tree records for the order-p path ("physics mode"): the same level-dense
+// quadtree as NBodySolverFMM_SYM_MORTON::updateTree
+// (src/nbodysolvers/cpu/nBodySolverFMM_SYM_MORTON.h:79-95, 328-470), built
+// without the FP64 arithmetic the reference-order path needs for bit parity.
+// FP64 runs at 1/64 of the FP32 rate on GB300, and the order-p solve reads
+// only cell-relative FP32 data, so here:
+// * Morton codes quantise (p - min) * (65536 / L) in FP32 after one FP64
+//   subtraction (a point within ~1e-7 L of a cell edge may land in the
+//   neighbouring cell; its cell-relative coordinates stay exact);
+// * leaf centres of mass and second moments are FP32 sums of the particles'
+//   cell-relative coordinates (written by the gather in FP64 arithmetic);
+// * internal nodes combine their children's relative centres of mass shifted
+//   by the exact child-centre offsets (+-h/4), mass-weighted (the physical
+//   parallel-axis second moment, not the reference's quirk).
+// The FP64 records (com64 = cell centre + relative COM, m0, m2, bbc, bblen)
+// are written for non-empty nodes only; readers test count first.
+#include "state.cuh"
+
+namespace tc {
+namespace {
+
+// (p - min) >= 0 and <= ext, tested on the bit patterns of the non-negative
+// difference (NaN fails both)
+__device__ inline bool in_range(double a, double ext)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(a);
+    const unsigned long long e = (unsigned long long)__double_as_longlong(ext);
+    return (b >> 63) == 0 && b <= e;
+}
+
+__device__ inline uint32_t quantise(double a, float s)
+{
+    const float v = (float)a * s;
+    const uint32_t q = v > 0.f ? (uint32_t)v : 0u;
+    return q < 65535u ? q : 65535u;
+}
+
+__global__ void k_morton_p(const double2* __restrict__ pos, int64_t n, double minx, double miny, double extx,
+                           double exty, float s65536, uint32_t* __restrict__ codes, uint32_t* __restrict__ err)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double2 p = pos[i];
+        const double ax = p.x - minx, ay = p.y - miny;
+        if (!(in_range(ax, extx) && in_range(ay, exty))) atomicOr(err, 1u);
+        codes[i] = (spread16(quantise(ay, s65536)) << 1) | spread16(quantise(ax, s65536));
+    }
+}
+
+__device__ inline double2 cell_centre(int64_t i, double minx, double miny, double h)
+{
+    const uint32_t ix = compact16((uint32_t)i), iy = compact16((uint32_t)i >> 1);
+    return make_double2(minx + ((double)ix + 0.5) * h, miny + ((double)iy + 0.5) * h);
+}
+
+// the node record from its relative COM and second moment (about the COM)
+__device__ inline void write_node(int64_t node, double2 centre, double h, uint32_t c, float rx, float ry, float a,
+                                  float b, float d, double2* com64, double* m0, double* m2, double2* bbc,
+                                  double* bblen, float* comrel, float* m0r, float* m2t)
+{
+    const float ic = 1.0f / (float)c;
+    com64[node] = make_double2(centre.x + (double)rx, centre.y + (double)ry);
+    m0[node] = (double)c;
+    m2[3 * node] = (double)a;
+    m2[3 * node + 1] = (double)b;
+    m2[3 * node + 2] = (double)d;
+    bbc[node] = centre;
+    bblen[node] = h;
+    comrel[2 * node] = rx;
+    comrel[2 * node + 1] = ry;
+    m0r[node] = (float)c;
+    m2t[3 * node] = a * ic;
+    m2t[3 * node + 1] = b * ic;
+    m2t[3 * node + 2] = d * ic;
+}
+
+// leaves of up to kLeafSmall particles, one thread each; larger leaves are
+// listed for k_leaf_big_p.  count holds the end index on entry.
+__global__ void k_leaf_small_p(int depth, double minx, double miny, double h, uint32_t* __restrict__ count,
+                               const uint32_t* __restrict__ first, const float2* __restrict__ prel,
+                               double2* __restrict__ com64, double* __restrict__ m0, double* __restrict__ m2,
+                               double2* __restrict__ bbc, double* __restrict__ bblen, float* __restrict__ comrel,
+                               float* __restrict__ m0r, float* __restrict__ m2t, uint32_t* __restrict__ big)
+{
+    const uint32_t li = level_index(depth);
+    const int64_t nl = (int64_t)1 << (2 * depth);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t node = li + i;
+        const uint32_t e = count[node];
+        if (e == 0) continue;  // empty (first and count were zeroed)
+        const uint32_t f = first[node];
+        const uint32_t c = e - f;
+        count[node] = c;
+        if (c > kLeafSmall) {
+            big[1 + atomicAdd(big, 1u)] = (uint32_t)i;
+            continue;
+        }
+        float sx = 0.f, sy = 0.f;
+        for (uint32_t p = f; p < e; p++) {
+            const float2 q = prel[p];
+            sx += q.x;
+            sy += q.y;
+        }
+        const float ic = 1.0f / (float)c;
+        sx *= ic;
+        sy *= ic;
+        float a = 0.f, b = 0.f, d = 0.f;
+        for (uint32_t p = f; p < e; p++) {
+            const float2 q = prel[p];
+            const float rx = q.x - sx, ry = q.y - sy;
+            a = fmaf(rx, rx, a);
+            b = fmaf(rx, ry, b);
+            d = fmaf(ry, ry, d);
+        }
+        write_node(node, cell_centre(i, minx, miny, h), h, c, sx, sy, a, b, d, com64, m0, m2, bbc, bblen, comrel,
+                   m0r, m2t);
+    }
+}
+
+__global__ void k_leaf_big_p(int depth, double minx, double miny, double h, const uint32_t* __restrict__ count,
+                             const uint32_t* __restrict__ first, const float2* __restrict__ prel,
+                             double2* __restrict__ com64, double* __restrict__ m0, double* __restrict__ m2,
+                             double2* __restrict__ bbc, double* __restrict__ bblen, float* __restrict__ comrel,
+                             float* __restrict__ m0r, float* __restrict__ m2t, const uint32_t* __restrict__ big)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t li = level_index(depth);
+    const int64_t nbig = big[0];
+    const int64_t wstride = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t w = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); w < nbig; w += wstride) {
+        const int64_t i = big[1 + w];
+        const int64_t node = li + i;
+        const uint32_t c = count[node], f = first[node];
+        float sx = 0.f, sy = 0.f;
+        for (uint32_t p = f + lane; p < f + c; p += 32) {
+            const float2 q = prel[p];
+            sx += q.x;
+            sy += q.y;
+        }
+        const float ic = 1.0f / (float)c;
+        sx = warp_sum(sx) * ic;
+        sy = warp_sum(sy) * ic;
+        float a = 0.f, b = 0.f, d = 0.f;
+        for (uint32_t p = f + lane; p < f + c; p += 32) {
+            const float2 q = prel[p];
+            const float rx = q.x - sx, ry = q.y - sy;
+            a = fmaf(rx, rx, a);
+            b = fmaf(rx, ry, b);
+            d = fmaf(ry, ry, d);
+        }
+        a = warp_sum(a);
+        b = warp_sum(b);
+        d = warp_sum(d);
+        if (lane == 0)
+            write_node(node, cell_centre(i, minx, miny, h), h, c, sx, sy, a, b, d, com64, m0, m2, bbc, bblen, comrel,
+                       m0r, m2t);
+    }
+}
+
+// level l from level l + 1: counts, first particle (lowest non-empty child),
+// mass-weighted COM and second moment in the node's cell-relative frame
+// (child centre = node centre + (+-h/4, +-h/4), bit 0 of the child slot is x)
+__global__ void k_bottom_up_p(int l, double minx, double miny, double hl, uint32_t* __restrict__ count,
+                              uint32_t* __restrict__ first, double2* __restrict__ com64, double* __restrict__ m0,
+                              double* __restrict__ m2, double2* __restrict__ bbc, double* __restrict__ bblen,
+                              float* __restrict__ comrel, float* __restrict__ m0r, float* __restrict__ m2t)
+{
+    const uint32_t li = level_index(l), lc = level_index(l + 1);
+    const int64_t nl = (int64_t)1 << (2 * l);
+    const float q = (float)(0.25 * hl);
+    const float2* cr2 = reinterpret_cast<const float2*>(comrel);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t node = li + i;
+        const int64_t fc = lc + 4 * i;
+        const uint32_t c4[4] = {count[fc], count[fc + 1], count[fc + 2], count[fc + 3]};
+        const uint32_t cnt = c4[0] + c4[1] + c4[2] + c4[3];
+        if (cnt == 0) {
+            count[node] = 0;
+            first[node] = 0;
+            continue;
+        }
+        uint32_t fp = 0;
+        float sx = 0.f, sy = 0.f;
+        float2 g[4];
+#pragma unroll
+        for (int j = 3; j >= 0; j--) {
+            g[j] = make_float2(0.f, 0.f);
+            if (c4[j] == 0) continue;
+            fp = first[fc + j];
+            const float2 r = cr2[fc + j];
+            g[j] = make_float2(r.x + ((j & 1) ? q : -q), r.y + ((j & 2) ? q : -q));
+            sx = fmaf((float)c4[j], g[j].x, sx);
+            sy = fmaf((float)c4[j], g[j].y, sy);
+        }
+        const float ic = 1.0f / (float)cnt;
+        sx *= ic;
+        sy *= ic;
+        float a = 0.f, b = 0.f, d = 0.f;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if (c4[j] == 0) continue;
+            const float w = (float)c4[j];
+            const float rx = g[j].x - sx, ry = g[j].y - sy;
+            a += w * (m2t[3 * (fc + j)] + rx * rx);
+            b += w * (m2t[3 * (fc + j) + 1] + rx * ry);
+            d += w * (m2t[3 * (fc + j) + 2] + ry * ry);
+        }
+        count[node] = cnt;
+        first[node] = fp;
+        write_node(node, cell_centre(i, minx, miny, hl), hl, cnt, sx, sy, a, b, d, com64, m0, m2, bbc, bblen, comrel,
+                   m0r, m2t);
+    }
+}
+
+}  // namespace
+
+int build_records_p(Handle& h, double hleaf)
+{
+    cudaStream_t s = h.stream;
+    const int depth = h.depth;
+    const int64_t nleaf = (int64_t)1 << (2 * depth);
+    const int64_t maxbig = h.n / (kLeafSmall + 1) + 1;
+    int rc;
+    if ((rc = ensure(h.bigleaf, (maxbig + 1) * 4))) return rc;
+    TC_CUDA_TRY(cudaMemsetAsync(h.bigleaf.p, 0, 4, s));
+    k_leaf_small_p<<<grid_for(nleaf, 128), 128, 0, s>>>(
+        depth, h.minx, h.miny, hleaf, P<uint32_t>(h.count), P<uint32_t>(h.first), P<float2>(h.prel),
+        P<double2>(h.com64), P<double>(h.m0), P<double>(h.m2), P<double2>(h.bbc), P<double>(h.bblen),
+        P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t), P<uint32_t>(h.bigleaf));
+    k_leaf_big_p<<<grid_for(maxbig * 32, 128), 128, 0, s>>>(
+        depth, h.minx, h.miny, hleaf, P<uint32_t>(h.count), P<uint32_t>(h.first), P<float2>(h.prel),
+        P<double2>(h.com64), P<double>(h.m0), P<double>(h.m2), P<double2>(h.bbc), P<double>(h.bblen),
+        P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t), P<uint32_t>(h.bigleaf));
+    h.launches += 2;
+    for (int l = depth - 1; l >= 0; l--) {
+        const double hl = h.L / (double)(1u << l);
+        const int64_t nl = (int64_t)1 << (2 * l);
+        k_bottom_up_p<<<grid_for(nl, 128), 128, 0, s>>>(l, h.minx, h.miny, hl, P<uint32_t>(h.count),
+                                                        P<uint32_t>(h.first), P<double2>(h.com64), P<double>(h.m0),
+                                                        P<double>(h.m2), P<double2>(h.bbc), P<double>(h.bblen),
+                                                        P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t));
+        h.launches++;
+    }
+    TC_CUDA_TRY(cudaGetLastError());
+    return TC_OK;
+}
+
+int morton_p(Handle& h, const double* d_pos, int64_t n, double maxx, double maxy)
+{
+    k_morton_p<<<grid_for(n, 256), 256, 0, h.stream>>>((const double2*)d_pos, n, h.minx, h.miny, maxx - h.minx,
+                                                      maxy - h.miny, (float)(65536.0 / h.L), P<uint32_t>(h.codes),
+                                                      P<uint32_t>(h.err));
+    h.launches++;
+    TC_CUDA_TRY(cudaGetLastError());
+    return TC_OK;
+}
+
+}  // namespace tc
