@@ -187,10 +187,10 @@ def run_ours(args, w, rank, world):
     torch.cuda.synchronize()
     ref = ref_d.cpu().numpy()
 
-    def make(theta, order=0, depth=None, controller=None, tau=None):
+    def make(theta, order=0, depth=None, controller=None, tau=None, mac="cell"):
         s = NBodySolverFMM_SYM_MORTON(w["kernel"], max_children=w["max_children"], tree_depth=depth, theta=theta,
                                       softening=w["softening"], precision="fp32", order=order,
-                                      device=dev.index, stream=stream.cuda_stream)
+                                      device=dev.index, stream=stream.cuda_stream, mac=mac)
         if controller is not None:
             s.set_controller(controller, tau)
         return s
@@ -225,11 +225,13 @@ def run_ours(args, w, rank, world):
     # plain order-p FMM, autotuned over (depth, theta, order); its order-12 line is the fixed-p=12 baseline
     target = TARGET_ERR * 0.9
     if args.order:
-        plain = {"depth": args.depth or None, "theta": args.theta or 0.5, "order": args.order}
+        plain = {"depth": args.depth or None, "theta": args.theta or 0.5, "order": args.order,
+                 "mac": "bmax" if args.mac == "bmax" else "cell"}
         trials = []
     else:
+        macs = ("cell", "bmax") if args.mac == "both" else (args.mac,)
         plain, trials = tune(pos_d, ref, rows_d, kernel=w["kernel"], softening=w["softening"],
-                             leaf=w["max_children"], target=target, stream=stream, device=dev.index)
+                             leaf=w["max_children"], target=target, stream=stream, device=dev.index, macs=macs)
         if plain is None:
             raise SystemExit("autotuner found no configuration meeting the error target")
     p12 = min((t for t in trials if t["order"] == 12 and t["err"] <= target), key=lambda t: t["ms"], default=None)
@@ -300,16 +302,17 @@ def run_ours(args, w, rank, world):
 
     # the arms: the learned-order method (headline, when it meets the target) and the plain ones beside it
     arms = {}
-    s_plain = make(plain["theta"], order=plain["order"], depth=plain["depth"])
+    s_plain = make(plain["theta"], order=plain["order"], depth=plain["depth"], mac=plain["mac"])
     arms["plain_best"] = timed(s_plain, args.steps, sample_clocks=True)
-    arms["plain_best"].update(theta=plain["theta"], order=plain["order"])
+    arms["plain_best"].update(theta=plain["theta"], order=plain["order"], mac=plain["mac"])
     if p12 is not None:
-        if plain["order"] == 12 and (p12["depth"], p12["theta"]) == (plain["depth"], plain["theta"]):
+        if plain["order"] == 12 and (p12["depth"], p12["theta"], p12["mac"]) == (plain["depth"], plain["theta"],
+                                                                                 plain["mac"]):
             arms["plain_p12"] = arms["plain_best"]
         else:
-            s12 = make(p12["theta"], order=12, depth=p12["depth"])
+            s12 = make(p12["theta"], order=12, depth=p12["depth"], mac=p12["mac"])
             arms["plain_p12"] = timed(s12, args.steps, sample_clocks=False)
-            arms["plain_p12"].update(theta=p12["theta"], order=12)
+            arms["plain_p12"].update(theta=p12["theta"], order=12, mac=p12["mac"])
             s12.close()
     s_head, head, s_l = s_plain, "plain_best", None
     if learned_cfg is not None:
@@ -733,6 +736,8 @@ def main():
     ap.add_argument("--workload", default="nbody_two_disks_4m", choices=sorted(WORKLOADS))
     ap.add_argument("--theta", type=float, default=None)
     ap.add_argument("--order", type=int, default=0, help="fix the expansion order instead of autotuning")
+    ap.add_argument("--mac", default="both", choices=["cell", "bmax", "both"],
+                    help="opening criterion of the plain arms (both: autotuned)")
     ap.add_argument("--depth", type=int, default=0)
     ap.add_argument("--skip-reference-order", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=262144)
@@ -812,6 +817,7 @@ def main():
     def arm_summary(a):
         return {"particles_per_s": n * args.steps / a["t_total"], "ms_per_step": 1e3 * a["t_total"] / args.steps,
                 "depth": a["depth"], "order": a.get("order"), "theta": a.get("theta"), "tau": a.get("tau"),
+                "mac": a.get("mac"),
                 "median_err": a["err"][0], "stages_ms": a["stages"], "counters": a["counters"]}
 
     comparison = {k: arm_summary(a) for k, a in r["arms"].items()}
@@ -822,8 +828,8 @@ def main():
                 comparison[f"learned_speedup_vs_{k}"] = lv / comparison[k]["particles_per_s"]
     method = {"learned": "learned-order symmetric Morton FMM: MLP controller (16-64-64-5, BF16 tensor-core "
                          "inference in the list build) picks accept/open and the order in {4,6,8,10,12} per pair",
-              "plain_best": "plain fixed-order symmetric Morton FMM (autotuned depth/theta/order)"}[r["head"]]
-    config.update({"theta": head.get("theta"), "tau": head.get("tau"), "depth": head["depth"],
+              "plain_best": "plain fixed-order symmetric Morton FMM (autotuned opening criterion/depth/theta/order)"}[r["head"]]
+    config.update({"theta": head.get("theta"), "tau": head.get("tau"), "depth": head["depth"], "mac": head.get("mac"),
                    "order": head.get("order"), "method": r["head"],
                    "expansion": "total-order Cartesian Taylor about the COM",
                    "autotune": r["calib"],

@@ -85,6 +85,18 @@ int tc_set_theta(tc_handle* h, double theta);
 #define TC_VARIANT_MORTON 1
 int tc_set_variant(tc_handle* h, int variant);
 
+/* Opening criterion of an order-p handle (no counterpart in the reference):
+ * TC_MAC_CELL  the reference's (L_A + L_B)/theta < |com_A - com_B| with L the
+ *              cell sizes (the default);
+ * TC_MAC_BMAX  (b_A + b_B)/theta < |com_A - com_B| with b the largest
+ *              distance of a node's particles from its centre of mass (the
+ *              radius the Taylor expansions about the COM converge in), so
+ *              nodes whose particles sit near their COM are accepted sooner.
+ * Takes effect at the next tc_update_tree.                                 */
+#define TC_MAC_CELL 0
+#define TC_MAC_BMAX 1
+int tc_set_mac(tc_handle* h, int mac);
+
 /* getDepth (nBodySolverFMM_SYM_MORTON.h:106-115), clamped at 0 for n < leaf. */
 int tc_get_depth(int max_children, int64_t n, uint32_t* depth);
 /* node count of the level-dense tree, initNodesSize (:117-151).             */

@@ -25,6 +25,8 @@ TC_PREC_FP32 = 0
 TC_PREC_FP64 = 1
 TC_VARIANT_SYM = 0
 TC_VARIANT_MORTON = 1
+TC_MAC_CELL = 0
+TC_MAC_BMAX = 1
 
 
 class TcConfig(ctypes.Structure):
@@ -50,6 +52,7 @@ SIGNATURES = {
     "tc_destroy": (_I, [_P]),
     "tc_set_theta": (_I, [_P, _D]),
     "tc_set_variant": (_I, [_P, _I]),
+    "tc_set_mac": (_I, [_P, _I]),
     "tc_get_depth": (_I, [_I, _I64, _P]),
     "tc_node_count": (_I, [ctypes.c_uint32, _P]),
     "tc_update_tree": (_I, [_P, _P, _P, _I64, _P, _P]),

@@ -1,5 +1,6 @@
-"""Autotuner for the order-p FMM: tree depth, opening angle and expansion order
-(and, for the learned-order controller, tree depth and tolerance tau).
+"""Autotuner for the order-p FMM: opening criterion, tree depth, opening angle
+and expansion order (and, for the learned-order controller, tree depth and
+tolerance tau).
 
 For a given particle set (device-resident) it measures, for each candidate
 (depth, theta, order), the device time of one updateTree + solveNbody (CUDA
@@ -17,6 +18,9 @@ from .solver import NBodySolverFMM_SYM_MORTON, get_depth
 
 ORDERS = (4, 6, 8, 10, 12)
 THETAS = (1.6, 1.4, 1.3, 1.2, 1.1, 1.0, 0.9, 0.8, 0.7, 0.6, 0.5, 0.4)
+# the bounding-radius criterion compares radii, not cell sizes: the expansions
+# converge only below 1
+THETAS_BMAX = (0.95, 0.9, 0.85, 0.8, 0.75, 0.7, 0.65, 0.6, 0.55, 0.5, 0.45, 0.4, 0.35, 0.3)
 TAUS = (3e-3, 2e-3, 1e-3, 7e-4, 5e-4, 3e-4, 2e-4, 1e-4, 5e-5)
 
 
@@ -26,8 +30,8 @@ def median_error(grad_rows: np.ndarray, ref_rows: np.ndarray) -> float:
 
 
 def tune(pos_d, ref_rows, rows_d, *, kernel: str, softening: float, leaf: int, target: float,
-         stream=None, depths=None, thetas=THETAS, orders=ORDERS, device: int = 0, log=None):
-    """Returns (best, trials).  best = dict(depth, theta, order, ms, err) or None."""
+         stream=None, depths=None, thetas=None, orders=ORDERS, device: int = 0, log=None, macs=("cell",)):
+    """Returns (best, trials).  best = dict(mac, depth, theta, order, ms, err) or None."""
     import torch
 
     n = pos_d.shape[0]
@@ -38,36 +42,35 @@ def tune(pos_d, ref_rows, rows_d, *, kernel: str, softening: float, leaf: int, t
     s_torch = torch.cuda.Stream(device=pos_d.device) if stream is None else stream
     trials = []
     best = None
-    for depth in depths:
+    for mac, depth, order in [(m, d, o) for m in macs for d in depths for o in orders]:
         if depth > 15:
             continue
-        for order in orders:
-            for theta in thetas:
-                s = NBodySolverFMM_SYM_MORTON(kernel, max_children=leaf, tree_depth=depth, theta=theta,
-                                              softening=softening, precision="fp32", order=order,
-                                              device=device, stream=s_torch.cuda_stream)
-                try:
-                    s.update_tree_device(pos_d)
-                    s.solve_device(grad_d, tot_d)
-                    e0 = torch.cuda.Event(enable_timing=True)
-                    e1 = torch.cuda.Event(enable_timing=True)
-                    e0.record(s_torch)
-                    s.update_tree_device(pos_d)
-                    s.solve_device(grad_d, tot_d)
-                    e1.record(s_torch)
-                    torch.cuda.synchronize()
-                    ms = e0.elapsed_time(e1)
-                    err = median_error(grad_d[rows_d].cpu().numpy(), ref_rows)
-                finally:
-                    s.close()
-                t = dict(depth=depth, theta=theta, order=order, ms=ms, err=err)
-                trials.append(t)
-                if log:
-                    log(t)
-                if err <= target:
-                    if best is None or ms < best["ms"]:
-                        best = t
-                    break  # smaller theta at this order only costs more
+        for theta in thetas or (THETAS_BMAX if mac == "bmax" else THETAS):
+            s = NBodySolverFMM_SYM_MORTON(kernel, max_children=leaf, tree_depth=depth, theta=theta,
+                                          softening=softening, precision="fp32", order=order,
+                                          device=device, stream=s_torch.cuda_stream, mac=mac)
+            try:
+                s.update_tree_device(pos_d)
+                s.solve_device(grad_d, tot_d)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(s_torch)
+                s.update_tree_device(pos_d)
+                s.solve_device(grad_d, tot_d)
+                e1.record(s_torch)
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1)
+                err = median_error(grad_d[rows_d].cpu().numpy(), ref_rows)
+            finally:
+                s.close()
+            t = dict(mac=mac, depth=depth, theta=theta, order=order, ms=ms, err=err)
+            trials.append(t)
+            if log:
+                log(t)
+            if err <= target:
+                if best is None or ms < best["ms"]:
+                    best = t
+                break  # smaller theta at this order only costs more
     return best, trials
 
 

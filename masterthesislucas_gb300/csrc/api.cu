@@ -295,7 +295,7 @@ int tc_destroy(tc_handle* t)
     if (h.stream) cudaStreamSynchronize(h.stream);
     Buf* bufs[] = {&h.codes, &h.perm, &h.alt_keys, &h.alt_vals, &h.pos_in, &h.pos64, &h.prel, &h.grad_acc,
                    &h.count, &h.first, &h.com64, &h.m0, &h.m2, &h.bbc, &h.bblen, &h.comrel, &h.m0r, &h.m2t,
-                   &h.loc, &h.locfin, &h.mu, &h.chunk, &h.zwork, &h.zloc, &h.counters, &h.ptr_pool, &h.idx_pool, &h.cnt_tmp, &h.lstat, &h.ord_pool, &h.nfeat, &h.dec, &h.bigleaf, &h.chunk_leaf, &h.act, &h.act_pos, &h.diagpart, &h.ctrl_w, &h.tmp, &h.err, &h.zpart, &h.dtotal, &h.sumtmp,
+                   &h.loc, &h.locfin, &h.mu, &h.chunk, &h.zwork, &h.zloc, &h.counters, &h.ptr_pool, &h.idx_pool, &h.cnt_tmp, &h.lstat, &h.ord_pool, &h.nfeat, &h.dec, &h.bigleaf, &h.chunk_leaf, &h.act, &h.act_pos, &h.bmax, &h.diagpart, &h.ctrl_w, &h.tmp, &h.err, &h.zpart, &h.dtotal, &h.sumtmp,
                    &h.host_stage};
     for (Buf* b : bufs) release(*b);
     if (h.step_graph) cudaGraphExecDestroy(h.step_graph);
@@ -604,6 +604,21 @@ extern "C" int tc_set_variant(tc_handle* t, int variant)
         return TC_ERR_INVALID;
     }
     t->h.variant = variant;
+    t->h.tree_ready = false;  // the interaction lists depend on the MAC
+    return TC_OK;
+}
+
+extern "C" int tc_set_mac(tc_handle* t, int mac)
+{
+    if (!t || (mac != TC_MAC_CELL && mac != TC_MAC_BMAX)) {
+        tc_set_error("tc_set_mac: unknown criterion");
+        return TC_ERR_INVALID;
+    }
+    if (mac == TC_MAC_BMAX && t->h.cfg.order == 0) {
+        tc_set_error("tc_set_mac: the bounding-radius criterion needs an order-p handle");
+        return TC_ERR_INVALID;
+    }
+    t->h.mac = mac;
     t->h.tree_ready = false;  // the interaction lists depend on the MAC
     return TC_OK;
 }

@@ -69,7 +69,8 @@ __global__ void k_lists(int l, double inv_theta, double theta, int variant, real
                         uint32_t* __restrict__ near_cnt, const uint32_t* __restrict__ nn_ptr,
                         uint32_t* __restrict__ nn_idx, uint32_t nn_cap, const uint32_t* __restrict__ near_ptr,
                         uint32_t* __restrict__ near_idx, uint32_t near_cap, uint32_t* __restrict__ ovf, int fill,
-                        const uint32_t* __restrict__ act, const uint32_t* __restrict__ act_pos)
+                        const uint32_t* __restrict__ act, const uint32_t* __restrict__ act_pos,
+                        const float* __restrict__ bmax, float theta2)
 {
     const uint32_t np = l ? (1u << (2 * (l - 1))) : 0u;
     const uint32_t li = level_index(l);
@@ -94,6 +95,7 @@ __global__ void k_lists(int l, double inv_theta, double theta, int variant, real
                 const real thr2 = thr * thr;
                 const int iax = (int)compact16((uint32_t)a), iay = (int)compact16((uint32_t)a >> 1);
                 const real cra[2] = {comrel[2 * (li + a)], comrel[2 * (li + a) + 1]};
+                const float ba = bmax ? bmax[li + a] : 0.f;
                 const uint32_t p = (uint32_t)(a >> 2);
                 const uint32_t nb = fill ? nn_ptr[a] : 0, rb = fill ? near_ptr[a] : 0;
                 const uint32_t pe1 = pnear_ptr[p + 1] < pcap ? pnear_ptr[p + 1] : pcap;
@@ -103,9 +105,22 @@ __global__ void k_lists(int l, double inv_theta, double theta, int variant, real
                     for (uint32_t j = 0; j < 4; j++) {
                         const uint32_t b = 4 * bp + j;
                         if (count[li + b] == 0) continue;
-                        if (mac_accept_fast<real>(iax - (int)compact16(b), iay - (int)compact16(b >> 1), hl, thr2, cra,
-                                                  comrel + 2 * (li + b), ca, com64[li + b], len, inv_theta, theta,
-                                                  variant)) {
+                        bool acc;
+                        if (bmax) {
+                            // bounding-radius MAC in the cell-relative FP32 frame:
+                            // theta^2 |com_A - com_B|^2 > (b_A + b_B)^2
+                            const float dx = (float)(iax - (int)compact16(b)) * (float)hl +
+                                             ((float)cra[0] - (float)comrel[2 * (li + b)]);
+                            const float dy = (float)(iay - (int)compact16(b >> 1)) * (float)hl +
+                                             ((float)cra[1] - (float)comrel[2 * (li + b) + 1]);
+                            const float rb2 = ba + bmax[li + b];
+                            acc = theta2 * fmaf(dx, dx, dy * dy) > rb2 * rb2;
+                        } else {
+                            acc = mac_accept_fast<real>(iax - (int)compact16(b), iay - (int)compact16(b >> 1), hl,
+                                                        thr2, cra, comrel + 2 * (li + b), ca, com64[li + b], len,
+                                                        inv_theta, theta, variant);
+                        }
+                        if (acc) {
                             if (fill) {
                                 if (nb + nn < nn_cap) nn_idx[nb + nn] = b;
                                 else atomicOr(ovf, 1u);
@@ -395,6 +410,7 @@ int build_lists(Handle& h)
     // order p (FP32): the tree build listed the non-empty nodes
     const uint32_t* act = h.cfg.order && h.cfg.precision != TC_PREC_FP64 ? P<uint32_t>(h.act) : nullptr;
     const uint32_t* act_pos = act ? P<uint32_t>(h.act_pos) : nullptr;
+    const float* bmax = act && h.mac == TC_MAC_BMAX ? P<float>(h.bmax) : nullptr;
     const double inv_theta = 1.0 / h.cfg.theta;
     uint32_t* ovf_flag = P<uint32_t>(h.err) + 1;
     auto launch = [&](int l, const uint32_t* pnp, const uint32_t* pni, uint32_t pcap, uint32_t* nnc, uint32_t* nrc,
@@ -422,13 +438,15 @@ int build_lists(Handle& h)
                                                              P<uint32_t>(h.count),
                                                              P<double2>(h.com64), P<double>(h.comrel),
                                                              P<double>(h.bblen), pnp, pni, pcap, nnc, nrc, nnp, nni,
-                                                             nncap, nrp, nri, nrcap, ovf_flag, fill, nullptr, nullptr);
+                                                             nncap, nrp, nri, nrcap, ovf_flag, fill, nullptr, nullptr, nullptr,
+                                                             0.f);
         else
             k_lists<float><<<grid_for(nl, 128), 128, 0, s>>>(l, inv_theta, h.cfg.theta, h.variant, (float)hl,
                                                             P<uint32_t>(h.count),
                                                             P<double2>(h.com64), P<float>(h.comrel),
                                                             P<double>(h.bblen), pnp, pni, pcap, nnc, nrc, nnp, nni,
-                                                            nncap, nrp, nri, nrcap, ovf_flag, fill, act, act_pos);
+                                                            nncap, nrp, nri, nrcap, ovf_flag, fill, act, act_pos, bmax,
+                                                            (float)(h.cfg.theta * h.cfg.theta));
         return 0;
     };
     if (h.ctrl_on) {

@@ -61,12 +61,16 @@ struct Handle {
     // exclusive scan of non-emptiness over all nodes (act_pos); level l owns
     // act[act_pos[li] .. act_pos[li + 4^l])
     Buf act, act_pos;
+    // order p: per node, the largest distance of its particles from its COM
+    // (an upper bound for internal nodes), FP32
+    Buf bmax;
     Buf diagpart;  // leapfrog diagnostics: per-block partial sums
     // learned order controller (order-p mode): weights + normalisation copy
     // no-sync mode (stream capture): no host round trips or stage events; the
     // outside-box and list-overflow flags are copied to pinned h_words[8], [40]
     // reference-order solver: 0 the symmetric FMM_SYM_MORTON, 1 the non-symmetric FMM_MORTON
     int variant = 0;
+    int mac = 0;  // TC_MAC_CELL or TC_MAC_BMAX (order p)
     bool nosync = false;
     double cap_slack = 0.25;  // fast-mode list capacity: exact total * (1 + slack) + 256
     bool ctrl_on = false;

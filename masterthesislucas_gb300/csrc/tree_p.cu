@@ -54,9 +54,10 @@ __device__ inline double2 cell_centre(int64_t i, double minx, double miny, doubl
 
 // the node record from its relative COM and second moment (about the COM)
 __device__ inline void write_node(int64_t node, double2 centre, double h, uint32_t c, float rx, float ry, float a,
-                                  float b, float d, double2* com64, double* m0, double* m2, double2* bbc,
-                                  double* bblen, float* comrel, float* m0r, float* m2t)
+                                  float b, float d, float br, double2* com64, double* m0, double* m2, double2* bbc,
+                                  double* bblen, float* comrel, float* m0r, float* m2t, float* bmax)
 {
+    bmax[node] = br;
     const float ic = 1.0f / (float)c;
     com64[node] = make_double2(centre.x + (double)rx, centre.y + (double)ry);
     m0[node] = (double)c;
@@ -79,7 +80,8 @@ __global__ void k_leaf_small_p(int depth, double minx, double miny, double h, ui
                                const uint32_t* __restrict__ first, const float2* __restrict__ prel,
                                double2* __restrict__ com64, double* __restrict__ m0, double* __restrict__ m2,
                                double2* __restrict__ bbc, double* __restrict__ bblen, float* __restrict__ comrel,
-                               float* __restrict__ m0r, float* __restrict__ m2t, uint32_t* __restrict__ big)
+                               float* __restrict__ m0r, float* __restrict__ m2t, uint32_t* __restrict__ big,
+                               float* __restrict__ bmax)
 {
     const uint32_t li = level_index(depth);
     const int64_t nl = (int64_t)1 << (2 * depth);
@@ -103,16 +105,17 @@ __global__ void k_leaf_small_p(int depth, double minx, double miny, double h, ui
         const float ic = 1.0f / (float)c;
         sx *= ic;
         sy *= ic;
-        float a = 0.f, b = 0.f, d = 0.f;
+        float a = 0.f, b = 0.f, d = 0.f, r2 = 0.f;
         for (uint32_t p = f; p < e; p++) {
             const float2 q = prel[p];
             const float rx = q.x - sx, ry = q.y - sy;
             a = fmaf(rx, rx, a);
             b = fmaf(rx, ry, b);
             d = fmaf(ry, ry, d);
+            r2 = fmaxf(r2, fmaf(rx, rx, ry * ry));
         }
-        write_node(node, cell_centre(i, minx, miny, h), h, c, sx, sy, a, b, d, com64, m0, m2, bbc, bblen, comrel,
-                   m0r, m2t);
+        write_node(node, cell_centre(i, minx, miny, h), h, c, sx, sy, a, b, d, sqrtf(r2), com64, m0, m2, bbc, bblen,
+                   comrel, m0r, m2t, bmax);
     }
 }
 
@@ -120,7 +123,8 @@ __global__ void k_leaf_big_p(int depth, double minx, double miny, double h, cons
                              const uint32_t* __restrict__ first, const float2* __restrict__ prel,
                              double2* __restrict__ com64, double* __restrict__ m0, double* __restrict__ m2,
                              double2* __restrict__ bbc, double* __restrict__ bblen, float* __restrict__ comrel,
-                             float* __restrict__ m0r, float* __restrict__ m2t, const uint32_t* __restrict__ big)
+                             float* __restrict__ m0r, float* __restrict__ m2t, const uint32_t* __restrict__ big,
+                             float* __restrict__ bmax)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t li = level_index(depth);
@@ -139,20 +143,22 @@ __global__ void k_leaf_big_p(int depth, double minx, double miny, double h, cons
         const float ic = 1.0f / (float)c;
         sx = warp_sum(sx) * ic;
         sy = warp_sum(sy) * ic;
-        float a = 0.f, b = 0.f, d = 0.f;
+        float a = 0.f, b = 0.f, d = 0.f, r2 = 0.f;
         for (uint32_t p = f + lane; p < f + c; p += 32) {
             const float2 q = prel[p];
             const float rx = q.x - sx, ry = q.y - sy;
             a = fmaf(rx, rx, a);
             b = fmaf(rx, ry, b);
             d = fmaf(ry, ry, d);
+            r2 = fmaxf(r2, fmaf(rx, rx, ry * ry));
         }
         a = warp_sum(a);
         b = warp_sum(b);
         d = warp_sum(d);
+        for (int o = 16; o > 0; o >>= 1) r2 = fmaxf(r2, __shfl_xor_sync(0xffffffffu, r2, o));
         if (lane == 0)
-            write_node(node, cell_centre(i, minx, miny, h), h, c, sx, sy, a, b, d, com64, m0, m2, bbc, bblen, comrel,
-                       m0r, m2t);
+            write_node(node, cell_centre(i, minx, miny, h), h, c, sx, sy, a, b, d, sqrtf(r2), com64, m0, m2, bbc,
+                       bblen, comrel, m0r, m2t, bmax);
     }
 }
 
@@ -162,7 +168,8 @@ __global__ void k_leaf_big_p(int depth, double minx, double miny, double h, cons
 __global__ void k_bottom_up_p(int l, double minx, double miny, double hl, uint32_t* __restrict__ count,
                               uint32_t* __restrict__ first, double2* __restrict__ com64, double* __restrict__ m0,
                               double* __restrict__ m2, double2* __restrict__ bbc, double* __restrict__ bblen,
-                              float* __restrict__ comrel, float* __restrict__ m0r, float* __restrict__ m2t)
+                              float* __restrict__ comrel, float* __restrict__ m0r, float* __restrict__ m2t,
+                              float* __restrict__ bmax)
 {
     const uint32_t li = level_index(l), lc = level_index(l + 1);
     const int64_t nl = (int64_t)1 << (2 * l);
@@ -194,7 +201,7 @@ __global__ void k_bottom_up_p(int l, double minx, double miny, double hl, uint32
         const float ic = 1.0f / (float)cnt;
         sx *= ic;
         sy *= ic;
-        float a = 0.f, b = 0.f, d = 0.f;
+        float a = 0.f, b = 0.f, d = 0.f, br = 0.f;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             if (c4[j] == 0) continue;
@@ -203,11 +210,13 @@ __global__ void k_bottom_up_p(int l, double minx, double miny, double hl, uint32
             a += w * (m2t[3 * (fc + j)] + rx * rx);
             b += w * (m2t[3 * (fc + j) + 1] + rx * ry);
             d += w * (m2t[3 * (fc + j) + 2] + ry * ry);
+            // every particle of child j lies within bmax_j of the child's COM
+            br = fmaxf(br, sqrtf(fmaf(rx, rx, ry * ry)) + bmax[fc + j]);
         }
         count[node] = cnt;
         first[node] = fp;
-        write_node(node, cell_centre(i, minx, miny, hl), hl, cnt, sx, sy, a, b, d, com64, m0, m2, bbc, bblen, comrel,
-                   m0r, m2t);
+        write_node(node, cell_centre(i, minx, miny, hl), hl, cnt, sx, sy, a, b, d, br, com64, m0, m2, bbc, bblen,
+                   comrel, m0r, m2t, bmax);
     }
 }
 
@@ -220,16 +229,16 @@ int build_records_p(Handle& h, double hleaf)
     const int64_t nleaf = (int64_t)1 << (2 * depth);
     const int64_t maxbig = h.n / (kLeafSmall + 1) + 1;
     int rc;
-    if ((rc = ensure(h.bigleaf, (maxbig + 1) * 4))) return rc;
+    if ((rc = ensure(h.bigleaf, (maxbig + 1) * 4)) || (rc = ensure(h.bmax, h.nnodes * 4))) return rc;
     TC_CUDA_TRY(cudaMemsetAsync(h.bigleaf.p, 0, 4, s));
     k_leaf_small_p<<<grid_for(nleaf, 128), 128, 0, s>>>(
         depth, h.minx, h.miny, hleaf, P<uint32_t>(h.count), P<uint32_t>(h.first), P<float2>(h.prel),
         P<double2>(h.com64), P<double>(h.m0), P<double>(h.m2), P<double2>(h.bbc), P<double>(h.bblen),
-        P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t), P<uint32_t>(h.bigleaf));
+        P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t), P<uint32_t>(h.bigleaf), P<float>(h.bmax));
     k_leaf_big_p<<<grid_for(maxbig * 32, 128), 128, 0, s>>>(
         depth, h.minx, h.miny, hleaf, P<uint32_t>(h.count), P<uint32_t>(h.first), P<float2>(h.prel),
         P<double2>(h.com64), P<double>(h.m0), P<double>(h.m2), P<double2>(h.bbc), P<double>(h.bblen),
-        P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t), P<uint32_t>(h.bigleaf));
+        P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t), P<uint32_t>(h.bigleaf), P<float>(h.bmax));
     h.launches += 2;
     for (int l = depth - 1; l >= 0; l--) {
         const double hl = h.L / (double)(1u << l);
@@ -237,7 +246,8 @@ int build_records_p(Handle& h, double hleaf)
         k_bottom_up_p<<<grid_for(nl, 128), 128, 0, s>>>(l, h.minx, h.miny, hl, P<uint32_t>(h.count),
                                                         P<uint32_t>(h.first), P<double2>(h.com64), P<double>(h.m0),
                                                         P<double>(h.m2), P<double2>(h.bbc), P<double>(h.bblen),
-                                                        P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t));
+                                                        P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t),
+                                                        P<float>(h.bmax));
         h.launches++;
     }
     TC_CUDA_TRY(cudaGetLastError());

@@ -65,7 +65,12 @@ class NBodySolverFMM_SYM_MORTON:
 
     def __init__(self, kernel: str = "tsne", max_children: int = 16, tree_depth: int | None = None,
                  theta: float = 0.5, softening: float = 1e-3, precision: str = "fp32", device: int = 0,
-                 stream=None, order: int = 0):
+                 stream=None, order: int = 0, mac: str = "cell"):
+        """mac (order p only): "cell", the reference's (L_A + L_B)/theta <
+        |dcom| with cell sizes L; "bmax", (b_A + b_B)/theta < |dcom| with b
+        the largest distance of a node's particles from its COM."""
+        if mac not in ("cell", "bmax"):
+            raise ValueError("mac must be 'cell' or 'bmax'")
         cfg = _lib.TcConfig()
         check(lib().tc_config_init(ctypes.byref(cfg)))
         cfg.kernel = KERNELS[kernel]
@@ -80,6 +85,9 @@ class NBodySolverFMM_SYM_MORTON:
         self.order = order
         self._h = ctypes.c_void_p()
         check(lib().tc_create(ctypes.byref(cfg), ctypes.byref(self._h)))
+        self.mac = mac
+        if mac == "bmax":
+            check(lib().tc_set_mac(self._h, _lib.TC_MAC_BMAX))
         self.maxChildren = max_children
         self._cfg_depth = cfg.depth
         self._theta = theta

@@ -58,3 +58,37 @@ def test_tsne_repulsion_order_p_normalised_gradient():
     g[pts.ID] = pts.derivative
     e = np.linalg.norm(g[rows] - fd, axis=1) / np.linalg.norm(fd, axis=1)
     assert np.median(e) < 1e-5
+
+
+@pytest.mark.parametrize("kernel", ["gravity", "tsne"])
+def test_bounding_radius_mac_converges(kernel):
+    """TC_MAC_BMAX: (b_A + b_B)/theta < |dcom| with b the nodes' bounding
+    radii about their COMs; the error falls with theta and with the order."""
+    n = 65536
+    if kernel == "gravity":
+        pos = datasets.two_disks(n, seed=21).astype(np.float64)
+    else:
+        pos = np.random.default_rng(22).normal(0.0, 10.0, (n, 2))
+    rows = np.random.default_rng(1).choice(n, 1024, replace=False)
+    fd, _ = direct(pos, kernel=kernel, softening=1e-3, precision="fp64", rows=rows)
+    meds = {}
+    for theta, p in [(0.8, 8), (0.6, 8), (0.4, 8), (0.6, 12)]:
+        s = NBodySolverFMM_SYM_MORTON(kernel, max_children=16, tree_depth=8, theta=theta, softening=1e-3, order=p,
+                                      mac="bmax")
+        pts = Points.from_positions(pos)
+        s.updateTree(pts, pos.min(0), pos.max(0))
+        s.solveNbody(0.0, pts)
+        g = np.zeros_like(pos)
+        g[pts.ID] = pts.derivative
+        meds[(theta, p)] = float(np.median(np.linalg.norm(g[rows] - fd, axis=1) / np.linalg.norm(fd, axis=1)))
+        s.close()
+    print(kernel, meds)
+    assert meds[(0.8, 8)] > meds[(0.6, 8)] > meds[(0.4, 8)]
+    assert meds[(0.6, 12)] < meds[(0.6, 8)]
+    assert meds[(0.4, 8)] < 1e-5
+
+
+def test_bounding_radius_mac_needs_order_p():
+    from masterthesislucas_gb300._lib import TreecodeError
+    with pytest.raises(TreecodeError):
+        NBodySolverFMM_SYM_MORTON("tsne", mac="bmax")
