@@ -108,6 +108,41 @@ __global__ void __launch_bounds__(128) k_p2m(int dep, float h, const uint32_t* _
     }
 }
 
+// the K coefficients of one node (stride KS, a multiple of 4) through 16-byte
+// accesses
+template <int K, int KS>
+__device__ __forceinline__ void load_coefs(const float* __restrict__ src, float* dst)
+{
+    const float4* s4 = reinterpret_cast<const float4*>(src);
+#pragma unroll
+    for (int c = 0; c < KS / 4; c++) {
+        const float4 v = s4[c];
+        if (4 * c < K) dst[4 * c] = v.x;
+        if (4 * c + 1 < K) dst[4 * c + 1] = v.y;
+        if (4 * c + 2 < K) dst[4 * c + 2] = v.z;
+        if (4 * c + 3 < K) dst[4 * c + 3] = v.w;
+    }
+}
+
+template <int K, int KS>
+__device__ __forceinline__ void store_coefs(float* __restrict__ dst, const float* src)
+{
+    float4* o4 = reinterpret_cast<float4*>(dst);
+#pragma unroll
+    for (int c = 0; c < KS / 4; c++)
+        o4[c] = make_float4(4 * c < K ? src[4 * c] : 0.f, 4 * c + 1 < K ? src[4 * c + 1] : 0.f,
+                            4 * c + 2 < K ? src[4 * c + 2] : 0.f, 4 * c + 3 < K ? src[4 * c + 3] : 0.f);
+}
+
+// coefficient k of degree d scaled by 2^-d (a child-scale multipole at the
+// parent's scale, or a parent-scale local expansion at the child's)
+template <int K>
+__device__ __forceinline__ void halve_by_degree(float* c)
+{
+#pragma unroll
+    for (int k = 0; k < K; k++) c[k] *= 1.0f / (float)(1 << cdeg(k));
+}
+
 // ------------------------------------------------------------------ M2M
 // one thread per node of level l: shift the children's multipoles (child
 // scale h/2) to the node's COM at scale h
@@ -134,17 +169,12 @@ __global__ void __launch_bounds__(128) k_m2m(int l, float hl, const uint32_t* __
             const float ox = ((j & 1) ? 0.25f : -0.25f) * hl, oy = ((j & 2) ? 0.25f : -0.25f) * hl;
             const float dx = (ox + comrel[2 * ch] - px) * ih, dy = (oy + comrel[2 * ch + 1] - py) * ih;
             float in[K], w[K];
-#pragma unroll
-            for (int ka = 0; ka <= P; ka++) {
-                const float sc = 1.0f / (float)(1 << ka);  // child scale -> parent scale
-#pragma unroll
-                for (int b = 0; b <= ka; b++) in[cidx(ka - b, b)] = mu[ch * kstride(P) + cidx(ka - b, b)] * sc;
-            }
+            load_coefs<K, kstride(P)>(mu + ch * kstride(P), in);
+            halve_by_degree<K>(in);  // child scale -> parent scale
             monomials<P>(dx, dy, w);
             shift_up<P>(in, w, acc);
         }
-#pragma unroll
-        for (int k = 0; k < K; k++) mu[node * kstride(P) + k] = acc[k];
+        store_coefs<K, kstride(P)>(mu + node * kstride(P), acc);
     }
 }
 
@@ -462,18 +492,12 @@ __global__ void __launch_bounds__(128) k_l2l(int l, float hl, const uint32_t* __
         const float ddx = ox + (comrel[2 * node] - comrel[2 * par]) * ih;
         const float ddy = oy + (comrel[2 * node + 1] - comrel[2 * par + 1]) * ih;
         float in[K], w[K], acc[K];
-#pragma unroll
-        for (int kb = 0; kb <= P; kb++) {
-            const float sc = 1.0f / (float)(1 << kb);  // parent scale 2h -> child scale h
-#pragma unroll
-            for (int b = 0; b <= kb; b++) in[cidx(kb - b, b)] = loc[par * kstride(P) + cidx(kb - b, b)] * sc;
-        }
-#pragma unroll
-        for (int k = 0; k < K; k++) acc[k] = loc[node * kstride(P) + k];
+        load_coefs<K, kstride(P)>(loc + par * kstride(P), in);
+        halve_by_degree<K>(in);  // parent scale 2h -> child scale h
+        load_coefs<K, kstride(P)>(loc + node * kstride(P), acc);
         monomials<P>(ddx, ddy, w);
         shift_down<P>(in, w, acc);
-#pragma unroll
-        for (int k = 0; k < K; k++) loc[node * kstride(P) + k] = acc[k];
+        store_coefs<K, kstride(P)>(loc + node * kstride(P), acc);
     }
 }
 
