@@ -188,9 +188,11 @@ def run_ours(args, w, rank, world):
     ref = ref_d.cpu().numpy()
 
     def make(theta, order=0, depth=None, controller=None, tau=None, mac="cell"):
+        kind, _, slack = mac.partition(":")
         s = NBodySolverFMM_SYM_MORTON(w["kernel"], max_children=w["max_children"], tree_depth=depth, theta=theta,
                                       softening=w["softening"], precision="fp32", order=order,
-                                      device=dev.index, stream=stream.cuda_stream, mac=mac)
+                                      device=dev.index, stream=stream.cuda_stream, mac=kind,
+                                      slack=float(slack or 1.0))
         if controller is not None:
             s.set_controller(controller, tau)
         return s
@@ -226,10 +228,10 @@ def run_ours(args, w, rank, world):
     target = TARGET_ERR * 0.9
     if args.order:
         plain = {"depth": args.depth or None, "theta": args.theta or 0.5, "order": args.order,
-                 "mac": "bmax" if args.mac == "bmax" else "cell"}
+                 "mac": "cell" if args.mac == "all" else args.mac}
         trials = []
     else:
-        macs = ("cell", "bmax") if args.mac == "both" else (args.mac,)
+        macs = ("cell", "bmax", "bmax_adaptive:0.03") if args.mac == "all" else (args.mac,)
         plain, trials = tune(pos_d, ref, rows_d, kernel=w["kernel"], softening=w["softening"],
                              leaf=w["max_children"], target=target, stream=stream, device=dev.index, macs=macs)
         if plain is None:
@@ -736,8 +738,9 @@ def main():
     ap.add_argument("--workload", default="nbody_two_disks_4m", choices=sorted(WORKLOADS))
     ap.add_argument("--theta", type=float, default=None)
     ap.add_argument("--order", type=int, default=0, help="fix the expansion order instead of autotuning")
-    ap.add_argument("--mac", default="both", choices=["cell", "bmax", "both"],
-                    help="opening criterion of the plain arms (both: autotuned)")
+    ap.add_argument("--mac", default="all",
+                    help="opening criterion of the plain arms: cell, bmax, bmax_adaptive:<slack> (per-pair "
+                         "orders), or all (autotuned over these)")
     ap.add_argument("--depth", type=int, default=0)
     ap.add_argument("--skip-reference-order", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=262144)

@@ -97,6 +97,16 @@ int tc_set_variant(tc_handle* h, int variant);
 #define TC_MAC_BMAX 1
 int tc_set_mac(tc_handle* h, int mac);
 
+/* Per-pair expansion order on a TC_MAC_BMAX handle of order p in {6, 8, 10,
+ * 12} (no counterpart in the reference): an accepted pair with ratio
+ * r = (b_A + b_B)/|com_A - com_B| < theta is evaluated at the lowest order
+ * q in {4, 6, 8, 10, 12}, q <= p, with r^(q+1) <= slack * theta^(p+1) (slack
+ * = 1 keeps every pair's truncation bound at the fixed-order one; smaller
+ * values are more conservative); the multipoles and local expansions keep
+ * order p.  slack <= 0 returns to order p for every pair.  Takes effect at
+ * the next tc_update_tree.                                                 */
+int tc_set_adaptive_order(tc_handle* h, double slack);
+
 /* getDepth (nBodySolverFMM_SYM_MORTON.h:106-115), clamped at 0 for n < leaf. */
 int tc_get_depth(int max_children, int64_t n, uint32_t* depth);
 /* node count of the level-dense tree, initNodesSize (:117-151).             */

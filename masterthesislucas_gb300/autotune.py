@@ -45,10 +45,15 @@ def tune(pos_d, ref_rows, rows_d, *, kernel: str, softening: float, leaf: int, t
     for mac, depth, order in [(m, d, o) for m in macs for d in depths for o in orders]:
         if depth > 15:
             continue
-        for theta in thetas or (THETAS_BMAX if mac == "bmax" else THETAS):
+        # "bmax_adaptive:<slack>": the per-pair order rule with that slack
+        kind, _, slack = mac.partition(":")
+        if kind == "bmax_adaptive" and order < 6:
+            continue
+        for theta in thetas or (THETAS_BMAX if kind.startswith("bmax") else THETAS):
             s = NBodySolverFMM_SYM_MORTON(kernel, max_children=leaf, tree_depth=depth, theta=theta,
                                           softening=softening, precision="fp32", order=order,
-                                          device=device, stream=s_torch.cuda_stream, mac=mac)
+                                          device=device, stream=s_torch.cuda_stream, mac=kind,
+                                          slack=float(slack or 1.0))
             try:
                 s.update_tree_device(pos_d)
                 s.solve_device(grad_d, tot_d)

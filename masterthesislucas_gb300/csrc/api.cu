@@ -608,6 +608,21 @@ extern "C" int tc_set_variant(tc_handle* t, int variant)
     return TC_OK;
 }
 
+extern "C" int tc_set_adaptive_order(tc_handle* t, double slack)
+{
+    if (!t || std::isnan(slack)) return TC_ERR_INVALID;
+    Handle& h = t->h;
+    const bool enable = slack > 0.0;
+    if (enable && (h.mac != TC_MAC_BMAX || h.cfg.order < 6 || (h.cfg.order & 1))) {
+        tc_set_error("tc_set_adaptive_order: needs TC_MAC_BMAX and order 6, 8, 10 or 12");
+        return TC_ERR_INVALID;
+    }
+    h.adapt = enable;
+    h.adapt_slack = enable ? slack : 0.0;
+    h.tree_ready = false;
+    return TC_OK;
+}
+
 extern "C" int tc_set_mac(tc_handle* t, int mac)
 {
     if (!t || (mac != TC_MAC_CELL && mac != TC_MAC_BMAX)) {
@@ -619,6 +634,7 @@ extern "C" int tc_set_mac(tc_handle* t, int mac)
         return TC_ERR_INVALID;
     }
     t->h.mac = mac;
+    if (mac != TC_MAC_BMAX) t->h.adapt = false;
     t->h.tree_ready = false;  // the interaction lists depend on the MAC
     return TC_OK;
 }

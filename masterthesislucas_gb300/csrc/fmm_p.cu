@@ -387,14 +387,16 @@ __global__ void __launch_bounds__(128) k_m2l_p(int l, float hl, PotParams pp, co
     }
 }
 
-// Controller lists: a node's accepted entries come sorted by order bucket
-// (orders 4, 6, 8, 10, 12).  Two launches per level: buckets 4..8 with an
-// order-8 accumulator (half the registers, twice the resident warps), which
-// writes the node's local expansion (zeros above order 8), then buckets 10
-// and 12 with an order-12 accumulator, which adds.  (A lower-order
-// contribution has no coefficients above its order, so the pair sum over the
-// stored coefficients equals the sum of the per-order sums.)
-template <int PACC, int OLO, int OHI>
+// Per-pair orders (the learned controller, or the bounding-radius rule): a
+// node's accepted entries come sorted by order bucket (orders 4, 6, 8, 10,
+// 12) over expansions stored at order PST.  The launch with OLO == 0 writes
+// the node's local expansion (zeros above PACC); a launch with OLO > 0 adds.
+// The learned controller (PST 12) takes two launches per level: buckets
+// 4..8 with an order-8 accumulator (half the registers, twice the resident
+// warps), then 10 and 12 with an order-12 one.  (A lower-order contribution
+// has no coefficients above its order, so the pair sum over the stored
+// coefficients equals the sum of the per-order sums.)
+template <int PST, int PACC, int OLO, int OHI>
 __global__ void __launch_bounds__(128) k_m2l_mixed(int l, float hl, PotParams pp, const uint32_t* __restrict__ nn_ptr,
                                                    const uint32_t* __restrict__ nn_idx,
                                                    const uint8_t* __restrict__ ord,
@@ -402,7 +404,7 @@ __global__ void __launch_bounds__(128) k_m2l_mixed(int l, float hl, PotParams pp
                                                    const float* __restrict__ comrel, const float* __restrict__ mu,
                                                    float* __restrict__ loc, double* __restrict__ zpart, const uint32_t* __restrict__ act, const uint32_t* __restrict__ act_pos)
 {
-    constexpr int K = ncoef(PACC), KS = kstride(12);
+    constexpr int K = ncoef(PACC), KS = kstride(PST);
     constexpr bool first = OLO == 0;
     const uint32_t li = level_index(l);
     const int64_t nl = (int64_t)1 << (2 * l);
@@ -620,27 +622,43 @@ __global__ void __launch_bounds__(32 * kNearWarps, 9)
                 moy = (float)((int)compact16(ti >> 1) - isy) * h;
                 has_self |= ti == (uint32_t)si;
             }
-            for (uint32_t t = 0; t < nt; t++) {
-                const uint32_t fT = __shfl_sync(0xffffffffu, mf, t), cT = __shfl_sync(0xffffffffu, mc, t);
-                const float ox = __shfl_sync(0xffffffffu, mox, t), oy = __shfl_sync(0xffffffffu, moy, t);
-                for (uint32_t q0 = 0; q0 < cT; q0 += 32) {
-                    const uint32_t mq = min(32u, cT - q0);
-                    if (fill + mq > (uint32_t)kNearBuf) {
-                        // evaluate the staged sources (the buffer is a multiple of 8g long)
-                        const uint32_t n8 = (fill + 8u * g - 1u) & ~(8u * g - 1u);
-                        for (uint32_t q = fill + lane; q < n8; q += 32) buf[q] = make_float2(kFarAway, kFarAway);
-                        __syncwarp();
-                        if (act) p2p_staged(ker, buf4, n8 / 2, r, g, px, py, gx, gy, zs);
-                        __syncwarp();
-                        staged += fill;
-                        fill = 0;
-                    }
-                    if (lane < mq) {
-                        const float2 t2 = prel2[fT + q0 + lane];
-                        buf[fill + lane] = make_float2(t2.x + ox, t2.y + oy);
-                    }
-                    fill += mq;
+            // the batch's particles as one flat range [0, tot): position q
+            // belongs to entry t with ex_t <= q < ex_t + c_t (exclusive
+            // prefix ex over the lanes), found by a binary search over lanes
+            uint32_t inc = mc;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= (uint32_t)o) inc += v;
+            }
+            const uint32_t ex = inc - mc, tot = __shfl_sync(0xffffffffu, inc, 31);
+            for (uint32_t q0 = 0; q0 < tot;) {
+                if (fill == (uint32_t)kNearBuf) {
+                    // evaluate the staged sources (kNearBuf is a multiple of 8g)
+                    __syncwarp();
+                    if (act) p2p_staged(ker, buf4, kNearBuf / 2, r, g, px, py, gx, gy, zs);
+                    __syncwarp();
+                    staged += fill;
+                    fill = 0;
                 }
+                const uint32_t take = min(tot - q0, (uint32_t)kNearBuf - fill);
+                for (uint32_t b0 = 0; b0 < take; b0 += 32) {
+                    const uint32_t q = q0 + b0 + lane;
+                    uint32_t t = 0;
+#pragma unroll
+                    for (uint32_t step = 16; step > 0; step >>= 1) {
+                        const uint32_t e = __shfl_sync(0xffffffffu, ex, t + step);
+                        if (t + step < nt && e <= q) t += step;
+                    }
+                    const uint32_t fT = __shfl_sync(0xffffffffu, mf, t), eT = __shfl_sync(0xffffffffu, ex, t);
+                    const float ox = __shfl_sync(0xffffffffu, mox, t), oy = __shfl_sync(0xffffffffu, moy, t);
+                    if (b0 + lane < take) {
+                        const float2 t2 = prel2[fT + (q - eT)];
+                        buf[fill + b0 + lane] = make_float2(t2.x + ox, t2.y + oy);
+                    }
+                }
+                fill += take;
+                q0 += take;
             }
         }
         if (fill > 0) {
@@ -752,14 +770,23 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
         const uint32_t* np_ = ptr + h.lists.nn_ptr_off[l];
         const uint32_t* ni_ = idx + h.lists.nn_idx_off[l];
         bool mixed = false;
+        const uint8_t* od = P<uint8_t>(h.ord_pool) + h.lists.nn_idx_off[l];
+        const uint32_t* act = P<uint32_t>(h.act);
+        const uint32_t* act_pos = P<uint32_t>(h.act_pos);
         if constexpr (ORD == 12) {
-            if (h.ctrl_on) {
-                const uint8_t* od = P<uint8_t>(h.ord_pool) + h.lists.nn_idx_off[l];
-                k_m2l_mixed<8, 0, 2><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, count, comrel, mu,
-                                                                       loc, zp, P<uint32_t>(h.act), P<uint32_t>(h.act_pos));
-                k_m2l_mixed<12, 3, 4><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, count, comrel, mu,
-                                                                        loc, zp, P<uint32_t>(h.act), P<uint32_t>(h.act_pos));
+            if (h.ctrl_on || h.adapt) {
+                k_m2l_mixed<12, 8, 0, 2><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, count, comrel,
+                                                                           mu, loc, zp, act, act_pos);
+                k_m2l_mixed<12, 12, 3, 4><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, count, comrel,
+                                                                            mu, loc, zp, act, act_pos);
                 h.launches++;
+                mixed = true;
+            }
+        } else if constexpr (ORD >= 6) {
+            if (h.adapt) {
+                constexpr int OB = (ORD - 4) / 2;  // the bucket of order ORD
+                k_m2l_mixed<ORD, ORD, 0, OB><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, count,
+                                                                              comrel, mu, loc, zp, act, act_pos);
                 mixed = true;
             }
         }

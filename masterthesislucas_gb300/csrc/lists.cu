@@ -17,6 +17,8 @@
 // near(parent), the lists hold exactly the reference's visited pairs.  The
 // MAC is evaluated in FP64 from the bit-exact COMs, so the decisions are the
 // reference's decisions.
+#include <cmath>
+
 #include "controller.cuh"
 #include "ctrl_mma.cuh"
 #include "state.cuh"
@@ -60,7 +62,17 @@ __device__ inline bool mac_accept_fast(int dix, int diy, real hl, real thr2, con
     return variant ? mac_accept_m(a, b, len, theta) : mac_accept(a, b, len, inv_theta);
 }
 
-// one thread per node of level l; fill == 0 counts, fill == 1 writes
+// Squared-ratio thresholds of the per-pair order rule: an accepted pair with
+// (b_A + b_B)^2 <= t[o] |dcom|^2 takes order bucket o (orders 4, 6, 8, 10, 12);
+// t[o] = (slack theta^(p + 1))^(2 / (q_o + 1)) below the handle's order p,
+// and unbounded at p.
+struct OrderRule {
+    float t[5];
+};
+
+// one thread per node of level l; fill == 0 counts, fill == 1 writes.  With
+// nn_ord (per-pair orders) the fill pass writes a node's accepted entries
+// grouped by order bucket, ascending, and the bucket of each in nn_ord.
 template <typename real>
 __global__ void k_lists(int l, double inv_theta, double theta, int variant, real hl, const uint32_t* __restrict__ count,
                         const double2* __restrict__ com64, const real* __restrict__ comrel,
@@ -70,7 +82,7 @@ __global__ void k_lists(int l, double inv_theta, double theta, int variant, real
                         uint32_t* __restrict__ nn_idx, uint32_t nn_cap, const uint32_t* __restrict__ near_ptr,
                         uint32_t* __restrict__ near_idx, uint32_t near_cap, uint32_t* __restrict__ ovf, int fill,
                         const uint32_t* __restrict__ act, const uint32_t* __restrict__ act_pos,
-                        const float* __restrict__ bmax, float theta2)
+                        const float* __restrict__ bmax, float theta2, uint8_t* __restrict__ nn_ord, OrderRule rule)
 {
     const uint32_t np = l ? (1u << (2 * (l - 1))) : 0u;
     const uint32_t li = level_index(l);
@@ -97,43 +109,68 @@ __global__ void k_lists(int l, double inv_theta, double theta, int variant, real
                 const real cra[2] = {comrel[2 * (li + a)], comrel[2 * (li + a) + 1]};
                 const float ba = bmax ? bmax[li + a] : 0.f;
                 const uint32_t p = (uint32_t)(a >> 2);
-                const uint32_t nb = fill ? nn_ptr[a] : 0, rb = fill ? near_ptr[a] : 0;
-                const uint32_t pe1 = pnear_ptr[p + 1] < pcap ? pnear_ptr[p + 1] : pcap;
-                for (uint32_t e = pnear_ptr[p]; e < pe1; e++) {
-                    const uint32_t bp = pnear_idx[e];
-                    if (bp >= np) continue;  // only after an overflowed parent level
-                    for (uint32_t j = 0; j < 4; j++) {
-                        const uint32_t b = 4 * bp + j;
-                        if (count[li + b] == 0) continue;
-                        bool acc;
-                        if (bmax) {
-                            // bounding-radius MAC in the cell-relative FP32 frame:
-                            // theta^2 |com_A - com_B|^2 > (b_A + b_B)^2
-                            const float dx = (float)(iax - (int)compact16(b)) * (float)hl +
-                                             ((float)cra[0] - (float)comrel[2 * (li + b)]);
-                            const float dy = (float)(iay - (int)compact16(b >> 1)) * (float)hl +
-                                             ((float)cra[1] - (float)comrel[2 * (li + b) + 1]);
-                            const float rb2 = ba + bmax[li + b];
-                            acc = theta2 * fmaf(dx, dx, dy * dy) > rb2 * rb2;
-                        } else {
-                            acc = mac_accept_fast<real>(iax - (int)compact16(b), iay - (int)compact16(b >> 1), hl,
-                                                        thr2, cra, comrel + 2 * (li + b), ca, com64[li + b], len,
-                                                        inv_theta, theta, variant);
-                        }
-                        if (acc) {
-                            if (fill) {
-                                if (nb + nn < nn_cap) nn_idx[nb + nn] = b;
-                                else atomicOr(ovf, 1u);
+                const uint32_t pe0 = pnear_ptr[p], pe1 = pnear_ptr[p + 1] < pcap ? pnear_ptr[p + 1] : pcap;
+                // every non-empty candidate: f(b, accepted, order bucket)
+                auto visit = [&](auto&& f) {
+                    for (uint32_t e = pe0; e < pe1; e++) {
+                        const uint32_t bp = pnear_idx[e];
+                        if (bp >= np) continue;  // only after an overflowed parent level
+                        for (uint32_t j = 0; j < 4; j++) {
+                            const uint32_t b = 4 * bp + j;
+                            if (count[li + b] == 0) continue;
+                            bool acc;
+                            int o = 0;
+                            if (bmax) {
+                                // bounding-radius MAC in the cell-relative FP32 frame:
+                                // theta^2 |com_A - com_B|^2 > (b_A + b_B)^2
+                                const float dx = (float)(iax - (int)compact16(b)) * (float)hl +
+                                                 ((float)cra[0] - (float)comrel[2 * (li + b)]);
+                                const float dy = (float)(iay - (int)compact16(b >> 1)) * (float)hl +
+                                                 ((float)cra[1] - (float)comrel[2 * (li + b) + 1]);
+                                const float rb = ba + bmax[li + b], rb2 = rb * rb, d2 = fmaf(dx, dx, dy * dy);
+                                acc = theta2 * d2 > rb2;
+                                if (nn_ord && acc)
+                                    while (o < 4 && rb2 > rule.t[o] * d2) o++;
+                            } else {
+                                acc = mac_accept_fast<real>(iax - (int)compact16(b), iay - (int)compact16(b >> 1), hl,
+                                                            thr2, cra, comrel + 2 * (li + b), ca, com64[li + b], len,
+                                                            inv_theta, theta, variant);
                             }
-                            nn++;
-                        } else {
-                            if (fill) {
-                                if (rb + nr < near_cap) near_idx[rb + nr] = b;
-                                else atomicOr(ovf, 1u);
-                            }
-                            nr++;
+                            f(b, acc, o);
                         }
                     }
+                };
+                if (!fill) {
+                    visit([&](uint32_t, bool acc, int) {
+                        if (acc) nn++;
+                        else nr++;
+                    });
+                } else {
+                    uint32_t start[5] = {nn_ptr[a], 0, 0, 0, 0};
+                    if (nn_ord) {
+                        uint32_t cnt[5] = {0, 0, 0, 0, 0};
+                        visit([&](uint32_t, bool acc, int o) {
+                            if (acc) cnt[o]++;
+                        });
+#pragma unroll
+                        for (int o = 1; o < 5; o++) start[o] = start[o - 1] + cnt[o - 1];
+                    }
+                    const uint32_t rb0 = near_ptr[a];
+                    visit([&](uint32_t b, bool acc, int o) {
+                        if (acc) {
+                            const uint32_t pos = start[o]++;
+                            if (pos < nn_cap) {
+                                nn_idx[pos] = b;
+                                if (nn_ord) nn_ord[pos] = (uint8_t)o;
+                            } else {
+                                atomicOr(ovf, 1u);
+                            }
+                        } else {
+                            if (rb0 + nr < near_cap) near_idx[rb0 + nr] = b;
+                            else atomicOr(ovf, 1u);
+                            nr++;
+                        }
+                    });
                 }
             }
         }
@@ -369,8 +406,8 @@ int prepare_nosync(Handle& h)
     for (int l = 0; l <= h.depth; l++) words += (int64_t)L.nn_cap[l] + L.near_cap[l];
     int rc;
     if ((rc = ensure(h.idx_pool, (size_t)words * 4 + 64))) return rc;
+    if ((h.adapt || h.ctrl_on) && (rc = ensure(h.ord_pool, h.idx_pool.bytes / 4 + 64))) return rc;
     if (h.ctrl_on) {
-        if ((rc = ensure(h.ord_pool, h.idx_pool.bytes / 4 + 64))) return rc;
         uint32_t pmax = 0;  // the controller's per-candidate decisions, sized for the widest parent level
         for (int l = 0; l < h.depth; l++) pmax = L.near_cap[l] > pmax ? L.near_cap[l] : pmax;
         if ((rc = ensure(h.dec, (size_t)pmax * 16 + 64))) return rc;
@@ -383,8 +420,11 @@ int build_lists(Handle& h)
     cudaStream_t s = h.stream;
     const int depth = h.depth;
     Lists& L = h.lists;
-    L.nn_total.assign(depth + 1, 0);
-    L.near_total.assign(depth + 1, 0);
+    if (!h.nosync || (int64_t)L.nn_total.size() != depth + 1) {
+        // a no-sync (captured) build keeps the totals of the last exact or fast build
+        L.nn_total.assign(depth + 1, 0);
+        L.near_total.assign(depth + 1, 0);
+    }
     L.nn_ptr_off.assign(depth + 1, 0);
     L.near_ptr_off.assign(depth + 1, 0);
     L.nn_idx_off.assign(depth + 1, 0);
@@ -411,6 +451,15 @@ int build_lists(Handle& h)
     const uint32_t* act = h.cfg.order && h.cfg.precision != TC_PREC_FP64 ? P<uint32_t>(h.act) : nullptr;
     const uint32_t* act_pos = act ? P<uint32_t>(h.act_pos) : nullptr;
     const float* bmax = act && h.mac == TC_MAC_BMAX ? P<float>(h.bmax) : nullptr;
+    // per-pair orders from the bounding-radius bound (orders 4..12 in steps of 2)
+    const bool adapt = bmax && h.adapt;
+    OrderRule rule{};
+    for (int o = 0; o < 5; o++) {
+        const int q = 4 + 2 * o;
+        rule.t[o] = q < h.cfg.order
+                        ? (float)std::pow(h.adapt_slack * std::pow(h.cfg.theta, h.cfg.order + 1), 2.0 / (q + 1))
+                        : 3.0e38f;
+    }
     const double inv_theta = 1.0 / h.cfg.theta;
     uint32_t* ovf_flag = P<uint32_t>(h.err) + 1;
     auto launch = [&](int l, const uint32_t* pnp, const uint32_t* pni, uint32_t pcap, uint32_t* nnc, uint32_t* nrc,
@@ -439,14 +488,18 @@ int build_lists(Handle& h)
                                                              P<double2>(h.com64), P<double>(h.comrel),
                                                              P<double>(h.bblen), pnp, pni, pcap, nnc, nrc, nnp, nni,
                                                              nncap, nrp, nri, nrcap, ovf_flag, fill, nullptr, nullptr, nullptr,
-                                                             0.f);
+                                                             0.f, nullptr, rule);
         else
             k_lists<float><<<grid_for(nl, 128), 128, 0, s>>>(l, inv_theta, h.cfg.theta, h.variant, (float)hl,
                                                             P<uint32_t>(h.count),
                                                             P<double2>(h.com64), P<float>(h.comrel),
                                                             P<double>(h.bblen), pnp, pni, pcap, nnc, nrc, nnp, nni,
                                                             nncap, nrp, nri, nrcap, ovf_flag, fill, act, act_pos, bmax,
-                                                            (float)(h.cfg.theta * h.cfg.theta));
+                                                            (float)(h.cfg.theta * h.cfg.theta),
+                                                            adapt && fill ? P<uint8_t>(h.ord_pool) +
+                                                                                (nni - P<uint32_t>(h.idx_pool))
+                                                                          : nullptr,
+                                                            rule);
         return 0;
     };
     if (h.ctrl_on) {
@@ -483,7 +536,7 @@ int build_lists(Handle& h)
             words += L.near_cap[l];
         }
         if ((rc = ensure(h.idx_pool, (size_t)words * 4 + 64))) return rc;
-        if (h.ctrl_on && (rc = ensure(h.ord_pool, h.idx_pool.bytes / 4 + 64))) return rc;
+        if ((h.ctrl_on || adapt) && (rc = ensure(h.ord_pool, h.idx_pool.bytes / 4 + 64))) return rc;
         for (int l = 0; l <= depth; l++) {
             const int64_t nl = (int64_t)1 << (2 * l);
             const uint32_t* pnp = l ? ptr + L.near_ptr_off[l - 1] : nullptr;
@@ -575,7 +628,7 @@ int build_lists(Handle& h)
             release(h.idx_pool);
             h.idx_pool = nb;
         }
-        if (h.ctrl_on && h.ord_pool.bytes < h.idx_pool.bytes / 4 + 64) {
+        if ((h.ctrl_on || adapt) && h.ord_pool.bytes < h.idx_pool.bytes / 4 + 64) {
             Buf nb;
             if ((rc = ensure(nb, h.idx_pool.bytes / 4 + 64))) return rc;
             if (h.ord_pool.p && L.nn_idx_off[l] > 0)

@@ -71,6 +71,9 @@ struct Handle {
     // reference-order solver: 0 the symmetric FMM_SYM_MORTON, 1 the non-symmetric FMM_MORTON
     int variant = 0;
     int mac = 0;  // TC_MAC_CELL or TC_MAC_BMAX (order p)
+    // order p with TC_MAC_BMAX: per-pair expansion order from the bound
+    bool adapt = false;
+    double adapt_slack = 0.0;
     bool nosync = false;
     double cap_slack = 0.25;  // fast-mode list capacity: exact total * (1 + slack) + 256
     bool ctrl_on = false;

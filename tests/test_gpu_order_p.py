@@ -92,3 +92,27 @@ def test_bounding_radius_mac_needs_order_p():
     from masterthesislucas_gb300._lib import TreecodeError
     with pytest.raises(TreecodeError):
         NBodySolverFMM_SYM_MORTON("tsne", mac="bmax")
+
+
+@pytest.mark.parametrize("order", [8, 12])
+def test_adaptive_order_keeps_the_error_of_fixed_order(order):
+    """bmax_adaptive: accepted pairs at the lowest order whose bound stays
+    below slack times the fixed-order one; at slack 0.01 the error stays
+    within a small factor of the fixed-order error at the same theta."""
+    n = 65536
+    pos = datasets.two_disks(n, seed=31).astype(np.float64)
+    rows = np.random.default_rng(2).choice(n, 1024, replace=False)
+    fd, _ = direct(pos, kernel="gravity", softening=1e-3, precision="fp64", rows=rows)
+    meds = {}
+    for mac in ("bmax", "bmax_adaptive"):
+        s = NBodySolverFMM_SYM_MORTON("gravity", max_children=16, tree_depth=8, theta=0.7, softening=1e-3,
+                                      order=order, mac=mac, slack=0.01)
+        pts = Points.from_positions(pos)
+        s.updateTree(pts, pos.min(0), pos.max(0))
+        s.solveNbody(0.0, pts)
+        g = np.zeros_like(pos)
+        g[pts.ID] = pts.derivative
+        meds[mac] = float(np.median(np.linalg.norm(g[rows] - fd, axis=1) / np.linalg.norm(fd, axis=1)))
+        s.close()
+    print(order, meds)
+    assert meds["bmax_adaptive"] < 1.5 * meds["bmax"]
