@@ -98,10 +98,10 @@ inline int grid_for(int64_t n, int block, int cap = kSMs * 32)
 // total in out[n].  tmp must hold scan_tmp_words(n) u32.
 int64_t scan_tmp_words(int64_t n);
 int exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* tmp, cudaStream_t s);
-// the same for two arrays of length n in one set of launches; tmp must hold
-// 2 * scan_tmp_words(n) u32
+// the same for two arrays of length n in one set of launches, every output
+// clamped to cap0 / cap1; tmp must hold 2 * scan_tmp_words(n) u32
 int exclusive_scan2_u32(const uint32_t* in0, uint32_t* out0, const uint32_t* in1, uint32_t* out1, int64_t n,
-                        uint32_t* tmp, cudaStream_t s);
+                        uint32_t* tmp, cudaStream_t s, uint32_t cap0 = UINT32_MAX, uint32_t cap1 = UINT32_MAX);
 
 // Deterministic FP64 sum of a[0..na) followed by c[0..*nc) (nc a device
 // pointer, may be NULL) into *out (+= when accumulate).  tmp holds

@@ -82,7 +82,8 @@ __global__ void k_lists(int l, double inv_theta, double theta, int variant, real
                         uint32_t* __restrict__ nn_idx, uint32_t nn_cap, const uint32_t* __restrict__ near_ptr,
                         uint32_t* __restrict__ near_idx, uint32_t near_cap, uint32_t* __restrict__ ovf, int fill,
                         const uint32_t* __restrict__ act, const uint32_t* __restrict__ act_pos,
-                        const float* __restrict__ bmax, float theta2, uint8_t* __restrict__ nn_ord, OrderRule rule)
+                        const float* __restrict__ bmax, float theta2, uint8_t* __restrict__ nn_ord, OrderRule rule,
+                        uint8_t* __restrict__ dec)
 {
     const uint32_t np = l ? (1u << (2 * (l - 1))) : 0u;
     const uint32_t li = level_index(l);
@@ -140,7 +141,59 @@ __global__ void k_lists(int l, double inv_theta, double theta, int variant, real
                         }
                     }
                 };
-                if (!fill) {
+                if (!fill && dec && !nn_ord) {
+                    // count pass that keeps its decisions: per parent near entry e and
+                    // sibling slot a & 3, bits 0-3 accepted child j, bits 4-7 non-empty child j
+                    for (uint32_t e = pe0; e < pe1; e++) {
+                        const uint32_t bp = pnear_idx[e];
+                        uint32_t bits = 0;
+                        if (bp < np) {
+                            for (uint32_t j = 0; j < 4; j++) {
+                                const uint32_t b = 4 * bp + j;
+                                if (count[li + b] == 0) continue;
+                                bool acc;
+                                if (bmax) {
+                                    const float dx = (float)(iax - (int)compact16(b)) * (float)hl +
+                                                     ((float)cra[0] - (float)comrel[2 * (li + b)]);
+                                    const float dy = (float)(iay - (int)compact16(b >> 1)) * (float)hl +
+                                                     ((float)cra[1] - (float)comrel[2 * (li + b) + 1]);
+                                    const float rb = ba + bmax[li + b];
+                                    acc = theta2 * fmaf(dx, dx, dy * dy) > rb * rb;
+                                } else {
+                                    acc = mac_accept_fast<real>(iax - (int)compact16(b), iay - (int)compact16(b >> 1),
+                                                                hl, thr2, cra, comrel + 2 * (li + b), ca, com64[li + b],
+                                                                len, inv_theta, theta, variant);
+                                }
+                                bits |= (acc ? 1u : 0u) << j | 16u << j;
+                                if (acc) nn++;
+                                else nr++;
+                            }
+                        }
+                        dec[4u * e + (uint32_t)(a & 3)] = (uint8_t)bits;
+                    }
+                } else if (fill && dec && !nn_ord) {
+                    // fill pass from the count pass's decisions
+                    uint32_t pos = nn_ptr[a];
+                    const uint32_t rb0 = near_ptr[a];
+                    for (uint32_t e = pe0; e < pe1; e++) {
+                        const uint32_t bits = dec[4u * e + (uint32_t)(a & 3)];
+                        if (bits == 0) continue;
+                        const uint32_t bp = pnear_idx[e];
+                        for (uint32_t j = 0; j < 4; j++) {
+                            if (!(bits & (16u << j))) continue;
+                            const uint32_t b = 4 * bp + j;
+                            if (bits & (1u << j)) {
+                                if (pos < nn_cap) nn_idx[pos] = b;
+                                else atomicOr(ovf, 1u);
+                                pos++;
+                            } else {
+                                if (rb0 + nr < near_cap) near_idx[rb0 + nr] = b;
+                                else atomicOr(ovf, 1u);
+                                nr++;
+                            }
+                        }
+                    }
+                } else if (!fill) {
                     visit([&](uint32_t, bool acc, int) {
                         if (acc) nn++;
                         else nr++;
@@ -371,16 +424,6 @@ __global__ void k_lists_ctrl_fill(int l, const uint32_t* __restrict__ count, con
     }
 }
 
-// No-sync builds cannot check the capacities before the lists are read: the
-// CSR pointers are clamped to the capacity so that every reader stays inside
-// the level's region (an overflowed level then yields truncated lists, and
-// the overflow flag tells the caller to redo the step).
-__global__ void k_clamp_ptr(uint32_t* __restrict__ ptr, int64_t n, uint32_t cap)
-{
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        if (ptr[i] > cap) ptr[i] = cap;
-}
-
 // per-level list totals (last entries of the CSR pointer arrays)
 __global__ void k_list_totals(const uint32_t* __restrict__ ptr, const int64_t* __restrict__ offs, int nlev,
                               uint32_t* __restrict__ out)
@@ -407,11 +450,11 @@ int prepare_nosync(Handle& h)
     int rc;
     if ((rc = ensure(h.idx_pool, (size_t)words * 4 + 64))) return rc;
     if ((h.adapt || h.ctrl_on) && (rc = ensure(h.ord_pool, h.idx_pool.bytes / 4 + 64))) return rc;
-    if (h.ctrl_on) {
-        uint32_t pmax = 0;  // the controller's per-candidate decisions, sized for the widest parent level
-        for (int l = 0; l < h.depth; l++) pmax = L.near_cap[l] > pmax ? L.near_cap[l] : pmax;
-        if ((rc = ensure(h.dec, (size_t)pmax * 16 + 64))) return rc;
-    }
+    // per-candidate decisions (controller: 16 bytes per parent near entry; MAC lists: 4), sized for the widest
+    // parent level
+    uint32_t pmax = 0;
+    for (int l = 0; l < h.depth; l++) pmax = L.near_cap[l] > pmax ? L.near_cap[l] : pmax;
+    if ((rc = ensure(h.dec, (size_t)pmax * (h.ctrl_on ? 16 : 4) + 64))) return rc;
     return TC_OK;
 }
 
@@ -482,14 +525,20 @@ int build_lists(Handle& h)
                                                                     P<uint8_t>(h.dec), nnp, nni, ordp, nncap, nrp,
                                                                     nri, nrcap, ovf_flag, act, act_pos);
             }
-        } else if (h.cfg.precision == TC_PREC_FP64)
+        } else if (h.cfg.precision == TC_PREC_FP64) {
             k_lists<double><<<grid_for(nl, 128), 128, 0, s>>>(l, inv_theta, h.cfg.theta, h.variant, hl,
                                                              P<uint32_t>(h.count),
                                                              P<double2>(h.com64), P<double>(h.comrel),
                                                              P<double>(h.bblen), pnp, pni, pcap, nnc, nrc, nnp, nni,
                                                              nncap, nrp, nri, nrcap, ovf_flag, fill, nullptr, nullptr, nullptr,
-                                                             0.f, nullptr, rule);
-        else
+                                                             0.f, nullptr, rule, nullptr);
+        } else {
+            // the count pass keeps its decisions for the fill pass (one byte per parent near entry and
+            // sibling slot)
+            if (!fill && l > 0 && !adapt) {
+                int rc2 = ensure(h.dec, (size_t)pcap * 4 + 64);
+                if (rc2) return rc2;
+            }
             k_lists<float><<<grid_for(nl, 128), 128, 0, s>>>(l, inv_theta, h.cfg.theta, h.variant, (float)hl,
                                                             P<uint32_t>(h.count),
                                                             P<double2>(h.com64), P<float>(h.comrel),
@@ -499,7 +548,8 @@ int build_lists(Handle& h)
                                                             adapt && fill ? P<uint8_t>(h.ord_pool) +
                                                                                 (nni - P<uint32_t>(h.idx_pool))
                                                                           : nullptr,
-                                                            rule);
+                                                            rule, l > 0 && !adapt ? P<uint8_t>(h.dec) : nullptr);
+        }
         return 0;
     };
     if (h.ctrl_on) {
@@ -550,15 +600,16 @@ int build_lists(Handle& h)
                 return rc;
             uint32_t* nnp = ptr + L.nn_ptr_off[l];
             uint32_t* nrp = ptr + L.near_ptr_off[l];
-            if ((rc = exclusive_scan2_u32(nn_cnt, nnp, near_cnt, nrp, nl, P<uint32_t>(h.tmp), s))) return rc;
+            // a captured build cannot check capacities before the lists are read: its CSR pointers are
+            // clamped to the capacities, so an overflowed level yields truncated lists (and the overflow
+            // flag) instead of out-of-range reads
+            if ((rc = exclusive_scan2_u32(nn_cnt, nnp, near_cnt, nrp, nl, P<uint32_t>(h.tmp), s,
+                                          h.nosync ? L.nn_cap[l] : UINT32_MAX,
+                                          h.nosync ? L.near_cap[l] : UINT32_MAX)))
+                return rc;
             if ((rc = launch(l, pnp, pni, pcap, nullptr, nullptr, nnp, P<uint32_t>(h.idx_pool) + L.nn_idx_off[l],
                              L.nn_cap[l], nrp, P<uint32_t>(h.idx_pool) + L.near_idx_off[l], L.near_cap[l], 1)))
                 return rc;
-            if (h.nosync) {
-                k_clamp_ptr<<<grid_for(nl + 1, 256), 256, 0, s>>>(nnp, nl + 1, L.nn_cap[l]);
-                k_clamp_ptr<<<grid_for(nl + 1, 256), 256, 0, s>>>(nrp, nl + 1, L.near_cap[l]);
-                h.launches += 2;
-            }
             h.launches += 2 + (nl <= 2048 ? 1 : 3);  // count, fill, scan
         }
         if (h.nosync) {

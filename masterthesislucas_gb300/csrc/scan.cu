@@ -102,13 +102,15 @@ __global__ void k_scan_partials2(uint32_t* partial, int64_t nb)
     }
 }
 
-// partial == nullptr: a single chunk (nb == 1), no carry
+// partial == nullptr: a single chunk (nb == 1), no carry.  Outputs are
+// clamped to cap0 / cap1.
 __global__ void k_scan_final2(const uint32_t* __restrict__ in0, uint32_t* __restrict__ out0,
                               const uint32_t* __restrict__ in1, uint32_t* __restrict__ out1, int64_t n,
-                              const uint32_t* __restrict__ partial, int64_t nb)
+                              const uint32_t* __restrict__ partial, int64_t nb, uint32_t cap0, uint32_t cap1)
 {
     const uint32_t* in = blockIdx.y ? in1 : in0;
     uint32_t* out = blockIdx.y ? out1 : out0;
+    const uint32_t cap = blockIdx.y ? cap1 : cap0;
     const uint32_t carry = partial ? partial[blockIdx.y * nb + blockIdx.x] : 0u;
     int64_t base = (int64_t)blockIdx.x * kScanChunk + (int64_t)threadIdx.x * kScanItems;
     uint32_t v[kScanItems];
@@ -124,10 +126,10 @@ __global__ void k_scan_final2(const uint32_t* __restrict__ in0, uint32_t* __rest
 #pragma unroll
     for (int i = 0; i < kScanItems; i++) {
         int64_t k = base + i;
-        if (k < n) out[k] = ex;
+        if (k < n) out[k] = min(ex, cap);
         ex += v[i];
     }
-    if (blockIdx.x == nb - 1 && threadIdx.x == 0) out[n] = carry + tot;
+    if (blockIdx.x == nb - 1 && threadIdx.x == 0) out[n] = min(carry + tot, cap);
 }
 
 constexpr int kSumBlocks = 2 * kSMs;
@@ -190,7 +192,7 @@ int exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* t
     }
     int64_t nb = (n + kScanChunk - 1) / kScanChunk;
     if (nb == 1) {
-        k_scan_final2<<<dim3(1, 1), kScanThreads, 0, s>>>(in, out, in, out, n, nullptr, 1);
+        k_scan_final2<<<dim3(1, 1), kScanThreads, 0, s>>>(in, out, in, out, n, nullptr, 1, UINT32_MAX, UINT32_MAX);
         TC_CUDA_TRY(cudaGetLastError());
         return TC_OK;
     }
@@ -202,7 +204,7 @@ int exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* t
 }
 
 int exclusive_scan2_u32(const uint32_t* in0, uint32_t* out0, const uint32_t* in1, uint32_t* out1, int64_t n,
-                        uint32_t* tmp, cudaStream_t s)
+                        uint32_t* tmp, cudaStream_t s, uint32_t cap0, uint32_t cap1)
 {
     if (n <= 0) {
         TC_CUDA_TRY(cudaMemsetAsync(out0, 0, sizeof(uint32_t), s));
@@ -211,11 +213,11 @@ int exclusive_scan2_u32(const uint32_t* in0, uint32_t* out0, const uint32_t* in1
     }
     int64_t nb = (n + kScanChunk - 1) / kScanChunk;
     if (nb == 1) {
-        k_scan_final2<<<dim3(1, 2), kScanThreads, 0, s>>>(in0, out0, in1, out1, n, nullptr, 1);
+        k_scan_final2<<<dim3(1, 2), kScanThreads, 0, s>>>(in0, out0, in1, out1, n, nullptr, 1, cap0, cap1);
     } else {
         k_scan_reduce2<<<dim3((unsigned)nb, 2), kScanThreads, 0, s>>>(in0, in1, n, tmp, nb);
         k_scan_partials2<<<2, 1024, 0, s>>>(tmp, nb);
-        k_scan_final2<<<dim3((unsigned)nb, 2), kScanThreads, 0, s>>>(in0, out0, in1, out1, n, tmp, nb);
+        k_scan_final2<<<dim3((unsigned)nb, 2), kScanThreads, 0, s>>>(in0, out0, in1, out1, n, tmp, nb, cap0, cap1);
     }
     TC_CUDA_TRY(cudaGetLastError());
     return TC_OK;
