@@ -125,10 +125,15 @@ __host__ __device__ inline double bbox_unkey(unsigned long long k)
 }
 
 // ---------------------------------------------------------------- sort
-// Stable LSD radix sort of 32-bit keys with 32-bit values (4 passes of 8 bits).
-// keys/vals are sorted in place; alt_* are scratch of n entries each.
+// Stable LSD radix sort of 32-bit keys by bits lo_bit..31 (passes of 8 bits)
+// with 32-bit values; the result lands in keys/vals, alt_* are scratch of n
+// entries each.  With an odd number of passes the input keys must be in
+// alt_keys instead of keys.  The values are the input positions (iota).
 int64_t radix_tmp_words(int64_t n);
 int radix_sort_u32(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32_t* alt_vals, int64_t n,
-                   uint32_t* tmp, cudaStream_t s, int* launches);
+                   uint32_t* tmp, cudaStream_t s, int* launches, int lo_bit = 0);
+// the lowest bit the sort must see for the leaf index of a depth-d tree
+// (2d top bits), rounded down to whole 8-bit passes
+inline int sort_lo_bit(int depth) { return 32 - 8 * (depth > 0 ? (2 * depth + 7) / 8 : 1); }
 
 }  // namespace tc

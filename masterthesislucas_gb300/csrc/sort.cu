@@ -112,7 +112,7 @@ int64_t radix_tmp_words(int64_t n)
 }
 
 int radix_sort_u32(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32_t* alt_vals, int64_t n,
-                   uint32_t* tmp, cudaStream_t s, int* launches)
+                   uint32_t* tmp, cudaStream_t s, int* launches, int lo_bit)
 {
     if (n <= 0) return TC_OK;
     const int nb = (int)((n + RTILE - 1) / RTILE);
@@ -120,12 +120,22 @@ int radix_sort_u32(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32_t*
     uint32_t* hist = tmp;
     uint32_t* offs = tmp + (h + 1);
     uint32_t* stmp = offs + (h + 1);
+    const int npass = (32 - lo_bit + 7) / 8;
+    // an odd number of passes starts from the alternate buffers (the keys are
+    // there), so that the result always lands in keys / vals
     uint32_t *ki = keys, *vi = vals, *ko = alt_keys, *vo = alt_vals;
-    for (int pass = 0; pass < 4; pass++) {
-        k_radix_hist<<<nb, RT, 0, s>>>(ki, n, pass * 8, hist, nb);
+    if (npass & 1) {
+        ki = alt_keys;
+        vi = alt_vals;
+        ko = keys;
+        vo = vals;
+    }
+    for (int pass = 0; pass < npass; pass++) {
+        const int shift = lo_bit + 8 * pass;
+        k_radix_hist<<<nb, RT, 0, s>>>(ki, n, shift, hist, nb);
         int rc = exclusive_scan_u32(hist, offs, h, stmp, s);
         if (rc) return rc;
-        k_radix_scatter<<<nb, RT, 0, s>>>(ki, vi, ko, vo, n, pass * 8, offs, nb, pass == 0);
+        k_radix_scatter<<<nb, RT, 0, s>>>(ki, vi, ko, vo, n, shift, offs, nb, pass == 0);
         if (launches) *launches += 2 + (h <= 2048 ? 1 : 3);  // histogram, scatter, scan
         uint32_t* t = ki; ki = ko; ko = t;
         t = vi; vi = vo; vo = t;

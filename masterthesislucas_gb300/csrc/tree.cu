@@ -304,8 +304,10 @@ int build_tree(Handle& h, const double* d_pos, int64_t n, double minx, double mi
         h.launches++;
     }
     TC_CUDA_TRY(cudaGetLastError());
+    // the reference-order path sorts whole codes (its tie order is part of the parity contract); the
+    // physics path only the leaf bits
     rc = radix_sort_u32(P<uint32_t>(h.codes), P<uint32_t>(h.perm), P<uint32_t>(h.alt_keys), P<uint32_t>(h.alt_vals), n,
-                        P<uint32_t>(h.tmp), s, &h.launches);
+                        P<uint32_t>(h.tmp), s, &h.launches, physics ? sort_lo_bit(depth) : 0);
     if (rc || (rc = record(h, 1))) return rc;
     const uint32_t li = level_index(depth);
     const int64_t nleaf = (int64_t)1 << (2 * depth);

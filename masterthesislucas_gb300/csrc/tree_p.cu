@@ -256,9 +256,11 @@ int build_records_p(Handle& h, double hleaf)
 
 int morton_p(Handle& h, const double* d_pos, int64_t n, double maxx, double maxy)
 {
+    // the sort reads only the leaf bits; with an odd number of passes it starts from alt_keys
+    const int npass = (32 - sort_lo_bit(h.depth) + 7) / 8;
+    uint32_t* out = (npass & 1) ? P<uint32_t>(h.alt_keys) : P<uint32_t>(h.codes);
     k_morton_p<<<grid_for(n, 256), 256, 0, h.stream>>>((const double2*)d_pos, n, h.minx, h.miny, maxx - h.minx,
-                                                      maxy - h.miny, (float)(65536.0 / h.L), P<uint32_t>(h.codes),
-                                                      P<uint32_t>(h.err));
+                                                      maxy - h.miny, (float)(65536.0 / h.L), out, P<uint32_t>(h.err));
     h.launches++;
     TC_CUDA_TRY(cudaGetLastError());
     return TC_OK;
