@@ -192,7 +192,7 @@ def run_ours(args, w, rank, world):
         s = NBodySolverFMM_SYM_MORTON(w["kernel"], max_children=w["max_children"], tree_depth=depth, theta=theta,
                                       softening=w["softening"], precision="fp32", order=order,
                                       device=dev.index, stream=stream.cuda_stream, mac=kind,
-                                      slack=float(slack or 1.0))
+                                      slack=float(slack or 1.0), leaf_p2p=args.leaf_p2p if order else 0)
         if controller is not None:
             s.set_controller(controller, tau)
         return s
@@ -233,7 +233,8 @@ def run_ours(args, w, rank, world):
     else:
         macs = ("cell", "bmax", "bmax_adaptive:0.03") if args.mac == "all" else (args.mac,)
         plain, trials = tune(pos_d, ref, rows_d, kernel=w["kernel"], softening=w["softening"],
-                             leaf=w["max_children"], target=target, stream=stream, device=dev.index, macs=macs)
+                             leaf=w["max_children"], target=target, stream=stream, device=dev.index, macs=macs,
+                             leaf_p2p=args.leaf_p2p)
         if plain is None:
             raise SystemExit("autotuner found no configuration meeting the error target")
     p12 = min((t for t in trials if t["order"] == 12 and t["err"] <= target), key=lambda t: t["ms"], default=None)
@@ -738,6 +739,8 @@ def main():
     ap.add_argument("--workload", default="nbody_two_disks_4m", choices=sorted(WORKLOADS))
     ap.add_argument("--theta", type=float, default=None)
     ap.add_argument("--order", type=int, default=0, help="fix the expansion order instead of autotuning")
+    ap.add_argument("--leaf-p2p", type=int, default=64,
+                    help="order-p arms: accepted leaf pairs with at most this many particle pairs use P2P")
     ap.add_argument("--mac", default="all",
                     help="opening criterion of the plain arms: cell, bmax, bmax_adaptive:<slack> (per-pair "
                          "orders), or all (autotuned over these)")
@@ -757,8 +760,9 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", 1))
     config = {"workload": args.workload, "n": w["n"], "distribution": w["dist"], "kernel": w["kernel"],
               "softening": w["softening"], "leaf_size": w["max_children"],
-              "precision": "fp32 expansions and P2P; fp64 tree build, MACs and Z",
-              "error_target": TARGET_ERR, "error_samples": N_SAMPLES}
+              "precision": ("fp32 expansions, P2P, MACs and tree records (cell-relative coordinates formed "
+                            "from fp64 positions); fp64 pair sum Z"),
+              "error_target": TARGET_ERR, "error_samples": N_SAMPLES, "leaf_p2p": args.leaf_p2p}
 
     if args.impl == "reference":
         if rank != 0:

@@ -107,6 +107,13 @@ int tc_set_mac(tc_handle* h, int mac);
  * the next tc_update_tree.                                                 */
 int tc_set_adaptive_order(tc_handle* h, double slack);
 
+/* Order-p handles (no counterpart in the reference): at the leaf level an
+ * accepted pair of leaves A, B with n_A * n_B <= max_pairs is evaluated by
+ * direct P2P instead of an M2L (an order-p M2L costs about as much as 70
+ * particle pairs; the direct sum is also exact).  0 (the default) turns it
+ * off.  Takes effect at the next tc_update_tree.                           */
+int tc_set_leaf_p2p(tc_handle* h, int max_pairs);
+
 /* getDepth (nBodySolverFMM_SYM_MORTON.h:106-115), clamped at 0 for n < leaf. */
 int tc_get_depth(int max_children, int64_t n, uint32_t* depth);
 /* node count of the level-dense tree, initNodesSize (:117-151).             */

@@ -54,6 +54,7 @@ SIGNATURES = {
     "tc_set_variant": (_I, [_P, _I]),
     "tc_set_mac": (_I, [_P, _I]),
     "tc_set_adaptive_order": (_I, [_P, _D]),
+    "tc_set_leaf_p2p": (_I, [_P, _I]),
     "tc_get_depth": (_I, [_I, _I64, _P]),
     "tc_node_count": (_I, [ctypes.c_uint32, _P]),
     "tc_update_tree": (_I, [_P, _P, _P, _I64, _P, _P]),

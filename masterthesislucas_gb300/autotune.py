@@ -30,7 +30,8 @@ def median_error(grad_rows: np.ndarray, ref_rows: np.ndarray) -> float:
 
 
 def tune(pos_d, ref_rows, rows_d, *, kernel: str, softening: float, leaf: int, target: float,
-         stream=None, depths=None, thetas=None, orders=ORDERS, device: int = 0, log=None, macs=("cell",)):
+         stream=None, depths=None, thetas=None, orders=ORDERS, device: int = 0, log=None, macs=("cell",),
+         leaf_p2p: int = 0):
     """Returns (best, trials).  best = dict(mac, depth, theta, order, ms, err) or None."""
     import torch
 
@@ -53,7 +54,7 @@ def tune(pos_d, ref_rows, rows_d, *, kernel: str, softening: float, leaf: int, t
             s = NBodySolverFMM_SYM_MORTON(kernel, max_children=leaf, tree_depth=depth, theta=theta,
                                           softening=softening, precision="fp32", order=order,
                                           device=device, stream=s_torch.cuda_stream, mac=kind,
-                                          slack=float(slack or 1.0))
+                                          slack=float(slack or 1.0), leaf_p2p=leaf_p2p)
             try:
                 s.update_tree_device(pos_d)
                 s.solve_device(grad_d, tot_d)

@@ -608,6 +608,18 @@ extern "C" int tc_set_variant(tc_handle* t, int variant)
     return TC_OK;
 }
 
+extern "C" int tc_set_leaf_p2p(tc_handle* t, int max_pairs)
+{
+    if (!t || max_pairs < 0) return TC_ERR_INVALID;
+    if (max_pairs > 0 && t->h.cfg.order == 0) {
+        tc_set_error("tc_set_leaf_p2p: needs an order-p handle (the reference order keeps its interaction set)");
+        return TC_ERR_INVALID;
+    }
+    t->h.p2p_cut = (uint32_t)max_pairs;
+    t->h.tree_ready = false;
+    return TC_OK;
+}
+
 extern "C" int tc_set_adaptive_order(tc_handle* t, double slack)
 {
     if (!t || std::isnan(slack)) return TC_ERR_INVALID;

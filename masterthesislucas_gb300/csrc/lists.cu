@@ -83,7 +83,7 @@ __global__ void k_lists(int l, double inv_theta, double theta, int variant, real
                         uint32_t* __restrict__ near_idx, uint32_t near_cap, uint32_t* __restrict__ ovf, int fill,
                         const uint32_t* __restrict__ act, const uint32_t* __restrict__ act_pos,
                         const float* __restrict__ bmax, float theta2, uint8_t* __restrict__ nn_ord, OrderRule rule,
-                        uint8_t* __restrict__ dec)
+                        uint8_t* __restrict__ dec, uint32_t p2p_cut)
 {
     const uint32_t np = l ? (1u << (2 * (l - 1))) : 0u;
     const uint32_t li = level_index(l);
@@ -111,6 +111,10 @@ __global__ void k_lists(int l, double inv_theta, double theta, int variant, real
                 const float ba = bmax ? bmax[li + a] : 0.f;
                 const uint32_t p = (uint32_t)(a >> 2);
                 const uint32_t pe0 = pnear_ptr[p], pe1 = pnear_ptr[p + 1] < pcap ? pnear_ptr[p + 1] : pcap;
+                // p2p_cut (leaf level only; 0 off): an accepted pair of leaves with at most p2p_cut
+                // particle pairs goes to the near list, where direct P2P is cheaper than an M2L
+                const uint32_t ca_n = p2p_cut ? count[li + a] : 0u;
+                auto direct_cheaper = [&](uint32_t b) { return p2p_cut && ca_n * count[li + b] <= p2p_cut; };
                 // every non-empty candidate: f(b, accepted, order bucket)
                 auto visit = [&](auto&& f) {
                     for (uint32_t e = pe0; e < pe1; e++) {
@@ -137,6 +141,7 @@ __global__ void k_lists(int l, double inv_theta, double theta, int variant, real
                                                             thr2, cra, comrel + 2 * (li + b), ca, com64[li + b], len,
                                                             inv_theta, theta, variant);
                             }
+                            if (acc && direct_cheaper(b)) acc = false;
                             f(b, acc, o);
                         }
                     }
@@ -164,6 +169,7 @@ __global__ void k_lists(int l, double inv_theta, double theta, int variant, real
                                                                 hl, thr2, cra, comrel + 2 * (li + b), ca, com64[li + b],
                                                                 len, inv_theta, theta, variant);
                                 }
+                                if (acc && direct_cheaper(b)) acc = false;
                                 bits |= (acc ? 1u : 0u) << j | 16u << j;
                                 if (acc) nn++;
                                 else nr++;
@@ -531,7 +537,7 @@ int build_lists(Handle& h)
                                                              P<double2>(h.com64), P<double>(h.comrel),
                                                              P<double>(h.bblen), pnp, pni, pcap, nnc, nrc, nnp, nni,
                                                              nncap, nrp, nri, nrcap, ovf_flag, fill, nullptr, nullptr, nullptr,
-                                                             0.f, nullptr, rule, nullptr);
+                                                             0.f, nullptr, rule, nullptr, 0u);
         } else {
             // the count pass keeps its decisions for the fill pass (one byte per parent near entry and
             // sibling slot)
@@ -548,7 +554,8 @@ int build_lists(Handle& h)
                                                             adapt && fill ? P<uint8_t>(h.ord_pool) +
                                                                                 (nni - P<uint32_t>(h.idx_pool))
                                                                           : nullptr,
-                                                            rule, l > 0 && !adapt ? P<uint8_t>(h.dec) : nullptr);
+                                                            rule, l > 0 && !adapt ? P<uint8_t>(h.dec) : nullptr,
+                                                            act && l == depth ? h.p2p_cut : 0u);
         }
         return 0;
     };

@@ -74,6 +74,8 @@ struct Handle {
     // order p with TC_MAC_BMAX: per-pair expansion order from the bound
     bool adapt = false;
     double adapt_slack = 0.0;
+    // order p: accepted leaf pairs with at most this many particle pairs are evaluated by P2P
+    uint32_t p2p_cut = 0;
     bool nosync = false;
     double cap_slack = 0.25;  // fast-mode list capacity: exact total * (1 + slack) + 256
     bool ctrl_on = false;

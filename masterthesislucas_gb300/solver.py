@@ -65,13 +65,15 @@ class NBodySolverFMM_SYM_MORTON:
 
     def __init__(self, kernel: str = "tsne", max_children: int = 16, tree_depth: int | None = None,
                  theta: float = 0.5, softening: float = 1e-3, precision: str = "fp32", device: int = 0,
-                 stream=None, order: int = 0, mac: str = "cell", slack: float = 1.0):
+                 stream=None, order: int = 0, mac: str = "cell", slack: float = 1.0, leaf_p2p: int = 0):
         """mac (order p only): "cell", the reference's (L_A + L_B)/theta <
         |dcom| with cell sizes L; "bmax", (b_A + b_B)/theta < |dcom| with b
         the largest distance of a node's particles from its COM;
         "bmax_adaptive", the same with each accepted pair evaluated at the
         lowest order in {4, 6, ..., order} whose bound ((b_A + b_B)/|dcom|)^(q+1)
-        stays below slack * theta^(order+1)."""
+        stays below slack * theta^(order+1).
+        leaf_p2p (order p): accepted leaf pairs with at most this many
+        particle pairs are summed directly instead of by an M2L."""
         if mac not in ("cell", "bmax", "bmax_adaptive"):
             raise ValueError("mac must be 'cell', 'bmax' or 'bmax_adaptive'")
         cfg = _lib.TcConfig()
@@ -93,6 +95,8 @@ class NBodySolverFMM_SYM_MORTON:
             check(lib().tc_set_mac(self._h, _lib.TC_MAC_BMAX))
         if mac == "bmax_adaptive":
             check(lib().tc_set_adaptive_order(self._h, float(slack)))
+        if leaf_p2p:
+            check(lib().tc_set_leaf_p2p(self._h, int(leaf_p2p)))
         self.maxChildren = max_children
         self._cfg_depth = cfg.depth
         self._theta = theta

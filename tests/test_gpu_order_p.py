@@ -116,3 +116,29 @@ def test_adaptive_order_keeps_the_error_of_fixed_order(order):
         s.close()
     print(order, meds)
     assert meds["bmax_adaptive"] < 1.5 * meds["bmax"]
+
+
+def test_leaf_p2p_switch_is_at_least_as_accurate():
+    """tc_set_leaf_p2p: accepted leaf pairs with few particle pairs are summed
+    directly; fewer M2L pairs, more P2P pairs, and no loss of accuracy."""
+    n = 65536
+    pos = datasets.two_disks(n, seed=41).astype(np.float64)
+    rows = np.random.default_rng(3).choice(n, 1024, replace=False)
+    fd, _ = direct(pos, kernel="gravity", softening=1e-3, precision="fp64", rows=rows)
+    out = {}
+    for cut in (0, 64):
+        s = NBodySolverFMM_SYM_MORTON("gravity", max_children=16, tree_depth=9, theta=0.7, softening=1e-3, order=8,
+                                      mac="bmax", leaf_p2p=cut)
+        pts = Points.from_positions(pos)
+        s.updateTree(pts, pos.min(0), pos.max(0))
+        s.solveNbody(0.0, pts)
+        g = np.zeros_like(pos)
+        g[pts.ID] = pts.derivative
+        out[cut] = (float(np.median(np.linalg.norm(g[rows] - fd, axis=1) / np.linalg.norm(fd, axis=1))), s.counters())
+        s.close()
+    print(out)
+    assert out[64][1]["m2l"] < out[0][1]["m2l"] and out[64][1]["p2p_pairs"] > out[0][1]["p2p_pairs"]
+    assert out[64][0] <= out[0][0] * 1.05
+    from masterthesislucas_gb300._lib import TreecodeError
+    with pytest.raises(TreecodeError):
+        NBodySolverFMM_SYM_MORTON("tsne", leaf_p2p=64)  # reference order keeps its interaction set
