@@ -82,6 +82,7 @@ def lib():
         L.orc_direct_rows.argtypes = [I, D, I64, P, I64, P, P, I]
         L.orc_bh.argtypes = [I, D, I, D, I64, P, P, P]
         L.orc_bhmp.argtypes = [I, D, I, D, I64, P, P, P]
+        L.orc_pm.argtypes = [I, D, I, I64, P, P, P]
         L.orc_bh.restype = I
         L.orc_tsne_attractive.argtypes = [I64, P, P, P, P, D, P]
         L.orc_tsne_step.argtypes = [I64, P, P, P, P, P, I, I, D, D, D, D, P, P, P]
@@ -100,6 +101,7 @@ def ref_lib():
         R.ref_naive.argtypes = [I, D, I64, P, P, P]
         R.ref_bh.argtypes = [I, D, I, D, I64, P, P, P, P]
         R.ref_bhmp.argtypes = [I, D, I, D, I64, P, P, P]
+        R.ref_pm.argtypes = [I, D, I, I64, P, P, P]
         _ref = R
     return _ref
 
@@ -158,6 +160,29 @@ def bhmp(pos, *, kernel=KERNEL_TSNE, eps=0.0, max_children=16, theta=0.5):
     g = np.zeros_like(pos)
     tot = np.zeros(1)
     lib().orc_bhmp(kernel, eps, max_children, theta, len(pos), _p(pos), _p(g), _p(tot))
+    return g, float(tot[0])
+
+
+def pm(pos, *, n_interp=4, cell_size=1.0, min_intervals=4):
+    """NBodySolverPM (FFT-accelerated interpolation t-SNE repulsion), input order."""
+    pos = np.ascontiguousarray(pos, np.float64)
+    g = np.zeros_like(pos)
+    tot = np.zeros(1)
+    rc = lib().orc_pm(n_interp, cell_size, min_intervals, len(pos), _p(pos), _p(g), _p(tot))
+    if rc != 0:
+        raise ValueError("orc_pm: invalid arguments")
+    return g, float(tot[0])
+
+
+def ref_pm(pos, *, n_interp=4, cell_size=1.0, min_intervals=4):
+    """The reference's own NBodySolverPM (oracle/_ref), or None where it was not built."""
+    R = ref_lib()
+    if R is None:
+        return None
+    pos = np.ascontiguousarray(pos, np.float64)
+    g = np.zeros_like(pos)
+    tot = np.zeros(1)
+    R.ref_pm(n_interp, cell_size, min_intervals, len(pos), _p(pos), _p(g), _p(tot))
     return g, float(tot[0])
 
 

@@ -1233,3 +1233,226 @@ void orc_tsne_step(int64_t n, const double* y, const double* y_prev, const uint3
     free(ps);
     free(gs);
 }
+
+/* ------------------------------------------------------------------ particle mesh
+ * NBodySolverPM::computeFftGradient (nBodySolverPM.h:763-1039) with its helpers
+ * precompute_2d (:686-760), n_body_fft_2d (:413-682) and interpolate (:380-410):
+ * the published FFT-accelerated interpolation scheme (Linderman et al.,
+ * FIt-SNE).  The square [min, max]^2 holds nb x nb boxes of p Lagrange nodes per
+ * dimension (p equispaced nodes at (k + 1/2)/p of the box); the charges
+ * (1, x, y, x^2 + y^2) are spread to the nodes, convolved with the squared
+ * Cauchy kernel (1 + r^2)^-2 on the uniform node grid through a zero-padded 2D
+ * DFT (a plain row/column DFT here; FFTW in the reference), and interpolated
+ * back.  min/max follow the reference's single pass with `else if`: a value
+ * that raises the running maximum is never taken for the minimum.           */
+typedef struct {
+    double re, im;
+} orc_c;
+
+static void pm_dft_r2c(int n, const double* in, orc_c* out, const double* cs, const double* sn)
+{
+    /* n x n real -> n x (n/2+1) complex, exp(-2 pi i (ia + kb)/n) */
+    const int h = n / 2 + 1;
+    orc_c* rows = (orc_c*)malloc((size_t)n * h * sizeof(orc_c));
+    for (int a = 0; a < n; a++)
+        for (int k = 0; k < h; k++) {
+            double re = 0.0, im = 0.0;
+            for (int b = 0; b < n; b++) {
+                const int t = (int)(((int64_t)k * b) % n);
+                re += in[(size_t)a * n + b] * cs[t];
+                im -= in[(size_t)a * n + b] * sn[t];
+            }
+            rows[(size_t)a * h + k].re = re;
+            rows[(size_t)a * h + k].im = im;
+        }
+    for (int k = 0; k < h; k++)
+        for (int i = 0; i < n; i++) {
+            double re = 0.0, im = 0.0;
+            for (int a = 0; a < n; a++) {
+                const int t = (int)(((int64_t)i * a) % n);
+                const orc_c v = rows[(size_t)a * h + k];
+                re += v.re * cs[t] + v.im * sn[t];
+                im += v.im * cs[t] - v.re * sn[t];
+            }
+            out[(size_t)i * h + k].re = re;
+            out[(size_t)i * h + k].im = im;
+        }
+    free(rows);
+}
+
+static void pm_dft_c2r(int n, const orc_c* in, double* out, const double* cs, const double* sn)
+{
+    /* unnormalised inverse of pm_dft_r2c */
+    const int h = n / 2 + 1;
+    orc_c* cols = (orc_c*)malloc((size_t)n * h * sizeof(orc_c));
+    for (int k = 0; k < h; k++)
+        for (int a = 0; a < n; a++) {
+            double re = 0.0, im = 0.0;
+            for (int i = 0; i < n; i++) {
+                const int t = (int)(((int64_t)i * a) % n);
+                const orc_c v = in[(size_t)i * h + k];
+                re += v.re * cs[t] - v.im * sn[t];
+                im += v.im * cs[t] + v.re * sn[t];
+            }
+            cols[(size_t)a * h + k].re = re;
+            cols[(size_t)a * h + k].im = im;
+        }
+    for (int a = 0; a < n; a++)
+        for (int b = 0; b < n; b++) {
+            double s = cols[(size_t)a * h].re;
+            int kmax = h - 1;
+            if (n % 2 == 0) {
+                s += cols[(size_t)a * h + n / 2].re * ((b & 1) ? -1.0 : 1.0);
+                kmax = n / 2 - 1;
+            }
+            for (int k = 1; k <= kmax; k++) {
+                const int t = (int)(((int64_t)k * b) % n);
+                const orc_c v = cols[(size_t)a * h + k];
+                s += 2.0 * (v.re * cs[t] - v.im * sn[t]);
+            }
+            out[(size_t)a * n + b] = s;
+        }
+    free(cols);
+}
+
+/* Lagrange basis values of the p nodes sp[] at t (interpolate, :380-410) */
+static void pm_lagrange(int p, const double* sp, const double* den, double t, double* v)
+{
+    for (int j = 0; j < p; j++) {
+        double num = 1.0;
+        for (int k = 0; k < p; k++)
+            if (j != k) num *= t - sp[k];
+        v[j] = num / den[j];
+    }
+}
+
+int orc_pm(int p, double cell_size, int min_intervals, int64_t n, const double* pos, double* grad,
+           double* total)
+{
+    if (n <= 0 || p < 1 || p > 16) return -1;
+    const double inf = (double)(float)(1e300 * 1e300);
+    double mn = inf, mx = -inf;
+    for (int64_t i = 0; i < n; i++)
+        for (int a = 0; a < 2; a++) {
+            const double v = pos[2 * i + a];
+            if (v > mx) mx = v;
+            else if (v < mn) mn = v;
+        }
+    int nb = (int)((mx - mn) / cell_size);
+    if (nb < min_intervals) nb = min_intervals;
+    const double bw = (mx - mn) / (double)nb;
+    /* node spacings inside a box, and the node coordinates of the whole grid */
+    double sp[16], den[16];
+    const double hs = 1.0 / (double)p;
+    sp[0] = hs / 2;
+    for (int i = 1; i < p; i++) sp[i] = sp[i - 1] + hs;
+    for (int i = 0; i < p; i++) {
+        den[i] = 1.0;
+        for (int j = 0; j < p; j++)
+            if (i != j) den[i] *= sp[i] - sp[j];
+    }
+    const int n1 = p * nb, nf = 2 * n1, hf = nf / 2 + 1;
+    double* xt = (double*)malloc((size_t)n1 * sizeof(double));
+    const double hw = hs * bw;
+    xt[0] = mn + hw / 2;
+    for (int i = 1; i < n1; i++) xt[i] = xt[i - 1] + hw;
+    /* the kernel on the node grid, mirrored into the zero-padded circulant generator */
+    double* cs = (double*)malloc((size_t)nf * sizeof(double));
+    double* sn = (double*)malloc((size_t)nf * sizeof(double));
+    for (int t = 0; t < nf; t++) {
+        const double ang = 2.0 * 3.14159265358979323846 * (double)t / (double)nf;
+        cs[t] = cos(ang);
+        sn[t] = sin(ang);
+    }
+    double* kt = (double*)calloc((size_t)nf * nf, sizeof(double));
+    for (int i = 0; i < n1; i++)
+        for (int j = 0; j < n1; j++) {
+            const double dy = xt[0] - xt[i], dx = xt[0] - xt[j];
+            const double v = pow(1.0 + pow(dy, 2) + pow(dx, 2), -2);
+            kt[(size_t)(n1 + i) * nf + (n1 + j)] = v;
+            kt[(size_t)(n1 - i) * nf + (n1 + j)] = v;
+            kt[(size_t)(n1 + i) * nf + (n1 - j)] = v;
+            kt[(size_t)(n1 - i) * nf + (n1 - j)] = v;
+        }
+    orc_c* kf = (orc_c*)malloc((size_t)nf * hf * sizeof(orc_c));
+    pm_dft_r2c(nf, kt, kf, cs, sn);
+    /* boxes, in-box coordinates and interpolation weights of every point */
+    int* bx = (int*)malloc((size_t)n * sizeof(int));
+    int* by = (int*)malloc((size_t)n * sizeof(int));
+    double* wx = (double*)malloc((size_t)n * p * sizeof(double));
+    double* wy = (double*)malloc((size_t)n * p * sizeof(double));
+    for (int64_t i = 0; i < n; i++) {
+        const double x = pos[2 * i], y = pos[2 * i + 1];
+        int ix = (int)((x - mn) / bw), iy = (int)((y - mn) / bw);
+        ix = ix >= nb ? nb - 1 : (ix < 0 ? 0 : ix);
+        iy = iy >= nb ? nb - 1 : (iy < 0 ? 0 : iy);
+        bx[i] = ix;
+        by[i] = iy;
+        const double x0 = ix * bw + mn, y0 = iy * bw + mn;
+        pm_lagrange(p, sp, den, (x - x0) / bw, wx + (size_t)i * p);
+        pm_lagrange(p, sp, den, (y - y0) / bw, wy + (size_t)i * p);
+    }
+    /* spread the four charges: node row = x node, column = y node */
+    double* w = (double*)calloc((size_t)n1 * n1 * 4, sizeof(double));
+    for (int64_t i = 0; i < n; i++) {
+        const double x = pos[2 * i], y = pos[2 * i + 1];
+        const double q[4] = {1.0, x, y, x * x + y * y};
+        for (int a = 0; a < p; a++)
+            for (int b = 0; b < p; b++) {
+                const size_t idx = (size_t)(bx[i] * p + a) * n1 + (size_t)(by[i] * p + b);
+                for (int d = 0; d < 4; d++) w[idx * 4 + d] += wy[(size_t)i * p + b] * wx[(size_t)i * p + a] * q[d];
+            }
+    }
+    /* convolve each charge with the kernel */
+    double* fin = (double*)malloc((size_t)nf * nf * sizeof(double));
+    orc_c* fw = (orc_c*)malloc((size_t)nf * hf * sizeof(orc_c));
+    double* fout = (double*)malloc((size_t)nf * nf * sizeof(double));
+    double* pot_grid = (double*)malloc((size_t)n1 * n1 * 4 * sizeof(double));
+    for (int d = 0; d < 4; d++) {
+        memset(fin, 0, (size_t)nf * nf * sizeof(double));
+        for (int i = 0; i < n1; i++)
+            for (int j = 0; j < n1; j++) fin[(size_t)i * nf + j] = w[((size_t)i * n1 + j) * 4 + d];
+        pm_dft_r2c(nf, fin, fw, cs, sn);
+        for (size_t k = 0; k < (size_t)nf * hf; k++) {
+            const double x_ = fw[k].re, y_ = fw[k].im, u_ = kf[k].re, v_ = kf[k].im;
+            fw[k].re = x_ * u_ - y_ * v_;
+            fw[k].im = x_ * v_ + y_ * u_;
+        }
+        pm_dft_c2r(nf, fw, fout, cs, sn);
+        for (int i = 0; i < n1; i++)
+            for (int j = 0; j < n1; j++)
+                pot_grid[((size_t)i * n1 + j) * 4 + d] = fout[(size_t)(n1 + i) * nf + (n1 + j)] / (double)((int64_t)nf * nf);
+    }
+    /* interpolate the potentials back, then Z and the repulsive gradient */
+    double sum_q = 0.0;
+    for (int64_t i = 0; i < n; i++) {
+        double phi[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int a = 0; a < p; a++)
+            for (int b = 0; b < p; b++) {
+                const size_t idx = (size_t)(bx[i] * p + a) * n1 + (size_t)(by[i] * p + b);
+                for (int d = 0; d < 4; d++)
+                    phi[d] += wx[(size_t)i * p + a] * wy[(size_t)i * p + b] * pot_grid[idx * 4 + d];
+            }
+        const double x = pos[2 * i], y = pos[2 * i + 1];
+        sum_q += (1 + x * x + y * y) * phi[0] - 2 * (x * phi[1] + y * phi[2]) + phi[3];
+        /* the reference stores dC = -(x phi1 - phi2) and returns derivative = -dC */
+        grad[2 * i] = x * phi[0] - phi[1];
+        grad[2 * i + 1] = y * phi[0] - phi[2];
+    }
+    *total = sum_q - (double)n;
+    free(xt);
+    free(cs);
+    free(sn);
+    free(kt);
+    free(kf);
+    free(bx);
+    free(by);
+    free(wx);
+    free(wy);
+    free(w);
+    free(fin);
+    free(fw);
+    free(fout);
+    free(pot_grid);
+    return 0;
+}

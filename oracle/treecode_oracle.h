@@ -101,6 +101,14 @@ int orc_bh(int kernel, double eps, int max_children, double theta, int64_t n,
 int orc_bhmp(int kernel, double eps, int max_children, double theta, int64_t n,
              const double* pos, double* grad, double* total);
 
+/* NBodySolverPM::solveNbody (nBodySolverPM.h:274-305, computeFftGradient
+ * :763-1039): FFT-accelerated interpolation of the t-SNE repulsion with p
+ * Lagrange nodes per box and boxes of side about cell_size (at least
+ * min_intervals per dimension).  grad (input order) = the reference's
+ * derivative (-dC), *total = the pair sum excluding self pairs.             */
+int orc_pm(int p, double cell_size, int min_intervals, int64_t n, const double* pos, double* grad,
+           double* total);
+
 /* TSNE::updateAttractive (tsne.h:356-381): grad[i] += exag * sum_j P_ij q_ij (y_j - y_i) */
 void orc_tsne_attractive(int64_t n, const uint32_t* row_ptr, const uint32_t* col,
                          const double* val, const double* pos, double exag, double* grad);

@@ -92,6 +92,25 @@ def bhmp_cases():
         save(f"bhmp_{tag}_3000", pos=pos, grad=g, total=t, kernel=kernel, eps=eps, max_children=16, theta=0.5)
 
 
+def pm_cases():
+    """NBodySolverPM: FFT-accelerated interpolation repulsion (the reference built with
+    oracle/fftw_stub.cpp in place of FFTW).  The first point of pm_first_min_800 is the
+    smallest coordinate, which the reference's min/max pass never takes for the minimum."""
+    rng = np.random.default_rng(21)
+    cases = [("pm_gauss_2000", rng.normal(0, 3, (2000, 2)), 1.0, 4),
+             ("pm_wide_3000", rng.normal(0, 8, (3000, 2)), 1.0, 4),
+             ("pm_small_cells_500", rng.normal(0, 1, (500, 2)), 0.3, 4),
+             ("pm_coarse_1000", rng.normal(0, 20, (1000, 2)), 2.0, 4),
+             ("pm_tiny_17", rng.normal(0, 0.5, (17, 2)), 1.0, 4)]
+    first_min = rng.normal(0, 2, (800, 2))
+    first_min[0] = first_min.min() - 1.0
+    cases.append(("pm_first_min_800", first_min, 1.0, 4))
+    for name, pos, cell, mn in cases:
+        pos = np.ascontiguousarray(pos, np.float64)
+        g, t = oracle.ref_pm(pos, n_interp=4, cell_size=cell, min_intervals=mn)
+        save(name, pos=pos, grad=g, total=t, n_interp=4, cell_size=cell, min_intervals=mn)
+
+
 def main():
     if oracle.build_ref() is None:
         raise SystemExit("reference sources not found; fixtures cannot be regenerated")
@@ -118,6 +137,7 @@ def main():
         save(f"bh_{tag}_3000", pos=pos, grad=g, total=t, kernel=kernel, eps=eps, max_children=16,
              theta=0.5)
     bhmp_cases()
+    pm_cases()
     tsne_step_case("tsne_step_600")
 
 
