@@ -220,6 +220,23 @@ int tc_bhmp_solve(int kernel, double softening, int max_children, double theta, 
 int tc_bhmp_solve_device(int kernel, double softening, int max_children, double theta, int precision,
                          const double* d_pos_xy, int64_t n, double* d_grad_xy, double* d_total, void* stream);
 
+/* ---------------------------------------------------------------- particle mesh
+ * NBodySolverPM::solveNbody (src/nbodysolvers/cpu/nBodySolverPM.h:274-305,
+ * computeFftGradient :763-1039): the FFT-accelerated interpolation t-SNE
+ * repulsion (FIt-SNE) in FP64.  Boxes of side about cell_size (at least
+ * min_intervals per dimension) on the square [min, max]^2 of all coordinates
+ * (min/max as the reference's single `if / else if` pass finds them),
+ * n_interp (1..8) Lagrange nodes per box and dimension; the reference's TSNE
+ * passes (4, cell_size, 4) (src/nBodyInstances/tsne.h:116).  grad_xy
+ * (input order) is overwritten with the reference's derivative
+ * (sum_j q_ij^2 (y_i - y_j)), *total with the pair sum over i != j of q_ij,
+ * as the reference overwrites both.  Needs libcufft (loaded at the first
+ * call).                                                                    */
+int tc_pm_solve(int n_interp, double cell_size, int min_intervals, const double* pos_xy, int64_t n,
+                double* grad_xy, double* total);
+int tc_pm_solve_device(int n_interp, double cell_size, int min_intervals, const double* d_pos_xy, int64_t n,
+                       double* d_grad_xy, double* d_total, void* stream);
+
 /* ---------------------------------------------------------------- N-body time step
  * Kick-drift-kick leapfrog on a gravity handle.  The reference's N-body
  * scenes step kick-then-drift around their solver call (2D, commented out:

@@ -55,6 +55,8 @@ SIGNATURES = {
     "tc_set_mac": (_I, [_P, _I]),
     "tc_set_adaptive_order": (_I, [_P, _D]),
     "tc_set_leaf_p2p": (_I, [_P, _I]),
+    "tc_pm_solve": (_I, [_I, _D, _I, _P, _I64, _P, _P]),
+    "tc_pm_solve_device": (_I, [_I, _D, _I, _P, _I64, _P, _P, _P]),
     "tc_get_depth": (_I, [_I, _I64, _P]),
     "tc_node_count": (_I, [ctypes.c_uint32, _P]),
     "tc_update_tree": (_I, [_P, _P, _P, _I64, _P, _P]),

@@ -18,7 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(PKG, "libtreecode.so")
 BUILD = os.path.join(PKG, "_build")
 
-SOURCES = ["scan.cu", "sort.cu", "tree.cu", "tree_p.cu", "lists.cu", "fmm.cu", "fmm_p.cu", "direct.cu", "bh.cu", "mlp.cu", "learned.cu", "tsne.cu", "integrate.cu", "api.cu"]
+SOURCES = ["scan.cu", "sort.cu", "tree.cu", "tree_p.cu", "lists.cu", "fmm.cu", "fmm_p.cu", "direct.cu", "bh.cu", "mlp.cu", "learned.cu", "tsne.cu", "integrate.cu", "pm.cu", "api.cu"]
 NO_FMA = {"tree.cu"}
 # FP32 force kernels: denormals flushed (squared distances never reach them) so
 # that rsqrt/reciprocal map to single SFU instructions

@@ -282,3 +282,37 @@ def barnes_hut(pos, *, kernel="tsne", softening=1e-3, max_children=16, theta=0.5
     check(fn(KERNELS[kernel], softening, max_children, theta, PRECISIONS[precision], ptr(pos), len(pos), ptr(g),
              ctypes.byref(tot)))
     return g, float(tot.value)
+
+
+def particle_mesh(pos, *, n_interp: int = 4, cell_size: float = 1.0, min_intervals: int = 4):
+    """NBodySolverPM::solveNbody on the GPU (FFT-accelerated interpolation
+    t-SNE repulsion, FP64): the reference's derivative sum_j q_ij^2 (y_i - y_j)
+    in input order and the pair sum over i != j of q_ij."""
+    pos = np.ascontiguousarray(pos, np.float64)
+    g = np.zeros_like(pos)
+    tot = ctypes.c_double(0.0)
+    check(lib().tc_pm_solve(int(n_interp), float(cell_size), int(min_intervals), ptr(pos), len(pos), ptr(g),
+                            ctypes.byref(tot)))
+    return g, float(tot.value)
+
+
+class NBodySolverPM:
+    """The reference's NBodySolverPM interface (nBodySolverPM.h:93-305): the
+    constructor takes the interpolation points per box, the box side
+    (cell_size) and the minimum number of boxes per dimension; updateTree does
+    nothing; solveNbody overwrites the points' derivatives and returns the
+    pair sum (the reference overwrites both)."""
+
+    def __init__(self, n_interpolation_points: int = 4, cell_size: float = 1.0, min_num_intervals: int = 4):
+        self.n_interpolation_points = int(n_interpolation_points)
+        self.cell_size = float(cell_size)
+        self.min_num_intervals = int(min_num_intervals)
+
+    def updateTree(self, points, min_pos=None, max_pos=None):
+        pass
+
+    def solveNbody(self, total: float, points: "Points") -> float:
+        g, t = particle_mesh(points.position, n_interp=self.n_interpolation_points, cell_size=self.cell_size,
+                             min_intervals=self.min_num_intervals)
+        points.derivative[:] = g
+        return t
