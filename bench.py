@@ -65,6 +65,8 @@ WORKLOADS = {
                            presteps=5),
     "bhmp_mixture_65k": dict(n=65536, dist="mixture", kernel="gravity", softening=1e-3, max_children=16,
                              method="bh", theta=0.5, multipole=True),
+    "pm_embedding_70k": dict(n=70000, scale=25.0, n_interp=4, cell_size=1.0, min_intervals=4, method="pm",
+                             dist="mixture", kernel="tsne", softening=0.0, max_children=16),
     "bh_mixture_65k": dict(n=65536, dist="mixture", kernel="gravity", softening=1e-3, max_children=16,
                            method="bh", theta=0.5),
 }
@@ -640,6 +642,82 @@ def run_bh(args, w):
     print(json.dumps(line))
 
 
+def run_pm(args, w):
+    """Particle-mesh (FFT-accelerated interpolation) t-SNE repulsion, NBodySolverPM, on the GPU: the
+    reference's settings (4 Lagrange nodes per box, unit boxes, at least 4 boxes per dimension)."""
+    import ctypes
+    import time as _t
+    import torch
+
+    from masterthesislucas_gb300._lib import check, lib, ptr
+
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    n = w["n"]
+    from masterthesislucas_gb300 import datasets
+    pos_h = np.ascontiguousarray(datasets.gaussian_mixture(n, seed=1000).astype(np.float64) * w["scale"])
+    pos_d = torch.from_numpy(pos_h).to(dev)
+    grad_d = torch.zeros((n, 2), dtype=torch.float64, device=dev)
+    tot_d = torch.zeros(1, dtype=torch.float64, device=dev)
+    rows = np.sort(np.random.default_rng(7).choice(n, N_SAMPLES, replace=False)).astype(np.int64)
+    rows_d = torch.from_numpy(rows).to(dev)
+    ref_d = torch.zeros((N_SAMPLES, 2), dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    check(lib().tc_direct_device(0, 0.0, 1, ptr(pos_d), n, ptr(rows_d), N_SAMPLES, ptr(ref_d), None, None))
+    torch.cuda.synchronize()
+    ref = ref_d.cpu().numpy()
+    cs = ctypes.c_void_p(stream.cuda_stream)
+    prm = (w["n_interp"], w["cell_size"], w["min_intervals"])
+
+    def step():
+        check(lib().tc_pm_solve_device(*prm, ptr(pos_d), n, ptr(grad_d), ptr(tot_d), cs))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    with ClockSampler(0) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(k))
+            ev0[k].record(stream)
+            step()
+            ev1[k].record(stream)
+        torch.cuda.synchronize()
+    ms = [ev0[k].elapsed_time(ev1[k]) for k in range(args.steps)]
+    err = median_error(grad_d[rows_d].cpu().numpy(), ref)
+    g_h = np.zeros((n, 2))
+    tot = ctypes.c_double(0.0)
+    e2e = []
+    for k in range(3):
+        t0 = _t.perf_counter()
+        check(lib().tc_pm_solve(*prm, ptr(pos_h), n, ptr(g_h), ctypes.byref(tot)))
+        e2e.append(_t.perf_counter() - t0)
+    import oracle
+    t0 = _t.perf_counter()
+    oracle.pm_numpy(pos_h, n_interp=prm[0], cell_size=prm[1], min_intervals=prm[2])
+    cpu_t = _t.perf_counter() - t0
+    t_total = sum(ms) / 1e3
+    line = {"metric": "particles/s per particle-mesh (NBodySolverPM) repulsion evaluation", "value": n * args.steps / t_total,
+            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded 8-cluster Gaussian mixture scaled to a t-SNE embedding's extent)",
+            "config": {"workload": args.workload, "n": n, "n_interp": prm[0], "cell_size": prm[1],
+                       "min_intervals": prm[2], "extent_scale": w["scale"],
+                       "method": "FFT-accelerated interpolation (FIt-SNE), the reference's grid, cuFFT convolution",
+                       "l2": "256 MB buffer written between timed steps"},
+            "error": {"median": err[0], "p90": err[1], "max": err[2], "vs": "fp64 direct sum", "samples": N_SAMPLES},
+            "e2e": {"value": n / float(np.median(e2e)), "unit": UNIT, "h2d_bytes_per_step": n * 16,
+                    "d2h_bytes_per_step": n * 16 + 8},
+            "clocks": clk.summary(),
+            "cpu_baseline": {"value": n / cpu_t, "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": f"the full {n}-point system, numpy restatement (pocketfft), {cpu_t:.2f} s"}}
+    print(json.dumps(line))
+
+
 def run_tsne(args, w):
     """t-SNE gradient steps (tree repulsion at order p + CSR attractive + Z + momentum), device resident."""
     import torch
@@ -803,6 +881,9 @@ def main():
         return
     if w.get("method") == "bh":
         run_bh(args, w)
+        return
+    if w.get("method") == "pm":
+        run_pm(args, w)
         return
     if w.get("method") == "tsne":
         run_tsne(args, w)

@@ -11,10 +11,14 @@
 //      Lagrange nodes per box and dimension; every point's p + p basis values.
 //   3. The charges (1, x, y, x^2 + y^2) spread to the nodes: points sorted by
 //      box (stable, so each node sums its points in input order like the
-//      reference), one warp per box, one lane per (node, charge) accumulator.
+//      reference), one warp per box, one lane per (node, charge) accumulator,
+//      the box's points staged through shared memory 32 at a time.
 //   4. Convolution with (1 + r^2)^-2 on the uniform node grid: zero-padded
-//      2n1 x 2n1 real FFTs (cuFFT D2Z / Z2D, batched over the four charges),
-//      the reference's complex product, the unnormalised inverse / (2n1)^2.
+//      real FFTs (cuFFT D2Z / Z2D, batched over the four charges) of the
+//      smallest 2,3,5,7-smooth size >= 2n1 (the reference's 2n1 can hold a
+//      large prime factor; the extracted block is the same linear
+//      convolution), the reference's complex product, the unnormalised inverse
+//      divided by the size squared.
 //   5. Potentials interpolated back; gradient x phi1 - phi2, y phi1 - phi3;
 //      Z = sum (1 + |y|^2) phi1 - 2 y.phi_(2,3) + phi4 - N (FP64, fixed order).
 // cuFFT is loaded at the first call (dlopen), so the rest of the library does
@@ -210,33 +214,66 @@ __global__ void k_pm_box_ranges(const uint32_t* __restrict__ skey, int64_t n, ui
 
 // one warp per box: accumulator u = ((a p) + b) 4 + d (x node a, y node b,
 // charge d) sums its box's points in input order and lands on node row
-// bx p + a, column by p + b of charge d's zero-padded FFT input
-__global__ void k_pm_spread(const double2* __restrict__ pos, const uint32_t* __restrict__ perm,
-                            const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bend,
-                            const double* __restrict__ wx, const double* __restrict__ wy, PmGrid g,
-                            double* __restrict__ fin)
+// bx p + a, column by p + b of charge d's zero-padded FFT input.  The box's
+// points are staged 32 at a time in shared memory (one lane each), so the
+// accumulators' sequential sums read no dependent global loads.
+constexpr int kPmSpreadWarps = 4;
+constexpr int kPmAccPerLane = kPmMaxInterp * kPmMaxInterp * 4 / 32;
+
+__global__ void __launch_bounds__(32 * kPmSpreadWarps)
+    k_pm_spread(const double2* __restrict__ pos, const uint32_t* __restrict__ perm,
+                const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bend,
+                const double* __restrict__ wx, const double* __restrict__ wy, PmGrid g, double* __restrict__ fin)
 {
-    const int lane = threadIdx.x & 31;
+    __shared__ double s_q[kPmSpreadWarps][32][4];
+    __shared__ double s_wx[kPmSpreadWarps][32][kPmMaxInterp];
+    __shared__ double s_wy[kPmSpreadWarps][32][kPmMaxInterp];
+    const int lane = threadIdx.x & 31, wv = threadIdx.x >> 5;
     const int64_t nbox = (int64_t)g.nb * g.nb;
     const int nacc = g.p * g.p * 4;
     const size_t plane = (size_t)g.nf * g.nf;
-    const int64_t wstride = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t box = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); box < nbox; box += wstride) {
+    const int64_t wstride = (int64_t)gridDim.x * kPmSpreadWarps;
+    for (int64_t box = blockIdx.x * (int64_t)kPmSpreadWarps + wv; box < nbox; box += wstride) {
         const uint32_t k0 = bstart[box], k1 = bend[box];
         if (k1 <= k0) continue;
         const int bx = (int)(box % g.nb), by = (int)(box / g.nb);
-        for (int u0 = 0; u0 < nacc; u0 += 32) {
-            const int u = u0 + lane;
-            const int d = u & 3, ab = u >> 2, a = ab / g.p, b = ab % g.p;
-            double acc = 0.0;
-            if (u < nacc)
-                for (uint32_t k = k0; k < k1; k++) {
-                    const uint32_t i = perm[k];
-                    const double2 q = pos[i];
-                    const double c = d == 0 ? 1.0 : (d == 1 ? q.x : (d == 2 ? q.y : q.x * q.x + q.y * q.y));
-                    acc += wy[(size_t)i * g.p + b] * wx[(size_t)i * g.p + a] * c;
+        double acc[kPmAccPerLane];
+#pragma unroll
+        for (int t = 0; t < kPmAccPerLane; t++) acc[t] = 0.0;
+        for (uint32_t c0 = k0; c0 < k1; c0 += 32) {
+            const uint32_t m = min(32u, k1 - c0);
+            if ((uint32_t)lane < m) {
+                const uint32_t i = perm[c0 + lane];
+                const double2 q = pos[i];
+                s_q[wv][lane][0] = 1.0;
+                s_q[wv][lane][1] = q.x;
+                s_q[wv][lane][2] = q.y;
+                s_q[wv][lane][3] = q.x * q.x + q.y * q.y;
+                for (int a = 0; a < g.p; a++) {
+                    s_wx[wv][lane][a] = wx[(size_t)i * g.p + a];
+                    s_wy[wv][lane][a] = wy[(size_t)i * g.p + a];
                 }
-            if (u < nacc) fin[d * plane + (size_t)(bx * g.p + a) * g.nf + (size_t)(by * g.p + b)] = acc;
+            }
+            __syncwarp();
+#pragma unroll
+            for (int t = 0; t < kPmAccPerLane; t++) {
+                const int u = lane + 32 * t;
+                if (u < nacc) {
+                    const int d = u & 3, ab = u >> 2, a = ab / g.p, b = ab % g.p;
+                    double s = acc[t];
+                    for (uint32_t j = 0; j < m; j++) s += s_wy[wv][j][b] * s_wx[wv][j][a] * s_q[wv][j][d];
+                    acc[t] = s;
+                }
+            }
+            __syncwarp();
+        }
+#pragma unroll
+        for (int t = 0; t < kPmAccPerLane; t++) {
+            const int u = lane + 32 * t;
+            if (u < nacc) {
+                const int d = u & 3, ab = u >> 2, a = ab / g.p, b = ab % g.p;
+                fin[d * plane + (size_t)(bx * g.p + a) * g.nf + (size_t)(by * g.p + b)] = acc[t];
+            }
         }
     }
 }
@@ -329,6 +366,16 @@ struct PmRelease {
     }
 };
 
+int smooth_size(int n)
+{
+    for (int m = n;; m++) {
+        int r = m;
+        for (int f : {2, 3, 5, 7})
+            while (r % f == 0) r /= f;
+        if (r == 1) return m;
+    }
+}
+
 int pm_plan(CufftApi& api, std::map<int, cufftHandle>& cache, int nf, cufftType type, int batch, cufftHandle* out)
 {
     auto it = cache.find(nf);
@@ -413,7 +460,10 @@ int pm_solve_device(int n_interp, double cell_size, int min_intervals, const dou
             if (i != j) g.den[i] *= g.sp[i] - g.sp[j];
     }
     g.n1 = g.p * g.nb;
-    g.nf = 2 * g.n1;
+    // any transform size >= 2 n1 holds the same linear convolution on the extracted
+    // [n1, 2 n1) block (the kernel generator is laid out around n1 either way); the
+    // smallest size >= 2 n1 with factors 2, 3, 5, 7 avoids slow prime-length FFTs
+    g.nf = smooth_size(2 * g.n1);
     const size_t plane = (size_t)g.nf * g.nf, nspec = (size_t)g.nf * (g.nf / 2 + 1);
     if (plane * 8 * 10 > ((size_t)48 << 30)) {
         tc_set_error("particle mesh: FFT grid %d x %d too large", g.nf, g.nf);
@@ -447,7 +497,7 @@ int pm_solve_device(int n_interp, double cell_size, int min_intervals, const dou
     k_pm_box_ranges<<<grid_for(n, 256), 256, 0, s>>>(P<uint32_t>(w.skey), n, P<uint32_t>(w.bstart),
                                                     P<uint32_t>(w.bend));
     TC_CUDA_TRY(cudaMemsetAsync(w.fin.p, 0, 4 * plane * 8, s));
-    k_pm_spread<<<grid_for(nbox * 32, 128), 128, 0, s>>>(pos2, P<uint32_t>(w.perm), P<uint32_t>(w.bstart),
+    k_pm_spread<<<grid_for(nbox, kPmSpreadWarps), 32 * kPmSpreadWarps, 0, s>>>(pos2, P<uint32_t>(w.perm), P<uint32_t>(w.bstart),
                                                         P<uint32_t>(w.bend), P<double>(w.wx), P<double>(w.wy), g,
                                                         P<double>(w.fin));
     // 4. the kernel's spectrum and the four convolutions

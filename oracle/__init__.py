@@ -174,6 +174,72 @@ def pm(pos, *, n_interp=4, cell_size=1.0, min_intervals=4):
     return g, float(tot[0])
 
 
+def pm_numpy(pos, *, n_interp=4, cell_size=1.0, min_intervals=4):
+    """The same NBodySolverPM restatement vectorised with numpy (pocketfft for the
+    transforms): the CPU baseline of the particle-mesh workload.  Same grid and
+    node sums as orc_pm; differs only in FFT rounding."""
+    pos = np.ascontiguousarray(pos, np.float64)
+    n, p = len(pos), int(n_interp)
+    v = pos.reshape(-1)
+    prefix = np.concatenate([[-np.inf], np.maximum.accumulate(v)[:-1]])
+    record = v > prefix                       # the reference's `if (v > max)` branch
+    mx = float(v.max())
+    rest = v[~record]
+    mn = float(rest.min()) if rest.size else float("inf")
+    nb = max(int(min_intervals), int((mx - mn) / cell_size))
+    bw = (mx - mn) / nb
+    hs = 1.0 / p
+    sp = [hs / 2]
+    for _ in range(1, p):
+        sp.append(sp[-1] + hs)
+    sp = np.array(sp)
+    den = np.array([np.prod([sp[i] - sp[j] for j in range(p) if j != i]) for i in range(p)])
+    n1, nf = p * nb, 2 * p * nb
+    xt = [mn + hs * bw / 2]
+    for _ in range(1, n1):
+        xt.append(xt[-1] + hs * bw)
+    xt = np.array(xt)
+    d = xt[0] - xt
+    ker = (1.0 + d[:, None] ** 2 + d[None, :] ** 2) ** -2
+    kt = np.zeros((nf, nf))
+    kt[n1:, n1:] = ker
+    kt[n1:0:-1, n1:] = ker[: n1]
+    kt[n1:, n1:0:-1] = ker[:, : n1]
+    kt[n1:0:-1, n1:0:-1] = ker[: n1, : n1]
+    kf = np.fft.rfft2(kt)
+    ix = np.clip(((pos[:, 0] - mn) / bw).astype(np.int64), 0, nb - 1)
+    iy = np.clip(((pos[:, 1] - mn) / bw).astype(np.int64), 0, nb - 1)
+
+    def lagrange(t):
+        out = np.ones((len(t), p))
+        for j in range(p):
+            for k in range(p):
+                if j != k:
+                    out[:, j] *= t - sp[k]
+            out[:, j] /= den[j]
+        return out
+
+    wx = lagrange((pos[:, 0] - (ix * bw + mn)) / bw)
+    wy = lagrange((pos[:, 1] - (iy * bw + mn)) / bw)
+    q = [np.ones(n), pos[:, 0], pos[:, 1], pos[:, 0] * pos[:, 0] + pos[:, 1] * pos[:, 1]]
+    phi = np.zeros((4, n))
+    for dd in range(4):
+        grid = np.zeros((n1, n1))
+        for a in range(p):
+            for b in range(p):
+                np.add.at(grid, (ix * p + a, iy * p + b), wy[:, b] * wx[:, a] * q[dd])
+        fin = np.zeros((nf, nf))
+        fin[:n1, :n1] = grid
+        pot = np.fft.irfft2(np.fft.rfft2(fin) * kf, s=(nf, nf))[n1:, n1:]
+        for a in range(p):
+            for b in range(p):
+                phi[dd] += wx[:, a] * wy[:, b] * pot[ix * p + a, iy * p + b]
+    x, y = pos[:, 0], pos[:, 1]
+    grad = np.stack([x * phi[0] - phi[1], y * phi[0] - phi[2]], axis=1)
+    total = float(np.sum((1 + x * x + y * y) * phi[0] - 2 * (x * phi[1] + y * phi[2]) + phi[3]) - n)
+    return grad, total
+
+
 def ref_pm(pos, *, n_interp=4, cell_size=1.0, min_intervals=4):
     """The reference's own NBodySolverPM (oracle/_ref), or None where it was not built."""
     R = ref_lib()

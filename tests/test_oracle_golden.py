@@ -90,6 +90,16 @@ def test_pm_matches_reference(golden, case):
     assert total == pytest.approx(float(g["total"]), rel=1e-12)
 
 
+@pytest.mark.parametrize("case", PM_CASES)
+def test_pm_numpy_baseline_matches_reference(golden, case):
+    """The vectorised numpy restatement timed as the PM workload's CPU baseline."""
+    g = golden(case)
+    grad, total = oracle.pm_numpy(g["pos"], n_interp=int(g["n_interp"]), cell_size=float(g["cell_size"]),
+                                  min_intervals=int(g["min_intervals"]))
+    assert np.abs(grad - g["grad"]).max() <= 1e-11 * np.abs(g["grad"]).max()
+    assert total == pytest.approx(float(g["total"]), rel=1e-12)
+
+
 def test_pm_min_max_quirk(golden):
     """The reference's min/max pass skips the first value for the minimum
     (`else if`): the box grid starts above the first point, which is clamped
