@@ -308,6 +308,15 @@ int tc_tsne_destroy(tc_tsne* t);
 int tc_tsne_set_theta(tc_tsne* t, double theta);
 /* tree depth of the next steps (0..15); the reference derives it from N */
 int tc_tsne_set_depth(tc_tsne* t, int depth);
+/* The repulsion of the next steps: the tree solver of the handle's config
+ * (TC_REPULSION_TREE, the default) or the particle-mesh solver with the
+ * reference's TSNE settings (TC_REPULSION_PM: 4 nodes per box, boxes of side
+ * cell_size, at least 4 per dimension; nBodySelect "PM", tsne.h:116, whose
+ * cell_size TSNE::setCellSizeForAll changes).  Particle-mesh systems cannot
+ * join a batch (their grid is sized on the host every step).              */
+#define TC_REPULSION_TREE 0
+#define TC_REPULSION_PM 1
+int tc_tsne_set_repulsion(tc_tsne* t, int method, double cell_size);
 /* One TSNE_buffers::timeStep (tsne_buffers.h:125-168): updateTree on the
  * current embedding, updateRepulsive (tsne.h:287-301), updateAttractive
  * (:356-381) with factor exag_code (the reference uses 16 for the first 250

@@ -26,6 +26,8 @@ TC_PREC_FP64 = 1
 TC_VARIANT_SYM = 0
 TC_VARIANT_MORTON = 1
 TC_MAC_CELL = 0
+TC_REPULSION_TREE = 0
+TC_REPULSION_PM = 1
 TC_MAC_BMAX = 1
 
 
@@ -56,6 +58,7 @@ SIGNATURES = {
     "tc_set_adaptive_order": (_I, [_P, _D]),
     "tc_set_leaf_p2p": (_I, [_P, _I]),
     "tc_pm_solve": (_I, [_I, _D, _I, _P, _I64, _P, _P]),
+    "tc_tsne_set_repulsion": (_I, [_P, _I, _D]),
     "tc_pm_solve_device": (_I, [_I, _D, _I, _P, _I64, _P, _P, _P]),
     "tc_get_depth": (_I, [_I, _I64, _P]),
     "tc_node_count": (_I, [ctypes.c_uint32, _P]),

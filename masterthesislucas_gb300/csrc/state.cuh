@@ -120,6 +120,9 @@ int build_multipoles(Handle& h);
 // gather of the sorted particles
 int morton_p(Handle& h, const double* d_pos, int64_t n, double maxx, double maxy);
 int build_records_p(Handle& h, double hleaf);
+// particle-mesh t-SNE repulsion (pm.cu): gradient in input order and Z
+int pm_solve_device(int n_interp, double cell_size, int min_intervals, const double* d_pos, int64_t n, double* d_grad,
+                    double* d_total, cudaStream_t s);
 int prepare_nosync(Handle& h);
 
 }  // namespace tc

@@ -84,6 +84,8 @@ struct tc_tsne {
     double* h_prm = nullptr;  // pinned staging of {exag, lr, momentum}
     double last_z = 0.0;
     int launches = 0;
+    // repulsion by the particle-mesh solver instead of the tree (cell_size > 0)
+    double pm_cell = 0.0;
 };
 
 namespace tc {
@@ -97,14 +99,22 @@ int tsne_enqueue(tc_tsne* t, const double* prm, const double* lrp, const double*
 {
     Handle& h = *t->hs;
     const double* y = P<double>(t->y[t->cur]);
-    int rc = box ? tc_update_tree_device(t->solver, y, t->n, box, box + 2)
+    int rc, launches = 0;
+    if (t->pm_cell > 0.0) {
+        // the reference's TSNE with nBodySelect "PM" (tsne.h:116: 4 nodes, cell_size, 4 boxes)
+        if ((rc = pm_solve_device(4, t->pm_cell, 4, y, t->n, P<double>(t->grad_rep), P<double>(t->z), h.stream)))
+            return rc;
+        launches = 40;
+    } else {
+        rc = box ? tc_update_tree_device(t->solver, y, t->n, box, box + 2)
                  : tc_update_tree_device(t->solver, y, t->n, nullptr, nullptr);
-    if (rc) return rc;
-    int launches = h.launches;
-    TC_CUDA_TRY(cudaMemsetAsync(t->z.p, 0, 8, h.stream));
-    rc = tc_solve_device(t->solver, P<double>(t->grad_rep), P<double>(t->z), 0, 1);
-    if (rc) return rc;
-    launches += h.launches;
+        if (rc) return rc;
+        launches = h.launches;
+        TC_CUDA_TRY(cudaMemsetAsync(t->z.p, 0, 8, h.stream));
+        rc = tc_solve_device(t->solver, P<double>(t->grad_rep), P<double>(t->z), 0, 1);
+        if (rc) return rc;
+        launches += h.launches;
+    }
     if (h.cfg.precision == TC_PREC_FP64)
         k_tsne_attr_update<double, double><<<grid_for(t->n * 32, 256, kSMs * 32), 256, 0, h.stream>>>(
             t->n, P<uint32_t>(t->row_ptr), P<uint32_t>(t->col), P<double>(t->val), P<double2>(t->y[t->cur]),
@@ -216,6 +226,17 @@ int tc_tsne_destroy(tc_tsne* t)
 }
 
 int tc_tsne_set_theta(tc_tsne* t, double theta) { return t ? tc_set_theta(t->solver, theta) : TC_ERR_INVALID; }
+
+int tc_tsne_set_repulsion(tc_tsne* t, int method, double cell_size)
+{
+    if (!t || (method != TC_REPULSION_TREE && method != TC_REPULSION_PM) ||
+        (method == TC_REPULSION_PM && !(cell_size > 0.0))) {
+        tc_set_error("tc_tsne_set_repulsion: invalid arguments");
+        return TC_ERR_INVALID;
+    }
+    t->pm_cell = method == TC_REPULSION_PM ? cell_size : 0.0;
+    return TC_OK;
+}
 
 int tc_tsne_set_depth(tc_tsne* t, int depth)
 {
@@ -457,8 +478,8 @@ int tc_tsne_batch_create(tc_tsne* const* systems, int count, double margin, tc_t
     for (int i = 0; i < count; i++) {
         const tc_tsne* t = systems[i];
         if (!t || t->hs->cfg.device != dev || t->hs->cfg.order == 0 || t->hs->cfg.precision != TC_PREC_FP32 ||
-            t->cur != systems[0]->cur) {
-            tc_set_error("tc_tsne_batch_create: systems must be FP32 order-p solvers on one device, in step");
+            t->cur != systems[0]->cur || t->pm_cell > 0.0) {
+            tc_set_error("tc_tsne_batch_create: systems must be FP32 order-p tree solvers on one device, in step");
             return TC_ERR_INVALID;
         }
     }

@@ -21,7 +21,12 @@ from ._lib import check, lib, ptr
 class TSNE:
     def __init__(self, row_ptr, col, val, y0, *, early_exaggeration: float = 4.0, min_theta: float = 0.5,
                  max_theta: float = 0.5, max_children: int = 16, precision: str = "fp32", device: int = 0,
-                 learn_rate: float | None = None, order: int = 0, depth: int = -1):
+                 learn_rate: float | None = None, order: int = 0, depth: int = -1, repulsion: str = "tree",
+                 cell_size: float = 1.0):
+        """repulsion: "tree" (the handle's FMM) or "pm", the reference's particle-mesh solver
+        (TSNE with nBodySelect "PM": 4 nodes per box, boxes of side cell_size)."""
+        if repulsion not in ("tree", "pm"):
+            raise ValueError("repulsion must be 'tree' or 'pm'")
         y0 = np.ascontiguousarray(y0, np.float64)
         self.n = len(y0)
         self.row_ptr = np.ascontiguousarray(row_ptr, np.uint32)
@@ -39,6 +44,10 @@ class TSNE:
         self._t = ctypes.c_void_p()
         check(lib().tc_tsne_create(ctypes.byref(cfg), self.n, ptr(self.row_ptr), ptr(self.col), ptr(self.val),
                                    ptr(y0), ctypes.byref(self._t)))
+        self.repulsion = repulsion
+        self.cell_size = float(cell_size)
+        if repulsion == "pm":
+            check(lib().tc_tsne_set_repulsion(self._t, _lib.TC_REPULSION_PM, self.cell_size))
         self.order = order
         self.max_children = max_children
         self.learnRate = self.n / 15.0 if learn_rate is None else learn_rate

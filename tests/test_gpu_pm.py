@@ -69,3 +69,27 @@ def test_pm_rejects_bad_input():
     # usable afterwards
     g, _ = particle_mesh(pos)
     assert np.isfinite(g).all()
+
+
+def test_tsne_step_with_particle_mesh_repulsion(golden):
+    """The device t-SNE step with the reference's default repulsion (nBodySelect
+    "PM"): gradient (4/Z) * repulsion + attraction and the momentum update,
+    against the oracle's particle mesh and attractive term."""
+    import oracle
+    from masterthesislucas_gb300.tsne import TSNE
+    g = golden("tsne_step_600")
+    exag = float(g["exag_code"])
+    lr = float(g["lr"])
+    t = TSNE(g["row_ptr"], g["col"], g["val"], g["y0"], early_exaggeration=exag / 4.0, precision="fp64",
+             learn_rate=lr, repulsion="pm", cell_size=1.0)
+    z = t.time_step(with_z=True)
+    y, yp, grad = t.embedding()
+    rep, zr = oracle.pm(g["y0"], cell_size=1.0)
+    expect = rep * (4.0 / zr)
+    oracle.tsne_attractive(np.ascontiguousarray(g["row_ptr"], np.uint32), np.ascontiguousarray(g["col"], np.uint32),
+                           np.ascontiguousarray(g["val"], np.float64), np.ascontiguousarray(g["y0"]), exag, expect)
+    assert z == pytest.approx(zr, rel=1e-10)
+    assert np.abs(grad - expect).max() <= 1e-8 * np.abs(expect).max()
+    np.testing.assert_allclose(y, g["y0"] + lr * expect, rtol=0, atol=1e-8 * np.abs(g["y0"]).max())
+    with pytest.raises(ValueError):
+        TSNE(g["row_ptr"], g["col"], g["val"], g["y0"], repulsion="fmm")
