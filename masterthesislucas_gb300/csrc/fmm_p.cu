@@ -143,6 +143,9 @@ __device__ __forceinline__ void halve_by_degree(float* c)
     for (int k = 0; k < K; k++) c[k] *= 1.0f / (float)(1 << cdeg(k));
 }
 
+// levels of up to this many cells (4^8) shift their children with four lanes per node
+constexpr int64_t kM2mQuadLevelNodes = (int64_t)1 << 16;
+
 // ------------------------------------------------------------------ M2M
 // one thread per node of level l: shift the children's multipoles (child
 // scale h/2) to the node's COM at scale h
@@ -238,6 +241,55 @@ __global__ void __launch_bounds__(128) k_m2m_stream(int l, float hl, const uint3
         for (int c = 0; c < KS / 4; c++)
             o4[c] = make_float4(4 * c < K ? acc[4 * c] : 0.f, 4 * c + 1 < K ? acc[4 * c + 1] : 0.f,
                                 4 * c + 2 < K ? acc[4 * c + 2] : 0.f, 4 * c + 3 < K ? acc[4 * c + 3] : 0.f);
+    }
+}
+
+// coarse levels: four lanes per node, one per child, summed by two butterfly
+// steps (the fine levels keep one thread per node and its children in turn)
+template <int P>
+__global__ void __launch_bounds__(128) k_m2m_quad(int l, float hl, const uint32_t* __restrict__ count,
+                                                  const float* __restrict__ comrel, float* __restrict__ mu,
+                                                  const uint32_t* __restrict__ act, const uint32_t* __restrict__ act_pos)
+{
+    constexpr int K = ncoef(P), KS = kstride(P);
+    const uint32_t li = level_index(l), lc = level_index(l + 1);
+    const int64_t nl = (int64_t)1 << (2 * l);
+    const float ih = 1.0f / hl;
+    const int j = threadIdx.x & 3;
+    const uint32_t k0 = act_pos[li], k1 = act_pos[li + nl];
+    const uint32_t nodes_per_pass = gridDim.x * (blockDim.x >> 2);
+    for (uint32_t base = k0; base < k1; base += nodes_per_pass) {
+        const uint32_t k = base + blockIdx.x * (blockDim.x >> 2) + (threadIdx.x >> 2);
+        const bool valid = k < k1;
+        float acc[K];
+#pragma unroll
+        for (int c = 0; c < K; c++) acc[c] = 0.f;
+        int64_t node = 0;
+        if (valid) {
+            node = act[k];
+            const int64_t i = node - li;
+            const int64_t ch = lc + 4 * i + j;
+            if (count[ch] != 0) {
+                const float px = comrel[2 * node], py = comrel[2 * node + 1];
+                const float ox = (j & 1) ? 0.25f : -0.25f, oy = (j & 2) ? 0.25f : -0.25f;
+                const float dx = ox + (comrel[2 * ch] - px) * ih, dy = oy + (comrel[2 * ch + 1] - py) * ih;
+                if constexpr (P >= 10) {
+                    m2m_child<P>(dx, dy, mu + ch * KS, acc);
+                } else {
+                    float in[K], w[K];
+                    load_coefs<K, KS>(mu + ch * KS, in);
+                    halve_by_degree<K>(in);  // child scale -> parent scale
+                    monomials<P>(dx, dy, w);
+                    shift_up<P>(in, w, acc);
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < K; c++) {
+            acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 1);
+            acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 2);
+        }
+        if (valid && j == 0) store_coefs<K, KS>(mu + node * KS, acc);
     }
 }
 
@@ -387,6 +439,50 @@ __global__ void __launch_bounds__(128) k_m2l_p(int l, float hl, PotParams pp, co
     }
 }
 
+// The coarse levels hold few sink nodes, so one thread per node leaves the GPU
+// idle behind each node's serial list: one warp per node instead, the lanes
+// taking the list's entries in turn (entry e to lane e mod 32) into their own
+// accumulators, then a fixed butterfly sum over the lanes.
+template <int P>
+__global__ void __launch_bounds__(128) k_m2l_warp(int l, float hl, PotParams pp, const uint32_t* __restrict__ nn_ptr,
+                                                  const uint32_t* __restrict__ nn_idx, const float* __restrict__ comrel,
+                                                  const float* __restrict__ mu, float* __restrict__ loc,
+                                                  double* __restrict__ zpart, const uint32_t* __restrict__ act,
+                                                  const uint32_t* __restrict__ act_pos)
+{
+    constexpr int K = ncoef(P), KS = kstride(P);
+    const uint32_t li = level_index(l);
+    const int64_t nl = (int64_t)1 << (2 * l);
+    const float ih = 1.0f / hl;
+    const float2* comrel2 = reinterpret_cast<const float2*>(comrel);
+    const int lane = threadIdx.x & 31;
+    const uint32_t k1 = act_pos[li + nl];
+    const uint32_t wstride = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t k = act_pos[li] + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < k1; k += wstride) {
+        const int64_t na = act[k];
+        const int64_t a = na - li;
+        const uint32_t b0 = nn_ptr[a], b1 = nn_ptr[a + 1];
+        float L[K];
+#pragma unroll
+        for (int c = 0; c < K; c++) L[c] = 0.f;
+        const int iax = (int)compact16((uint32_t)a), iay = (int)compact16((uint32_t)a >> 1);
+        const float2 ca = comrel2[na];
+        for (uint32_t e = b0 + lane; e < b1; e += 32) {
+            const uint32_t b = nn_idx[e];
+            const int64_t nb = li + b;
+            const float2 cb = comrel2[nb];
+            const float Rx = (float)(iax - (int)compact16(b)) + (ca.x - cb.x) * ih;
+            const float Ry = (float)(iay - (int)compact16(b >> 1)) + (ca.y - cb.y) * ih;
+            m2l_acc<P, KS>(Rx, Ry, hl, pp, mu + nb * KS, L);
+        }
+#pragma unroll
+        for (int c = 0; c < K; c++)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) L[c] += __shfl_xor_sync(0xffffffffu, L[c], o);
+        if (lane == 0) m2l_store<K, KS>(na, b0 != b1, pp.kappa, L, mu, loc, zpart);
+    }
+}
+
 // Per-pair orders (the learned controller, or the bounding-radius rule): a
 // node's accepted entries come sorted by order bucket (orders 4, 6, 8, 10,
 // 12) over expansions stored at order PST.  The launch with OLO == 0 writes
@@ -502,6 +598,11 @@ __global__ void __launch_bounds__(128) k_l2l(int l, float hl, const uint32_t* __
         store_coefs<K, kstride(P)>(loc + node * kstride(P), acc);
     }
 }
+
+// levels of up to this many cells (4^8) take a warp per sink node in the M2L
+// (measured: at level 9 of a 4M-particle tree the thread-per-node form is
+// already faster)
+constexpr int64_t kM2lWarpLevelNodes = (int64_t)1 << 16;
 
 // ------------------------------------------------------------------ near field
 constexpr int kNearWarps = 4;
@@ -790,8 +891,14 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
                 mixed = true;
             }
         }
-        if (!mixed)
-            k_m2l_p<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, count, comrel, mu, loc, zp, P<uint32_t>(h.act), P<uint32_t>(h.act_pos));
+        if (!mixed) {
+            if (nl <= kM2lWarpLevelNodes)
+                k_m2l_warp<ORD><<<grid_for(nl * 32, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, comrel, mu, loc, zp,
+                                                                       act, act_pos);
+            else
+                k_m2l_p<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, count, comrel, mu, loc, zp,
+                                                               act, act_pos);
+        }
     }
     for (int l = 1; l <= dep; l++) {
         const int64_t nl = (int64_t)1 << (2 * l);
@@ -839,7 +946,10 @@ int multipoles_p(Handle& h)
         dep, hl(dep), count, P<uint32_t>(h.first), comrel, P<float>(h.prel), P<uint32_t>(h.bigleaf), mu);
     for (int l = dep - 1; l >= 0; l--) {
         const int64_t nl = (int64_t)1 << (2 * l);
-        if constexpr (ORD >= 10)
+        if (nl <= kM2mQuadLevelNodes)
+            k_m2m_quad<ORD><<<grid_for(nl * 4, 128), 128, 0, s>>>(l, hl(l), count, comrel, mu, P<uint32_t>(h.act),
+                                                                  P<uint32_t>(h.act_pos));
+        else if constexpr (ORD >= 10)
             k_m2m_stream<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, mu, P<uint32_t>(h.act), P<uint32_t>(h.act_pos));
         else
             k_m2m<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, mu, P<uint32_t>(h.act), P<uint32_t>(h.act_pos));
