@@ -62,6 +62,9 @@ __device__ inline bool mac_accept_fast(int dix, int diy, real hl, real thr2, con
     return variant ? mac_accept_m(a, b, len, theta) : mac_accept(a, b, len, inv_theta);
 }
 
+// levels of up to this many cells (4^8) build their lists with a warp per node
+constexpr int64_t kListsWarpLevelNodes = (int64_t)1 << 16;
+
 // Squared-ratio thresholds of the per-pair order rule: an accepted pair with
 // (b_A + b_B)^2 <= t[o] |dcom|^2 takes order bucket o (orders 4, 6, 8, 10, 12);
 // t[o] = (slack theta^(p + 1))^(2 / (q_o + 1)) below the handle's order p,
@@ -234,6 +237,93 @@ __global__ void k_lists(int l, double inv_theta, double theta, int variant, real
             }
         }
         if (!fill) {
+            nn_cnt[a] = nn;
+            near_cnt[a] = nr;
+        }
+    }
+}
+
+// Coarse levels (few sink nodes, long candidate lists per node): one warp per
+// non-empty node, the lanes taking the candidates (parent near entry e, child
+// j) in order 32 at a time; ballots count them and place each accepted /
+// opened entry at its rank, so the lists equal the one-thread form's entry for
+// entry.  FP32 order-p path without per-pair orders; l >= 1.
+__global__ void __launch_bounds__(128) k_lists_warp(int l, double inv_theta, double theta, int variant, float hl,
+                                                    const uint32_t* __restrict__ count,
+                                                    const double2* __restrict__ com64, const float* __restrict__ comrel,
+                                                    const double* __restrict__ bblen,
+                                                    const uint32_t* __restrict__ pnear_ptr,
+                                                    const uint32_t* __restrict__ pnear_idx, uint32_t pcap,
+                                                    uint32_t* __restrict__ nn_cnt, uint32_t* __restrict__ near_cnt,
+                                                    const uint32_t* __restrict__ nn_ptr, uint32_t* __restrict__ nn_idx,
+                                                    uint32_t nn_cap, const uint32_t* __restrict__ near_ptr,
+                                                    uint32_t* __restrict__ near_idx, uint32_t near_cap,
+                                                    uint32_t* __restrict__ ovf, int fill,
+                                                    const uint32_t* __restrict__ act,
+                                                    const uint32_t* __restrict__ act_pos,
+                                                    const float* __restrict__ bmax, float theta2, uint32_t p2p_cut)
+{
+    const uint32_t np = 1u << (2 * (l - 1));
+    const uint32_t li = level_index(l);
+    const int64_t nl = (int64_t)1 << (2 * l);
+    const int lane = threadIdx.x & 31;
+    const uint32_t lt = (1u << lane) - 1u;
+    const uint32_t k1 = act_pos[li + nl];
+    const uint32_t wstride = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t k = act_pos[li] + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < k1; k += wstride) {
+        const int64_t a = (int64_t)act[k] - li;
+        const double2 ca = com64[li + a];
+        const double len = bblen[li + a];
+        const float thr = (float)((len + len) * inv_theta);
+        const float thr2 = thr * thr;
+        const int iax = (int)compact16((uint32_t)a), iay = (int)compact16((uint32_t)a >> 1);
+        const float cra[2] = {comrel[2 * (li + a)], comrel[2 * (li + a) + 1]};
+        const float ba = bmax ? bmax[li + a] : 0.f;
+        const uint32_t ca_n = p2p_cut ? count[li + a] : 0u;
+        const uint32_t p = (uint32_t)(a >> 2);
+        const uint32_t pe0 = pnear_ptr[p], pe1 = pnear_ptr[p + 1] < pcap ? pnear_ptr[p + 1] : pcap;
+        const uint32_t ncand = 4u * (pe1 > pe0 ? pe1 - pe0 : 0u);
+        uint32_t nn = 0, nr = 0;
+        const uint32_t nb0 = fill ? nn_ptr[a] : 0u, rb0 = fill ? near_ptr[a] : 0u;
+        for (uint32_t c0 = 0; c0 < ncand; c0 += 32) {
+            const uint32_t c = c0 + lane;
+            bool valid = false, acc = false;
+            uint32_t b = 0;
+            if (c < ncand) {
+                const uint32_t bp = pnear_idx[pe0 + (c >> 2)];
+                b = 4 * bp + (c & 3);
+                if (bp < np && count[li + b] != 0) {
+                    valid = true;
+                    if (bmax) {
+                        const float dx = (float)(iax - (int)compact16(b)) * hl + (cra[0] - comrel[2 * (li + b)]);
+                        const float dy = (float)(iay - (int)compact16(b >> 1)) * hl + (cra[1] - comrel[2 * (li + b) + 1]);
+                        const float rb = ba + bmax[li + b];
+                        acc = theta2 * fmaf(dx, dx, dy * dy) > rb * rb;
+                    } else {
+                        acc = mac_accept_fast<float>(iax - (int)compact16(b), iay - (int)compact16(b >> 1), hl, thr2,
+                                                     cra, comrel + 2 * (li + b), ca, com64[li + b], len, inv_theta,
+                                                     theta, variant);
+                    }
+                    if (acc && p2p_cut && ca_n * count[li + b] <= p2p_cut) acc = false;
+                }
+            }
+            const uint32_t m_acc = __ballot_sync(0xffffffffu, valid && acc);
+            const uint32_t m_rej = __ballot_sync(0xffffffffu, valid && !acc);
+            if (fill && valid) {
+                if (acc) {
+                    const uint32_t pos = nb0 + nn + __popc(m_acc & lt);
+                    if (pos < nn_cap) nn_idx[pos] = b;
+                    else atomicOr(ovf, 1u);
+                } else {
+                    const uint32_t pos = rb0 + nr + __popc(m_rej & lt);
+                    if (pos < near_cap) near_idx[pos] = b;
+                    else atomicOr(ovf, 1u);
+                }
+            }
+            nn += __popc(m_acc);
+            nr += __popc(m_rej);
+        }
+        if (!fill && lane == 0) {
             nn_cnt[a] = nn;
             near_cnt[a] = nr;
         }
@@ -544,6 +634,14 @@ int build_lists(Handle& h)
             if (!fill && l > 0 && !adapt) {
                 int rc2 = ensure(h.dec, (size_t)pcap * 4 + 64);
                 if (rc2) return rc2;
+            }
+            if (act && !adapt && l > 0 && nl <= kListsWarpLevelNodes) {
+                k_lists_warp<<<grid_for(nl * 32, 128), 128, 0, s>>>(
+                    l, inv_theta, h.cfg.theta, h.variant, (float)hl, P<uint32_t>(h.count), P<double2>(h.com64),
+                    P<float>(h.comrel), P<double>(h.bblen), pnp, pni, pcap, nnc, nrc, nnp, nni, nncap, nrp, nri, nrcap,
+                    ovf_flag, fill, act, act_pos, bmax, (float)(h.cfg.theta * h.cfg.theta),
+                    l == depth ? h.p2p_cut : 0u);
+                return 0;
             }
             k_lists<float><<<grid_for(nl, 128), 128, 0, s>>>(l, inv_theta, h.cfg.theta, h.variant, (float)hl,
                                                             P<uint32_t>(h.count),
