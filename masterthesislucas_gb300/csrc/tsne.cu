@@ -490,7 +490,9 @@ int tc_tsne_batch_create(tc_tsne* const* systems, int count, double margin, tc_t
     b->g.assign(count, {nullptr, nullptr, nullptr});
     b->margin = margin;
     b->device = dev;
-    for (tc_tsne* t : b->sys) t->hs->cap_slack = 0.5;  // fewer overflow re-steps while the embedding grows
+    // list regions twice the last exact totals: while the embeddings grow, a region that
+    // overflows costs an uncaptured re-step and a re-capture of that system
+    for (tc_tsne* t : b->sys) t->hs->cap_slack = 1.0;
     cudaError_t e = cudaStreamCreateWithFlags(&b->s0, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_prm, 64);
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_ext, 64);
