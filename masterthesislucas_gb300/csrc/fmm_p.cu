@@ -568,6 +568,81 @@ __global__ void __launch_bounds__(128) k_m2l_mixed(int l, float hl, PotParams pp
     }
 }
 
+// the same on the coarse levels: a warp per sink node, lanes taking the
+// entries in turn whatever their bucket (each entry evaluated at its own
+// order), then a butterfly sum
+template <int PST, int PACC, int OLO, int OHI>
+__global__ void __launch_bounds__(128) k_m2l_mixed_warp(int l, float hl, PotParams pp,
+                                                        const uint32_t* __restrict__ nn_ptr,
+                                                        const uint32_t* __restrict__ nn_idx,
+                                                        const uint8_t* __restrict__ ord,
+                                                        const float* __restrict__ comrel, const float* __restrict__ mu,
+                                                        float* __restrict__ loc, double* __restrict__ zpart,
+                                                        const uint32_t* __restrict__ act,
+                                                        const uint32_t* __restrict__ act_pos)
+{
+    constexpr int K = ncoef(PACC), KS = kstride(PST);
+    constexpr bool first = OLO == 0;
+    const uint32_t li = level_index(l);
+    const int64_t nl = (int64_t)1 << (2 * l);
+    const float ih = 1.0f / hl;
+    const float2* comrel2 = reinterpret_cast<const float2*>(comrel);
+    const int lane = threadIdx.x & 31;
+    const uint32_t k1 = act_pos[li + nl];
+    const uint32_t wstride = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t k = act_pos[li] + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < k1; k += wstride) {
+        const int64_t na = act[k];
+        const int64_t a = na - li;
+        const uint32_t p0 = nn_ptr[a], b1 = nn_ptr[a + 1];
+        float L[K];
+#pragma unroll
+        for (int c = 0; c < K; c++) L[c] = 0.f;
+        const int iax = (int)compact16((uint32_t)a), iay = (int)compact16((uint32_t)a >> 1);
+        const float2 ca = comrel2[na];
+        bool mine = false;
+        for (uint32_t e = p0 + lane; e < b1; e += 32) {
+            const int o = ord[e];
+            if (o < OLO || o > OHI) continue;
+            mine = true;
+            const uint32_t b = nn_idx[e];
+            const int64_t nb = li + b;
+            const float2 cb = comrel2[nb];
+            const float Rx = (float)(iax - (int)compact16(b)) + (ca.x - cb.x) * ih;
+            const float Ry = (float)(iay - (int)compact16(b >> 1)) + (ca.y - cb.y) * ih;
+            if constexpr (OLO <= 0 && 0 <= OHI && 4 <= PACC) if (o == 0) m2l_acc<4, KS>(Rx, Ry, hl, pp, mu + nb * KS, L);
+            if constexpr (OLO <= 1 && 1 <= OHI && 6 <= PACC) if (o == 1) m2l_acc<6, KS>(Rx, Ry, hl, pp, mu + nb * KS, L);
+            if constexpr (OLO <= 2 && 2 <= OHI && 8 <= PACC) if (o == 2) m2l_acc<8, KS>(Rx, Ry, hl, pp, mu + nb * KS, L);
+            if constexpr (OLO <= 3 && 3 <= OHI && 10 <= PACC) if (o == 3) m2l_acc<10, KS>(Rx, Ry, hl, pp, mu + nb * KS, L);
+            if constexpr (OLO <= 4 && 4 <= OHI && 12 <= PACC) if (o == 4) m2l_acc<12, KS>(Rx, Ry, hl, pp, mu + nb * KS, L);
+        }
+        const bool any = __any_sync(0xffffffffu, mine);
+#pragma unroll
+        for (int c = 0; c < K; c++)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) L[c] += __shfl_xor_sync(0xffffffffu, L[c], o);
+        if (lane != 0) continue;
+        if (first) {
+            m2l_store<K, KS>(na, any, pp.kappa, L, mu, loc, zpart);
+        } else if (any) {
+            const float* m = mu + na * KS;
+            float zs = 0.f;
+#pragma unroll
+            for (int c = 0; c < K; c++) zs += L[c] * m[c];
+            zpart[na] += (double)pp.kappa * (double)zs;
+            float4* o4 = reinterpret_cast<float4*>(loc + na * KS);
+#pragma unroll
+            for (int c = 0; c < KS / 4; c++) {
+                float4 v = o4[c];
+                v.x += 4 * c < K ? L[4 * c] : 0.f;
+                v.y += 4 * c + 1 < K ? L[4 * c + 1] : 0.f;
+                v.z += 4 * c + 2 < K ? L[4 * c + 2] : 0.f;
+                v.w += 4 * c + 3 < K ? L[4 * c + 3] : 0.f;
+                o4[c] = v;
+            }
+        }
+    }
+}
+
 // ------------------------------------------------------------------ L2L
 // one thread per node of level l >= 1: L_fin = L_own + shift(L_fin(parent))
 template <int P>
@@ -874,20 +949,32 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
         const uint8_t* od = P<uint8_t>(h.ord_pool) + h.lists.nn_idx_off[l];
         const uint32_t* act = P<uint32_t>(h.act);
         const uint32_t* act_pos = P<uint32_t>(h.act_pos);
+        const bool coarse = nl <= kM2lWarpLevelNodes;
         if constexpr (ORD == 12) {
             if (h.ctrl_on || h.adapt) {
-                k_m2l_mixed<12, 8, 0, 2><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, count, comrel,
-                                                                           mu, loc, zp, act, act_pos);
-                k_m2l_mixed<12, 12, 3, 4><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, count, comrel,
-                                                                            mu, loc, zp, act, act_pos);
+                if (coarse) {
+                    k_m2l_mixed_warp<12, 8, 0, 2><<<grid_for(nl * 32, 128), 128, 0, s>>>(
+                        l, hl(l), pp, np_, ni_, od, comrel, mu, loc, zp, act, act_pos);
+                    k_m2l_mixed_warp<12, 12, 3, 4><<<grid_for(nl * 32, 128), 128, 0, s>>>(
+                        l, hl(l), pp, np_, ni_, od, comrel, mu, loc, zp, act, act_pos);
+                } else {
+                    k_m2l_mixed<12, 8, 0, 2><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, count,
+                                                                               comrel, mu, loc, zp, act, act_pos);
+                    k_m2l_mixed<12, 12, 3, 4><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, count,
+                                                                                comrel, mu, loc, zp, act, act_pos);
+                }
                 h.launches++;
                 mixed = true;
             }
         } else if constexpr (ORD >= 6) {
             if (h.adapt) {
                 constexpr int OB = (ORD - 4) / 2;  // the bucket of order ORD
-                k_m2l_mixed<ORD, ORD, 0, OB><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, count,
-                                                                              comrel, mu, loc, zp, act, act_pos);
+                if (coarse)
+                    k_m2l_mixed_warp<ORD, ORD, 0, OB><<<grid_for(nl * 32, 128), 128, 0, s>>>(
+                        l, hl(l), pp, np_, ni_, od, comrel, mu, loc, zp, act, act_pos);
+                else
+                    k_m2l_mixed<ORD, ORD, 0, OB><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), pp, np_, ni_, od, count,
+                                                                                  comrel, mu, loc, zp, act, act_pos);
                 mixed = true;
             }
         }
