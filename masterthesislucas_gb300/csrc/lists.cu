@@ -14,9 +14,13 @@
 //   near(A) - partners not accepted (refined at the next level; at the leaf
 //             level they are the P2P / PN partners, including A itself).
 // Since near(child) and nn(child) are drawn from the non-empty children of
-// near(parent), the lists hold exactly the reference's visited pairs.  The
-// MAC is evaluated in FP64 from the bit-exact COMs, so the decisions are the
-// reference's decisions.
+// near(parent), the lists hold exactly the reference's visited pairs.  At the
+// reference's expansion order the MAC is decided as the reference decides it
+// (FP64 from the bit-exact COMs wherever FP32 is not conclusive).  Order-p
+// handles build physics-mode trees (FP32 records) and may open by the nodes'
+// bounding radii instead of their cell sizes, send cheap accepted leaf pairs
+// to P2P, or give accepted pairs their own expansion order; the structure of
+// the lists is the same.
 #include <cmath>
 
 #include "controller.cuh"
