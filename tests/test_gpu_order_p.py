@@ -142,3 +142,29 @@ def test_leaf_p2p_switch_is_at_least_as_accurate():
     from masterthesislucas_gb300._lib import TreecodeError
     with pytest.raises(TreecodeError):
         NBodySolverFMM_SYM_MORTON("tsne", leaf_p2p=64)  # reference order keeps its interaction set
+
+
+@pytest.mark.parametrize("mac", ["cell", "bmax"])
+def test_deep_tree_uses_both_level_kernels(mac):
+    """A depth-10 tree runs the coarse-level kernels (a warp per node for the
+    lists and the M2L, four lanes per node for the M2M, levels <= 8) and the
+    fine-level ones (a thread per node, levels 9-10) in one solve; the forces
+    must meet the accuracy the same settings reach on shallow trees."""
+    n = 262144
+    pos = datasets.two_disks(n, seed=51).astype(np.float64)
+    rows = np.random.default_rng(4).choice(n, 2048, replace=False)
+    fd, _ = direct(pos, kernel="gravity", softening=1e-3, precision="fp64", rows=rows)
+    theta = 1.0 if mac == "cell" else 0.7
+    s = NBodySolverFMM_SYM_MORTON("gravity", max_children=16, tree_depth=10, theta=theta, softening=1e-3, order=10,
+                                  mac=mac, leaf_p2p=64)
+    pts = Points.from_positions(pos)
+    s.updateTree(pts, pos.min(0), pos.max(0))
+    s.solveNbody(0.0, pts)
+    g = np.zeros_like(pos)
+    g[pts.ID] = pts.derivative
+    err = np.linalg.norm(g[rows] - fd, axis=1) / np.linalg.norm(fd, axis=1)
+    print(mac, np.median(err), np.percentile(err, 99))
+    assert np.median(err) < 5e-5
+    assert np.percentile(err, 99) < 2e-3
+    c = s.counters()
+    assert c["m2l"] > 0 and c["p2p_pairs"] > 0
