@@ -90,18 +90,66 @@ def load_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms in the timed region."""
+    """SM clock, its maximum and the clock event (throttle) reasons, sampled in
+    the timed region: every 2 ms by read-only NVML queries through the driver's
+    libnvidia-ml (the timed regions last tens of milliseconds), else every 25 ms
+    by nvidia-smi."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReason* bits (nvml.h)
+    BITS = ((0x8, "hw_slowdown"), (0x40, "hw_thermal_slowdown"), (0x20, "sw_thermal_slowdown"),
+            (0x4, "sw_power_cap"))
 
     def __init__(self, gpu: int):
         self.gpu = gpu
         self.proc = None
         self.lines = []
+        self.samples = []  # (sm MHz, max MHz, reason bits) from NVML
+        self.stop = None
+
+    def _nvml(self):
+        import ctypes
+        import torch
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            return None
+        dev = ctypes.c_void_p()
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(self.gpu).uuid)
+        if lib.nvmlDeviceGetHandleByUUID(uuid.encode(), ctypes.byref(dev)) != 0:
+            return None
+        reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx, sm, bits = ctypes.c_uint(0), ctypes.c_uint(0), ctypes.c_ulonglong(0)
+        if lib.nvmlDeviceGetMaxClockInfo(dev, 1, ctypes.byref(mx)) != 0:  # NVML_CLOCK_SM
+            return None
+
+        def read():
+            if lib.nvmlDeviceGetClockInfo(dev, 1, ctypes.byref(sm)) == 0 and reasons(dev, ctypes.byref(bits)) == 0:
+                return float(sm.value), float(mx.value), int(bits.value)
+            return None
+        return read if read() is not None else None
 
     def __enter__(self):
+        read = None
+        try:
+            read = self._nvml()
+        except Exception:
+            read = None
+        if read is not None:
+            self.stop = threading.Event()
+
+            def poll():
+                while not self.stop.is_set():
+                    r = read()
+                    if r is not None:
+                        self.samples.append(r)
+                    self.stop.wait(0.002)
+            self.samples.append(read())
+            self.t = threading.Thread(target=poll, daemon=True)
+            self.t.start()
+            return self
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "25"],
@@ -117,6 +165,9 @@ class ClockSampler:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
+        if self.stop is not None:
+            self.stop.set()
+            self.t.join(timeout=5)
         if self.proc:
             self.proc.terminate()
             try:
@@ -126,6 +177,10 @@ class ClockSampler:
 
     def summary(self):
         sm, mx, reasons = [], None, set()
+        for c, m, bits in self.samples:
+            sm.append(c)
+            mx = m
+            reasons.update(name for bit, name in self.BITS if bits & bit)
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             f = [x.strip() for x in ln.split(",")]
@@ -140,7 +195,7 @@ class ClockSampler:
                 if v.lower().startswith("active"):
                     reasons.add(name)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvml" if self.samples else "nvidia-smi"}
 
 
 def median_error(grad, ref):
@@ -942,7 +997,8 @@ def main():
                      "frac": (achieved / fp32_peak) if achieved else None, "traffic": None,
                      "flops_per_pair": 20, "peak_source": f"nominal: 152 SMs x 128 FP32 lanes x 2 x {sm_mhz:.0f} MHz "
                                                           f"(MEASURED_PEAKS.json holds no FP32 figure; {peak_src})"},
-        "e2e": {"value": n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * 16,
+        # H2D: positions, IDs, the gradient the forces add to; D2H: sorted positions, IDs, gradient, pair sum
+        "e2e": {"value": n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * 16 + n * 4 + n * 16,
                 "d2h_bytes_per_step": n * 16 + n * 4 + n * 16 + 8},
         "gpu_launches": head["launches"],
         "clocks": head["clocks"],

@@ -126,6 +126,14 @@ inline double unkey(unsigned long long k)
     return d;
 }
 
+// the caller's point IDs follow the points through the sort: out[k] = in[perm[k]]
+__global__ void k_gather_ids(const int32_t* __restrict__ in, const uint32_t* __restrict__ perm, int64_t n,
+                             int32_t* __restrict__ out)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        out[k] = in[perm[k]];
+}
+
 // refreshes the compute copy of the positions after tc_solve received new ones
 template <typename real>
 __global__ void k_prel(const double2* __restrict__ pos64, const uint32_t* __restrict__ codes, int64_t n, int depth,
@@ -296,7 +304,7 @@ int tc_destroy(tc_handle* t)
     Buf* bufs[] = {&h.codes, &h.perm, &h.alt_keys, &h.alt_vals, &h.pos_in, &h.pos64, &h.prel, &h.grad_acc,
                    &h.count, &h.first, &h.com64, &h.m0, &h.m2, &h.bbc, &h.bblen, &h.comrel, &h.m0r, &h.m2t,
                    &h.loc, &h.locfin, &h.mu, &h.chunk, &h.zwork, &h.zloc, &h.counters, &h.ptr_pool, &h.idx_pool, &h.cnt_tmp, &h.lstat, &h.ord_pool, &h.nfeat, &h.dec, &h.bigleaf, &h.chunk_leaf, &h.act, &h.act_pos, &h.bmax, &h.diagpart, &h.ctrl_w, &h.tmp, &h.err, &h.zpart, &h.dtotal, &h.sumtmp,
-                   &h.host_stage};
+                   &h.host_stage, &h.ids_dev};
     for (Buf* b : bufs) release(*b);
     if (h.step_graph) cudaGraphExecDestroy(h.step_graph);
     if (h.h_total) cudaFreeHost(h.h_total);
@@ -356,14 +364,17 @@ int tc_update_tree(tc_handle* t, double* pos_xy, int32_t* ids, int64_t n, const 
     if ((rc = update_common(h, P<double>(h.pos_in), n, min_xy, max_xy))) return rc;
     TC_CUDA_TRY(cudaMemcpyAsync(pos_xy, h.pos64.p, (size_t)n * 16, cudaMemcpyDeviceToHost, h.stream));
     if (ids) {
-        std::vector<uint32_t> perm(n);
-        TC_CUDA_TRY(cudaMemcpyAsync(perm.data(), h.perm.p, (size_t)n * 4, cudaMemcpyDeviceToHost, h.stream));
-        TC_CUDA_TRY(cudaStreamSynchronize(h.stream));
-        std::vector<int32_t> old(ids, ids + n);
-        for (int64_t k = 0; k < n; k++) ids[k] = old[perm[k]];
-    } else {
-        TC_CUDA_TRY(cudaStreamSynchronize(h.stream));
+        // the records' IDs move with them on the device: no host gather
+        if ((rc = ensure(h.ids_dev, (size_t)n * 8))) return rc;
+        int32_t* ids_in = P<int32_t>(h.ids_dev);
+        int32_t* ids_out = ids_in + n;
+        TC_CUDA_TRY(cudaMemcpyAsync(ids_in, ids, (size_t)n * 4, cudaMemcpyHostToDevice, h.stream));
+        k_gather_ids<<<grid_for(n, 256), 256, 0, h.stream>>>(ids_in, P<uint32_t>(h.perm), n, ids_out);
+        TC_CUDA_TRY(cudaGetLastError());
+        h.launches++;
+        TC_CUDA_TRY(cudaMemcpyAsync(ids, ids_out, (size_t)n * 4, cudaMemcpyDeviceToHost, h.stream));
     }
+    TC_CUDA_TRY(cudaStreamSynchronize(h.stream));
     return TC_OK;
 }
 
@@ -427,15 +438,16 @@ int tc_solve(tc_handle* t, double* total, const double* pos_xy, double* grad_xy,
         TC_CUDA_TRY(cudaMemcpyAsync(h.pos64.p, pos_xy, (size_t)n * 16, cudaMemcpyHostToDevice, h.stream));
         if ((rc = refresh_positions(h))) return rc;
     }
+    // the forces add to the caller's (applyForces accumulates into derivative): the sum is taken on the
+    // device, result + grad_xy[i] in one FP64 add per component, and copied straight back
+    TC_CUDA_TRY(cudaMemcpyAsync(h.grad_acc.p, grad_xy, (size_t)n * 16, cudaMemcpyHostToDevice, h.stream));
     TC_CUDA_TRY(cudaMemsetAsync(h.dtotal.p, 0, 8, h.stream));
-    rc = h.cfg.order ? solve_fmm_order(h, P<double>(h.grad_acc), P<double>(h.dtotal), 0, 0)
-                     : solve_fmm(h, P<double>(h.grad_acc), P<double>(h.dtotal), 0, 0);
+    rc = h.cfg.order ? solve_fmm_order(h, P<double>(h.grad_acc), P<double>(h.dtotal), 1, 0)
+                     : solve_fmm(h, P<double>(h.grad_acc), P<double>(h.dtotal), 1, 0);
     if (rc) return rc;
-    std::vector<double> g((size_t)n * 2);
-    TC_CUDA_TRY(cudaMemcpyAsync(g.data(), h.grad_acc.p, (size_t)n * 16, cudaMemcpyDeviceToHost, h.stream));
+    TC_CUDA_TRY(cudaMemcpyAsync(grad_xy, h.grad_acc.p, (size_t)n * 16, cudaMemcpyDeviceToHost, h.stream));
     TC_CUDA_TRY(cudaMemcpyAsync(h.h_total, h.dtotal.p, 8, cudaMemcpyDeviceToHost, h.stream));
     TC_CUDA_TRY(cudaStreamSynchronize(h.stream));
-    for (int64_t i = 0; i < 2 * n; i++) grad_xy[i] += g[i];
     *total += h.h_total[0];
     return TC_OK;
 }

@@ -41,26 +41,60 @@ __global__ void k_scan_partials(uint32_t* partial, int64_t nb)
     }
 }
 
+// A chunk moves between global and shared memory in coalesced rows (row i,
+// thread t: item i * kScanThreads + t) and each thread scans its own
+// kScanItems consecutive items from shared memory; the padded index keeps
+// both access patterns free of bank conflicts.
+__device__ __forceinline__ int chunk_slot(int x) { return x + (x >> 5); }
+constexpr int kChunkWords = kScanChunk + kScanChunk / 32;
+
+__device__ __forceinline__ void load_chunk(const uint32_t* __restrict__ in, int64_t base, int64_t n, uint32_t* sm,
+                                           uint32_t (&v)[kScanItems])
+{
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++) {
+        const int x = i * kScanThreads + threadIdx.x;
+        sm[chunk_slot(x)] = base + x < n ? in[base + x] : 0u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++) v[i] = sm[chunk_slot(threadIdx.x * kScanItems + i)];
+}
+
+// v holds this thread's exclusive results; sm still holds the inputs, so the block syncs before overwriting
+__device__ __forceinline__ void store_chunk(uint32_t* __restrict__ out, int64_t base, int64_t n, uint32_t* sm,
+                                            const uint32_t (&v)[kScanItems])
+{
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++) sm[chunk_slot(threadIdx.x * kScanItems + i)] = v[i];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++) {
+        const int x = i * kScanThreads + threadIdx.x;
+        if (base + x < n) out[base + x] = sm[chunk_slot(x)];
+    }
+}
+
 __global__ void k_scan_final(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, int64_t n,
                              const uint32_t* __restrict__ partial, int64_t nb)
 {
-    int64_t base = (int64_t)blockIdx.x * kScanChunk + (int64_t)threadIdx.x * kScanItems;
+    __shared__ uint32_t sm[kChunkWords];
+    const int64_t base = (int64_t)blockIdx.x * kScanChunk;
     uint32_t v[kScanItems];
+    load_chunk(in, base, n, sm, v);
     uint32_t s = 0;
 #pragma unroll
-    for (int i = 0; i < kScanItems; i++) {
-        int64_t k = base + i;
-        v[i] = k < n ? in[k] : 0u;
-        s += v[i];
-    }
+    for (int i = 0; i < kScanItems; i++) s += v[i];
     uint32_t tot;
     uint32_t ex = block_exclusive_scan(s, tot) + partial[blockIdx.x];
 #pragma unroll
     for (int i = 0; i < kScanItems; i++) {
-        int64_t k = base + i;
-        if (k < n) out[k] = ex;
-        ex += v[i];
+        const uint32_t x = v[i];
+        v[i] = ex;
+        ex += x;
     }
+    store_chunk(out, base, n, sm, v);
     if (blockIdx.x == nb - 1 && threadIdx.x == 0) out[n] = partial[blockIdx.x] + tot;
 }
 
@@ -112,23 +146,22 @@ __global__ void k_scan_final2(const uint32_t* __restrict__ in0, uint32_t* __rest
     uint32_t* out = blockIdx.y ? out1 : out0;
     const uint32_t cap = blockIdx.y ? cap1 : cap0;
     const uint32_t carry = partial ? partial[blockIdx.y * nb + blockIdx.x] : 0u;
-    int64_t base = (int64_t)blockIdx.x * kScanChunk + (int64_t)threadIdx.x * kScanItems;
+    __shared__ uint32_t sm[kChunkWords];
+    const int64_t base = (int64_t)blockIdx.x * kScanChunk;
     uint32_t v[kScanItems];
+    load_chunk(in, base, n, sm, v);
     uint32_t s = 0;
 #pragma unroll
-    for (int i = 0; i < kScanItems; i++) {
-        int64_t k = base + i;
-        v[i] = k < n ? in[k] : 0u;
-        s += v[i];
-    }
+    for (int i = 0; i < kScanItems; i++) s += v[i];
     uint32_t tot;
     uint32_t ex = block_exclusive_scan(s, tot) + carry;
 #pragma unroll
     for (int i = 0; i < kScanItems; i++) {
-        int64_t k = base + i;
-        if (k < n) out[k] = min(ex, cap);
-        ex += v[i];
+        const uint32_t x = v[i];
+        v[i] = min(ex, cap);
+        ex += x;
     }
+    store_chunk(out, base, n, sm, v);
     if (blockIdx.x == nb - 1 && threadIdx.x == 0) out[n] = min(carry + tot, cap);
 }
 

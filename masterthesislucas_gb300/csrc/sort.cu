@@ -1,8 +1,8 @@
 // Stable LSD radix sort of (u32 key, u32 value): 4 passes of 8 bits, each a
 // per-tile digit histogram, a device-wide scan of the digit-major histogram
 // table, and a stable scatter.  The scatter ranks keys in their input order
-// with warp match-any groups, stages the tile digit-sorted in shared memory
-// and writes each digit run contiguously.  Stability makes ties between equal
+// with warp match-any groups against warp-private digit counters, stages the
+// tile digit-sorted in shared memory and writes each digit run contiguously.  Stability makes ties between equal
 // Morton codes keep input order, which defines the permutation where the
 // reference's unstable integer_sort (nBodySolverFMM_SYM_MORTON.h:89) does not.
 #include "common.cuh"
@@ -22,12 +22,16 @@ __global__ void __launch_bounds__(RT) k_radix_hist(const uint32_t* __restrict__ 
     __shared__ uint32_t h[RADIX];
     h[threadIdx.x] = 0;
     __syncthreads();
-    int64_t base = (int64_t)blockIdx.x * RTILE;
+    const int64_t base = (int64_t)blockIdx.x * RTILE;
+    uint32_t k[RI];
 #pragma unroll
     for (int r = 0; r < RI; r++) {
-        int64_t p = base + (int64_t)r * RT + threadIdx.x;
-        if (p < n) atomicAdd(&h[(keys[p] >> shift) & 255u], 1u);
+        const int64_t p = base + (int64_t)r * RT + threadIdx.x;
+        k[r] = p < n ? keys[p] : 0u;
     }
+#pragma unroll
+    for (int r = 0; r < RI; r++)
+        if (base + (int64_t)r * RT + threadIdx.x < n) atomicAdd(&h[(k[r] >> shift) & 255u], 1u);
     __syncthreads();
     hist[(int64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
 }
@@ -39,66 +43,72 @@ __global__ void __launch_bounds__(RT) k_radix_scatter(const uint32_t* __restrict
 {
     __shared__ uint32_t s_keys[RTILE];
     __shared__ uint32_t s_vals[RTILE];
-    __shared__ uint32_t s_wh[NW][RADIX];
-    __shared__ uint32_t s_run[RADIX];
+    __shared__ uint32_t s_wh[NW][RADIX];  // per warp: digit counts, then the warp's offset within the digit
     __shared__ uint32_t s_start[RADIX];
+    __shared__ uint32_t s_gofs[RADIX];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t lt_mask = (1u << lane) - 1u;
-    s_run[tid] = 0;
+    for (int i = tid; i < NW * RADIX; i += RT) (&s_wh[0][0])[i] = 0;
+    __syncthreads();
+    // this block's global start of each digit, fetched while the tile is ranked
+    const uint32_t goff = offs[(int64_t)tid * nblocks + blockIdx.x];
     uint32_t key[RI], val[RI], rank[RI], dig[RI];
-    const int64_t base = (int64_t)blockIdx.x * RTILE;
+    const int64_t base = (int64_t)blockIdx.x * RTILE + (int64_t)warp * (32 * RI);
+    uint32_t* wh = s_wh[warp];
+    // warp w ranks the tile's w-th run of RT * RI / NW consecutive keys, 32 at a time, against its own counters:
+    // warps cover the tile in input order, so (warp, row, lane) order is input order and the sort is stable.
+    // All of the warp's loads first (independent, in flight together), then the ranking.
 #pragma unroll
     for (int r = 0; r < RI; r++) {
-        const int64_t p = base + (int64_t)r * RT + tid;
+        const int64_t p = base + r * 32 + lane;
         const bool valid = p < n;
-        uint32_t k = valid ? kin[p] : 0xFFFFFFFFu;
-        uint32_t v = valid ? (iota_vals ? (uint32_t)p : vin[p]) : 0u;
-        uint32_t d = valid ? ((k >> shift) & 255u) : 256u;
-        for (int i = tid; i < NW * RADIX; i += RT) (&s_wh[0][0])[i] = 0;
-        __syncthreads();
-        uint32_t peers = __match_any_sync(0xffffffffu, d);
-        int leader = __ffs(peers) - 1;
-        uint32_t rw = __popc(peers & lt_mask);
-        if (lane == leader && d < 256u) s_wh[warp][d] = __popc(peers);
-        __syncthreads();
-        {
-            uint32_t run = s_run[tid];
+        key[r] = valid ? kin[p] : 0u;
+        val[r] = valid ? (iota_vals ? (uint32_t)p : vin[p]) : 0u;
+    }
 #pragma unroll
-            for (int w = 0; w < NW; w++) {
-                uint32_t c = s_wh[w][tid];
-                s_wh[w][tid] = run;
-                run += c;
-            }
-            s_run[tid] = run;
-        }
-        __syncthreads();
-        rank[r] = d < 256u ? s_wh[warp][d] + rw : 0u;
-        key[r] = k;
-        val[r] = v;
+    for (int r = 0; r < RI; r++) {
+        const uint32_t d = base + r * 32 + lane < n ? ((key[r] >> shift) & 255u) : 256u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t before = d < 256u ? wh[d] : 0u;
+        __syncwarp();
+        if (d < 256u && lane == (uint32_t)(__ffs(peers) - 1)) wh[d] = before + __popc(peers);
+        __syncwarp();
+        rank[r] = before + __popc(peers & lt_mask);
         dig[r] = d;
-        __syncthreads();
+    }
+    __syncthreads();
+    uint32_t run = 0;
+#pragma unroll
+    for (int w = 0; w < NW; w++) {
+        const uint32_t c = s_wh[w][tid];
+        s_wh[w][tid] = run;
+        run += c;
     }
     uint32_t tot;
-    uint32_t st = block_exclusive_scan(s_run[tid], tot);
+    const uint32_t st = block_exclusive_scan(run, tot);
     s_start[tid] = st;
+    s_gofs[tid] = goff - st;  // global position of tile slot j of digit d: s_gofs[d] + j (mod 2^32)
     __syncthreads();
 #pragma unroll
     for (int r = 0; r < RI; r++) {
         if (dig[r] < 256u) {
-            uint32_t idx = s_start[dig[r]] + rank[r];
+            const uint32_t idx = s_start[dig[r]] + wh[dig[r]] + rank[r];
             s_keys[idx] = key[r];
             s_vals[idx] = val[r];
         }
     }
     __syncthreads();
-    int64_t rem = n - base;
+    const int64_t rem = n - (int64_t)blockIdx.x * RTILE;
     const int cnt = rem < RTILE ? (int)rem : RTILE;
-    for (int j = tid; j < cnt; j += RT) {
-        uint32_t k = s_keys[j];
-        uint32_t d = (k >> shift) & 255u;
-        uint32_t o = offs[(int64_t)d * nblocks + blockIdx.x] + (uint32_t)j - s_start[d];
-        kout[o] = k;
-        vout[o] = s_vals[j];
+#pragma unroll
+    for (int r = 0; r < RI; r++) {
+        const int j = r * RT + tid;
+        if (j < cnt) {
+            const uint32_t k = s_keys[j];
+            const uint32_t o = s_gofs[(k >> shift) & 255u] + (uint32_t)j;
+            kout[o] = k;
+            vout[o] = s_vals[j];
+        }
     }
 }
 

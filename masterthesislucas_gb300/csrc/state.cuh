@@ -86,6 +86,7 @@ struct Handle {
     Lists lists;
     // scratch
     Buf tmp, err, zpart, dtotal, host_stage, sumtmp;
+    Buf ids_dev;  // tc_update_tree: the caller's IDs in, permuted by the sort out
     // stage timing (CUDA events on the handle's stream) and interaction counters
     cudaGraphExec_t step_graph = nullptr;  // a captured update + solve (tc_step_capture)
     int graph_launches = 0;
