@@ -375,20 +375,23 @@ __device__ __forceinline__ void m2l_acc(float Rx, float Ry, float hl, const PotP
     }
 }
 
-// the node's local expansion, the far-field pair sum kappa * sum_b L_b mu_b(A)
+// the far-field pair sum of node A, kappa * sum_b L_b mu_b(A), from its M2L sum alone
 template <int K, int KS>
-__device__ __forceinline__ void m2l_store(int64_t na, bool any, float kappa, const float* L,
-                                          const float* __restrict__ mu, float* __restrict__ loc,
+__device__ __forceinline__ double m2l_pairsum(int64_t na, bool any, float kappa, const float* L,
+                                              const float* __restrict__ mu)
+{
+    if (!any) return 0.0;
+    const float* m = mu + na * KS;
+    float zs = 0.f;
+#pragma unroll
+    for (int k = 0; k < K; k++) zs += L[k] * m[k];
+    return (double)kappa * (double)zs;
+}
+
+template <int K, int KS>
+__device__ __forceinline__ void m2l_write(int64_t na, double z, const float* L, float* __restrict__ loc,
                                           double* __restrict__ zpart)
 {
-    double z = 0.0;
-    if (any) {
-        const float* m = mu + na * KS;
-        float zs = 0.f;
-#pragma unroll
-        for (int k = 0; k < K; k++) zs += L[k] * m[k];
-        z = (double)kappa * (double)zs;
-    }
     zpart[na] = z;
     float4* o4 = reinterpret_cast<float4*>(loc + na * KS);
 #pragma unroll
@@ -397,9 +400,42 @@ __device__ __forceinline__ void m2l_store(int64_t na, bool any, float kappa, con
                             4 * c + 2 < K ? L[4 * c + 2] : 0.f, 4 * c + 3 < K ? L[4 * c + 3] : 0.f);
 }
 
-// one thread per sink node A of level l: L(A) = sum over nn(A) of M2L
+// the node's local expansion and its far-field pair sum
+template <int K, int KS>
+__device__ __forceinline__ void m2l_store(int64_t na, bool any, float kappa, const float* L,
+                                          const float* __restrict__ mu, float* __restrict__ loc,
+                                          double* __restrict__ zpart)
+{
+    m2l_write<K, KS>(na, m2l_pairsum<K, KS>(na, any, kappa, L, mu), L, loc, zpart);
+}
+
+// L2L into node (level l) from its parent's final local expansion: the same
+// arithmetic as k_l2l, with the node's own sum acc still in registers
 template <int P>
-__global__ void __launch_bounds__(128) k_m2l_p(int l, float hl, PotParams pp, const uint32_t* __restrict__ nn_ptr,
+__device__ __forceinline__ void l2l_into(int64_t node, int l, float ih, const float* __restrict__ comrel,
+                                         const float* __restrict__ loc, float* acc)
+{
+    constexpr int K = ncoef(P);
+    const uint32_t li = level_index(l), lp = level_index(l - 1);
+    const int64_t i = node - li;
+    const int64_t par = lp + (i >> 2);
+    const int j = (int)(i & 3);
+    const float ox = ((j & 1) ? 0.5f : -0.5f), oy = ((j & 2) ? 0.5f : -0.5f);
+    const float ddx = ox + (comrel[2 * node] - comrel[2 * par]) * ih;
+    const float ddy = oy + (comrel[2 * node + 1] - comrel[2 * par + 1]) * ih;
+    float in[K], w[K];
+    load_coefs<K, kstride(P)>(loc + par * kstride(P), in);
+    halve_by_degree<K>(in);  // parent scale 2h -> child scale h
+    monomials<P>(ddx, ddy, w);
+    shift_down<P>(in, w, acc);
+}
+
+// one thread per sink node A of level l: L(A) = sum over nn(A) of M2L; with
+// L2L, plus the parent's final local expansion shifted to A (the level's L2L
+// fused in: A's sum is not written and read back), held to the unfused form's
+// registers so the M2L loop keeps its resident warps
+template <int P, bool L2L = false>
+__global__ void __launch_bounds__(128, L2L ? (P >= 8 ? 4 : P >= 6 ? 5 : 7) : 1) k_m2l_p(int l, float hl, PotParams pp, const uint32_t* __restrict__ nn_ptr,
                                                const uint32_t* __restrict__ nn_idx, const uint32_t* __restrict__ count,
                                                const float* __restrict__ comrel, const float* __restrict__ mu,
                                                float* __restrict__ loc, double* __restrict__ zpart, const uint32_t* __restrict__ act, const uint32_t* __restrict__ act_pos)
@@ -435,7 +471,13 @@ __global__ void __launch_bounds__(128) k_m2l_p(int l, float hl, PotParams pp, co
             const float Ry = (float)(iay - (int)compact16(b >> 1)) + (ca.y - cb.y) * ih;
             m2l_acc<P, KS>(Rx, Ry, hl, pp, mu + nb * KS, L);
         }
-        m2l_store<K, KS>(na, b0 != b1, pp.kappa, L, mu, loc, zpart);
+        if constexpr (L2L) {
+            const double z = m2l_pairsum<K, KS>(na, b0 != b1, pp.kappa, L, mu);
+            l2l_into<P>(na, l, ih, comrel, loc, L);
+            m2l_write<K, KS>(na, z, L, loc, zpart);
+        } else {
+            m2l_store<K, KS>(na, b0 != b1, pp.kappa, L, mu, loc, zpart);
+        }
     }
 }
 
@@ -941,8 +983,15 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
     TC_CUDA_TRY(cudaMemsetAsync(zp, 0, 8, s));
     const uint32_t* ptr = P<uint32_t>(h.ptr_pool);
     const uint32_t* idx = P<uint32_t>(h.idx_pool);
+    // fixed order below 10: the fine levels' L2L runs inside their M2L launch (after the coarse levels' L2L)
+    bool per_pair = false;
+    if constexpr (ORD == 12) per_pair = h.ctrl_on || h.adapt;
+    else if constexpr (ORD >= 6) per_pair = h.adapt;
+    const bool fuse = ORD < 10 && !per_pair;
+    int nfused = 0;
     for (int l = 1; l <= dep; l++) {
         const int64_t nl = (int64_t)1 << (2 * l);
+        if (fuse && nl > kM2lWarpLevelNodes) continue;
         const uint32_t* np_ = ptr + h.lists.nn_ptr_off[l];
         const uint32_t* ni_ = idx + h.lists.nn_idx_off[l];
         bool mixed = false;
@@ -989,6 +1038,15 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
     }
     for (int l = 1; l <= dep; l++) {
         const int64_t nl = (int64_t)1 << (2 * l);
+        if constexpr (ORD < 10) {
+            if (fuse && nl > kM2lWarpLevelNodes) {
+                k_m2l_p<ORD, true><<<grid_for(nl, 128), 128, 0, s>>>(
+                    l, hl(l), pp, ptr + h.lists.nn_ptr_off[l], idx + h.lists.nn_idx_off[l], count, comrel, mu, loc,
+                    zp, P<uint32_t>(h.act), P<uint32_t>(h.act_pos));
+                nfused++;
+                continue;
+            }
+        }
         if constexpr (ORD >= 10)
             k_l2l_stream<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, loc, P<uint32_t>(h.act), P<uint32_t>(h.act_pos));
         else
@@ -1009,7 +1067,7 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
     if ((rc = ensure(h.sumtmp, sum_tmp_doubles() * 8)) ||
         (rc = sum_f64(zp, nn, P<double>(h.zwork), chunk_ptr + nleaf, d_total, 1, P<double>(h.sumtmp), s)))
         return rc;
-    h.launches += 3 + 2 * dep + 6;
+    h.launches += 3 + 2 * dep + 6 - nfused;
     TC_CUDA_TRY(cudaGetLastError());
     return record(h, 7);
 }

@@ -165,18 +165,27 @@ __global__ void k_scan_final2(const uint32_t* __restrict__ in0, uint32_t* __rest
     if (blockIdx.x == nb - 1 && threadIdx.x == 0) out[n] = min(carry + tot, cap);
 }
 
-constexpr int kSumBlocks = 2 * kSMs;
+constexpr int kSumBlocks = 8 * kSMs;
 
 // stage 1 of sum_f64: block b sums the grid-stride slice b of a[0..na) ++ c[0..*nc)
+// (four loads in flight per thread over a, then the rest one at a time)
 __global__ void k_sum_partial(const double* __restrict__ a, int64_t na, const double* __restrict__ c,
                               const uint32_t* __restrict__ nc, double* __restrict__ partial)
 {
     __shared__ double ws[32];
     const int64_t ncv = nc ? (int64_t)*nc : 0;
     const int64_t tot = na + ncv;
-    double s = 0.0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x)
-        s += i < na ? a[i] : c[i - na];
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < na; i += 4 * stride) {
+        s0 += a[i];
+        s1 += a[i + stride];
+        s2 += a[i + 2 * stride];
+        s3 += a[i + 3 * stride];
+    }
+    for (; i < tot; i += stride) s0 += i < na ? a[i] : c[i - na];
+    double s = (s0 + s1) + (s2 + s3);
     s = warp_sum(s);
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
     __syncthreads();
