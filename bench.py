@@ -980,6 +980,15 @@ def main():
                    "step": ("one CUDA graph launch per step (update + solve captured over the exact box, "
                             "stage times from the uncaptured warm-up steps)" if head.get("graph")
                             else "updateTree + solveNbody calls")})
+    # DRAM bytes (read + write) of one k_near_p launch from the committed ncu capture of this configuration
+    # (profiles/k_near_p_two_disks_4m.md: 225.7 MB + 94.7 MB), taken before the leaf-pair P2P switch
+    # (2.27e9 pair evaluations there, counters.p2p_pairs here); other configurations have no capture
+    traffic, traffic_src = None, "no ncu capture of this configuration"
+    if (n == 4194304 and w["dist"] == "two_disks" and config.get("order") == 8 and config.get("depth") == 11
+            and config.get("mac") == "bmax" and config.get("theta") == 0.75):
+        traffic = 225.7e6 + 94.7e6
+        traffic_src = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at this configuration, "
+                       "captured before the leaf-pair P2P switch (2.27e9 pair evaluations)")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * head["t_total"] / args.steps, "higher_is_better": True,
@@ -994,7 +1003,8 @@ def main():
         "counters": head["counters"],
         "roofline": {"kernel": "k_near_p (P2P + L2P)", "bound": "fp32",
                      "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": (achieved / fp32_peak) if achieved else None, "traffic": None,
+                     "frac": (achieved / fp32_peak) if achieved else None, "traffic": traffic,
+                     "traffic_source": traffic_src,
                      "flops_per_pair": 20, "peak_source": f"nominal: 152 SMs x 128 FP32 lanes x 2 x {sm_mhz:.0f} MHz "
                                                           f"(MEASURED_PEAKS.json holds no FP32 figure; {peak_src})"},
         # H2D: positions, IDs, the gradient the forces add to; D2H: sorted positions, IDs, gradient, pair sum
