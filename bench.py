@@ -108,6 +108,7 @@ class ClockSampler:
         self.lines = []
         self.samples = []  # (sm MHz, max MHz, reason bits) from NVML
         self.stop = None
+        self.nvml = None
 
     def _nvml(self):
         import ctypes
@@ -116,20 +117,21 @@ class ClockSampler:
         if lib.nvmlInit_v2() != 0:
             return None
         dev = ctypes.c_void_p()
-        uuid = "GPU-" + str(torch.cuda.get_device_properties(self.gpu).uuid)
-        if lib.nvmlDeviceGetHandleByUUID(uuid.encode(), ctypes.byref(dev)) != 0:
-            return None
+        mx, sm, bits = ctypes.c_uint(0), ctypes.c_uint(0), ctypes.c_ulonglong(0)
         reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
             lib.nvmlDeviceGetCurrentClocksThrottleReasons
-        mx, sm, bits = ctypes.c_uint(0), ctypes.c_uint(0), ctypes.c_ulonglong(0)
-        if lib.nvmlDeviceGetMaxClockInfo(dev, 1, ctypes.byref(mx)) != 0:  # NVML_CLOCK_SM
-            return None
 
         def read():
             if lib.nvmlDeviceGetClockInfo(dev, 1, ctypes.byref(sm)) == 0 and reasons(dev, ctypes.byref(bits)) == 0:
                 return float(sm.value), float(mx.value), int(bits.value)
             return None
-        return read if read() is not None else None
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(self.gpu).uuid)
+        if (lib.nvmlDeviceGetHandleByUUID(uuid.encode(), ctypes.byref(dev)) != 0 or
+                lib.nvmlDeviceGetMaxClockInfo(dev, 1, ctypes.byref(mx)) != 0 or read() is None):  # NVML_CLOCK_SM
+            lib.nvmlShutdown()
+            return None
+        self.nvml = lib
+        return read
 
     def __enter__(self):
         read = None
@@ -139,6 +141,9 @@ class ClockSampler:
             read = None
         if read is not None:
             self.stop = threading.Event()
+            first = read()
+            if first is not None:
+                self.samples.append(first)
 
             def poll():
                 while not self.stop.is_set():
@@ -146,7 +151,6 @@ class ClockSampler:
                     if r is not None:
                         self.samples.append(r)
                     self.stop.wait(0.002)
-            self.samples.append(read())
             self.t = threading.Thread(target=poll, daemon=True)
             self.t.start()
             return self
@@ -168,6 +172,7 @@ class ClockSampler:
         if self.stop is not None:
             self.stop.set()
             self.t.join(timeout=5)
+            self.nvml.nvmlShutdown()
         if self.proc:
             self.proc.terminate()
             try:
