@@ -113,6 +113,7 @@ class ClockSampler:
     def _nvml(self):
         import ctypes
         import torch
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(self.gpu).uuid)
         lib = ctypes.CDLL("libnvidia-ml.so.1")
         if lib.nvmlInit_v2() != 0:
             return None
@@ -125,7 +126,6 @@ class ClockSampler:
             if lib.nvmlDeviceGetClockInfo(dev, 1, ctypes.byref(sm)) == 0 and reasons(dev, ctypes.byref(bits)) == 0:
                 return float(sm.value), float(mx.value), int(bits.value)
             return None
-        uuid = "GPU-" + str(torch.cuda.get_device_properties(self.gpu).uuid)
         if (lib.nvmlDeviceGetHandleByUUID(uuid.encode(), ctypes.byref(dev)) != 0 or
                 lib.nvmlDeviceGetMaxClockInfo(dev, 1, ctypes.byref(mx)) != 0 or read() is None):  # NVML_CLOCK_SM
             lib.nvmlShutdown()
