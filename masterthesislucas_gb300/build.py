@@ -18,12 +18,18 @@ CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(PKG, "libtreecode.so")
 BUILD = os.path.join(PKG, "_build")
 
-SOURCES = ["scan.cu", "sort.cu", "tree.cu", "tree_p.cu", "lists.cu", "fmm.cu", "fmm_p.cu", "direct.cu", "bh.cu", "mlp.cu", "learned.cu", "tsne.cu", "integrate.cu", "pm.cu", "api.cu"]
+# longest compiles first
+SOURCES = ["fmm_p.cu", "lists.cu", "fmm.cu", "tree.cu", "tree_p.cu", "bh.cu", "pm.cu", "tsne.cu", "learned.cu",
+           "mlp.cu", "direct.cu", "integrate.cu", "sort.cu", "scan.cu", "api.cu"]
 NO_FMA = {"tree.cu"}
 # FP32 force kernels: denormals flushed (squared distances never reach them) so
 # that rsqrt/reciprocal map to single SFU instructions
 FTZ = {"fmm.cu", "fmm_p.cu", "tree_p.cu"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# fmm_p.cu is compiled once per expansion order (each object holds one order's
+# kernels) and once for the order switch, so the orders compile in parallel
+ORDERS = (12, 10, 8, 6, 4, 3)
+OBJECTS = {"fmm_p.cu": [(f"fmm_p_o{p}.o", [f"-DTC_FMM_ORDER={p}"]) for p in ORDERS] + [("fmm_p.o", [])]}
 
 
 def nvcc() -> str:
@@ -59,10 +65,11 @@ def build(verbose: bool = False, force: bool = False) -> str:
     objs = []
     for s in SOURCES:
         src = os.path.join(CSRC, s)
-        obj = os.path.join(BUILD, s.replace(".cu", ".o"))
-        objs.append(obj)
-        if force or _stale(obj, [src] + headers):
-            jobs.append([cc, "-c", src, "-o", obj] + _flags(s))
+        for name, defs in OBJECTS.get(s, [(s.replace(".cu", ".o"), [])]):
+            obj = os.path.join(BUILD, name)
+            objs.append(obj)
+            if force or _stale(obj, [src] + headers):
+                jobs.append([cc, "-c", src, "-o", obj] + _flags(s) + defs)
     with cf.ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:
         for cmd, res in zip(jobs, ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs)):
             if verbose and (res.stdout or res.stderr):

@@ -1124,15 +1124,39 @@ int dispatch_kernel(Handle& h, double* d_grad, int accumulate, int scatter, doub
 
 }  // namespace
 
+// Each expansion order's kernels live in their own object: the build compiles
+// this file once per order with TC_FMM_ORDER set (in parallel) and once without
+// it for the order switch below.
+template <int P>
+int multipoles_order(Handle& h);
+template <int P>
+int solve_order(Handle& h, double* d_grad, double* d_total, int accumulate, int scatter);
+
+#ifdef TC_FMM_ORDER
+template <int P>
+int multipoles_order(Handle& h)
+{
+    return multipoles_p<P>(h);
+}
+
+template <int P>
+int solve_order(Handle& h, double* d_grad, double* d_total, int accumulate, int scatter)
+{
+    return dispatch_kernel<P>(h, d_grad, accumulate, scatter, d_total);
+}
+
+template int multipoles_order<TC_FMM_ORDER>(Handle& h);
+template int solve_order<TC_FMM_ORDER>(Handle& h, double* d_grad, double* d_total, int accumulate, int scatter);
+#else
 int build_multipoles(Handle& h)
 {
     switch (h.cfg.order) {
-    case 3: return multipoles_p<3>(h);
-    case 4: return multipoles_p<4>(h);
-    case 6: return multipoles_p<6>(h);
-    case 8: return multipoles_p<8>(h);
-    case 10: return multipoles_p<10>(h);
-    case 12: return multipoles_p<12>(h);
+    case 3: return multipoles_order<3>(h);
+    case 4: return multipoles_order<4>(h);
+    case 6: return multipoles_order<6>(h);
+    case 8: return multipoles_order<8>(h);
+    case 10: return multipoles_order<10>(h);
+    case 12: return multipoles_order<12>(h);
     default:
         tc_set_error("unsupported expansion order %d (3, 4, 6, 8, 10, 12)", h.cfg.order);
         return TC_ERR_INVALID;
@@ -1142,16 +1166,17 @@ int build_multipoles(Handle& h)
 int solve_fmm_order(Handle& h, double* d_grad, double* d_total, int accumulate, int scatter)
 {
     switch (h.cfg.order) {
-    case 3: return dispatch_kernel<3>(h, d_grad, accumulate, scatter, d_total);
-    case 4: return dispatch_kernel<4>(h, d_grad, accumulate, scatter, d_total);
-    case 6: return dispatch_kernel<6>(h, d_grad, accumulate, scatter, d_total);
-    case 8: return dispatch_kernel<8>(h, d_grad, accumulate, scatter, d_total);
-    case 10: return dispatch_kernel<10>(h, d_grad, accumulate, scatter, d_total);
-    case 12: return dispatch_kernel<12>(h, d_grad, accumulate, scatter, d_total);
+    case 3: return solve_order<3>(h, d_grad, d_total, accumulate, scatter);
+    case 4: return solve_order<4>(h, d_grad, d_total, accumulate, scatter);
+    case 6: return solve_order<6>(h, d_grad, d_total, accumulate, scatter);
+    case 8: return solve_order<8>(h, d_grad, d_total, accumulate, scatter);
+    case 10: return solve_order<10>(h, d_grad, d_total, accumulate, scatter);
+    case 12: return solve_order<12>(h, d_grad, d_total, accumulate, scatter);
     default:
         tc_set_error("unsupported expansion order %d (3, 4, 6, 8, 10, 12)", h.cfg.order);
         return TC_ERR_INVALID;
     }
 }
+#endif
 
 }  // namespace tc
