@@ -12,7 +12,7 @@ import ctypes
 
 import numpy as np
 
-from . import _lib, datasets
+from . import datasets
 from ._lib import check, lib, ptr
 from .solver import NBodySolverFMM_SYM_MORTON
 
