@@ -234,7 +234,9 @@ int exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* t
     }
     int64_t nb = (n + kScanChunk - 1) / kScanChunk;
     if (nb == 1) {
-        k_scan_final2<<<dim3(1, 1), kScanThreads, 0, s>>>(in, out, in, out, n, nullptr, 1, UINT32_MAX, UINT32_MAX);
+        // one array: blockIdx.y is 0, the second pair is never read
+        k_scan_final2<<<dim3(1, 1), kScanThreads, 0, s>>>(in, out, nullptr, nullptr, n, nullptr, 1, UINT32_MAX,
+                                                          UINT32_MAX);
         TC_CUDA_TRY(cudaGetLastError());
         return TC_OK;
     }
