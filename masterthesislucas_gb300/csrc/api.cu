@@ -479,6 +479,12 @@ int tc_get_tree(tc_handle* t, uint32_t* codes, int32_t* perm, double* pos_sorted
         TC_CUDA_TRY(cudaStreamSynchronize(s));
         for (int64_t k = 0; k < nn; k++) {
             double* o = nodes + k * 27;
+            if (cnt[k] == 0) {
+                // an empty node is the reference's default-constructed record; the order-p path leaves
+                // the device records of empty nodes unwritten
+                for (int j = 0; j < 27; j++) o[j] = 0.0;
+                continue;
+            }
             int l = 0;
             while (l < h.depth && (int64_t)level_index(l + 1) <= k) l++;
             const int64_t i = k - level_index(l);

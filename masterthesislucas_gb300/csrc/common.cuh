@@ -132,8 +132,5 @@ __host__ __device__ inline double bbox_unkey(unsigned long long k)
 int64_t radix_tmp_words(int64_t n);
 int radix_sort_u32(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32_t* alt_vals, int64_t n,
                    uint32_t* tmp, cudaStream_t s, int* launches, int lo_bit = 0);
-// the lowest bit the sort must see for the leaf index of a depth-d tree
-// (2d top bits), rounded down to whole 8-bit passes
-inline int sort_lo_bit(int depth) { return 32 - 8 * (depth > 0 ? (2 * depth + 7) / 8 : 1); }
 
 }  // namespace tc

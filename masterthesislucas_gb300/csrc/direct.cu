@@ -128,7 +128,9 @@ using namespace tc;
 extern "C" int tc_direct_device(int kernel, double softening, int precision, const double* d_pos, int64_t n,
                                 const int64_t* d_rows, int64_t m, double* d_grad_rows, double* d_total, void* stream)
 {
-    if (!d_pos || !d_grad_rows || n <= 0 || m <= 0 || (kernel != TC_KERNEL_TSNE && kernel != TC_KERNEL_GRAVITY)) {
+    // without a row list the sinks are points 0..m-1, so m may not exceed n
+    if (!d_pos || !d_grad_rows || n <= 0 || m <= 0 || (kernel != TC_KERNEL_TSNE && kernel != TC_KERNEL_GRAVITY) ||
+        (precision != TC_PREC_FP32 && precision != TC_PREC_FP64) || (!d_rows && m > n)) {
         tc_set_error("tc_direct_device: invalid arguments");
         return TC_ERR_INVALID;
     }

@@ -117,9 +117,8 @@ int solve_fmm(Handle& h, double* d_grad, double* d_total, int accumulate, int sc
 // fmm_p.cu (tc_config.order != 0)
 int solve_fmm_order(Handle& h, double* d_grad, double* d_total, int accumulate, int scatter);
 int build_multipoles(Handle& h);
-// order-p FP32 tree (tree_p.cu): Morton codes, and the node records after the
-// gather of the sorted particles
-int morton_p(Handle& h, const double* d_pos, int64_t n, double maxx, double maxy);
+// order-p FP32 tree (tree_p.cu): the node records after the gather of the
+// sorted particles
 int build_records_p(Handle& h, double hleaf);
 // particle-mesh t-SNE repulsion (pm.cu): gradient in input order and Z
 int pm_solve_device(int n_interp, double cell_size, int min_intervals, const double* d_pos, int64_t n, double* d_grad,

@@ -294,20 +294,16 @@ int build_tree(Handle& h, const double* d_pos, int64_t n, double minx, double mi
 
     if ((rc = record(h, 0))) return rc;
     TC_CUDA_TRY(cudaMemsetAsync(h.err.p, 0, sizeof(uint32_t), s));
-    // order p in FP32: the physics-mode records of tree_p.cu (no FP64-exact codes or moments)
+    // order p in FP32: the physics-mode moments of tree_p.cu.  Codes, permutation and topology are the
+    // reference's on every path: FP64 Morton quantisation and a sort over all 32 code bits, whose tie
+    // order (stable) fixes the in-leaf order the reference's unstable sort leaves undefined.
     const bool physics = h.cfg.order && !f64;
-    if (physics) {
-        if ((rc = morton_p(h, d_pos, n, maxx, maxy))) return rc;
-    } else {
-        k_morton<<<grid_for(n, 256), 256, 0, s>>>((const double2*)d_pos, n, minx, miny, maxx, maxy, L,
-                                                   P<uint32_t>(h.codes), P<uint32_t>(h.err));
-        h.launches++;
-    }
+    k_morton<<<grid_for(n, 256), 256, 0, s>>>((const double2*)d_pos, n, minx, miny, maxx, maxy, L,
+                                               P<uint32_t>(h.codes), P<uint32_t>(h.err));
+    h.launches++;
     TC_CUDA_TRY(cudaGetLastError());
-    // the reference-order path sorts whole codes (its tie order is part of the parity contract); the
-    // physics path only the leaf bits
     rc = radix_sort_u32(P<uint32_t>(h.codes), P<uint32_t>(h.perm), P<uint32_t>(h.alt_keys), P<uint32_t>(h.alt_vals), n,
-                        P<uint32_t>(h.tmp), s, &h.launches, physics ? sort_lo_bit(depth) : 0);
+                        P<uint32_t>(h.tmp), s, &h.launches, 0);
     if (rc || (rc = record(h, 1))) return rc;
     const uint32_t li = level_index(depth);
     const int64_t nleaf = (int64_t)1 << (2 * depth);

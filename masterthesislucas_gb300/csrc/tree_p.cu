@@ -1,12 +1,12 @@
 // Tree records for the order-p path ("physics mode"): the same level-dense
 // quadtree as NBodySolverFMM_SYM_MORTON::updateTree
-// (src/nbodysolvers/cpu/nBodySolverFMM_SYM_MORTON.h:79-95, 328-470), built
-// without the FP64 arithmetic the reference-order path needs for bit parity.
-// FP64 runs at 1/64 of the FP32 rate on GB300, and the order-p solve reads
-// only cell-relative FP32 data, so here:
-// * Morton codes quantise (p - min) * (65536 / L) in FP32 after one FP64
-//   subtraction (a point within ~1e-7 L of a cell edge may land in the
-//   neighbouring cell; its cell-relative coordinates stay exact);
+// (src/nbodysolvers/cpu/nBodySolverFMM_SYM_MORTON.h:79-95, 328-470).  Codes,
+// permutation and topology come from the bit-exact k_morton + 32-bit sort of
+// tree.cu, so counts, first particles, child links and the FP64 boxes
+// (BBcentre, BBlength, rounded in the reference's operation order) are the
+// reference's.  The moments are built without the FP64 arithmetic the
+// reference-order path needs for bit parity -- FP64 runs at 1/64 of the FP32
+// rate on GB300, and the order-p solve reads only cell-relative FP32 data:
 // * leaf centres of mass and second moments are FP32 sums of the particles'
 //   cell-relative coordinates (written by the gather in FP64 arithmetic);
 // * internal nodes combine their children's relative centres of mass shifted
@@ -19,43 +19,28 @@
 namespace tc {
 namespace {
 
-// (p - min) >= 0 and <= ext, tested on the bit patterns of the non-negative
-// difference (NaN fails both)
-__device__ inline bool in_range(double a, double ext)
-{
-    const unsigned long long b = (unsigned long long)__double_as_longlong(a);
-    const unsigned long long e = (unsigned long long)__double_as_longlong(ext);
-    return (b >> 63) == 0 && b <= e;
-}
-
-__device__ inline uint32_t quantise(double a, float s)
-{
-    const float v = (float)a * s;
-    const uint32_t q = v > 0.f ? (uint32_t)v : 0u;
-    return q < 65535u ? q : 65535u;
-}
-
-__global__ void k_morton_p(const double2* __restrict__ pos, int64_t n, double minx, double miny, double extx,
-                           double exty, float s65536, uint32_t* __restrict__ codes, uint32_t* __restrict__ err)
-{
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double2 p = pos[i];
-        const double ax = p.x - minx, ay = p.y - miny;
-        if (!(in_range(ax, extx) && in_range(ay, exty))) atomicOr(err, 1u);
-        codes[i] = (spread16(quantise(ay, s65536)) << 1) | spread16(quantise(ax, s65536));
-    }
-}
-
 __device__ inline double2 cell_centre(int64_t i, double minx, double miny, double h)
 {
     const uint32_t ix = compact16((uint32_t)i), iy = compact16((uint32_t)i >> 1);
     return make_double2(minx + ((double)ix + 0.5) * h, miny + ((double)iy + 0.5) * h);
 }
 
-// the node record from its relative COM and second moment (about the COM)
-__device__ inline void write_node(int64_t node, double2 centre, double h, uint32_t c, float rx, float ry, float a,
-                                  float b, float d, float br, double2* com64, double* m0, double* m2, double2* bbc,
-                                  double* bblen, float* comrel, float* m0r, float* m2t, float* bmax)
+// createLeafNodes' box (:343-345): BBcentre = (minPos + h * g) + 0.5 * h, with
+// round-to-nearest operations the compiler does not contract into FMAs
+__device__ inline double2 leaf_box(int64_t i, double minx, double miny, double h)
+{
+    const uint32_t ix = compact16((uint32_t)i), iy = compact16((uint32_t)i >> 1);
+    const double hh = __dmul_rn(0.5, h);
+    return make_double2(__dadd_rn(__dadd_rn(minx, __dmul_rn(h, (double)ix)), hh),
+                        __dadd_rn(__dadd_rn(miny, __dmul_rn(h, (double)iy)), hh));
+}
+
+// the node record from its relative COM and second moment (about the COM);
+// centre is the compute frame's cell centre, box the reference's BBcentre
+__device__ inline void write_node(int64_t node, double2 centre, double2 box, double h, uint32_t c, float rx,
+                                  float ry, float a, float b, float d, float br, double2* com64, double* m0,
+                                  double* m2, double2* bbc, double* bblen, float* comrel, float* m0r, float* m2t,
+                                  float* bmax)
 {
     bmax[node] = br;
     const float ic = 1.0f / (float)c;
@@ -64,7 +49,7 @@ __device__ inline void write_node(int64_t node, double2 centre, double h, uint32
     m2[3 * node] = (double)a;
     m2[3 * node + 1] = (double)b;
     m2[3 * node + 2] = (double)d;
-    bbc[node] = centre;
+    bbc[node] = box;
     bblen[node] = h;
     comrel[2 * node] = rx;
     comrel[2 * node + 1] = ry;
@@ -114,8 +99,8 @@ __global__ void k_leaf_small_p(int depth, double minx, double miny, double h, ui
             d = fmaf(ry, ry, d);
             r2 = fmaxf(r2, fmaf(rx, rx, ry * ry));
         }
-        write_node(node, cell_centre(i, minx, miny, h), h, c, sx, sy, a, b, d, sqrtf(r2), com64, m0, m2, bbc, bblen,
-                   comrel, m0r, m2t, bmax);
+        write_node(node, cell_centre(i, minx, miny, h), leaf_box(i, minx, miny, h), h, c, sx, sy, a, b, d,
+                   sqrtf(r2), com64, m0, m2, bbc, bblen, comrel, m0r, m2t, bmax);
     }
 }
 
@@ -157,8 +142,8 @@ __global__ void k_leaf_big_p(int depth, double minx, double miny, double h, cons
         d = warp_sum(d);
         for (int o = 16; o > 0; o >>= 1) r2 = fmaxf(r2, __shfl_xor_sync(0xffffffffu, r2, o));
         if (lane == 0)
-            write_node(node, cell_centre(i, minx, miny, h), h, c, sx, sy, a, b, d, sqrtf(r2), com64, m0, m2, bbc,
-                       bblen, comrel, m0r, m2t, bmax);
+            write_node(node, cell_centre(i, minx, miny, h), leaf_box(i, minx, miny, h), h, c, sx, sy, a, b, d,
+                       sqrtf(r2), com64, m0, m2, bbc, bblen, comrel, m0r, m2t, bmax);
     }
 }
 
@@ -188,11 +173,18 @@ __global__ void k_bottom_up_p(int l, double minx, double miny, double hl, uint32
         uint32_t fp = 0;
         float sx = 0.f, sy = 0.f;
         float2 g[4];
+        double2 box = make_double2(0.0, 0.0);
 #pragma unroll
         for (int j = 3; j >= 0; j--) {
             g[j] = make_float2(0.f, 0.f);
             if (c4[j] == 0) continue;
             fp = first[fc + j];
+            // bottomUpNodeConstruction's box (:381-470): offset[j] * L_child + BBcentre_child, the lowest
+            // non-empty child last (bit 0 of the child slot is x)
+            const double cl = bblen[fc + j];
+            const double2 cb = bbc[fc + j];
+            box = make_double2(__dadd_rn(__dmul_rn((j & 1) ? -0.5 : 0.5, cl), cb.x),
+                               __dadd_rn(__dmul_rn((j & 2) ? -0.5 : 0.5, cl), cb.y));
             const float2 r = cr2[fc + j];
             g[j] = make_float2(r.x + ((j & 1) ? q : -q), r.y + ((j & 2) ? q : -q));
             sx = fmaf((float)c4[j], g[j].x, sx);
@@ -215,8 +207,8 @@ __global__ void k_bottom_up_p(int l, double minx, double miny, double hl, uint32
         }
         count[node] = cnt;
         first[node] = fp;
-        write_node(node, cell_centre(i, minx, miny, hl), hl, cnt, sx, sy, a, b, d, br, com64, m0, m2, bbc, bblen,
-                   comrel, m0r, m2t, bmax);
+        write_node(node, cell_centre(i, minx, miny, hl), box, hl, cnt, sx, sy, a, b, d, br, com64, m0, m2, bbc,
+                   bblen, comrel, m0r, m2t, bmax);
     }
 }
 
@@ -250,18 +242,6 @@ int build_records_p(Handle& h, double hleaf)
                                                         P<float>(h.bmax));
         h.launches++;
     }
-    TC_CUDA_TRY(cudaGetLastError());
-    return TC_OK;
-}
-
-int morton_p(Handle& h, const double* d_pos, int64_t n, double maxx, double maxy)
-{
-    // the sort reads only the leaf bits; with an odd number of passes it starts from alt_keys
-    const int npass = (32 - sort_lo_bit(h.depth) + 7) / 8;
-    uint32_t* out = (npass & 1) ? P<uint32_t>(h.alt_keys) : P<uint32_t>(h.codes);
-    k_morton_p<<<grid_for(n, 256), 256, 0, h.stream>>>((const double2*)d_pos, n, h.minx, h.miny, maxx - h.minx,
-                                                      maxy - h.miny, (float)(65536.0 / h.L), out, P<uint32_t>(h.err));
-    h.launches++;
     TC_CUDA_TRY(cudaGetLastError());
     return TC_OK;
 }

@@ -133,6 +133,23 @@ def sort_perm(codes):
     return perm
 
 
+def build_tree(pos, *, depth, mn=None, mx=None):
+    """updateTree alone (createMortonCode, the stable code sort,
+    createLeafNodes, bottomUpNodeConstruction): sorted codes, permutation,
+    sorted positions and the node records (NODE_DTYPE; the C fields zero)."""
+    pos = np.ascontiguousarray(pos, np.float64)
+    if mn is None:
+        mn, mx = bbox(pos)
+    mn = np.ascontiguousarray(mn, np.float64)
+    mx = np.ascontiguousarray(mx, np.float64)
+    codes = morton_codes(pos, mn, mx)
+    perm = sort_perm(codes)
+    ps = np.ascontiguousarray(pos[perm])
+    nodes = np.zeros(node_count(depth), NODE_DTYPE)
+    lib().orc_build_tree(depth, len(pos), _p(ps), _p(mn), _p(mx), _p(nodes))
+    return dict(codes=codes[perm], ids=perm, pos=ps, nodes=nodes)
+
+
 def sym_fmm(pos, *, kernel=KERNEL_TSNE, eps=0.0, max_children=16, depth=-1, theta=0.5,
             mn=None, mx=None, want_nodes=True, symmetric=True):
     """updateTree + solveNbody of the symmetric Morton FMM (sorted-order

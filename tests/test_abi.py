@@ -72,3 +72,15 @@ def test_dropin_adaptor_builds_against_reference_interface(L):
                        text=True)
     assert r.returncode == 0, r.stderr
     assert os.path.exists(os.path.join(ROOT, "oracle", "_ref", "dropin_check"))
+
+
+@pytest.mark.parametrize("fn", ["tc_direct_device", "tc_direct_device_noalloc"])
+def test_direct_rejects_more_rows_than_points_without_a_row_list(L, fn):
+    """Without a row list the sinks are points 0..m-1: m > n must be rejected
+    before anything is launched (the pointers are never dereferenced)."""
+    fake = ctypes.c_void_p(256)
+    f = getattr(L, fn)
+    assert f(1, 1e-3, 1, fake, 100, None, 101, fake, None, None) == -1
+    assert b"invalid" in L.tc_last_error()
+    # an unknown precision code is rejected the same way
+    assert f(1, 1e-3, 7, fake, 100, None, 10, fake, None, None) == -1

@@ -38,6 +38,21 @@ def test_sym_fmm_bit_exact(golden, case):
     assert r["total"] == float(g["total"])
 
 
+@pytest.mark.parametrize("case", SYM_CASES)
+def test_tree_build_alone_bit_exact(golden, case):
+    """oracle.build_tree (updateTree without the solve) gives the reference's
+    codes, permutation, sorted positions and node records: the large-N tree
+    tests use it where a full solve would take minutes."""
+    g = golden(case)
+    r = oracle.build_tree(g["pos"], depth=int(g["depth"]), mn=g["minmax"][:2], mx=g["minmax"][2:])
+    np.testing.assert_array_equal(r["codes"], g["codes"])
+    np.testing.assert_array_equal(r["ids"], g["ids"])
+    np.testing.assert_array_equal(r["pos"], g["pos_sorted"])
+    ref_nodes = oracle.ref_nodes_to_struct(g["nodes"])
+    for f in ("bb_c", "bb_len", "first_child", "first_part", "count", "com", "m0", "m2"):
+        np.testing.assert_array_equal(r["nodes"][f], ref_nodes[f], err_msg=f)
+
+
 def test_depth_rule_matches_reference(golden):
     # getDepth(16, N) = ceil(log((4/pi) * (N/16)) / log 4) with integer N/16
     assert oracle.get_depth(16, 70000) == 7
