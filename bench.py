@@ -942,7 +942,9 @@ def compact_calib(calib):
 # DRAM bytes (read + write) of one k_near_p launch, from an ncu capture of the force step at that configuration
 # (dram__bytes_read.sum + dram__bytes_write.sum), keyed by (n, depth, order, opening criterion, theta, leaf P2P).
 NEAR_TRAFFIC = {
-    (4194304, 11, 8, "bmax", 0.75, 64): (None, "not captured"),
+    (4194304, 11, 8, "bmax", 0.75, 64): (249966080 + 98462208,
+                                          "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_near_p launch "
+                                          "of the force step at this configuration (bit-exact tree)"),
 }
 
 

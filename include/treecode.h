@@ -97,6 +97,37 @@ int tc_set_variant(tc_handle* h, int variant);
 #define TC_MAC_BMAX 1
 int tc_set_mac(tc_handle* h, int mac);
 
+/* Expansion centre of an order-p FP32 handle (no counterpart in the
+ * reference, whose expansions are about each node's centre of mass):
+ * TC_CENTRE_COM  multipoles and locals about each node's centre of mass (the
+ *                default);
+ * TC_CENTRE_BOX  about each node's cell centre.  Every same-level pair is then
+ *                an integer multiple of the cell size apart, so the M2L
+ *                operator of a pair depends only on its level and grid
+ *                offset; TC_MAC_BMAX measures the particles' distance from
+ *                the cell centre.
+ * Takes effect at the next tc_update_tree.                                 */
+#define TC_CENTRE_COM 0
+#define TC_CENTRE_BOX 1
+int tc_set_expansion_centre(tc_handle* h, int centre);
+
+/* M2L engine of a box-centred order-p handle (no counterpart in the
+ * reference, whose M2L is TSNE_FMM_SYM_MORTON_NN_Kernel,
+ * nBodySolverFMM_SYM_MORTON.h:622-723, in FP64 on the CPU):
+ * TC_M2L_SIMT    FP32 kernels, one sink node per thread or warp (default);
+ * TC_M2L_TENSOR  the 5th-generation tensor cores: per level, tiles of 128
+ *                sink nodes times the level's per-offset K x K operators in
+ *                BF16 with a hi/lo split (three products, FP32 accumulation,
+ *                about 16 significant bits).  Fixed order only; opening
+ *                angles that reach list offsets beyond 15 cells (theta below
+ *                about 0.2 with TC_MAC_BMAX) are rejected at tc_solve.  Its
+ *                operators take (depth + 1) * (2R+1)^2 * 4 * K_pad^2 bytes
+ *                and its BF16 multipole copy 4 * K_pad bytes per node.
+ * Needs TC_CENTRE_BOX set first; setting TC_CENTRE_COM returns to SIMT.  */
+#define TC_M2L_SIMT 0
+#define TC_M2L_TENSOR 1
+int tc_set_m2l_engine(tc_handle* h, int engine);
+
 /* Per-pair expansion order on a TC_MAC_BMAX handle of order p in {6, 8, 10,
  * 12} (no counterpart in the reference): an accepted pair with ratio
  * r = (b_A + b_B)/|com_A - com_B| < theta is evaluated at the lowest order

@@ -29,6 +29,10 @@ TC_MAC_CELL = 0
 TC_REPULSION_TREE = 0
 TC_REPULSION_PM = 1
 TC_MAC_BMAX = 1
+TC_CENTRE_COM = 0
+TC_CENTRE_BOX = 1
+TC_M2L_SIMT = 0
+TC_M2L_TENSOR = 1
 
 
 class TcConfig(ctypes.Structure):
@@ -55,6 +59,8 @@ SIGNATURES = {
     "tc_set_theta": (_I, [_P, _D]),
     "tc_set_variant": (_I, [_P, _I]),
     "tc_set_mac": (_I, [_P, _I]),
+    "tc_set_expansion_centre": (_I, [_P, _I]),
+    "tc_set_m2l_engine": (_I, [_P, _I]),
     "tc_set_adaptive_order": (_I, [_P, _D]),
     "tc_set_leaf_p2p": (_I, [_P, _I]),
     "tc_pm_solve": (_I, [_I, _D, _I, _P, _I64, _P, _P]),

@@ -28,6 +28,19 @@ int tc_cuda_fail(cudaError_t e, const char* what)
 
 namespace tc {
 
+int sm_count()
+{
+    static int cache[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (cache[dev] == 0) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 152;
+        cache[dev] = v;
+    }
+    return cache[dev];
+}
+
 int ensure(Buf& b, size_t bytes)
 {
     if (bytes == 0) bytes = 16;
@@ -155,7 +168,7 @@ __global__ void k_prel(const double2* __restrict__ pos64, const uint32_t* __rest
 int bbox_keys(const double* d_pos, int64_t n, double* d_keys4, uint32_t* d_err, cudaStream_t s)
 {
     k_bbox_init<<<1, 1, 0, s>>>(d_keys4);
-    k_bbox<<<grid_for(n, 256, kSMs * 4), 256, 0, s>>>((const double2*)d_pos, n, d_keys4, d_err);
+    k_bbox<<<grid_for(n, 256, sm_count() * 4), 256, 0, s>>>((const double2*)d_pos, n, d_keys4, d_err);
     TC_CUDA_TRY(cudaGetLastError());
     return TC_OK;
 }
@@ -167,7 +180,7 @@ int device_bbox(Handle& h, const double* d_pos, int64_t n, double mn[2], double 
     double* o = P<double>(h.dtotal) + 2;
     TC_CUDA_TRY(cudaMemsetAsync(h.err.p, 0, 4, h.stream));
     k_bbox_init<<<1, 1, 0, h.stream>>>(o);
-    k_bbox<<<grid_for(n, 256, kSMs * 4), 256, 0, h.stream>>>((const double2*)d_pos, n, o, P<uint32_t>(h.err));
+    k_bbox<<<grid_for(n, 256, sm_count() * 4), 256, 0, h.stream>>>((const double2*)d_pos, n, o, P<uint32_t>(h.err));
     h.launches += 2;
     TC_CUDA_TRY(cudaMemcpyAsync(h.h_words, o, 32, cudaMemcpyDeviceToHost, h.stream));
     TC_CUDA_TRY(cudaMemcpyAsync(h.h_words + 8, h.err.p, 4, cudaMemcpyDeviceToHost, h.stream));
@@ -303,7 +316,7 @@ int tc_destroy(tc_handle* t)
     if (h.stream) cudaStreamSynchronize(h.stream);
     Buf* bufs[] = {&h.codes, &h.perm, &h.alt_keys, &h.alt_vals, &h.pos_in, &h.pos64, &h.prel, &h.grad_acc,
                    &h.count, &h.first, &h.com64, &h.m0, &h.m2, &h.bbc, &h.bblen, &h.comrel, &h.m0r, &h.m2t,
-                   &h.loc, &h.locfin, &h.mu, &h.chunk, &h.zwork, &h.zloc, &h.counters, &h.ptr_pool, &h.idx_pool, &h.cnt_tmp, &h.lstat, &h.ord_pool, &h.nfeat, &h.dec, &h.bigleaf, &h.chunk_leaf, &h.act, &h.act_pos, &h.bmax, &h.diagpart, &h.ctrl_w, &h.tmp, &h.err, &h.zpart, &h.dtotal, &h.sumtmp,
+                   &h.loc, &h.locfin, &h.mu, &h.chunk, &h.zwork, &h.zloc, &h.counters, &h.ptr_pool, &h.idx_pool, &h.cnt_tmp, &h.lstat, &h.ord_pool, &h.nfeat, &h.dec, &h.bigleaf, &h.chunk_leaf, &h.act, &h.act_pos, &h.bmax, &h.celloff, &h.mqueue, &h.tc_ops, &h.tc_mubf, &h.diagpart, &h.ctrl_w, &h.tmp, &h.err, &h.zpart, &h.dtotal, &h.sumtmp,
                    &h.host_stage, &h.ids_dev};
     for (Buf* b : bufs) release(*b);
     if (h.step_graph) cudaGraphExecDestroy(h.step_graph);
@@ -608,7 +621,7 @@ extern "C" int tc_async_status(tc_handle* t)
 {
     if (!t) return TC_ERR_INVALID;
     const Handle& h = t->h;
-    return (h.h_words[8] ? 1 : 0) | (h.h_words[40] ? 2 : 0);
+    return (h.h_words[8] ? 1 : 0) | (h.h_words[40] ? 2 : 0) | (h.h_words[48] ? 4 : 0);
 }
 
 extern "C" int tc_set_variant(tc_handle* t, int variant)
@@ -650,6 +663,36 @@ extern "C" int tc_set_adaptive_order(tc_handle* t, double slack)
     h.adapt = enable;
     h.adapt_slack = enable ? slack : 0.0;
     h.tree_ready = false;
+    return TC_OK;
+}
+
+extern "C" int tc_set_expansion_centre(tc_handle* t, int centre)
+{
+    if (!t || (centre != TC_CENTRE_COM && centre != TC_CENTRE_BOX)) {
+        tc_set_error("tc_set_expansion_centre: unknown centre");
+        return TC_ERR_INVALID;
+    }
+    if (centre == TC_CENTRE_BOX && (t->h.cfg.order == 0 || t->h.cfg.precision != TC_PREC_FP32)) {
+        tc_set_error("tc_set_expansion_centre: box-centred expansions need an order-p FP32 handle");
+        return TC_ERR_INVALID;
+    }
+    t->h.centre = centre;
+    if (centre != TC_CENTRE_BOX) t->h.m2l_tc = false;
+    t->h.tree_ready = false;
+    return TC_OK;
+}
+
+extern "C" int tc_set_m2l_engine(tc_handle* t, int engine)
+{
+    if (!t || (engine != TC_M2L_SIMT && engine != TC_M2L_TENSOR)) {
+        tc_set_error("tc_set_m2l_engine: unknown engine");
+        return TC_ERR_INVALID;
+    }
+    if (engine == TC_M2L_TENSOR && t->h.centre != TC_CENTRE_BOX) {
+        tc_set_error("tc_set_m2l_engine: the tensor-core M2L needs box-centred expansions (set them first)");
+        return TC_ERR_INVALID;
+    }
+    t->h.m2l_tc = engine == TC_M2L_TENSOR;
     return TC_OK;
 }
 

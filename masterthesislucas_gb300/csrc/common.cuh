@@ -17,7 +17,9 @@ void tc_set_error(const char* fmt, ...);
 
 namespace tc {
 
-constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs
+// multiprocessors of the current device (cudaDevAttrMultiProcessorCount, looked
+// up once per device; 152 on GB300): grids are sized in multiples of it
+int sm_count();
 // leaves above this many particles take a warp (leaf moments, P2M) in the order-p path
 constexpr uint32_t kLeafSmall = 32;
 
@@ -85,7 +87,7 @@ __device__ inline uint32_t block_exclusive_scan(uint32_t v, uint32_t& total)
 }
 
 
-inline int grid_for(int64_t n, int block, int cap = kSMs * 32)
+inline int grid_for(int64_t n, int block, int cap = sm_count() * 32)
 {
     int64_t g = (n + block - 1) / block;
     if (g < 1) g = 1;

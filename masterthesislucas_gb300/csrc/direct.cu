@@ -100,7 +100,7 @@ int direct_t(K ker, const double* d_pos, int64_t n, const int64_t* d_rows, int64
 {
     const int64_t rb = (m + DT - 1) / DT;
     // enough slices to fill the GPU several times over
-    int64_t nslice = (kSMs * 8 + rb - 1) / rb;
+    int64_t nslice = (sm_count() * 8 + rb - 1) / rb;
     if (nslice < 1) nslice = 1;
     int64_t slice = (n + nslice - 1) / nslice;
     slice = ((slice + DT - 1) / DT) * DT;
@@ -236,7 +236,7 @@ int direct_noalloc_t(K ker, const double* d_pos, int64_t n, const int64_t* d_row
     const int64_t rb = (m + DT - 1) / DT;
     // as many source slices as fill the GPU and fit beside the m row sums
     int64_t fit = (kNoAllocScratch - m) / (3 * m);
-    int64_t nslice = (kSMs * 8 + rb - 1) / rb;
+    int64_t nslice = (sm_count() * 8 + rb - 1) / rb;
     if (nslice > fit) nslice = fit;
     if (nslice < 1) nslice = 1;
     int64_t slice = (n + nslice - 1) / nslice;

@@ -24,6 +24,9 @@ struct PotParams {
     float c;     // u = r^2 + c (before scaling)
     float kappa; // pair term t = kappa * phi
     int kind;    // TC_KERNEL_*
+    // expansions about the centre of mass have no dipole; about the cell centre
+    // (TC_CENTRE_BOX) the M2L includes it
+    int dipole = 0;
 };
 
 // scaled derivatives D_g, |g| <= P, at scaled offset (x, y) for a level of size h

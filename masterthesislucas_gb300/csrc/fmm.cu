@@ -552,7 +552,7 @@ int solve_t(Handle& h, K ker, double* d_grad, int accumulate, int scatter, doubl
     for (int l = 1; l <= dep; l++) {
         const int64_t nl = (int64_t)1 << (2 * l);
         const real hl = (real)(h.L / (double)(1u << l));
-        k_m2l<real, K><<<grid_for(nl * 32, 128, kSMs * 64), 128, 0, s>>>(
+        k_m2l<real, K><<<grid_for(nl * 32, 128, sm_count() * 64), 128, 0, s>>>(
             ker, l, hl, ptr + h.lists.nn_ptr_off[l], idx + h.lists.nn_idx_off[l], P<real>(h.comrel), P<real>(h.m0r),
             P<real>(h.m2t), loc, zp);
         h.launches++;
@@ -572,7 +572,7 @@ int solve_t(Handle& h, K ker, double* d_grad, int accumulate, int scatter, doubl
     uint32_t* nchunk = P<uint32_t>(h.cnt_tmp);
     uint32_t* chunk_ptr = P<uint32_t>(h.chunk);
     const int64_t nblk = (nleaf + kLeafWarps - 1) / kLeafWarps;
-    k_leaf_local<real, K><<<(unsigned)(nblk < kSMs * 256 ? nblk : kSMs * 256), 32 * kLeafWarps, 0, s>>>(
+    k_leaf_local<real, K><<<(unsigned)(nblk < sm_count() * 256 ? nblk : sm_count() * 256), 32 * kLeafWarps, 0, s>>>(
         ker, geo, P<uint32_t>(h.count), P<uint32_t>(h.first), P<double2>(h.com64), P<double>(h.bblen),
         P<real>(h.comrel), P<real>(h.m0r), loc, ptr + h.lists.near_ptr_off[dep], idx + h.lists.near_idx_off[dep],
         P<double2>(h.pos64), P<real>(h.prel), P<real>(h.locfin), P<double>(h.zloc), nchunk,
@@ -580,7 +580,7 @@ int solve_t(Handle& h, K ker, double* d_grad, int accumulate, int scatter, doubl
     if ((rc = exclusive_scan_u32(nchunk, chunk_ptr, nleaf, P<uint32_t>(h.tmp), s))) return rc;
     if ((rc = record(h, 5))) return rc;
     const int64_t wblk = (wmax + kLeafWarps - 1) / kLeafWarps;
-    k_leaf_near<real, K><<<(unsigned)(wblk < kSMs * 256 ? wblk : kSMs * 256), 32 * kLeafWarps, 0, s>>>(
+    k_leaf_near<real, K><<<(unsigned)(wblk < sm_count() * 256 ? wblk : sm_count() * 256), 32 * kLeafWarps, 0, s>>>(
         ker, geo, P<uint32_t>(h.count), P<uint32_t>(h.first), P<double2>(h.com64), P<double>(h.bblen),
         P<real>(h.comrel), P<real>(h.m0r), P<real>(h.m2t), P<real>(h.locfin), ptr + h.lists.near_ptr_off[dep],
         idx + h.lists.near_idx_off[dep], chunk_ptr, P<double2>(h.pos64), P<real>(h.prel), P<uint32_t>(h.perm),

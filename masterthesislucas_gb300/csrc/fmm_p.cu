@@ -20,6 +20,7 @@
 
 #include "expansion.cuh"
 #include "kernels.cuh"
+#include "m2l_tc.cuh"
 #include "state.cuh"
 
 namespace tc {
@@ -356,22 +357,37 @@ __device__ __forceinline__ void m2l_acc(float Rx, float Ry, float hl, const PotP
     float D[K];
     derivs<P>(Rx, Ry, hl, pp, D);
     const float4* m4 = reinterpret_cast<const float4*>(m);
+    float dip[2] = {0.f, 0.f};
 #pragma unroll
     for (int c = 0; c < KS / 4; c++) {
         const float4 q = __ldg(m4 + c);
         const float mv[4] = {q.x, q.y, q.z, q.w};
+        if (c == 0) {
+            dip[0] = q.y;
+            dip[1] = q.z;
+        }
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             const int ia = 4 * c + j;
             if (ia >= K) continue;
             const int ka = cdeg(ia), ba = ia - ka * (ka + 1) / 2;
-            if (ka == 1) continue;  // dipole vanishes about the COM
+            if (ka == 1) continue;  // the dipole vanishes about the COM (added below about the cell centre)
             const float ma = (ka & 1) ? -mv[j] : mv[j];
 #pragma unroll
             for (int kb = 0; kb + ka <= P; kb++)
 #pragma unroll
                 for (int bb = 0; bb <= kb; bb++) L[cidx(kb - bb, bb)] += ma * D[cidx(ka - ba + kb - bb, ba + bb)];
         }
+    }
+    if (pp.dipole) {
+        // a = (1, 0) and (0, 1): sign (-1)^1
+#pragma unroll
+        for (int kb = 0; kb + 1 <= P; kb++)
+#pragma unroll
+            for (int bb = 0; bb <= kb; bb++) {
+                const int ab = kb - bb;
+                L[cidx(ab, bb)] -= dip[0] * D[cidx(ab + 1, bb)] + dip[1] * D[cidx(ab, bb + 1)];
+            }
     }
 }
 
@@ -950,6 +966,64 @@ __global__ void k_sum_z2(const double* __restrict__ a, int64_t na, const double*
     }
 }
 
+// M2L of every level on the tensor cores (box-centred expansions): the level's
+// operators, the BF16 hi/lo multipole rows, then one persistent launch per
+// level writing loc and zpart as the SIMT M2L does
+template <int Q>
+int m2l_tensor(Handle& h, const PotParams& pp)
+{
+    using S = tcm::Shape<Q>;
+    cudaStream_t s = h.stream;
+    const int dep = h.depth;
+    if (h.centre != TC_CENTRE_BOX) {
+        tc_set_error("tensor-core M2L: needs box-centred expansions (tc_set_expansion_centre)");
+        return TC_ERR_STATE;
+    }
+    if (h.adapt || h.ctrl_on) {
+        tc_set_error("tensor-core M2L: fixed order only (no per-pair orders or controller)");
+        return TC_ERR_STATE;
+    }
+    const int R = tcm::offset_radius(h.mac == TC_MAC_BMAX, h.cfg.theta);
+    if (R > tcm::kMaxR) {
+        tc_set_error("tensor-core M2L: theta %g reaches offsets beyond %d cells", h.cfg.theta, tcm::kMaxR);
+        return TC_ERR_INVALID;
+    }
+    const int W = 2 * R + 1;
+    const size_t ops_level = (size_t)W * W * 2 * S::OPB;
+    int rc;
+    if ((rc = ensure(h.tc_ops, ops_level * (dep + 1))) ||
+        (rc = ensure(h.tc_mubf, (size_t)h.nnodes * 2 * S::ROWB)))
+        return rc;
+    static bool attr_set = false;
+    if (!attr_set) {
+        TC_CUDA_TRY(cudaFuncSetAttribute(tcm::k_m2l_tc<Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM));
+        attr_set = true;
+    }
+    uint32_t* status = P<uint32_t>(h.err) + 6;
+    TC_CUDA_TRY(cudaMemsetAsync(status, 0, 4, s));
+    const uint32_t* act = P<uint32_t>(h.act);
+    const uint32_t* act_pos = P<uint32_t>(h.act_pos);
+    tcm::k_mu_split<Q><<<grid_for(h.nnodes, 128), 128, 0, s>>>(h.nnodes, P<float>(h.mu), act, act_pos,
+                                                               P<uint8_t>(h.tc_mubf));
+    const uint32_t* ptr = P<uint32_t>(h.ptr_pool);
+    const uint32_t* idx = P<uint32_t>(h.idx_pool);
+    for (int l = 1; l <= dep; l++) {
+        const float hl = (float)(h.L / (double)(1u << l));
+        uint8_t* ops = P<uint8_t>(h.tc_ops) + ops_level * l;
+        tcm::k_m2l_tc_ops<Q><<<W * W, 128, 0, s>>>(hl, pp, R, ops);
+        const int64_t nl = (int64_t)1 << (2 * l);
+        const int64_t tiles = (nl + tcm::kRows - 1) / tcm::kRows;
+        const int grid = (int)(tiles < sm_count() ? tiles : sm_count());
+        tcm::k_m2l_tc<Q><<<grid, 128, S::SMEM, s>>>(l, R, ptr + h.lists.nn_ptr_off[l], idx + h.lists.nn_idx_off[l],
+                                                     P<float>(h.mu), P<uint8_t>(h.tc_mubf), ops, pp.kappa,
+                                                     P<float>(h.loc), P<double>(h.zpart), act, act_pos, status);
+        h.launches += 2;
+    }
+    h.launches += 1;
+    TC_CUDA_TRY(cudaGetLastError());
+    return TC_OK;
+}
+
 template <int ORD, typename KN>
 int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumulate, int scatter, double* d_total)
 {
@@ -987,9 +1061,13 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
     bool per_pair = false;
     if constexpr (ORD == 12) per_pair = h.ctrl_on || h.adapt;
     else if constexpr (ORD >= 6) per_pair = h.adapt;
-    const bool fuse = ORD < 10 && !per_pair;
+    const bool tc_m2l = h.m2l_tc;
+    const bool fuse = ORD < 10 && !per_pair && !tc_m2l;
     int nfused = 0;
-    for (int l = 1; l <= dep; l++) {
+    if (tc_m2l) {
+        if ((rc = m2l_tensor<ORD>(h, pp))) return rc;
+    }
+    for (int l = 1; l <= dep && !tc_m2l; l++) {
         const int64_t nl = (int64_t)1 << (2 * l);
         if (fuse && nl > kM2lWarpLevelNodes) continue;
         const uint32_t* np_ = ptr + h.lists.nn_ptr_off[l];
@@ -1059,7 +1137,7 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
     k_chunk_leaf<<<grid_for(nleaf, 256), 256, 0, s>>>(dep, chunk_ptr, P<uint32_t>(h.chunk_leaf), (uint32_t)wmax);
     if ((rc = record(h, 5))) return rc;
     const int64_t wblk = (wmax + kNearWarps - 1) / kNearWarps;
-    k_near_p<ORD, KN><<<(unsigned)(wblk < kSMs * 256 ? wblk : kSMs * 256), 32 * kNearWarps, 0, s>>>(
+    k_near_p<ORD, KN><<<(unsigned)(wblk < sm_count() * 256 ? wblk : sm_count() * 256), 32 * kNearWarps, 0, s>>>(
         ker, dep, hl(dep), count, P<uint32_t>(h.first), comrel, loc, ptr + h.lists.near_ptr_off[dep],
         idx + h.lists.near_idx_off[dep], chunk_ptr, P<uint32_t>(h.chunk_leaf), (uint32_t)wmax, P<float>(h.prel),
         P<uint32_t>(h.perm), d_grad, accumulate, scatter, P<double>(h.zwork), P<unsigned long long>(h.counters));
@@ -1069,6 +1147,19 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
         return rc;
     h.launches += 3 + 2 * dep + 6 - nfused;
     TC_CUDA_TRY(cudaGetLastError());
+    if (tc_m2l) {
+        // the tensor-core M2L's status word (list offsets beyond its operators, a bounded wait that gave up)
+        TC_CUDA_TRY(cudaMemcpyAsync(h.h_words + 48, P<uint32_t>(h.err) + 6, 4, cudaMemcpyDeviceToHost, s));
+        if (!h.nosync) {
+            TC_CUDA_TRY(cudaStreamSynchronize(s));
+            if (h.h_words[48]) {
+                tc_set_error("tensor-core M2L: %s", (h.h_words[48] & tcm::kErrTimeout)
+                                                          ? "a bounded device wait gave up"
+                                                          : "a list offset beyond the operator table");
+                return (h.h_words[48] & tcm::kErrTimeout) ? TC_ERR_TIMEOUT : TC_ERR_INVALID;
+            }
+        }
+    }
     return record(h, 7);
 }
 
@@ -1110,6 +1201,7 @@ int dispatch_kernel(Handle& h, double* d_grad, int accumulate, int scatter, doub
 {
     PotParams pp;
     pp.kind = h.cfg.kernel;
+    pp.dipole = h.centre == TC_CENTRE_BOX;
     if (h.cfg.kernel == TC_KERNEL_GRAVITY) {
         pp.nu = 0.5f;
         pp.c = (float)(h.cfg.softening * h.cfg.softening);

@@ -199,7 +199,7 @@ extern "C" int tc_lc_pair_errors(tc_handle* t, const int32_t* d_pairs, int64_t n
     TC_CUDA_TRY(cudaMemcpyAsync(dh.p, hl, sizeof(hl), cudaMemcpyHostToDevice, h.stream));
     PotParams pp;
     pp.kind = h.cfg.kernel;
-    const int grid = (int)(n < kSMs * 16 ? n : kSMs * 16);
+    const int grid = (int)(n < sm_count() * 16 ? n : sm_count() * 16);
     if (h.cfg.kernel == TC_KERNEL_GRAVITY) {
         pp.nu = 0.5f;
         pp.c = (float)(h.cfg.softening * h.cfg.softening);

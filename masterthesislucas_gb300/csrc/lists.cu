@@ -614,7 +614,7 @@ int build_lists(Handle& h)
             if (!fill) {
                 int rc2 = ensure(h.dec, (size_t)pcap * 16 + 64);
                 if (rc2) return rc2;
-                k_lists_ctrl_count<<<grid_for(nl, 32 * ctrl::kWarps, kSMs * 16), 32 * ctrl::kWarps, 0, s>>>(
+                k_lists_ctrl_count<<<grid_for(nl, 32 * ctrl::kWarps, sm_count() * 16), 32 * ctrl::kWarps, 0, s>>>(
                     l, (float)hl, (float)(h.ctrl_c / (hl * hl)), P<uint32_t>(h.count), P<float>(h.comrel),
                     P<float4>(h.nfeat), pnp, pni, pcap, nnc, nrc, P<uint8_t>(h.dec), P<float>(h.ctrl_w),
                     h.ctrl_log_tau, act, act_pos);

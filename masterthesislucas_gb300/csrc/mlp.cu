@@ -334,7 +334,7 @@ int tc_mlp_forward_tc(tc_mlp* m, const float* d_x, int64_t n, float* d_y)
 {
     if (!m || !d_x || !d_y || n <= 0) return TC_ERR_INVALID;
     const int64_t blocks = (n + 32 * ctrl::kWarps - 1) / (32 * ctrl::kWarps);
-    k_mlp_forward_tc<<<(unsigned)(blocks < kSMs * 16 ? blocks : kSMs * 16), 32 * ctrl::kWarps>>>(
+    k_mlp_forward_tc<<<(unsigned)(blocks < sm_count() * 16 ? blocks : sm_count() * 16), 32 * ctrl::kWarps>>>(
         P<float>(m->rounded), P<float>(m->mean), P<float>(m->stdv), d_x, n, d_y);
     TC_CUDA_TRY(cudaGetLastError());
     TC_CUDA_TRY(cudaDeviceSynchronize());
@@ -428,7 +428,7 @@ int tc_mlp_train(tc_mlp* m, const float* d_x, const float* d_t, int64_t n, int s
 int tc_mlp_forward(tc_mlp* m, const float* d_x, int64_t n, float* d_y)
 {
     if (!m || !d_x || !d_y || n <= 0) return TC_ERR_INVALID;
-    k_mlp_forward<<<grid_for(n, 128, kSMs * 8), 128>>>(P<float>(m->rounded), d_x, P<float>(m->mean),
+    k_mlp_forward<<<grid_for(n, 128, sm_count() * 8), 128>>>(P<float>(m->rounded), d_x, P<float>(m->mean),
                                                        P<float>(m->stdv), n, d_y);
     TC_CUDA_TRY(cudaGetLastError());
     TC_CUDA_TRY(cudaDeviceSynchronize());

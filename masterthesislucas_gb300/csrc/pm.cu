@@ -103,15 +103,47 @@ __global__ void __launch_bounds__(kPmThreads) k_pm_chunk_max(const double* __res
     if (threadIdx.x == 0) cmax[blockIdx.x] = mx;
 }
 
-// exclusive prefix maximum of the chunk maxima (one block)
-__global__ void k_pm_chunk_premax(double* __restrict__ c, int64_t nc)
+// exclusive prefix maximum of the chunk maxima: one block of kPmScanThreads
+// threads walks the chunks in tiles, each tile a warp-shuffle scan plus a
+// scan of the warp totals, carrying the running maximum between tiles (max is
+// exact, so the result does not depend on the grouping)
+constexpr int kPmScanThreads = 1024;
+
+__device__ inline double dmax_cmp(double a, double b) { return b > a ? b : a; }
+
+__global__ void __launch_bounds__(kPmScanThreads) k_pm_chunk_premax(double* __restrict__ c, int64_t nc)
 {
-    if (threadIdx.x != 0) return;
-    double run = -INFINITY;
-    for (int64_t i = 0; i < nc; i++) {
-        const double v = c[i];
-        c[i] = run;
-        if (v > run) run = v;
+    __shared__ double wtot[kPmScanThreads / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double carry = -INFINITY;
+    for (int64_t base = 0; base < nc; base += kPmScanThreads) {
+        const int64_t i = base + threadIdx.x;
+        const double v = i < nc ? c[i] : -INFINITY;
+        double inc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double u = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc = dmax_cmp(inc, u);
+        }
+        if (lane == 31) wtot[w] = inc;
+        __syncthreads();
+        if (w == 0) {
+            double t = wtot[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const double u = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= o) t = dmax_cmp(t, u);
+            }
+            wtot[lane] = t;  // inclusive maximum over warps 0..lane
+        }
+        __syncthreads();
+        double before = carry;
+        if (w > 0) before = dmax_cmp(before, wtot[w - 1]);
+        const double prev = __shfl_up_sync(0xffffffffu, inc, 1);
+        if (lane > 0) before = dmax_cmp(before, prev);
+        if (i < nc) c[i] = before;
+        carry = dmax_cmp(carry, wtot[kPmScanThreads / 32 - 1]);
+        __syncthreads();
     }
 }
 
@@ -155,17 +187,37 @@ __global__ void __launch_bounds__(kPmThreads) k_pm_chunk_min(const double* __res
     }
 }
 
-__global__ void k_pm_minmax_final(const double* __restrict__ cmin, const double* __restrict__ cmax_raw,
-                                  int64_t nc, double* __restrict__ mm)
+// the smallest non-record value and the largest chunk maximum, one block of
+// kPmScanThreads threads (comparison form, so NaN never enters)
+__global__ void __launch_bounds__(kPmScanThreads) k_pm_minmax_final(const double* __restrict__ cmin,
+                                                                    const double* __restrict__ cmax_raw, int64_t nc,
+                                                                    double* __restrict__ mm)
 {
-    if (threadIdx.x != 0) return;
+    __shared__ double smn[kPmScanThreads / 32], smx[kPmScanThreads / 32];
     double mn = INFINITY, mx = -INFINITY;
-    for (int64_t i = 0; i < nc; i++) {
+    for (int64_t i = threadIdx.x; i < nc; i += kPmScanThreads) {
         if (cmin[i] < mn) mn = cmin[i];
         if (cmax_raw[i] > mx) mx = cmax_raw[i];
     }
-    mm[0] = mn;
-    mm[1] = mx;
+    for (int o = 16; o > 0; o >>= 1) {
+        const double a = __shfl_xor_sync(0xffffffffu, mn, o), b = __shfl_xor_sync(0xffffffffu, mx, o);
+        if (a < mn) mn = a;
+        if (b > mx) mx = b;
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        smn[w] = mn;
+        smx[w] = mx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < kPmScanThreads / 32; k++) {
+            if (smn[k] < mn) mn = smn[k];
+            if (smx[k] > mx) mx = smx[k];
+        }
+        mm[0] = mn;
+        mm[1] = mx;
+    }
 }
 
 // ------------------------------------------------------------------ points and grid
@@ -427,9 +479,9 @@ int pm_solve_device(int n_interp, double cell_size, int min_intervals, const dou
     double* cmax = P<double>(w.vals_max);  // [0, nc): prefix maxima, [nc, 2nc): raw chunk maxima
     k_pm_chunk_max<<<(unsigned)nc, kPmThreads, 0, s>>>(d_pos, m, cmax + nc);
     TC_CUDA_TRY(cudaMemcpyAsync(cmax, cmax + nc, nc * 8, cudaMemcpyDeviceToDevice, s));
-    k_pm_chunk_premax<<<1, 32, 0, s>>>(cmax, nc);
+    k_pm_chunk_premax<<<1, kPmScanThreads, 0, s>>>(cmax, nc);
     k_pm_chunk_min<<<(unsigned)nc, kPmThreads, 0, s>>>(d_pos, m, cmax, P<double>(w.vals_min));
-    k_pm_minmax_final<<<1, 32, 0, s>>>(P<double>(w.vals_min), cmax + nc, nc, P<double>(w.mm));
+    k_pm_minmax_final<<<1, kPmScanThreads, 0, s>>>(P<double>(w.vals_min), cmax + nc, nc, P<double>(w.mm));
     double mm[2];
     TC_CUDA_TRY(cudaMemcpyAsync(mm, w.mm.p, 16, cudaMemcpyDeviceToHost, s));
     TC_CUDA_TRY(cudaStreamSynchronize(s));

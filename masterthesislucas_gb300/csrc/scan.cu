@@ -165,7 +165,9 @@ __global__ void k_scan_final2(const uint32_t* __restrict__ in0, uint32_t* __rest
     if (blockIdx.x == nb - 1 && threadIdx.x == 0) out[n] = min(carry + tot, cap);
 }
 
-constexpr int kSumBlocks = 8 * kSMs;
+// fixed (8 per SM of a 152-SM GB300) so that the order of the deterministic
+// sums does not depend on the device
+constexpr int kSumBlocks = 8 * 152;
 
 // stage 1 of sum_f64: block b sums the grid-stride slice b of a[0..na) ++ c[0..*nc)
 // (four loads in flight per thread over a, then the rest one at a time)

@@ -64,6 +64,8 @@ struct Handle {
     // order p: per node, the largest distance of its particles from its COM
     // (an upper bound for internal nodes), FP32
     Buf bmax;
+    Buf celloff;  // FP32 gather: leaf cell centres relative to the box corner
+    Buf mqueue;   // Morton codes: per-block queues of points for the FP64 path, then the per-block counts
     Buf diagpart;  // leapfrog diagnostics: per-block partial sums
     // learned order controller (order-p mode): weights + normalisation copy
     // no-sync mode (stream capture): no host round trips or stage events; the
@@ -71,6 +73,13 @@ struct Handle {
     // reference-order solver: 0 the symmetric FMM_SYM_MORTON, 1 the non-symmetric FMM_MORTON
     int variant = 0;
     int mac = 0;  // TC_MAC_CELL or TC_MAC_BMAX (order p)
+    // order p: TC_CENTRE_COM (expansions about each node's centre of mass) or TC_CENTRE_BOX (about its cell
+    // centre; comrel is then zero and bmax the particles' distance from the cell centre)
+    int centre = 0;
+    // order p, box-centred: M2L on the tensor cores (m2l_tc.cuh) instead of the FP32 SIMT kernels
+    bool m2l_tc = false;
+    Buf tc_ops;   // tensor-core M2L: BF16 hi/lo operators per level and offset
+    Buf tc_mubf;  // tensor-core M2L: BF16 hi/lo multipole rows per non-empty node
     // order p with TC_MAC_BMAX: per-pair expansion order from the bound
     bool adapt = false;
     double adapt_slack = 0.0;

@@ -1,6 +1,7 @@
 // Tree construction, bit-exact to NBodySolverFMM_SYM_MORTON::updateTree
 // (src/nbodysolvers/cpu/nBodySolverFMM_SYM_MORTON.h:79-95):
-//   createMortonCode (:538-561)  -> k_morton         (FP64, same op order)
+//   createMortonCode (:538-561)  -> k_morton_fast + k_morton_exact (FP32
+//                                   where its floor provably agrees, else FP64)
 //   integer_sort (:89)           -> radix_sort_u32   (stable on input order)
 //   createLeafNodes (:328-379)   -> k_gather_bounds + k_leaf_moments
 //   bottomUpNodeConstruction (:381-470) -> k_bottom_up, one launch per level
@@ -34,17 +35,106 @@ __device__ inline uint32_t morton_coord(double p, double nm, double L, double s6
     return (uint32_t)v;
 }
 
-__global__ void k_morton(const double2* __restrict__ pos, int64_t n, double minx, double miny, double maxx,
-                         double maxy, double L, uint32_t* __restrict__ codes, uint32_t* __restrict__ err)
+// IEEE double as an integer with the same order (for box tests on the integer pipe)
+__device__ inline long long dorder(double v)
+{
+    const long long b = __double_as_longlong(v);
+    return b >= 0 ? b : (long long)(0x8000000000000000ull - (unsigned long long)b);
+}
+
+// v rounded to the nearest float (ties to even) with integer operations: the
+// FP64 -> FP32 conversion instruction shares GB300's narrow FP64 pipe.
+// Results below the smallest normal float flush to a signed zero.
+__device__ inline float f32_rn(double v)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+    const int e = (int)((b >> 52) & 0x7FFull);
+    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+    if (e == 0x7FF) return m ? __uint_as_float(0x7FC00000u) : __uint_as_float(sign | 0x7F800000u);
+    const int ef = e - 1023 + 127;
+    if (ef <= 0) return __uint_as_float(sign);
+    if (ef >= 255) return __uint_as_float(sign | 0x7F800000u);
+    unsigned long long r = m >> 29;
+    const unsigned long long rem = m & ((1ull << 29) - 1ull);
+    if (rem > (1ull << 28) || (rem == (1ull << 28) && (r & 1ull))) r++;
+    // a mantissa carry (r = 2^23) moves into the exponent, as rounding does
+    const uint32_t bits = ((uint32_t)ef << 23) + (uint32_t)r;
+    return __uint_as_float(sign | (bits < 0x7F800000u ? bits : 0x7F800000u));
+}
+
+// createMortonCode's quantisation, fast form.  FP64 runs at 1/64 of the FP32
+// rate on GB300, so the quotient ((p - min) / L) * 65536 is first formed in
+// FP32 from the FP64 difference: fl32(fl32(p - min) * fl32(65536 / L)) is
+// within 3 * 2^-24 relative (<= 0.012 absolute below 65536) of the
+// reference's FP64 value, so its floor is the reference's whenever its
+// fraction lies in [1/64, 63/64).  Points with a coordinate closer than that
+// to a cell edge are queued, and k_morton_exact recomputes them with the
+// reference's FP64 arithmetic.  Each block queues into its own region of
+// morton_region(n, grid) entries (shared-memory counter, no global atomics).
+// The box test compares the doubles' order-preserving integer images.
+constexpr int kMortonThreads = 256;
+
+__host__ __device__ inline int64_t morton_region(int64_t n, int64_t grid)
+{
+    const int64_t per = grid * kMortonThreads;
+    return ((n + per - 1) / per) * kMortonThreads;
+}
+
+__global__ void __launch_bounds__(kMortonThreads)
+    k_morton_fast(const double2* __restrict__ pos, int64_t n, double minx, double miny, double maxx, double maxy,
+                  float s65536, uint32_t* __restrict__ codes, uint32_t* __restrict__ err,
+                  uint32_t* __restrict__ queue, uint32_t* __restrict__ qcount)
+{
+    __shared__ uint32_t s_count;
+    if (threadIdx.x == 0) s_count = 0;
+    __syncthreads();
+    uint32_t* region = queue + (int64_t)blockIdx.x * morton_region(n, gridDim.x);
+    const long long kx0 = dorder(minx), kx1 = dorder(maxx), ky0 = dorder(miny), ky1 = dorder(maxy);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double2 p = pos[i];
+        const long long kx = dorder(p.x), ky = dorder(p.y);
+        // NaN images lie outside every finite box
+        if (!(kx >= kx0 && kx <= kx1 && ky >= ky0 && ky <= ky1)) atomicOr(err, 1u);
+        const float vx = f32_rn(p.x - minx) * s65536, vy = f32_rn(p.y - miny) * s65536;
+        bool exact = false;
+        uint32_t q[2];
+        const float v2[2] = {vx, vy};
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+            const float v = v2[c];
+            if (v >= 65535.0f + 1.0f / 64.0f) {
+                q[c] = 65535u;  // the reference's clamp whatever the last bits
+            } else {
+                const float f = v - floorf(v);
+                exact |= !(f >= 1.0f / 64.0f && f < 63.0f / 64.0f);
+                q[c] = v > 0.0f ? (uint32_t)v : 0u;
+            }
+        }
+        if (exact)
+            region[atomicAdd(&s_count, 1u)] = (uint32_t)i;
+        else
+            codes[i] = (spread16(q[1]) << 1) | spread16(q[0]);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) qcount[blockIdx.x] = s_count;
+}
+
+// the queued points of k_morton_fast, in the reference's FP64 arithmetic: block
+// b of the same grid takes region b
+__global__ void __launch_bounds__(kMortonThreads)
+    k_morton_exact(const double2* __restrict__ pos, int64_t n, double minx, double miny, double L,
+                   const uint32_t* __restrict__ queue, const uint32_t* __restrict__ qcount,
+                   uint32_t* __restrict__ codes)
 {
     const double nmx = -minx, nmy = -miny;
     const double s65536 = 65536.0 / L;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double2 p = pos[i];
-        if (!(p.x >= minx && p.x <= maxx && p.y >= miny && p.y <= maxy)) atomicOr(err, 1u);
-        const uint32_t qx = morton_coord(p.x, nmx, L, s65536);
-        const uint32_t qy = morton_coord(p.y, nmy, L, s65536);
-        codes[i] = (spread16(qy) << 1) | spread16(qx);
+    const uint32_t* region = queue + (int64_t)blockIdx.x * morton_region(n, gridDim.x);
+    const uint32_t nq = qcount[blockIdx.x];
+    for (uint32_t k = threadIdx.x; k < nq; k += blockDim.x) {
+        const uint32_t i = region[k];
+        const double2 p = pos[i];
+        codes[i] = (spread16(morton_coord(p.y, nmy, L, s65536)) << 1) | spread16(morton_coord(p.x, nmx, L, s65536));
     }
 }
 
@@ -65,6 +155,35 @@ __global__ void k_gather_bounds(const uint32_t* __restrict__ codes, const uint32
         double cy = miny + ((double)iy + 0.5) * h;
         prel[2 * k] = (real)(p.x - cx);
         prel[2 * k + 1] = (real)(p.y - cy);
+        if (k == 0 || (depth ? (codes[k - 1] >> shift) : 0u) != leaf) first[li + leaf] = (uint32_t)k;
+        if (k == n - 1 || (depth ? (codes[k + 1] >> shift) : 0u) != leaf) endp[li + leaf] = (uint32_t)(k + 1);
+    }
+}
+
+// cell centres relative to the box corner, (i + 0.5) h for i < 2^depth
+__global__ void k_cell_offsets(int w, double h, double* __restrict__ off)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w; i += gridDim.x * blockDim.x)
+        off[i] = ((double)i + 0.5) * h;
+}
+
+// k_gather_bounds for FP32 compute copies: p - centre as (p - min) - (i + 0.5) h
+// from the offset table (two FP64 additions per coordinate; the difference is
+// the FP64 one to within its last bits, far below FP32 resolution)
+__global__ void k_gather_bounds_f32(const uint32_t* __restrict__ codes, const uint32_t* __restrict__ perm,
+                                    const double2* __restrict__ pos_in, int64_t n, int depth, double minx,
+                                    double miny, const double* __restrict__ off, double2* __restrict__ pos64,
+                                    float2* __restrict__ prel, uint32_t* __restrict__ first,
+                                    uint32_t* __restrict__ endp)
+{
+    const int shift = 32 - 2 * depth;
+    const uint32_t li = level_index(depth);
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t leaf = depth ? (codes[k] >> shift) : 0u;
+        const double2 p = pos_in[perm[k]];
+        pos64[k] = p;
+        const uint32_t ix = compact16(leaf), iy = compact16(leaf >> 1);
+        prel[k] = make_float2(f32_rn((p.x - minx) - off[ix]), f32_rn((p.y - miny) - off[iy]));
         if (k == 0 || (depth ? (codes[k - 1] >> shift) : 0u) != leaf) first[li + leaf] = (uint32_t)k;
         if (k == n - 1 || (depth ? (codes[k + 1] >> shift) : 0u) != leaf) endp[li + leaf] = (uint32_t)(k + 1);
     }
@@ -298,9 +417,17 @@ int build_tree(Handle& h, const double* d_pos, int64_t n, double minx, double mi
     // reference's on every path: FP64 Morton quantisation and a sort over all 32 code bits, whose tie
     // order (stable) fixes the in-leaf order the reference's unstable sort leaves undefined.
     const bool physics = h.cfg.order && !f64;
-    k_morton<<<grid_for(n, 256), 256, 0, s>>>((const double2*)d_pos, n, minx, miny, maxx, maxy, L,
-                                               P<uint32_t>(h.codes), P<uint32_t>(h.err));
-    h.launches++;
+    // codes by the FP32 fast path; points near a cell edge queued per block for the FP64 path
+    const int mgrid = grid_for(n, kMortonThreads);
+    if ((rc = ensure(h.mqueue, (size_t)(mgrid * morton_region(n, mgrid) + mgrid) * 4))) return rc;
+    uint32_t* mq = P<uint32_t>(h.mqueue);
+    uint32_t* mcount = mq + mgrid * morton_region(n, mgrid);
+    k_morton_fast<<<mgrid, kMortonThreads, 0, s>>>((const double2*)d_pos, n, minx, miny, maxx, maxy,
+                                                   (float)(65536.0 / L), P<uint32_t>(h.codes), P<uint32_t>(h.err), mq,
+                                                   mcount);
+    k_morton_exact<<<mgrid, kMortonThreads, 0, s>>>((const double2*)d_pos, n, minx, miny, L, mq, mcount,
+                                                    P<uint32_t>(h.codes));
+    h.launches += 2;
     TC_CUDA_TRY(cudaGetLastError());
     rc = radix_sort_u32(P<uint32_t>(h.codes), P<uint32_t>(h.perm), P<uint32_t>(h.alt_keys), P<uint32_t>(h.alt_vals), n,
                         P<uint32_t>(h.tmp), s, &h.launches, 0);
@@ -320,10 +447,15 @@ int build_tree(Handle& h, const double* d_pos, int64_t n, double minx, double mi
             P<double2>(h.com64), P<double>(h.m0), P<double>(h.m2), P<double2>(h.bbc), P<double>(h.bblen),
             P<double>(h.comrel), P<double>(h.m0r), P<double>(h.m2t));
     } else {
-        k_gather_bounds<float><<<grid_for(n, 256), 256, 0, s>>>(P<uint32_t>(h.codes), P<uint32_t>(h.perm),
-                                                                (const double2*)d_pos, n, depth, minx, miny, hleaf,
-                                                                P<double2>(h.pos64), P<float>(h.prel),
-                                                                P<uint32_t>(h.first), P<uint32_t>(h.count));
+        const int w = 1 << depth;
+        if ((rc = ensure(h.celloff, (size_t)w * 8))) return rc;
+        k_cell_offsets<<<grid_for(w, 256), 256, 0, s>>>(w, hleaf, P<double>(h.celloff));
+        k_gather_bounds_f32<<<grid_for(n, 256), 256, 0, s>>>(P<uint32_t>(h.codes), P<uint32_t>(h.perm),
+                                                             (const double2*)d_pos, n, depth, minx, miny,
+                                                             P<double>(h.celloff), P<double2>(h.pos64),
+                                                             P<float2>(h.prel), P<uint32_t>(h.first),
+                                                             P<uint32_t>(h.count));
+        h.launches++;
         if (physics) {
             if ((rc = build_records_p(h, hleaf))) return rc;
         } else {

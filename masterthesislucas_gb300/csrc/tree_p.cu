@@ -66,7 +66,7 @@ __global__ void k_leaf_small_p(int depth, double minx, double miny, double h, ui
                                double2* __restrict__ com64, double* __restrict__ m0, double* __restrict__ m2,
                                double2* __restrict__ bbc, double* __restrict__ bblen, float* __restrict__ comrel,
                                float* __restrict__ m0r, float* __restrict__ m2t, uint32_t* __restrict__ big,
-                               float* __restrict__ bmax)
+                               float* __restrict__ bmax, int box)
 {
     const uint32_t li = level_index(depth);
     const int64_t nl = (int64_t)1 << (2 * depth);
@@ -90,7 +90,7 @@ __global__ void k_leaf_small_p(int depth, double minx, double miny, double h, ui
         const float ic = 1.0f / (float)c;
         sx *= ic;
         sy *= ic;
-        float a = 0.f, b = 0.f, d = 0.f, r2 = 0.f;
+        float a = 0.f, b = 0.f, d = 0.f, r2 = 0.f, c2 = 0.f;
         for (uint32_t p = f; p < e; p++) {
             const float2 q = prel[p];
             const float rx = q.x - sx, ry = q.y - sy;
@@ -98,9 +98,10 @@ __global__ void k_leaf_small_p(int depth, double minx, double miny, double h, ui
             b = fmaf(rx, ry, b);
             d = fmaf(ry, ry, d);
             r2 = fmaxf(r2, fmaf(rx, rx, ry * ry));
+            c2 = fmaxf(c2, fmaf(q.x, q.x, q.y * q.y));
         }
-        write_node(node, cell_centre(i, minx, miny, h), leaf_box(i, minx, miny, h), h, c, sx, sy, a, b, d,
-                   sqrtf(r2), com64, m0, m2, bbc, bblen, comrel, m0r, m2t, bmax);
+        write_node(node, cell_centre(i, minx, miny, h), leaf_box(i, minx, miny, h), h, c, box ? 0.f : sx,
+                   box ? 0.f : sy, a, b, d, sqrtf(box ? c2 : r2), com64, m0, m2, bbc, bblen, comrel, m0r, m2t, bmax);
     }
 }
 
@@ -109,7 +110,7 @@ __global__ void k_leaf_big_p(int depth, double minx, double miny, double h, cons
                              double2* __restrict__ com64, double* __restrict__ m0, double* __restrict__ m2,
                              double2* __restrict__ bbc, double* __restrict__ bblen, float* __restrict__ comrel,
                              float* __restrict__ m0r, float* __restrict__ m2t, const uint32_t* __restrict__ big,
-                             float* __restrict__ bmax)
+                             float* __restrict__ bmax, int box)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t li = level_index(depth);
@@ -128,7 +129,7 @@ __global__ void k_leaf_big_p(int depth, double minx, double miny, double h, cons
         const float ic = 1.0f / (float)c;
         sx = warp_sum(sx) * ic;
         sy = warp_sum(sy) * ic;
-        float a = 0.f, b = 0.f, d = 0.f, r2 = 0.f;
+        float a = 0.f, b = 0.f, d = 0.f, r2 = 0.f, c2 = 0.f;
         for (uint32_t p = f + lane; p < f + c; p += 32) {
             const float2 q = prel[p];
             const float rx = q.x - sx, ry = q.y - sy;
@@ -136,14 +137,19 @@ __global__ void k_leaf_big_p(int depth, double minx, double miny, double h, cons
             b = fmaf(rx, ry, b);
             d = fmaf(ry, ry, d);
             r2 = fmaxf(r2, fmaf(rx, rx, ry * ry));
+            c2 = fmaxf(c2, fmaf(q.x, q.x, q.y * q.y));
         }
         a = warp_sum(a);
         b = warp_sum(b);
         d = warp_sum(d);
-        for (int o = 16; o > 0; o >>= 1) r2 = fmaxf(r2, __shfl_xor_sync(0xffffffffu, r2, o));
+        for (int o = 16; o > 0; o >>= 1) {
+            r2 = fmaxf(r2, __shfl_xor_sync(0xffffffffu, r2, o));
+            c2 = fmaxf(c2, __shfl_xor_sync(0xffffffffu, c2, o));
+        }
         if (lane == 0)
-            write_node(node, cell_centre(i, minx, miny, h), leaf_box(i, minx, miny, h), h, c, sx, sy, a, b, d,
-                       sqrtf(r2), com64, m0, m2, bbc, bblen, comrel, m0r, m2t, bmax);
+            write_node(node, cell_centre(i, minx, miny, h), leaf_box(i, minx, miny, h), h, c, box ? 0.f : sx,
+                       box ? 0.f : sy, a, b, d, sqrtf(box ? c2 : r2), com64, m0, m2, bbc, bblen, comrel, m0r, m2t,
+                       bmax);
     }
 }
 
@@ -154,7 +160,7 @@ __global__ void k_bottom_up_p(int l, double minx, double miny, double hl, uint32
                               uint32_t* __restrict__ first, double2* __restrict__ com64, double* __restrict__ m0,
                               double* __restrict__ m2, double2* __restrict__ bbc, double* __restrict__ bblen,
                               float* __restrict__ comrel, float* __restrict__ m0r, float* __restrict__ m2t,
-                              float* __restrict__ bmax)
+                              float* __restrict__ bmax, int box)
 {
     const uint32_t li = level_index(l), lc = level_index(l + 1);
     const int64_t nl = (int64_t)1 << (2 * l);
@@ -173,7 +179,7 @@ __global__ void k_bottom_up_p(int l, double minx, double miny, double hl, uint32
         uint32_t fp = 0;
         float sx = 0.f, sy = 0.f;
         float2 g[4];
-        double2 box = make_double2(0.0, 0.0);
+        double2 bbox = make_double2(0.0, 0.0);
 #pragma unroll
         for (int j = 3; j >= 0; j--) {
             g[j] = make_float2(0.f, 0.f);
@@ -183,7 +189,7 @@ __global__ void k_bottom_up_p(int l, double minx, double miny, double hl, uint32
             // non-empty child last (bit 0 of the child slot is x)
             const double cl = bblen[fc + j];
             const double2 cb = bbc[fc + j];
-            box = make_double2(__dadd_rn(__dmul_rn((j & 1) ? -0.5 : 0.5, cl), cb.x),
+            bbox = make_double2(__dadd_rn(__dmul_rn((j & 1) ? -0.5 : 0.5, cl), cb.x),
                                __dadd_rn(__dmul_rn((j & 2) ? -0.5 : 0.5, cl), cb.y));
             const float2 r = cr2[fc + j];
             g[j] = make_float2(r.x + ((j & 1) ? q : -q), r.y + ((j & 2) ? q : -q));
@@ -193,6 +199,9 @@ __global__ void k_bottom_up_p(int l, double minx, double miny, double hl, uint32
         const float ic = 1.0f / (float)cnt;
         sx *= ic;
         sy *= ic;
+        // box-centred expansions: the node's frame is its cell centre, and bmax bounds its particles'
+        // distance from there
+        if (box) sx = sy = 0.f;
         float a = 0.f, b = 0.f, d = 0.f, br = 0.f;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
@@ -207,7 +216,7 @@ __global__ void k_bottom_up_p(int l, double minx, double miny, double hl, uint32
         }
         count[node] = cnt;
         first[node] = fp;
-        write_node(node, cell_centre(i, minx, miny, hl), box, hl, cnt, sx, sy, a, b, d, br, com64, m0, m2, bbc,
+        write_node(node, cell_centre(i, minx, miny, hl), bbox, hl, cnt, sx, sy, a, b, d, br, com64, m0, m2, bbc,
                    bblen, comrel, m0r, m2t, bmax);
     }
 }
@@ -220,17 +229,18 @@ int build_records_p(Handle& h, double hleaf)
     const int depth = h.depth;
     const int64_t nleaf = (int64_t)1 << (2 * depth);
     const int64_t maxbig = h.n / (kLeafSmall + 1) + 1;
+    const int box = h.centre == TC_CENTRE_BOX;
     int rc;
     if ((rc = ensure(h.bigleaf, (maxbig + 1) * 4)) || (rc = ensure(h.bmax, h.nnodes * 4))) return rc;
     TC_CUDA_TRY(cudaMemsetAsync(h.bigleaf.p, 0, 4, s));
     k_leaf_small_p<<<grid_for(nleaf, 128), 128, 0, s>>>(
         depth, h.minx, h.miny, hleaf, P<uint32_t>(h.count), P<uint32_t>(h.first), P<float2>(h.prel),
         P<double2>(h.com64), P<double>(h.m0), P<double>(h.m2), P<double2>(h.bbc), P<double>(h.bblen),
-        P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t), P<uint32_t>(h.bigleaf), P<float>(h.bmax));
+        P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t), P<uint32_t>(h.bigleaf), P<float>(h.bmax), box);
     k_leaf_big_p<<<grid_for(maxbig * 32, 128), 128, 0, s>>>(
         depth, h.minx, h.miny, hleaf, P<uint32_t>(h.count), P<uint32_t>(h.first), P<float2>(h.prel),
         P<double2>(h.com64), P<double>(h.m0), P<double>(h.m2), P<double2>(h.bbc), P<double>(h.bblen),
-        P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t), P<uint32_t>(h.bigleaf), P<float>(h.bmax));
+        P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t), P<uint32_t>(h.bigleaf), P<float>(h.bmax), box);
     h.launches += 2;
     for (int l = depth - 1; l >= 0; l--) {
         const double hl = h.L / (double)(1u << l);
@@ -239,7 +249,7 @@ int build_records_p(Handle& h, double hleaf)
                                                         P<uint32_t>(h.first), P<double2>(h.com64), P<double>(h.m0),
                                                         P<double>(h.m2), P<double2>(h.bbc), P<double>(h.bblen),
                                                         P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t),
-                                                        P<float>(h.bmax));
+                                                        P<float>(h.bmax), box);
         h.launches++;
     }
     TC_CUDA_TRY(cudaGetLastError());

@@ -116,12 +116,12 @@ int tsne_enqueue(tc_tsne* t, const double* prm, const double* lrp, const double*
         launches += h.launches;
     }
     if (h.cfg.precision == TC_PREC_FP64)
-        k_tsne_attr_update<double, double><<<grid_for(t->n * 32, 256, kSMs * 32), 256, 0, h.stream>>>(
+        k_tsne_attr_update<double, double><<<grid_for(t->n * 32, 256, sm_count() * 32), 256, 0, h.stream>>>(
             t->n, P<uint32_t>(t->row_ptr), P<uint32_t>(t->col), P<double>(t->val), P<double2>(t->y[t->cur]),
             P<double2>(t->y[t->prev]), P<double>(t->grad_rep), P<double>(t->z), prm, lrp, P<double2>(t->y[t->next]),
             P<double>(t->grad));
     else
-        k_tsne_attr_update<float, float><<<grid_for(t->n * 32, 256, kSMs * 32), 256, 0, h.stream>>>(
+        k_tsne_attr_update<float, float><<<grid_for(t->n * 32, 256, sm_count() * 32), 256, 0, h.stream>>>(
             t->n, P<uint32_t>(t->row_ptr), P<uint32_t>(t->col), P<float>(t->val), P<double2>(t->y[t->cur]),
             P<double2>(t->y[t->prev]), P<double>(t->grad_rep), P<double>(t->z), prm, lrp, P<double2>(t->y[t->next]),
             P<double>(t->grad));
@@ -359,7 +359,7 @@ int batch_box(tc_tsne_batch* b, size_t i)
     int rc = device_bbox(h, P<double>(t->y[t->cur]), t->n, mn, mx);
     if (rc) return rc;
     TC_CUDA_TRY(cudaMemsetAsync(b->ext.p, 0, 8, h.stream));
-    k_step_extent<<<grid_for(t->n, 256, kSMs * 4), 256, 0, h.stream>>>(
+    k_step_extent<<<grid_for(t->n, 256, sm_count() * 4), 256, 0, h.stream>>>(
         P<double2>(t->y[t->cur]), P<double2>(t->y[t->prev]), t->n, P<unsigned long long>(b->ext));
     TC_CUDA_TRY(cudaMemcpyAsync(b->h_ext, b->ext.p, 8, cudaMemcpyDeviceToHost, h.stream));
     TC_CUDA_TRY(cudaStreamSynchronize(h.stream));

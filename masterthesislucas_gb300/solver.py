@@ -65,7 +65,8 @@ class NBodySolverFMM_SYM_MORTON:
 
     def __init__(self, kernel: str = "tsne", max_children: int = 16, tree_depth: int | None = None,
                  theta: float = 0.5, softening: float = 1e-3, precision: str = "fp32", device: int = 0,
-                 stream=None, order: int = 0, mac: str = "cell", slack: float = 1.0, leaf_p2p: int = 0):
+                 stream=None, order: int = 0, mac: str = "cell", slack: float = 1.0, leaf_p2p: int = 0,
+                 centre: str = "com", m2l: str = "simt"):
         """mac (order p only): "cell", the reference's (L_A + L_B)/theta <
         |dcom| with cell sizes L; "bmax", (b_A + b_B)/theta < |dcom| with b
         the largest distance of a node's particles from its COM;
@@ -73,7 +74,16 @@ class NBodySolverFMM_SYM_MORTON:
         lowest order in {4, 6, ..., order} whose bound ((b_A + b_B)/|dcom|)^(q+1)
         stays below slack * theta^(order+1).
         leaf_p2p (order p): accepted leaf pairs with at most this many
-        particle pairs are summed directly instead of by an M2L."""
+        particle pairs are summed directly instead of by an M2L.
+        centre (order p, fp32): "com" expands about each node's centre of
+        mass; "box" about its cell centre (M2L operators then depend only on
+        the level and the grid offset of a pair).
+        m2l (centre "box"): "simt" FP32 kernels, or "tensor" the tensor-core
+        M2L (BF16 hi/lo split, FP32 accumulation)."""
+        if centre not in ("com", "box"):
+            raise ValueError("centre must be 'com' or 'box'")
+        if m2l not in ("simt", "tensor"):
+            raise ValueError("m2l must be 'simt' or 'tensor'")
         if mac not in ("cell", "bmax", "bmax_adaptive"):
             raise ValueError("mac must be 'cell', 'bmax' or 'bmax_adaptive'")
         cfg = _lib.TcConfig()
@@ -97,6 +107,12 @@ class NBodySolverFMM_SYM_MORTON:
             check(lib().tc_set_adaptive_order(self._h, float(slack)))
         if leaf_p2p:
             check(lib().tc_set_leaf_p2p(self._h, int(leaf_p2p)))
+        if centre == "box":
+            check(lib().tc_set_expansion_centre(self._h, _lib.TC_CENTRE_BOX))
+        if m2l == "tensor":
+            check(lib().tc_set_m2l_engine(self._h, _lib.TC_M2L_TENSOR))
+        self.centre = centre
+        self.m2l = m2l
         self.maxChildren = max_children
         self._cfg_depth = cfg.depth
         self._theta = theta

@@ -4,6 +4,7 @@ import numpy as np
 import pytest
 
 from masterthesislucas_gb300 import learned
+from oracle import mlp_reference
 
 pytestmark = pytest.mark.gpu
 
@@ -18,7 +19,7 @@ def test_gpu_gradient_matches_cpu_oracle():
     X = rng.normal(0, 1, (777, 16)).astype(np.float32)
     T = rng.normal(-3, 1, (777, 5)).astype(np.float32)
     g_gpu, loss_sum = c.gradient(torch.from_numpy(X).cuda(), torch.from_numpy(T).cuda())
-    loss, g_ref = learned.reference_loss_grad(c.params(), X.astype(np.float64), T.astype(np.float64),
+    loss, g_ref = mlp_reference.reference_loss_grad(c.params(), X.astype(np.float64), T.astype(np.float64),
                                              mean.astype(np.float64), std.astype(np.float64), round_weights=True)
     assert loss_sum / T.size == pytest.approx(loss, rel=1e-4)
     scale = np.abs(g_ref).max()
@@ -38,8 +39,8 @@ def test_tensor_core_forward_matches_bf16_oracle():
     Xd = torch.from_numpy(X).cuda()
     y_tc = c.predict_tc(Xd).cpu().numpy()
     y32 = c.predict(Xd).cpu().numpy()
-    ref_bf = learned.reference_forward(c.params(), X, mean, std, round_activations=True)
-    ref_32 = learned.reference_forward(c.params(), X, mean, std, round_activations=False)
+    ref_bf = mlp_reference.reference_forward(c.params(), X, mean, std, round_activations=True)
+    ref_32 = mlp_reference.reference_forward(c.params(), X, mean, std, round_activations=False)
     scale = np.abs(ref_32).max()
     d = np.abs(y_tc - ref_bf)
     # an activation that lands on a BF16 rounding boundary may round the other way

@@ -168,3 +168,34 @@ def test_deep_tree_uses_both_level_kernels(mac):
     assert np.percentile(err, 99) < 2e-3
     c = s.counters()
     assert c["m2l"] > 0 and c["p2p_pairs"] > 0
+
+
+@pytest.mark.parametrize("kernel", ["gravity", "tsne"])
+def test_box_centred_expansions_converge(kernel):
+    """Expansions about the cell centre (the dipole kept, the bounding-radius
+    criterion measured from the cell centre): the error against the FP64
+    direct sum falls with the order and the pair sum converges, as for the
+    expansions about the centre of mass."""
+    n = 65536
+    if kernel == "gravity":
+        pos = datasets.two_disks(n, seed=11).astype(np.float64)
+    else:
+        pos = np.random.default_rng(12).normal(0.0, 10.0, (n, 2))
+    rows = np.random.default_rng(0).choice(n, 1024, replace=False)
+    fd, _ = direct(pos, kernel=kernel, softening=1e-3, precision="fp64", rows=rows)
+    _, ztot = direct(pos, kernel=kernel, softening=1e-3, precision="fp64")
+    meds, tots = [], []
+    for p in (4, 8, 12):
+        s = NBodySolverFMM_SYM_MORTON(kernel, max_children=16, tree_depth=8, theta=0.6, softening=1e-3, order=p,
+                                      mac="bmax", centre="box")
+        pts = Points.from_positions(pos)
+        s.updateTree(pts, pos.min(0), pos.max(0))
+        tots.append(s.solveNbody(0.0, pts))
+        g = np.zeros_like(pos)
+        g[pts.ID] = pts.derivative
+        meds.append(float(np.median(np.linalg.norm(g[rows] - fd, axis=1) / np.linalg.norm(fd, axis=1))))
+        s.close()
+    print(kernel, meds)
+    assert meds[0] > meds[1] > meds[2]
+    assert meds[2] < 1e-5
+    assert tots[2] == pytest.approx(ztot, rel=1e-4)

@@ -3,7 +3,7 @@ central finite differences (FP64), which pins the reference the GPU training
 kernels are checked against (tests/test_gpu_learned.py)."""
 import numpy as np
 
-from masterthesislucas_gb300.learned import NPARAM, reference_loss_grad
+from oracle.mlp_reference import NPARAM, reference_loss_grad
 
 
 def test_reference_gradient_matches_finite_differences():
