@@ -255,12 +255,13 @@ def run_ours(args, w, rank, world):
     ref = ref_d.cpu().numpy()
     ref_eval = ref_eval_d.cpu().numpy()
 
-    def make(theta, order=0, depth=None, controller=None, tau=None, mac="cell"):
+    def make(theta, order=0, depth=None, controller=None, tau=None, mac="cell", centre="com", m2l="simt"):
         kind, _, slack = mac.partition(":")
         s = NBodySolverFMM_SYM_MORTON(w["kernel"], max_children=w["max_children"], tree_depth=depth, theta=theta,
                                       softening=w["softening"], precision="fp32", order=order,
                                       device=dev.index, stream=stream.cuda_stream, mac=kind,
-                                      slack=float(slack or 1.0), leaf_p2p=args.leaf_p2p if order else 0)
+                                      slack=float(slack or 1.0), leaf_p2p=args.leaf_p2p if order else 0,
+                                      centre=centre, m2l=m2l)
         if controller is not None:
             s.set_controller(controller, tau)
         return s
@@ -295,15 +296,30 @@ def run_ours(args, w, rank, world):
 
     # plain order-p FMM, autotuned over (depth, theta, order); its order-12 line is the fixed-p=12 baseline
     target = TARGET_ERR * 0.9
+    tensor_best = None
     if args.order:
         plain = {"depth": args.depth or None, "theta": args.theta or 0.5, "order": args.order,
-                 "mac": "cell" if args.mac == "all" else args.mac}
+                 "mac": "cell" if args.mac == "all" else args.mac, "centre": args.centre, "m2l": args.m2l}
         trials = []
     else:
-        macs = ("cell", "bmax", "bmax_adaptive:0.03") if args.mac == "all" else (args.mac,)
-        plain, trials = tune(pos_d, ref, rows_d, kernel=w["kernel"], softening=w["softening"],
-                             leaf=w["max_children"], target=target, stream=stream, device=dev.index, macs=macs,
-                             leaf_p2p=args.leaf_p2p)
+        # expansion engines: about each node's centre of mass with the FP32 SIMT M2L (three opening criteria),
+        # and about each cell centre with the tensor-core M2L (bounding-radius criterion)
+        engines = []
+        if args.engines in ("all", "com"):
+            engines.append(("com", "simt", ("cell", "bmax", "bmax_adaptive:0.03") if args.mac == "all"
+                            else (args.mac,)))
+        if args.engines in ("all", "box"):
+            engines.append(("box", "tensor", ("bmax",)))
+        plain, trials = None, []
+        for centre, m2l, macs in engines:
+            best, tr = tune(pos_d, ref, rows_d, kernel=w["kernel"], softening=w["softening"],
+                            leaf=w["max_children"], target=target, stream=stream, device=dev.index, macs=macs,
+                            leaf_p2p=args.leaf_p2p, centre=centre, m2l=m2l)
+            trials += tr
+            if m2l == "tensor":
+                tensor_best = best
+            if best is not None and (plain is None or best["ms"] < plain["ms"]):
+                plain = best
         if plain is None:
             raise SystemExit("autotuner found no configuration meeting the error target")
     p12 = min((t for t in trials if t["order"] == 12 and t["err"] <= target), key=lambda t: t["ms"], default=None)
@@ -318,7 +334,7 @@ def run_ours(args, w, rank, world):
     elif ctrl is not None:
         learned_cfg, ltrials = tune_learned(pos_d, ref, rows_d, ctrl, kernel=w["kernel"], softening=w["softening"],
                                             leaf=w["max_children"], target=target, stream=stream, device=dev.index)
-    calib = {"plain_best": plain, "plain_p12": p12, "learned_best": learned_cfg, "plain_trials": trials,
+    calib = {"plain_best": plain, "plain_p12": p12, "plain_tensor": tensor_best, "learned_best": learned_cfg, "plain_trials": trials,
              "learned_trials": ltrials, "controller": ctrl_stats, "reference_order": ref_order}
 
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > L2 (129 MB)
@@ -377,18 +393,30 @@ def run_ours(args, w, rank, world):
 
     # the arms: the learned-order method (headline, when it meets the target) and the plain ones beside it
     arms = {}
-    s_plain = make(plain["theta"], order=plain["order"], depth=plain["depth"], mac=plain["mac"])
+    s_plain = make(plain["theta"], order=plain["order"], depth=plain["depth"], mac=plain["mac"],
+                   centre=plain["centre"], m2l=plain["m2l"])
     arms["plain_best"] = timed(s_plain, args.steps, sample_clocks=True)
-    arms["plain_best"].update(theta=plain["theta"], order=plain["order"], mac=plain["mac"])
+    arms["plain_best"].update(theta=plain["theta"], order=plain["order"], mac=plain["mac"], centre=plain["centre"],
+                              m2l=plain["m2l"])
     if p12 is not None:
-        if plain["order"] == 12 and (p12["depth"], p12["theta"], p12["mac"]) == (plain["depth"], plain["theta"],
-                                                                                 plain["mac"]):
+        key = ("depth", "theta", "mac", "centre", "m2l")
+        if plain["order"] == 12 and all(p12[k] == plain[k] for k in key):
             arms["plain_p12"] = arms["plain_best"]
         else:
-            s12 = make(p12["theta"], order=12, depth=p12["depth"], mac=p12["mac"])
+            s12 = make(p12["theta"], order=12, depth=p12["depth"], mac=p12["mac"], centre=p12["centre"],
+                       m2l=p12["m2l"])
             arms["plain_p12"] = timed(s12, args.steps, sample_clocks=False)
-            arms["plain_p12"].update(theta=p12["theta"], order=12, mac=p12["mac"])
+            arms["plain_p12"].update(theta=p12["theta"], order=12, mac=p12["mac"], centre=p12["centre"],
+                                     m2l=p12["m2l"])
             s12.close()
+    # the tensor-core M2L engine's fastest configuration meeting the target, beside the headline
+    if tensor_best is not None and plain.get("m2l") != "tensor":
+        st = make(tensor_best["theta"], order=tensor_best["order"], depth=tensor_best["depth"],
+                  mac=tensor_best["mac"], centre="box", m2l="tensor")
+        arms["plain_tensor"] = timed(st, args.steps, sample_clocks=False)
+        arms["plain_tensor"].update(theta=tensor_best["theta"], order=tensor_best["order"], mac=tensor_best["mac"],
+                                    centre="box", m2l="tensor")
+        st.close()
     s_head, head, s_l = s_plain, "plain_best", None
     if learned_cfg is not None:
         s_l = make(1.0, order=12, depth=learned_cfg["depth"], controller=ctrl, tau=learned_cfg["tau"])
@@ -922,14 +950,14 @@ def step_roofline(n, arm, hbm_gbs, fp32_tflops):
 def arm_summary(n, steps, a):
     return {"particles_per_s": n * steps / a["t_total"], "ms_per_step": 1e3 * a["t_total"] / steps,
             "depth": a["depth"], "order": a.get("order"), "theta": a.get("theta"), "tau": a.get("tau"),
-            "mac": a.get("mac"), "median_err": a["err"][0]}
+            "mac": a.get("mac"), "centre": a.get("centre"), "m2l": a.get("m2l"), "median_err": a["err"][0]}
 
 
 def compact_calib(calib):
     """The chosen configurations only; the trial lists go to the record file."""
-    keep = ("mac", "depth", "theta", "order", "tau", "ms", "err", "median_err", "particles_per_s")
+    keep = ("mac", "centre", "m2l", "depth", "theta", "order", "tau", "ms", "err", "median_err", "particles_per_s")
     out = {}
-    for k in ("plain_best", "plain_p12", "learned_best", "reference_order"):
+    for k in ("plain_best", "plain_p12", "plain_tensor", "learned_best", "reference_order"):
         v = calib.get(k)
         out[k] = None if v is None else {a: v[a] for a in keep if a in v}
     if calib.get("controller"):
@@ -940,9 +968,10 @@ def compact_calib(calib):
 
 
 # DRAM bytes (read + write) of one k_near_p launch, from an ncu capture of the force step at that configuration
-# (dram__bytes_read.sum + dram__bytes_write.sum), keyed by (n, depth, order, opening criterion, theta, leaf P2P).
+# (dram__bytes_read.sum + dram__bytes_write.sum), keyed by (n, depth, order, opening criterion, theta, leaf P2P,
+# expansion centre).
 NEAR_TRAFFIC = {
-    (4194304, 11, 8, "bmax", 0.75, 64): (249966080 + 98462208,
+    (4194304, 11, 8, "bmax", 0.75, 64, "com"): (249966080 + 98462208,
                                           "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_near_p launch "
                                           "of the force step at this configuration (bit-exact tree)"),
 }
@@ -970,11 +999,15 @@ def headline_line(args, w, r, world, config, peaks, peak_src, sms):
                                                                 "particles_per_s", "depth")}
     method = {"learned": "learned-order symmetric Morton FMM: MLP controller (16-64-64-5, BF16 tensor-core "
                          "inference in the list build) picks accept/open and the order in {4,6,8,10,12} per pair",
-              "plain_best": "plain fixed-order symmetric Morton FMM (autotuned opening criterion/depth/theta/order)"}[r["head"]]
+              "plain_best": "plain fixed-order symmetric Morton FMM (autotuned expansion centre and M2L engine, "
+                            "opening criterion, depth, theta and order)"}[r["head"]]
     config = dict(config)
     config.update({"theta": head.get("theta"), "tau": head.get("tau"), "depth": head["depth"], "mac": head.get("mac"),
                    "order": head.get("order"), "method": r["head"],
-                   "expansion": "total-order Cartesian Taylor about the COM",
+                   "centre": head.get("centre"), "m2l": head.get("m2l"),
+                   "expansion": ("total-order Cartesian Taylor about the cell centre, M2L on the tensor cores (BF16 "
+                                 "hi/lo split, FP32 accumulation) on the deep levels" if head.get("centre") == "box"
+                                 else "total-order Cartesian Taylor about the COM, FP32 SIMT M2L"),
                    "tree": "Morton codes, permutation and topology bit-exact to the reference (FP64 quantisation, "
                            "32-bit stable sort)",
                    "autotune": compact_calib(r["calib"]),
@@ -983,7 +1016,7 @@ def headline_line(args, w, r, world, config, peaks, peak_src, sms):
                    "step": ("one CUDA graph launch per step (update + solve captured over the exact box, "
                             "stage times from the uncaptured warm-up steps)" if head.get("graph")
                             else "updateTree + solveNbody calls")})
-    key = (n, config["depth"], config["order"], config["mac"], config["theta"], args.leaf_p2p)
+    key = (n, config["depth"], config["order"], config["mac"], config["theta"], args.leaf_p2p, config["centre"])
     traffic, traffic_src = NEAR_TRAFFIC.get(key, (None, "no ncu capture of this configuration"))
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -1088,6 +1121,12 @@ def main():
                     help="opening criterion of the plain arms: cell, bmax, bmax_adaptive:<slack> (per-pair "
                          "orders), or all (autotuned over these)")
     ap.add_argument("--depth", type=int, default=0)
+    ap.add_argument("--centre", default="com", choices=["com", "box"],
+                    help="with --order: expansion centre (centre of mass, or cell centre)")
+    ap.add_argument("--m2l", default="simt", choices=["simt", "tensor", "tensor_all"],
+                    help="with --order and --centre box: the M2L engine")
+    ap.add_argument("--engines", default="all", choices=["all", "com", "box"],
+                    help="autotuned arms: COM-centred with the SIMT M2L, box-centred with the tensor-core M2L")
     ap.add_argument("--skip-reference-order", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=262144)
     ap.add_argument("--ref-sample", type=int, default=REF_SAMPLE,

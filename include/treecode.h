@@ -123,9 +123,13 @@ int tc_set_expansion_centre(tc_handle* h, int centre);
  *                about 0.2 with TC_MAC_BMAX) are rejected at tc_solve.  Its
  *                operators take (depth + 1) * (2R+1)^2 * 4 * K_pad^2 bytes
  *                and its BF16 multipole copy 4 * K_pad bytes per node.
+ * Levels whose parents number fewer than 128 per SM keep the SIMT kernels
+ * (a tile's offsets run in sequence, so a level needs tiles for every SM);
+ * TC_M2L_TENSOR_ALL runs every level on the tensor cores.
  * Needs TC_CENTRE_BOX set first; setting TC_CENTRE_COM returns to SIMT.  */
 #define TC_M2L_SIMT 0
 #define TC_M2L_TENSOR 1
+#define TC_M2L_TENSOR_ALL 2
 int tc_set_m2l_engine(tc_handle* h, int engine);
 
 /* Per-pair expansion order on a TC_MAC_BMAX handle of order p in {6, 8, 10,

@@ -33,6 +33,7 @@ TC_CENTRE_COM = 0
 TC_CENTRE_BOX = 1
 TC_M2L_SIMT = 0
 TC_M2L_TENSOR = 1
+TC_M2L_TENSOR_ALL = 2
 
 
 class TcConfig(ctypes.Structure):

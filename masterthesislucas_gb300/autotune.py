@@ -31,7 +31,7 @@ def median_error(grad_rows: np.ndarray, ref_rows: np.ndarray) -> float:
 
 def tune(pos_d, ref_rows, rows_d, *, kernel: str, softening: float, leaf: int, target: float,
          stream=None, depths=None, thetas=None, orders=ORDERS, device: int = 0, log=None, macs=("cell",),
-         leaf_p2p: int = 0, centre: str = "com"):
+         leaf_p2p: int = 0, centre: str = "com", m2l: str = "simt"):
     """Returns (best, trials).  best = dict(mac, depth, theta, order, ms, err) or None."""
     import torch
 
@@ -54,7 +54,7 @@ def tune(pos_d, ref_rows, rows_d, *, kernel: str, softening: float, leaf: int, t
             s = NBodySolverFMM_SYM_MORTON(kernel, max_children=leaf, tree_depth=depth, theta=theta,
                                           softening=softening, precision="fp32", order=order,
                                           device=device, stream=s_torch.cuda_stream, mac=kind,
-                                          slack=float(slack or 1.0), leaf_p2p=leaf_p2p, centre=centre)
+                                          slack=float(slack or 1.0), leaf_p2p=leaf_p2p, centre=centre, m2l=m2l)
             try:
                 s.update_tree_device(pos_d)
                 s.solve_device(grad_d, tot_d)
@@ -69,7 +69,7 @@ def tune(pos_d, ref_rows, rows_d, *, kernel: str, softening: float, leaf: int, t
                 err = median_error(grad_d[rows_d].cpu().numpy(), ref_rows)
             finally:
                 s.close()
-            t = dict(mac=mac, depth=depth, theta=theta, order=order, ms=ms, err=err, centre=centre)
+            t = dict(mac=mac, depth=depth, theta=theta, order=order, ms=ms, err=err, centre=centre, m2l=m2l)
             trials.append(t)
             if log:
                 log(t)

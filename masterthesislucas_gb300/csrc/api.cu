@@ -684,15 +684,16 @@ extern "C" int tc_set_expansion_centre(tc_handle* t, int centre)
 
 extern "C" int tc_set_m2l_engine(tc_handle* t, int engine)
 {
-    if (!t || (engine != TC_M2L_SIMT && engine != TC_M2L_TENSOR)) {
+    if (!t || (engine != TC_M2L_SIMT && engine != TC_M2L_TENSOR && engine != TC_M2L_TENSOR_ALL)) {
         tc_set_error("tc_set_m2l_engine: unknown engine");
         return TC_ERR_INVALID;
     }
-    if (engine == TC_M2L_TENSOR && t->h.centre != TC_CENTRE_BOX) {
+    if (engine != TC_M2L_SIMT && t->h.centre != TC_CENTRE_BOX) {
         tc_set_error("tc_set_m2l_engine: the tensor-core M2L needs box-centred expansions (set them first)");
         return TC_ERR_INVALID;
     }
-    t->h.m2l_tc = engine == TC_M2L_TENSOR;
+    t->h.m2l_tc = engine != TC_M2L_SIMT;
+    t->h.m2l_tc_all = engine == TC_M2L_TENSOR_ALL;
     return TC_OK;
 }
 

@@ -1003,23 +1003,47 @@ int m2l_tensor(Handle& h, const PotParams& pp)
     TC_CUDA_TRY(cudaMemsetAsync(status, 0, 4, s));
     const uint32_t* act = P<uint32_t>(h.act);
     const uint32_t* act_pos = P<uint32_t>(h.act_pos);
-    tcm::k_mu_split<Q><<<grid_for(h.nnodes, 128), 128, 0, s>>>(h.nnodes, P<float>(h.mu), act, act_pos,
-                                                               P<uint8_t>(h.tc_mubf));
+    const float* comrel = P<float>(h.comrel);
+    float* mu = P<float>(h.mu);
+    float* loc = P<float>(h.loc);
+    double* zp = P<double>(h.zpart);
+    const uint32_t* count = P<uint32_t>(h.count);
     const uint32_t* ptr = P<uint32_t>(h.ptr_pool);
     const uint32_t* idx = P<uint32_t>(h.idx_pool);
+    // levels with few parents keep the SIMT kernels: a tile's offsets run one after another, so a level
+    // needs tiles for every SM before the tensor cores pay
+    int lmin = dep + 1;
+    for (int l = dep; l >= 2 && ((int64_t)1 << (2 * (l - 1))) >= (int64_t)tcm::kRows * sm_count(); l--) lmin = l;
+    if (h.m2l_tc_all) lmin = 1;
+    if (lmin <= dep) {
+        tcm::k_mu_split<Q><<<grid_for((int64_t)h.nnodes * S::KC, 256), 256, 0, s>>>(
+            h.nnodes, level_index(lmin), mu, act, act_pos, P<uint8_t>(h.tc_mubf));
+        h.launches++;
+    }
     for (int l = 1; l <= dep; l++) {
         const float hl = (float)(h.L / (double)(1u << l));
+        const int64_t nl = (int64_t)1 << (2 * l);
+        if (l < lmin) {
+            if (nl <= kM2lWarpLevelNodes)
+                k_m2l_warp<Q><<<grid_for(nl * 32, 128), 128, 0, s>>>(l, hl, pp, ptr + h.lists.nn_ptr_off[l],
+                                                                   idx + h.lists.nn_idx_off[l], comrel, mu, loc,
+                                                                   zp, act, act_pos);
+            else
+                k_m2l_p<Q><<<grid_for(nl, 128), 128, 0, s>>>(l, hl, pp, ptr + h.lists.nn_ptr_off[l],
+                                                             idx + h.lists.nn_idx_off[l], count, comrel, mu, loc,
+                                                             zp, act, act_pos);
+            h.launches++;
+            continue;
+        }
         uint8_t* ops = P<uint8_t>(h.tc_ops) + ops_level * l;
         tcm::k_m2l_tc_ops<Q><<<W * W, 128, 0, s>>>(hl, pp, R, ops);
-        const int64_t nl = (int64_t)1 << (2 * l);
-        const int64_t tiles = (nl + tcm::kRows - 1) / tcm::kRows;
+        const int64_t tiles = 4 * ((nl / 4 + tcm::kRows - 1) / tcm::kRows);
         const int grid = (int)(tiles < sm_count() ? tiles : sm_count());
         tcm::k_m2l_tc<Q><<<grid, 128, S::SMEM, s>>>(l, R, ptr + h.lists.nn_ptr_off[l], idx + h.lists.nn_idx_off[l],
-                                                     P<float>(h.mu), P<uint8_t>(h.tc_mubf), ops, pp.kappa,
-                                                     P<float>(h.loc), P<double>(h.zpart), act, act_pos, status);
+                                                     count, mu, P<uint8_t>(h.tc_mubf), ops, pp.kappa, loc, zp,
+                                                     act, act_pos, status);
         h.launches += 2;
     }
-    h.launches += 1;
     TC_CUDA_TRY(cudaGetLastError());
     return TC_OK;
 }

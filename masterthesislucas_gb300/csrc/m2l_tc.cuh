@@ -9,7 +9,8 @@
 // apart, so the order-p translation
 //     L_b += sum_a (-1)^|a| mu_a D_(a+b)(o h),    |a| + |b| <= p,
 // is one K x K matrix T_o (K = (p+1)(p+2)/2) per level and offset.  A CTA
-// takes 128 consecutive non-empty sink nodes of a level and, for every offset
+// takes 128 sink nodes of a level (one child slot of 128 consecutive non-empty
+// parents) and, for every offset
 // o in the union of their interaction lists, multiplies the 128 x K block of
 // source multipoles at that offset (a zero row where a sink has no source
 // there) by T_o, accumulating all offsets of the tile in tensor memory:
@@ -41,6 +42,8 @@
 
 namespace tc {
 namespace tcm {
+// internal linkage: every order's object of fmm_p.cu includes these kernels
+namespace {
 
 constexpr int kRows = 128;                   // sinks per tile (the MMA's M)
 constexpr int kChunk = 32;                   // union offsets per refill of a row's source table
@@ -62,8 +65,8 @@ struct Shape {
     static constexpr int ROWB = KP * 2;             // one BF16 multipole row (hi or lo)
     static constexpr int AB = kRows * KP * 2;       // one A operand (hi or lo)
     static constexpr int STAGE = 2 * AB + 2 * OPB;  // A_hi A_lo B_hi B_lo
-    static constexpr int kStages = STAGE <= 40 * 1024 ? 4 : (STAGE <= 70 * 1024 ? 3 : 2);
-    static constexpr int kAhead = kStages >= 4 ? 2 : 1;  // steps whose copies run ahead of the MMAs
+    static constexpr int kStages = STAGE <= 36 * 1024 ? 5 : (STAGE <= 60 * 1024 ? 3 : 2);
+    static constexpr int kAhead = kStages >= 4 ? kStages - 2 : 1;  // steps whose copies run ahead of the MMAs
     static constexpr int TCOLS = KP <= 32 ? 32 : (KP <= 64 ? 64 : 128);
     // shared memory: stages, row-source table, offset list, bit words, prefix, barriers, tmem slot, flags
     static constexpr int OFF_ROWSRC = kStages * STAGE;
@@ -240,38 +243,53 @@ __global__ void __launch_bounds__(128) k_m2l_tc_ops(float hl, PotParams pp, int 
     }
 }
 
-// multipoles of every non-empty node as BF16 hi and lo rows (KP entries each,
-// zero-padded), at the node's position in the non-empty list
+// multipoles of the non-empty nodes from first_node on as BF16 hi and lo rows
+// (KP entries each, zero-padded), at the node's position in the non-empty
+// list; one thread per 8 coefficients (a 16-byte chunk of each row)
 template <int P>
-__global__ void k_mu_split(int64_t nn, const float* __restrict__ mu, const uint32_t* __restrict__ act,
-                           const uint32_t* __restrict__ act_pos, uint8_t* __restrict__ mu_bf)
+__global__ void k_mu_split(int64_t nn, uint32_t first_node, const float* __restrict__ mu,
+                           const uint32_t* __restrict__ act, const uint32_t* __restrict__ act_pos,
+                           uint8_t* __restrict__ mu_bf)
 {
     using S = Shape<P>;
-    constexpr int K = S::K, KP = S::KP, KS = kstride(P);
-    const uint32_t na_total = act_pos[nn];
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < na_total; k += gridDim.x * blockDim.x) {
-        const int64_t node = act[k];
-        const float* m = mu + node * KS;
-        __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(mu_bf + (size_t)k * 2 * S::ROWB);
-        __nv_bfloat16* lo = hi + KP;
-#pragma unroll 4
-        for (int c = 0; c < KP; c++) {
-            const float v = c < K ? m[c] : 0.f;
-            const __nv_bfloat16 h = __float2bfloat16_rn(v);
-            hi[c] = h;
-            lo[c] = __float2bfloat16_rn(v - __bfloat162float(h));
+    constexpr int K = S::K, KC = S::KC, KS = kstride(P);
+    const uint32_t k0 = act_pos[first_node], k1 = act_pos[nn];
+    const int64_t items = (int64_t)(k1 - k0) * KC;
+    for (int64_t it = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; it < items;
+         it += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t k = k0 + (uint32_t)(it / KC);
+        const int c = (int)(it % KC);
+        const float* m = mu + (int64_t)act[k] * KS;
+        uint32_t hw[4], lw[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int i0 = 8 * c + 2 * j, i1 = i0 + 1;
+            const float v0 = i0 < K ? m[i0] : 0.f, v1 = i1 < K ? m[i1] : 0.f;
+            const __nv_bfloat16 h0 = __float2bfloat16_rn(v0), h1 = __float2bfloat16_rn(v1);
+            const __nv_bfloat16 l0 = __float2bfloat16_rn(v0 - __bfloat162float(h0));
+            const __nv_bfloat16 l1 = __float2bfloat16_rn(v1 - __bfloat162float(h1));
+            hw[j] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+            lw[j] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
         }
+        uint8_t* row = mu_bf + (size_t)k * 2 * S::ROWB;
+        *reinterpret_cast<uint4*>(row + 16 * c) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+        *reinterpret_cast<uint4*>(row + S::ROWB + 16 * c) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
     }
 }
 
 // ------------------------------------------------------------------ M2L
-// Persistent: each CTA walks tiles of 128 consecutive non-empty sinks of level
-// l.  Writes loc (the node's M2L sum, as the SIMT M2L does) and its far-field
+// Persistent: each CTA walks tiles of level l.  Tile t holds child slot
+// j = t % 4 of 128 consecutive non-empty parents (level l - 1) in Morton
+// order: row r is child j of parent r when that child is non-empty.  Sinks in
+// the same slot of their parent have the same candidate offsets (the children
+// of the parent's near list), so a tile's union of offsets stays small.
+// Writes loc (the node's M2L sum, as the SIMT M2L does) and its far-field
 // pair sum zpart.
 template <int P>
 __global__ void __launch_bounds__(128, 1)
     k_m2l_tc(int l, int R, const uint32_t* __restrict__ nn_ptr, const uint32_t* __restrict__ nn_idx,
-             const float* __restrict__ mu, const uint8_t* __restrict__ mu_bf, const uint8_t* __restrict__ ops,
+             const uint32_t* __restrict__ count, const float* __restrict__ mu, const uint8_t* __restrict__ mu_bf,
+             const uint8_t* __restrict__ ops,
              float kappa, float* __restrict__ loc, double* __restrict__ zpart, const uint32_t* __restrict__ act,
              const uint32_t* __restrict__ act_pos, uint32_t* __restrict__ err)
 {
@@ -289,10 +307,9 @@ __global__ void __launch_bounds__(128, 1)
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + S::OFF_BARS);  // [0, NS) operators, [NS, 2NS) MMAs
     uint32_t* misc = reinterpret_cast<uint32_t*>(smem + S::OFF_MISC);  // [0] tmem base, [1] union size, [2] abort
     const int tid = threadIdx.x, warp = tid >> 5;
-    const uint32_t li = level_index(l);
-    const int64_t nl = (int64_t)1 << (2 * l);
-    const uint32_t k0 = act_pos[li], k1 = act_pos[li + nl];
-    const uint32_t ntiles = (k1 - k0 + kRows - 1) / kRows;
+    const uint32_t li = level_index(l), lp = level_index(l - 1);
+    const uint32_t k0 = act_pos[lp], k1 = act_pos[li];  // the non-empty parents
+    const uint32_t ntiles = 4u * ((k1 - k0 + kRows - 1) / kRows);
     if (blockIdx.x >= ntiles) return;  // uniform: the whole CTA leaves before any allocation
     const int W = 2 * R + 1, nwords = (W * W + 31) / 32;
     auto stage_a = [&](int s, int lohalf) { return smem + s * S::STAGE + lohalf * S::AB; };
@@ -323,10 +340,10 @@ __global__ void __launch_bounds__(128, 1)
     bool abort = false;
 
     for (uint32_t tile = blockIdx.x; tile < ntiles && !abort; tile += gridDim.x) {
-        const uint32_t kk = k0 + tile * kRows + tid;
-        const bool row_ok = kk < k1;
-        const int64_t na = row_ok ? (int64_t)act[kk] : 0;
-        const uint32_t a = (uint32_t)(na - li);
+        const uint32_t kk = k0 + (tile >> 2) * kRows + tid;
+        const uint32_t a = kk < k1 ? 4u * (act[kk] - lp) + (tile & 3u) : 0u;  // level-local child index
+        const int64_t na = (int64_t)li + a;
+        const bool row_ok = kk < k1 && count[na] != 0;
         const uint32_t e0 = row_ok ? nn_ptr[a] : 0u, e1 = row_ok ? nn_ptr[a + 1] : 0u;
         const int iax = (int)compact16(a), iay = (int)compact16(a >> 1);
         auto offset_of = [&](uint32_t b, int& oid) {
@@ -369,7 +386,8 @@ __global__ void __launch_bounds__(128, 1)
             const uint32_t w = bits[oid >> 5];
             return wpre[oid >> 5] + (uint32_t)__popc(w & ((1u << (oid & 31)) - 1u));
         };
-        // this thread's sources at the union offsets [c * kChunk, (c + 1) * kChunk)
+        // this thread's sources at the union offsets [c * kChunk, (c + 1) * kChunk), as their positions in the
+        // non-empty list (the rows of the BF16 copy)
         auto refill = [&](uint32_t c) {
 #pragma unroll 8
             for (int j = 0; j < kChunk; j++) rowsrc[j * kRows + tid] = kNoSrc;
@@ -378,7 +396,8 @@ __global__ void __launch_bounds__(128, 1)
                 int oid;
                 if (!offset_of(b, oid)) continue;
                 const uint32_t u = union_index(oid);
-                if (u >= c * kChunk && u < (c + 1) * kChunk) rowsrc[(u - c * kChunk) * kRows + tid] = b;
+                // the source's row in the BF16 copy, looked up once per chunk rather than once per step
+                if (u >= c * kChunk && u < (c + 1) * kChunk) rowsrc[(u - c * kChunk) * kRows + tid] = act_pos[li + b];
             }
         };
         // copies of union offset u into stage (step0 + u) % NS
@@ -399,7 +418,7 @@ __global__ void __launch_bounds__(128, 1)
             const uint32_t src = rowsrc[(u % kChunk) * kRows + tid];
             const uint32_t ahi = saddr(stage_a(s, 0)), alo = saddr(stage_a(s, 1));
             if (src != kNoSrc) {
-                const uint8_t* g8 = mu_bf + (size_t)act_pos[li + src] * 2 * S::ROWB;
+                const uint8_t* g8 = mu_bf + (size_t)src * 2 * S::ROWB;
 #pragma unroll
                 for (int c = 0; c < KC; c++) {
                     cp16(ahi + cano(tid, 8 * c, kRows), g8 + 16 * c);
@@ -417,7 +436,13 @@ __global__ void __launch_bounds__(128, 1)
             cp_commit();
         };
         // 2. the offsets of the union, copies running LA steps ahead of the MMAs
-        for (uint32_t u = 0; u < (uint32_t)LA && u < U; u++) issue_copies(u);
+        // LA groups in flight from the start (empty ones past the union's end)
+        for (uint32_t u = 0; u < (uint32_t)LA; u++) {
+            if (u < U)
+                issue_copies(u);
+            else
+                cp_commit();
+        }
         for (uint32_t u = 0; u < U; u++) {
             if (u + LA < U)
                 issue_copies(u + LA);
@@ -512,5 +537,6 @@ __global__ void __launch_bounds__(128, 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(S::TCOLS) : "memory");
 }
 
+}  // namespace
 }  // namespace tcm
 }  // namespace tc

@@ -78,6 +78,7 @@ struct Handle {
     int centre = 0;
     // order p, box-centred: M2L on the tensor cores (m2l_tc.cuh) instead of the FP32 SIMT kernels
     bool m2l_tc = false;
+    bool m2l_tc_all = false;  // every level on the tensor cores (else levels with few parents stay SIMT)
     Buf tc_ops;   // tensor-core M2L: BF16 hi/lo operators per level and offset
     Buf tc_mubf;  // tensor-core M2L: BF16 hi/lo multipole rows per non-empty node
     // order p with TC_MAC_BMAX: per-pair expansion order from the bound

@@ -79,11 +79,12 @@ class NBodySolverFMM_SYM_MORTON:
         mass; "box" about its cell centre (M2L operators then depend only on
         the level and the grid offset of a pair).
         m2l (centre "box"): "simt" FP32 kernels, or "tensor" the tensor-core
-        M2L (BF16 hi/lo split, FP32 accumulation)."""
+        M2L (BF16 hi/lo split, FP32 accumulation) on the levels with enough
+        nodes to fill the GPU, or "tensor_all" on every level."""
         if centre not in ("com", "box"):
             raise ValueError("centre must be 'com' or 'box'")
-        if m2l not in ("simt", "tensor"):
-            raise ValueError("m2l must be 'simt' or 'tensor'")
+        if m2l not in ("simt", "tensor", "tensor_all"):
+            raise ValueError("m2l must be 'simt', 'tensor' or 'tensor_all'")
         if mac not in ("cell", "bmax", "bmax_adaptive"):
             raise ValueError("mac must be 'cell', 'bmax' or 'bmax_adaptive'")
         cfg = _lib.TcConfig()
@@ -109,8 +110,9 @@ class NBodySolverFMM_SYM_MORTON:
             check(lib().tc_set_leaf_p2p(self._h, int(leaf_p2p)))
         if centre == "box":
             check(lib().tc_set_expansion_centre(self._h, _lib.TC_CENTRE_BOX))
-        if m2l == "tensor":
-            check(lib().tc_set_m2l_engine(self._h, _lib.TC_M2L_TENSOR))
+        if m2l != "simt":
+            check(lib().tc_set_m2l_engine(self._h, _lib.TC_M2L_TENSOR if m2l == "tensor"
+                                          else _lib.TC_M2L_TENSOR_ALL))
         self.centre = centre
         self.m2l = m2l
         self.maxChildren = max_children

@@ -47,7 +47,7 @@ def test_tensor_m2l_matches_simt_and_direct(kernel, order, theta, depth):
     else:
         pos = np.random.default_rng(22).normal(0.0, 10.0, (n, 2))
     g_s, z_s, c_s = run(pos, kernel, order, theta, depth, "simt")
-    g_t, z_t, c_t = run(pos, kernel, order, theta, depth, "tensor")
+    g_t, z_t, c_t = run(pos, kernel, order, theta, depth, "tensor_all")
     assert c_t["m2l"] == c_s["m2l"] > 0 and c_t["p2p_pairs"] == c_s["p2p_pairs"]
     d = rel(g_t, g_s)
     print(kernel, order, "median", np.median(d), "max", d.max())
@@ -63,9 +63,21 @@ def test_tensor_m2l_matches_simt_and_direct(kernel, order, theta, depth):
 def test_tensor_m2l_repeat_is_identical():
     """The tile sums run in a fixed order: two solves give the same bits."""
     pos = datasets.two_disks(32768, seed=5).astype(np.float64)
-    g1, z1, _ = run(pos, "gravity", 8, 0.6, 8, "tensor")
-    g2, z2, _ = run(pos, "gravity", 8, 0.6, 8, "tensor")
+    g1, z1, _ = run(pos, "gravity", 8, 0.6, 8, "tensor_all")
+    g2, z2, _ = run(pos, "gravity", 8, 0.6, 8, "tensor_all")
     assert np.array_equal(g1, g2) and z1 == z2
+
+
+def test_tensor_m2l_on_the_deep_levels_only():
+    """The default engine puts the levels with at least 128 parents per SM on
+    the tensor cores (here levels 9 and 10) and keeps the coarse ones SIMT."""
+    n = 262144
+    pos = datasets.two_disks(n, seed=23).astype(np.float64)
+    g_s, z_s, _ = run(pos, "gravity", 8, 0.7, 10, "simt")
+    g_t, z_t, _ = run(pos, "gravity", 8, 0.7, 10, "tensor")
+    d = rel(g_t, g_s)
+    assert 0 < np.median(d) < MEDIAN_AGREE
+    assert z_t == pytest.approx(z_s, rel=1e-5)
 
 
 def test_tensor_m2l_rejects_angles_beyond_its_operator_table():
