@@ -220,6 +220,31 @@ int tc_direct(int kernel, double softening, int precision, const double* pos_xy,
 int tc_direct_device(int kernel, double softening, int precision, const double* d_pos_xy, int64_t n,
                      const int64_t* d_rows, int64_t m, double* d_grad_rows, double* d_total, void* stream);
 
+/* ---------------------------------------------------------------- affinities
+ * The t-SNE P matrix that the reference reads from openTSNE's output
+ * (MnistLoader.ipynb cell 14; CSR by TSNE::setupEfficientPmatrix,
+ * src/nBodyInstances/tsne.h:462-520), built on the GPU.  All pointers are
+ * device memory on the current device; stream may be NULL.
+ *
+ * tc_knn_device: the k nearest neighbours of each of the n rows of d_x
+ * (n x dim FP32, row-major), self excluded, by squared distance summed over
+ * the dimensions in order in FP32 (one fused multiply-add per dimension);
+ * each row of d_dist / d_idx (n x k) ordered by (distance, index).
+ * 1 <= k <= 128, k < n.                                                    */
+int tc_knn_device(const float* d_x, int64_t n, int dim, int k, float* d_dist, int32_t* d_idx, void* stream);
+/* tc_perplexity_device: per row, the Gaussian precision beta bisected (start
+ * 1, doubled until bracketed, at most max_iter steps) until the entropy of
+ * p_j = exp(-beta (d_j - d_0)) / s is within tol of log(perplexity); writes
+ * p (n x k FP64).  exp and log are the library's own FP64 series.         */
+int tc_perplexity_device(const float* d_dist, int64_t n, int k, double perplexity, int max_iter, double tol,
+                         double* d_p, void* stream);
+/* tc_symmetrize_device: (P + P^T) / (2N) as CSR with rows sorted and columns
+ * sorted within each row: d_row_ptr (n + 1), d_col and d_val with capacity
+ * 2 n k; *nnz receives the entry count (the call synchronises the stream).
+ * Allocates its sort scratch from the stream's memory pool.               */
+int tc_symmetrize_device(const int32_t* d_idx, const double* d_p, int64_t n, int k, uint32_t* d_row_ptr,
+                         uint32_t* d_col, double* d_val, int64_t* nnz, void* stream);
+
 /* Same result as tc_direct_device, but allocates no device memory at all.
  * No counterpart in the reference: it exists for callers that cannot call
  * cudaMalloc (a stream under CUDA-graph capture, a host framework that owns

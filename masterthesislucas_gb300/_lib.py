@@ -61,6 +61,9 @@ SIGNATURES = {
     "tc_set_variant": (_I, [_P, _I]),
     "tc_set_mac": (_I, [_P, _I]),
     "tc_set_expansion_centre": (_I, [_P, _I]),
+    "tc_knn_device": (_I, [_P, _I64, _I, _I, _P, _P, _P]),
+    "tc_perplexity_device": (_I, [_P, _I64, _I, ctypes.c_double, _I, ctypes.c_double, _P, _P]),
+    "tc_symmetrize_device": (_I, [_P, _P, _I64, _I, _P, _P, _P, _P, _P]),
     "tc_set_m2l_engine": (_I, [_P, _I]),
     "tc_set_adaptive_order": (_I, [_P, _D]),
     "tc_set_leaf_p2p": (_I, [_P, _I]),

@@ -1,122 +1,93 @@
-"""Perplexity-calibrated kNN affinities (the t-SNE P matrix) as CSR.
+"""Perplexity-calibrated kNN affinities (the t-SNE P matrix) as CSR, built on
+the GPU by the library's kernels (csrc/affinity.cu).
 
 The reference reads P from Matrix Market files written offline by openTSNE
 (``MnistLoader.ipynb`` cell 14: PCA(50) -> PerplexityBasedNN(perplexity,
 k = 3*perplexity, symmetrize=True) -> mmwrite) and converts them to CSR in
 ``TSNE::setupEfficientPmatrix`` (src/nBodyInstances/tsne.h:462-520: rows
 sorted, columns sorted within a row).  openTSNE and the data files are not
-available, so this module restates the published algorithm: exact kNN on
-squared Euclidean distances, per-point binary search of the Gaussian
-precision to the target perplexity, symmetrisation P = (P + P^T) / (2N).
-The affinity values are therefore not pinned to the reference's files.
+available, so the published algorithm is restated: exact kNN on squared
+Euclidean distances (FP32, summed over the dimensions in order), a per-point
+bisection of the Gaussian precision to the target perplexity (FP64), and the
+symmetrisation P = (P + P^T) / (2N).  The affinity values are therefore not
+pinned to the reference's files; the kernels are pinned bit for bit to the
+CPU restatement in the oracle.
 
-Setup code (not timed): it runs with torch on whatever device is given.
+Setup code (not timed): inputs are copied to the device with torch, which is
+used for memory only.
 """
 from __future__ import annotations
 
-import math
+import ctypes
 
 import numpy as np
-import torch
+
+from ._lib import check, lib, ptr
+
+MAX_K = 128
 
 
-def knn(x: torch.Tensor, k: int, block: int = 4096):
-    """Exact k nearest neighbours (self excluded) by blocked squared distances."""
-    n = x.shape[0]
-    x = x.float()
-    sq = (x * x).sum(1)
-    d_out = torch.empty(n, k, device=x.device)
-    i_out = torch.empty(n, k, dtype=torch.int64, device=x.device)
-    for s in range(0, n, block):
-        e = min(n, s + block)
-        d = sq[s:e, None] + sq[None, :] - 2.0 * (x[s:e] @ x.T)
-        d[torch.arange(e - s, device=x.device), torch.arange(s, e, device=x.device)] = float("inf")
-        vals, idx = torch.topk(d, k, dim=1, largest=False)
-        d_out[s:e] = vals.clamp_min(0.0)
-        i_out[s:e] = idx
-    return d_out, i_out
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("the affinity build runs on the GPU (no CUDA device)")
+    return torch
 
 
-def perplexity_rows(d2: torch.Tensor, perplexity: float, iters: int = 100, tol: float = 1e-5):
-    """Binary search of beta_i so that H(P_i) = log(perplexity); rows sum to 1."""
-    d2 = d2.double()
-    n = d2.shape[0]
-    target = math.log(perplexity)
-    beta = torch.ones(n, dtype=torch.float64, device=d2.device)
-    lo = torch.zeros_like(beta)
-    hi = torch.full_like(beta, float("inf"))
-    dmin = d2[:, :1]
-    for _ in range(iters):
-        w = torch.exp(-(d2 - dmin) * beta[:, None])
-        s = w.sum(1)
-        p = w / s[:, None]
-        h = torch.log(s) + beta * ((d2 - dmin) * p).sum(1)
-        diff = h - target
-        if float(diff.abs().max()) < tol:
-            break
-        up = diff > 0
-        lo = torch.where(up, beta, lo)
-        hi = torch.where(up, hi, beta)
-        beta = torch.where(torch.isinf(hi), beta * 2.0, (lo + hi) / 2.0)
-    w = torch.exp(-(d2 - dmin) * beta[:, None])
-    return w / w.sum(1, keepdim=True)
+def knn(x, k: int, stream=None):
+    """Exact k nearest neighbours (self excluded) of device float32 rows x (n x
+    dim): (dist n x k float32, idx n x k int32) on the device, each row
+    ordered by (squared distance, index)."""
+    torch = _torch()
+    x = x.contiguous()
+    n, dim = x.shape
+    d = torch.empty((n, k), dtype=torch.float32, device=x.device)
+    i = torch.empty((n, k), dtype=torch.int32, device=x.device)
+    check(lib().tc_knn_device(ptr(x), n, dim, k, ptr(d), ptr(i), stream))
+    return d, i
 
 
-def build_p_csr(x, perplexity: float = 30.0, k: int | None = None, device=None):
-    """Symmetric affinity matrix P (sums to 1) as CSR: (row_ptr u32, col u32, val f64)."""
+def perplexity_rows(dist, perplexity: float, max_iter: int = 100, tol: float = 1e-5, stream=None):
+    """Row-normalised Gaussian affinities (FP64, device) whose entropy is
+    log(perplexity) to within tol, from the kNN distances."""
+    torch = _torch()
+    n, k = dist.shape
+    p = torch.empty((n, k), dtype=torch.float64, device=dist.device)
+    check(lib().tc_perplexity_device(ptr(dist.contiguous()), n, k, float(perplexity), int(max_iter), float(tol),
+                                     ptr(p), stream))
+    return p
+
+
+def symmetrize(idx, p, stream=None):
+    """(P + P^T) / (2N) as CSR on the host: (row_ptr u32, col u32, val f64)."""
+    torch = _torch()
+    n, k = idx.shape
+    rp = torch.empty(n + 1, dtype=torch.int32, device=idx.device)
+    col = torch.empty(2 * n * k, dtype=torch.int32, device=idx.device)
+    val = torch.empty(2 * n * k, dtype=torch.float64, device=idx.device)
+    nnz = ctypes.c_int64(0)
+    check(lib().tc_symmetrize_device(ptr(idx.contiguous()), ptr(p.contiguous()), n, k, ptr(rp), ptr(col), ptr(val),
+                                     ctypes.byref(nnz), stream))
+    m = nnz.value
+    return (rp.cpu().numpy().view(np.uint32).copy(), col[:m].cpu().numpy().view(np.uint32).copy(),
+            val[:m].cpu().numpy().copy())
+
+
+def build_p_csr(x, perplexity: float = 30.0, k: int | None = None, device="cuda", max_iter: int = 100,
+                tol: float = 1e-5):
+    """Symmetric affinity matrix P (sums to 1) as CSR: (row_ptr u32, col u32, val f64).
+
+    x: n x dim input points (host array or device tensor).  k defaults to
+    3 * perplexity, as openTSNE's PerplexityBasedNN."""
+    torch = _torch()
     if k is None:
         k = int(3 * perplexity)
-    xt = torch.as_tensor(np.asarray(x), device=device or "cpu")
+    xt = torch.as_tensor(np.asarray(x, np.float32) if not torch.is_tensor(x) else x, device=device)
+    xt = xt.to(torch.float32).contiguous()
     n = xt.shape[0]
     k = min(k, n - 1)
-    d2, idx = knn(xt, k)
-    if xt.is_cuda:
-        return _symmetrize_device(perplexity_rows(d2, perplexity), idx, n)
-    return _symmetrize_host(perplexity_rows(d2, perplexity).cpu().numpy(), idx.cpu().numpy(), n)
-
-
-def _symmetrize_host(p: np.ndarray, idx: np.ndarray, n: int):
-    """(P + P^T) / (2N) as CSR (rows and columns sorted), on the host."""
-    k = idx.shape[1]
-    rows = np.repeat(np.arange(n, dtype=np.int64), k)
-    cols = idx.reshape(-1)
-    vals = p.reshape(-1)
-    # symmetrise: (P + P^T) / (2N)
-    r2 = np.concatenate([rows, cols])
-    c2 = np.concatenate([cols, rows])
-    v2 = np.concatenate([vals, vals]) * (1.0 / (2.0 * n))  # as the device path scales
-    key = r2 * n + c2
-    order = np.argsort(key, kind="stable")
-    key = key[order]
-    v2 = v2[order]
-    uniq, start = np.unique(key, return_index=True)
-    vsum = np.add.reduceat(v2, start)
-    r = (uniq // n).astype(np.int64)
-    c = (uniq % n).astype(np.uint32)
-    row_ptr = np.zeros(n + 1, np.uint32)
-    np.add.at(row_ptr, r + 1, 1)
-    row_ptr = np.cumsum(row_ptr).astype(np.uint32)
-    return row_ptr, c, vsum.astype(np.float64)
-
-
-def _symmetrize_device(p: torch.Tensor, idx: torch.Tensor, n: int):
-    """(P + P^T) / (2N) as CSR, on the GPU (each entry sums at most two
-    values, so the result does not depend on the summation order)."""
-    k = idx.shape[1]
-    dev = idx.device
-    rows = torch.arange(n, device=dev, dtype=torch.int64).repeat_interleave(k)
-    cols = idx.reshape(-1).to(torch.int64)
-    vals = p.reshape(-1).to(torch.float64)
-    key = torch.cat([rows * n + cols, cols * n + rows])
-    v2 = torch.cat([vals, vals]) * (1.0 / (2.0 * n))
-    key, order = torch.sort(key, stable=True)
-    v2 = v2[order]
-    uniq, counts = torch.unique_consecutive(key, return_counts=True)
-    seg = torch.repeat_interleave(torch.arange(len(uniq), device=dev), counts)
-    vsum = torch.zeros(len(uniq), dtype=torch.float64, device=dev).index_add_(0, seg, v2)
-    r = uniq // n
-    c = (uniq % n).to(torch.int32)
-    row_ptr = torch.zeros(n + 1, dtype=torch.int64, device=dev)
-    row_ptr[1:] = torch.cumsum(torch.bincount(r, minlength=n), 0)
-    return (row_ptr.cpu().numpy().astype(np.uint32), c.cpu().numpy().astype(np.uint32),
-            vsum.cpu().numpy().astype(np.float64))
+    if k > MAX_K:
+        raise ValueError(f"k = {k} exceeds the kNN kernel's {MAX_K} neighbours")
+    d, i = knn(xt, k)
+    p = perplexity_rows(d, perplexity, max_iter, tol)
+    return symmetrize(i, p)

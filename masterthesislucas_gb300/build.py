@@ -20,8 +20,9 @@ BUILD = os.path.join(PKG, "_build")
 
 # longest compiles first
 SOURCES = ["fmm_p.cu", "lists.cu", "fmm.cu", "tree.cu", "tree_p.cu", "bh.cu", "pm.cu", "tsne.cu", "learned.cu",
-           "mlp.cu", "direct.cu", "integrate.cu", "sort.cu", "scan.cu", "api.cu"]
-NO_FMA = {"tree.cu"}
+           "mlp.cu", "direct.cu", "integrate.cu", "affinity.cu", "sort.cu", "scan.cu", "api.cu"]
+# FP64 tree build and the affinity matrix: operations in a fixed, stated form (fused only where written)
+NO_FMA = {"tree.cu", "affinity.cu"}
 # FP32 force kernels: denormals flushed (squared distances never reach them) so
 # that rsqrt/reciprocal map to single SFU instructions
 FTZ = {"fmm.cu", "fmm_p.cu", "tree_p.cu"}

@@ -86,6 +86,14 @@ def lib():
         L.orc_bh.restype = I
         L.orc_tsne_attractive.argtypes = [I64, P, P, P, P, D, P]
         L.orc_tsne_step.argtypes = [I64, P, P, P, P, P, I, I, D, D, D, D, P, P, P]
+        L.orc_knn.argtypes = [I64, I, P, I, P, P]
+        L.orc_exp.argtypes = [D]
+        L.orc_exp.restype = D
+        L.orc_log.argtypes = [D]
+        L.orc_log.restype = D
+        L.orc_perplexity.argtypes = [I64, I, P, D, I, D, P]
+        L.orc_symmetrize.argtypes = [I64, I, P, P, P, P, P]
+        L.orc_symmetrize.restype = I64
         _lib = L
     return _lib
 
@@ -169,6 +177,45 @@ def sym_fmm(pos, *, kernel=KERNEL_TSNE, eps=0.0, max_children=16, depth=-1, thet
     fn(kernel, eps, max_children, d, theta, n, _p(pos), _p(np.asarray(mn, np.float64)),
        _p(np.asarray(mx, np.float64)), _p(codes), _p(ids), _p(ps), _p(g), _p(tot), _p(nodes))
     return dict(codes=codes, ids=ids, pos=ps, grad=g, total=float(tot[0]), nodes=nodes, depth=d)
+
+
+def knn(x, k):
+    """Exact k nearest neighbours (FP32 distances summed in dimension order,
+    ties by index, self excluded): (dist n x k float32, idx n x k int32)."""
+    x = np.ascontiguousarray(x, np.float32)
+    n, dim = x.shape
+    d = np.empty((n, k), np.float32)
+    i = np.empty((n, k), np.int32)
+    lib().orc_knn(n, dim, _p(x), k, _p(d), _p(i))
+    return d, i
+
+
+def perplexity_rows(dist, perplexity, max_iter=100, tol=1e-5):
+    """Row-normalised Gaussian affinities calibrated to the perplexity (FP64)."""
+    dist = np.ascontiguousarray(dist, np.float32)
+    n, k = dist.shape
+    p = np.empty((n, k))
+    lib().orc_perplexity(n, k, _p(dist), perplexity, max_iter, tol, _p(p))
+    return p
+
+
+def symmetrize(idx, p):
+    """(P + P^T) / (2N) as CSR (row_ptr u32, col u32, val f64)."""
+    idx = np.ascontiguousarray(idx, np.int32)
+    p = np.ascontiguousarray(p, np.float64)
+    n, k = idx.shape
+    rp = np.empty(n + 1, np.uint32)
+    col = np.empty(2 * n * k, np.uint32)
+    val = np.empty(2 * n * k)
+    nnz = lib().orc_symmetrize(n, k, _p(idx), _p(p), _p(rp), _p(col), _p(val))
+    return rp, col[:nnz].copy(), val[:nnz].copy()
+
+
+def affinity_csr(x, perplexity=30.0, k=None, max_iter=100, tol=1e-5):
+    """The whole affinity build: kNN, bandwidths, symmetrisation."""
+    k = int(3 * perplexity) if k is None else k
+    d, i = knn(x, min(k, len(x) - 1))
+    return symmetrize(i, perplexity_rows(d, perplexity, max_iter, tol))
 
 
 def bhmp(pos, *, kernel=KERNEL_TSNE, eps=0.0, max_children=16, theta=0.5):

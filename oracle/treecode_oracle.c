@@ -1456,3 +1456,208 @@ int orc_pm(int p, double cell_size, int min_intervals, int64_t n, const double* 
     free(pot_grid);
     return 0;
 }
+
+/* ------------------------------------------------------------------ affinities
+ * The t-SNE affinity matrix the reference reads from openTSNE's output
+ * (MnistLoader.ipynb cell 14: PerplexityBasedNN, k = 3 * perplexity,
+ * symmetrize=True; CSR by TSNE::setupEfficientPmatrix, tsne.h:462-520).
+ * openTSNE is absent, so the published algorithm is restated with every
+ * operation fixed (fused only where fma/fmaf is written; this file is built
+ * with -ffp-contract=off): FP32 squared distances summed over the dimensions
+ * in order, neighbours ordered by (distance, index); per-row FP64 bisection
+ * of the bandwidth to the perplexity with exp and log written from their
+ * series; (P + P^T) / (2N) with the two contributions to an entry added.   */
+
+static const double A_LN2_HI = 0x1.62e42fee00000p-1;
+static const double A_LN2_LO = 0x1.a39ef35793c76p-33;
+static const double A_INV_LN2 = 0x1.71547652b82fep+0;
+
+static double a_scale2(double v, int k)
+{
+    uint64_t b;
+    double f;
+    if (k < -1000) {
+        v *= 0x1p-600;
+        k += 600;
+    }
+    b = (uint64_t)(k + 1023) << 52;
+    memcpy(&f, &b, 8);
+    return v * f;
+}
+
+double orc_exp(double x)
+{
+    double kf, r, q;
+    int k;
+    if (!(x > -745.0)) return 0.0;
+    if (x > 709.0) return INFINITY;
+    kf = floor(x * A_INV_LN2 + 0.5);
+    k = (int)kf;
+    r = fma(-kf, A_LN2_HI, x);
+    r = fma(-kf, A_LN2_LO, r);
+    /* Taylor series of e^r to degree 13 (|r| <= ln 2 / 2), Horner form */
+    q = 0x1.6124613a86d09p-33;
+    q = fma(q, r, 0x1.1eed8eff8d898p-29);
+    q = fma(q, r, 0x1.ae64567f544e4p-26);
+    q = fma(q, r, 0x1.27e4fb7789f5cp-22);
+    q = fma(q, r, 0x1.71de3a556c734p-19);
+    q = fma(q, r, 0x1.a01a01a01a01ap-16);
+    q = fma(q, r, 0x1.a01a01a01a01ap-13);
+    q = fma(q, r, 0x1.6c16c16c16c17p-10);
+    q = fma(q, r, 0x1.1111111111111p-7);
+    q = fma(q, r, 0x1.5555555555555p-5);
+    q = fma(q, r, 0x1.5555555555555p-3);
+    q = fma(q, r, 0.5);
+    q = fma(q, r, 1.0);
+    q = fma(q, r, 1.0);
+    return a_scale2(q, k);
+}
+
+double orc_log(double x)
+{
+    uint64_t b;
+    double m, z, z2, q, lm, ed;
+    int e;
+    memcpy(&b, &x, 8);
+    e = (int)((b >> 52) & 0x7FF) - 1023;
+    b = (b & 0x000FFFFFFFFFFFFFull) | 0x3FF0000000000000ull;
+    memcpy(&m, &b, 8);
+    if (m > 1.4142135623730951) {
+        m *= 0.5;
+        e += 1;
+    }
+    /* log m = 2 atanh((m - 1)/(m + 1)), odd series to z^27 */
+    z = (m - 1.0) / (m + 1.0);
+    z2 = z * z;
+    q = 0.037037037037037035;
+    q = fma(q, z2, 0.04);
+    q = fma(q, z2, 0.043478260869565216);
+    q = fma(q, z2, 0.047619047619047616);
+    q = fma(q, z2, 0.05263157894736842);
+    q = fma(q, z2, 0.058823529411764705);
+    q = fma(q, z2, 0.06666666666666667);
+    q = fma(q, z2, 0.07692307692307693);
+    q = fma(q, z2, 0.09090909090909091);
+    q = fma(q, z2, 0.1111111111111111);
+    q = fma(q, z2, 0.14285714285714285);
+    q = fma(q, z2, 0.2);
+    q = fma(q, z2, 0.3333333333333333);
+    lm = 2.0 * fma(z * z2, q, z);
+    ed = (double)e;
+    return fma(ed, A_LN2_HI, fma(ed, A_LN2_LO, lm));
+}
+
+static int a_before(float da, int32_t ja, float db, int32_t jb)
+{
+    return da < db || (da == db && ja < jb);
+}
+
+void orc_knn(int64_t n, int dim, const float* x, int k, float* dist, int32_t* idx)
+{
+    for (int64_t i = 0; i < n; i++) {
+        float* rd = dist + i * k;
+        int32_t* ri = idx + i * k;
+        int cnt = 0;
+        for (int64_t j = 0; j < n; j++) {
+            float d = 0.f;
+            int pos, e;
+            if (j == i) continue;
+            for (int t = 0; t < dim; t++) {
+                const float df = x[i * dim + t] - x[j * dim + t];
+                d = fmaf(df, df, d);
+            }
+            if (cnt == k && !a_before(d, (int32_t)j, rd[k - 1], ri[k - 1])) continue;
+            pos = 0;
+            while (pos < cnt && a_before(rd[pos], ri[pos], d, (int32_t)j)) pos++;
+            e = cnt < k ? cnt : k - 1;
+            for (; e > pos; e--) {
+                rd[e] = rd[e - 1];
+                ri[e] = ri[e - 1];
+            }
+            rd[pos] = d;
+            ri[pos] = (int32_t)j;
+            if (cnt < k) cnt++;
+        }
+    }
+}
+
+void orc_perplexity(int64_t n, int k, const float* dist, double perplexity, int max_iter, double tol, double* p)
+{
+    const double log_perp = orc_log(perplexity);
+    for (int64_t i = 0; i < n; i++) {
+        const float* d = dist + i * k;
+        const double dmin = (double)d[0];
+        double beta = 1.0, lo = 0.0, hi = INFINITY, s;
+        for (int it = 0; it < max_iter; it++) {
+            double ss = 0.0, sd = 0.0, h, diff;
+            for (int j = 0; j < k; j++) {
+                const double dj = (double)d[j] - dmin;
+                const double w = orc_exp(-dj * beta);
+                ss += w;
+                sd = fma(dj, w, sd);
+            }
+            h = orc_log(ss) + beta * sd / ss;
+            diff = h - log_perp;
+            if (fabs(diff) < tol) break;
+            if (diff > 0.0) {
+                lo = beta;
+                beta = isinf(hi) ? beta * 2.0 : (lo + hi) * 0.5;
+            } else {
+                hi = beta;
+                beta = (lo + hi) * 0.5;
+            }
+        }
+        s = 0.0;
+        for (int j = 0; j < k; j++) s += orc_exp(-((double)d[j] - dmin) * beta);
+        for (int j = 0; j < k; j++) p[i * k + j] = orc_exp(-((double)d[j] - dmin) * beta) / s;
+    }
+}
+
+typedef struct {
+    uint32_t row, col;
+    int64_t e;
+    double v;
+} a_entry;
+
+static int a_cmp(const void* a, const void* b)
+{
+    const a_entry* x = (const a_entry*)a;
+    const a_entry* y = (const a_entry*)b;
+    if (x->row != y->row) return x->row < y->row ? -1 : 1;
+    if (x->col != y->col) return x->col < y->col ? -1 : 1;
+    return x->e < y->e ? -1 : (x->e > y->e);
+}
+
+int64_t orc_symmetrize(int64_t n, int k, const int32_t* idx, const double* p, uint32_t* row_ptr, uint32_t* col,
+                       double* val)
+{
+    const int64_t nk = n * k, m = 2 * nk;
+    const double c = 1.0 / (2.0 * (double)n);
+    a_entry* t = (a_entry*)malloc((size_t)m * sizeof(a_entry));
+    int64_t u = 0;
+    for (int64_t e = 0; e < nk; e++) {
+        const double w = p[e] * c;
+        t[e].row = (uint32_t)(e / k);
+        t[e].col = (uint32_t)idx[e];
+        t[e].e = e;
+        t[e].v = w;
+        t[nk + e].row = (uint32_t)idx[e];
+        t[nk + e].col = (uint32_t)(e / k);
+        t[nk + e].e = nk + e;
+        t[nk + e].v = w;
+    }
+    qsort(t, (size_t)m, sizeof(a_entry), a_cmp);
+    for (int64_t q = 0; q < m; q++) {
+        if (q > 0 && t[q].row == t[q - 1].row && t[q].col == t[q - 1].col) {
+            val[u - 1] = val[u - 1] + t[q].v;
+            continue;
+        }
+        if (q == 0 || t[q].row != t[q - 1].row) row_ptr[t[q].row] = (uint32_t)u;
+        col[u] = t[q].col;
+        val[u] = t[q].v;
+        u++;
+    }
+    row_ptr[n] = (uint32_t)u;
+    free(t);
+    return u;
+}

@@ -123,6 +123,22 @@ void orc_tsne_step(int64_t n, const double* y, const double* y_prev,
                    int max_children, int depth, double theta, double exag_code,
                    double lr, double momentum, double* y_next, double* grad_out, double* z_out);
 
+/* The t-SNE affinity matrix (openTSNE's PerplexityBasedNN restated, see
+ * treecode_oracle.c): exact kNN with FP32 squared distances summed over the
+ * dimensions in order (fmaf), neighbours ordered by (distance, index), self
+ * excluded; dist/idx are n x k.                                             */
+void orc_knn(int64_t n, int dim, const float* x, int k, float* dist, int32_t* idx);
+/* FP64 exp and log from their series (range reduction by ln 2).            */
+double orc_exp(double x);
+double orc_log(double x);
+/* Per-row bisection of the Gaussian bandwidth to the perplexity; p (n x k)
+ * holds the row-normalised conditional probabilities.                     */
+void orc_perplexity(int64_t n, int k, const float* dist, double perplexity, int max_iter, double tol, double* p);
+/* (P + P^T) / (2N) as CSR with rows and columns sorted (setupEfficientPmatrix
+ * layout); row_ptr n + 1, col/val capacity 2nk.  Returns nnz.              */
+int64_t orc_symmetrize(int64_t n, int k, const int32_t* idx, const double* p, uint32_t* row_ptr, uint32_t* col,
+                       double* val);
+
 #ifdef __cplusplus
 }
 #endif

@@ -4,7 +4,8 @@ import os
 import numpy as np
 import pytest
 
-from masterthesislucas_gb300 import affinity, datasets, mtx
+import oracle
+from masterthesislucas_gb300 import datasets, mtx
 
 
 def dense(rp, col, val, n):
@@ -16,7 +17,7 @@ def dense(rp, col, val, n):
 
 def test_round_trip_is_exact(tmp_path):
     x, _ = datasets.cluster_data(400, 8, k=4, seed=3)
-    rp, col, val = affinity.build_p_csr(x, perplexity=10.0, device="cpu")
+    rp, col, val = oracle.affinity_csr(x, perplexity=10.0)
     p = os.path.join(tmp_path, "P.mtx")
     mtx.write_p_matrix(p, rp, col, val, comment="test")
     rp2, col2, val2 = mtx.read_p_matrix(p)
