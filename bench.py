@@ -49,9 +49,9 @@ TARGET_ERR = 1e-4
 N_SAMPLES = 4096
 THETAS = (0.4, 0.35, 0.3, 0.25, 0.2, 0.15, 0.1)
 # learned-order controller training: systems x pairs sampled per level x Adam steps
-CTRL_SYSTEMS = 8
-CTRL_PER_LEVEL = 200000
-CTRL_STEPS = 6000
+CTRL_SYSTEMS = 24
+CTRL_PER_LEVEL = 400000
+CTRL_STEPS = 12000
 
 WORKLOADS = {
     "nbody_two_disks_4m": dict(n=4194304, dist="two_disks", kernel="gravity", softening=1e-3, max_children=64),
@@ -229,7 +229,7 @@ def run_ours(args, w, rank, world):
 
     from masterthesislucas_gb300 import NBodySolverFMM_SYM_MORTON
     from masterthesislucas_gb300._lib import check, lib, ptr
-    from masterthesislucas_gb300.autotune import tune, tune_learned
+    from masterthesislucas_gb300.autotune import refine_leaf_p2p, tune, tune_learned
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
@@ -255,12 +255,14 @@ def run_ours(args, w, rank, world):
     ref = ref_d.cpu().numpy()
     ref_eval = ref_eval_d.cpu().numpy()
 
-    def make(theta, order=0, depth=None, controller=None, tau=None, mac="cell", centre="com", m2l="simt"):
+    def make(theta, order=0, depth=None, controller=None, tau=None, mac="cell", centre="com", m2l="simt",
+             leaf_p2p=None):
         kind, _, slack = mac.partition(":")
+        lp = args.leaf_p2p if leaf_p2p is None else leaf_p2p
         s = NBodySolverFMM_SYM_MORTON(w["kernel"], max_children=w["max_children"], tree_depth=depth, theta=theta,
                                       softening=w["softening"], precision="fp32", order=order,
                                       device=dev.index, stream=stream.cuda_stream, mac=kind,
-                                      slack=float(slack or 1.0), leaf_p2p=args.leaf_p2p if order else 0,
+                                      slack=float(slack or 1.0), leaf_p2p=lp if order else 0,
                                       centre=centre, m2l=m2l)
         if controller is not None:
             s.set_controller(controller, tau)
@@ -322,6 +324,10 @@ def run_ours(args, w, rank, world):
                 plain = best
         if plain is None:
             raise SystemExit("autotuner found no configuration meeting the error target")
+        # the leaf-pair threshold, refined at the chosen configuration
+        plain, tr = refine_leaf_p2p(plain, pos_d, ref, rows_d, kernel=w["kernel"], softening=w["softening"],
+                                    leaf=w["max_children"], target=target, stream=stream, device=dev.index)
+        trials += tr
     p12 = min((t for t in trials if t["order"] == 12 and t["err"] <= target), key=lambda t: t["ms"], default=None)
 
     # learned-order controller
@@ -339,9 +345,11 @@ def run_ours(args, w, rank, world):
 
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > L2 (129 MB)
 
-    def timed(s, steps, sample_clocks):
+    def timed(s, steps, sample_clocks, judge=None):
         for _ in range(args.warmup):
             step(s)
+            if judge is not None:  # the check's first call sets up its kernels: keep it out of the timing
+                judge.check_async(pos_d, grad_d, torch.zeros(1, dtype=torch.float64, device=dev), stream)
         torch.cuda.synchronize()
         stages_sync = s.stage_times()
         graph = not args.no_graph
@@ -357,6 +365,7 @@ def run_ours(args, w, rank, world):
             torch.distributed.barrier()
         ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
         ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        judge_err = torch.zeros(steps, dtype=torch.float64, device=dev)
         stage_sum, launches = None, 0
         with ClockSampler(dev.index) as clk:
             for k in range(steps):
@@ -371,6 +380,9 @@ def run_ours(args, w, rank, world):
                     launches += s.launches()
                     s.solve_device(grad_d, tot_d, accumulate=False, scatter=True)
                     launches += s.launches()
+                if judge is not None:
+                    # sampled-error check of this step on the same stream, read after the loop
+                    judge.check_async(pos_d, grad_d, judge_err[k:k + 1], stream)
                 ev1[k].record(stream)
                 st = stages_sync if graph else s.stage_times()
                 stage_sum = st if stage_sum is None else {a: stage_sum[a] + st[a] for a in st}
@@ -378,6 +390,24 @@ def run_ours(args, w, rank, world):
         if graph and s.async_status():
             raise SystemExit("a captured step was flagged invalid (box or list capacity)")
         ms = [ev0[k].elapsed_time(ev1[k]) for k in range(steps)]
+        judged = None
+        if judge is not None:
+            # the plain FMM is the fallback: a step whose sampled error missed the target is redone by it, and
+            # the redo's device time is added to that step
+            errs = judge_err.cpu().numpy()
+            failed = [k for k in range(steps) if not errs[k] <= judge.tol]
+            for k in failed:
+                f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                f0.record(stream)
+                judge.plain.update_tree_device(pos_d)
+                judge.plain.solve_device(grad_d, tot_d, accumulate=False, scatter=True)
+                f1.record(stream)
+                torch.cuda.synchronize()
+                ms[k] += f0.elapsed_time(f1)
+            judge.steps += steps
+            judge.recomputed += len(failed)
+            judged = {"checked_steps": steps, "fallback_steps": len(failed), "sampled_err_max": float(np.nanmax(errs)),
+                      "check_rows": int(len(judge.rows))}
         t_total = sum(ms) / 1e3
         if world > 1:
             t = torch.tensor([t_total], device=dev)
@@ -386,7 +416,8 @@ def run_ours(args, w, rank, world):
         err = median_error(grad_d[rows_eval_d].cpu().numpy(), ref_eval)
         nodes = s.getNodesBufferData(-1).shape[0]
         nn_pairs, near_pairs = s.list_stats()
-        return dict(ms=ms, t_total=t_total, stages={a: v / steps for a, v in stage_sum.items()}, graph=graph,
+        return dict(ms=ms, t_total=t_total, judge=judged, stages={a: v / steps for a, v in stage_sum.items()},
+                    graph=graph,
                     counters=s.counters(), err=err, clocks=clk.summary() if sample_clocks else None,
                     launches=launches, depth=s.depth(), nonempty_nodes=int(nodes),
                     near_pairs=int(np.asarray(near_pairs, np.int64).sum()))
@@ -394,17 +425,17 @@ def run_ours(args, w, rank, world):
     # the arms: the learned-order method (headline, when it meets the target) and the plain ones beside it
     arms = {}
     s_plain = make(plain["theta"], order=plain["order"], depth=plain["depth"], mac=plain["mac"],
-                   centre=plain["centre"], m2l=plain["m2l"])
+                   centre=plain["centre"], m2l=plain["m2l"], leaf_p2p=plain.get("leaf_p2p"))
     arms["plain_best"] = timed(s_plain, args.steps, sample_clocks=True)
     arms["plain_best"].update(theta=plain["theta"], order=plain["order"], mac=plain["mac"], centre=plain["centre"],
-                              m2l=plain["m2l"])
+                              m2l=plain["m2l"], leaf_p2p=plain.get("leaf_p2p", args.leaf_p2p))
     if p12 is not None:
-        key = ("depth", "theta", "mac", "centre", "m2l")
-        if plain["order"] == 12 and all(p12[k] == plain[k] for k in key):
+        key = ("depth", "theta", "mac", "centre", "m2l", "leaf_p2p")
+        if plain["order"] == 12 and all(p12.get(k) == plain.get(k) for k in key):
             arms["plain_p12"] = arms["plain_best"]
         else:
             s12 = make(p12["theta"], order=12, depth=p12["depth"], mac=p12["mac"], centre=p12["centre"],
-                       m2l=p12["m2l"])
+                       m2l=p12["m2l"], leaf_p2p=p12.get("leaf_p2p"))
             arms["plain_p12"] = timed(s12, args.steps, sample_clocks=False)
             arms["plain_p12"].update(theta=p12["theta"], order=12, mac=p12["mac"], centre=p12["centre"],
                                      m2l=p12["m2l"])
@@ -420,8 +451,17 @@ def run_ours(args, w, rank, world):
     s_head, head, s_l = s_plain, "plain_best", None
     if learned_cfg is not None:
         s_l = make(1.0, order=12, depth=learned_cfg["depth"], controller=ctrl, tau=learned_cfg["tau"])
-        arms["learned"] = timed(s_l, args.steps, sample_clocks=True)
+        # the plain FMM is the fallback and the judge: each timed learned step is checked on 64 sampled
+        # particles against an FP32 direct sum (about 0.55 ms at 4M; 32 samples proved too noisy a median) and
+        # redone by the plain FMM when it misses the target
+        from masterthesislucas_gb300.learned import CheckedSolve
+        s_fb = make(plain["theta"], order=plain["order"], depth=plain["depth"], mac=plain["mac"],
+                    centre=plain["centre"], m2l=plain["m2l"], leaf_p2p=plain.get("leaf_p2p"))
+        judge = CheckedSolve(s_l, s_fb, n, kernel=w["kernel"], softening=w["softening"], tol=TARGET_ERR,
+                             n_check=64, seed=11, device=dev.index)
+        arms["learned"] = timed(s_l, args.steps, sample_clocks=True, judge=judge)
         arms["learned"].update(tau=learned_cfg["tau"], order=12)
+        s_fb.close()
         # the headline is the faster of the two methods (both meet the error target)
         if arms["learned"]["t_total"] < arms["plain_best"]["t_total"]:
             s_head, head = s_l, "learned"
@@ -950,12 +990,14 @@ def step_roofline(n, arm, hbm_gbs, fp32_tflops):
 def arm_summary(n, steps, a):
     return {"particles_per_s": n * steps / a["t_total"], "ms_per_step": 1e3 * a["t_total"] / steps,
             "depth": a["depth"], "order": a.get("order"), "theta": a.get("theta"), "tau": a.get("tau"),
-            "mac": a.get("mac"), "centre": a.get("centre"), "m2l": a.get("m2l"), "median_err": a["err"][0]}
+            "mac": a.get("mac"), "centre": a.get("centre"), "m2l": a.get("m2l"), "median_err": a["err"][0],
+            **({"judge": a["judge"]} if a.get("judge") else {})}
 
 
 def compact_calib(calib):
     """The chosen configurations only; the trial lists go to the record file."""
-    keep = ("mac", "centre", "m2l", "depth", "theta", "order", "tau", "ms", "err", "median_err", "particles_per_s")
+    keep = ("mac", "centre", "m2l", "depth", "theta", "order", "leaf_p2p", "tau", "ms", "err", "median_err",
+            "particles_per_s")
     out = {}
     for k in ("plain_best", "plain_p12", "plain_tensor", "learned_best", "reference_order"):
         v = calib.get(k)
@@ -1005,6 +1047,7 @@ def headline_line(args, w, r, world, config, peaks, peak_src, sms):
     config.update({"theta": head.get("theta"), "tau": head.get("tau"), "depth": head["depth"], "mac": head.get("mac"),
                    "order": head.get("order"), "method": r["head"],
                    "centre": head.get("centre"), "m2l": head.get("m2l"),
+                   "leaf_p2p": head.get("leaf_p2p", config.get("leaf_p2p")),
                    "expansion": ("total-order Cartesian Taylor about the cell centre, M2L on the tensor cores (BF16 "
                                  "hi/lo split, FP32 accumulation) on the deep levels" if head.get("centre") == "box"
                                  else "total-order Cartesian Taylor about the COM, FP32 SIMT M2L"),
@@ -1016,7 +1059,7 @@ def headline_line(args, w, r, world, config, peaks, peak_src, sms):
                    "step": ("one CUDA graph launch per step (update + solve captured over the exact box, "
                             "stage times from the uncaptured warm-up steps)" if head.get("graph")
                             else "updateTree + solveNbody calls")})
-    key = (n, config["depth"], config["order"], config["mac"], config["theta"], args.leaf_p2p, config["centre"])
+    key = (n, config["depth"], config["order"], config["mac"], config["theta"], config["leaf_p2p"], config["centre"])
     traffic, traffic_src = NEAR_TRAFFIC.get(key, (None, "no ncu capture of this configuration"))
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

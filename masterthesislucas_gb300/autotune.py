@@ -80,6 +80,41 @@ def tune(pos_d, ref_rows, rows_d, *, kernel: str, softening: float, leaf: int, t
     return best, trials
 
 
+LEAF_P2P = (0, 16, 32, 64, 128, 256)
+
+
+def refine_leaf_p2p(best, pos_d, ref_rows, rows_d, *, kernel: str, softening: float, leaf: int, target: float,
+                    stream=None, device: int = 0, values=LEAF_P2P):
+    """Second pass over the leaf-pair threshold at the chosen configuration:
+    accepted leaf pairs with at most that many particle pairs are summed
+    directly (trading M2L + L2P work for near-field pairs, which moves the
+    balance between the tensor-free FP32 near field and the expansions).
+    Returns (best with its leaf_p2p, trials)."""
+    import torch
+
+    n = pos_d.shape[0]
+    grad_d = torch.zeros((n, 2), dtype=torch.float64, device=pos_d.device)
+    tot_d = torch.zeros(1, dtype=torch.float64, device=pos_d.device)
+    s_torch = torch.cuda.Stream(device=pos_d.device) if stream is None else stream
+    kind, _, slack = best["mac"].partition(":")
+    out, trials = dict(best), []
+    for v in values:
+        s = NBodySolverFMM_SYM_MORTON(kernel, max_children=leaf, tree_depth=best["depth"], theta=best["theta"],
+                                      softening=softening, precision="fp32", order=best["order"], device=device,
+                                      stream=s_torch.cuda_stream, mac=kind, slack=float(slack or 1.0), leaf_p2p=v,
+                                      centre=best.get("centre", "com"), m2l=best.get("m2l", "simt"))
+        try:
+            ms = _time_step(s, pos_d, grad_d, tot_d, s_torch)
+            err = median_error(grad_d[rows_d].cpu().numpy(), ref_rows)
+        finally:
+            s.close()
+        t = dict(best, leaf_p2p=v, ms=ms, err=err)
+        trials.append(t)
+        if err <= target and ms < out["ms"]:
+            out = t
+    return out, trials
+
+
 def _time_step(s, pos_d, grad_d, tot_d, s_torch):
     import torch
     s.update_tree_device(pos_d)

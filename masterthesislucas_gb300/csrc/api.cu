@@ -304,6 +304,9 @@ int tc_create(const tc_config* cfg, tc_handle** out)
         tc_destroy(t);
         return tc_cuda_fail(e, "cudaMallocHost");
     }
+    // status words the asynchronous paths report through (tc_async_status): none raised yet
+    std::memset(t->h.h_words, 0, 64 * 4);
+    std::memset(t->h.h_total, 0, 64);
     *out = t;
     return TC_OK;
 }

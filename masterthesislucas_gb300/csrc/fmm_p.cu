@@ -768,32 +768,40 @@ constexpr int kNearBuf = 256;
 constexpr float kFarAway = 1.0e18f;
 
 // One sink (px, py) against its share of the staged sources: g lanes share a
-// sink, lane r of the group takes float4 slots r, r + g, r + 2g, ... (two
-// sources each; consecutive lanes read consecutive 16-byte slots, so the
-// group's loads are conflict-free and the groups' identical loads broadcast).
-// n4 is a multiple of 4g, so every lane runs the same number of trips.
+// sink, lane r of the group takes 16-byte slots r, r + g, r + 2g, ... (two
+// sources each, stored (x0, x1, y0, y1) so that each pair of coordinates is
+// one packed FP32x2 operand; consecutive lanes read consecutive slots, so the
+// group's loads are conflict-free and the groups' identical loads
+// broadcast).  Both sources of a slot go through each instruction together
+// (fma/add/sub/mul.f32x2), halving the instructions per pair; the two
+// partial sums per accumulator are added at the end.  n4 is a multiple of 4g,
+// so every lane runs the same number of trips.
 template <typename KN>
 __device__ __forceinline__ void p2p_staged(const KN& ker, const float4* __restrict__ s4, uint32_t n4, uint32_t r,
                                            uint32_t g, float px, float py, float& gx, float& gy, float& zs)
 {
+    const unsigned long long px2 = f2_pack(px, px), py2 = f2_pack(py, py);
+    unsigned long long ax = 0ull, ay = 0ull, az = 0ull;  // packed +0.0f, +0.0f
     for (uint32_t j = r; j < n4; j += 4 * g) {
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             const float4 t4 = s4[j + u * g];
-            float D1, t;
-            float Rx = px - t4.x, Ry = py - t4.y;
-            ker.near_xy(Rx, Ry, D1, t);
-            gx = fmaf(D1, Rx, gx);
-            gy = fmaf(D1, Ry, gy);
-            zs += t;
-            Rx = px - t4.z;
-            Ry = py - t4.w;
-            ker.near_xy(Rx, Ry, D1, t);
-            gx = fmaf(D1, Rx, gx);
-            gy = fmaf(D1, Ry, gy);
-            zs += t;
+            const unsigned long long Rx = f2_sub(px2, f2_pack(t4.x, t4.y));
+            const unsigned long long Ry = f2_sub(py2, f2_pack(t4.z, t4.w));
+            unsigned long long a, tt;
+            ker.near_xy2(Rx, Ry, a, tt);
+            ax = f2_fma(a, Rx, ax);
+            ay = f2_fma(a, Ry, ay);
+            az = f2_add(az, tt);
         }
     }
+    float a0, a1;
+    f2_unpack(ax, a0, a1);
+    gx += KN::kSign * (a0 + a1);
+    f2_unpack(ay, a0, a1);
+    gy += KN::kSign * (a0 + a1);
+    f2_unpack(az, a0, a1);
+    zs += KN::kSign * (a0 + a1);
 }
 
 // One warp per work item (leaf S, chunk of m <= 32 sinks): L2P of the final
@@ -815,11 +823,16 @@ __global__ void __launch_bounds__(32 * kNearWarps, 9)
              double* __restrict__ zwork, unsigned long long* __restrict__ counters)
 {
     constexpr int KW = ncoef(P - 1);
-    __shared__ __align__(16) float2 s_src[kNearWarps][kNearBuf];
+    // staged sources, two per 16-byte slot as (x0, x1, y0, y1)
+    __shared__ __align__(16) float s_src[kNearWarps][2 * kNearBuf];
     uint32_t n_pp = 0;
     const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    float2* buf = s_src[w];
+    float* buf = s_src[w];
     const float4* buf4 = reinterpret_cast<const float4*>(s_src[w]);
+    auto stage = [&](uint32_t q, float x, float y) {
+        buf[(q >> 1) * 4 + (q & 1)] = x;
+        buf[(q >> 1) * 4 + 2 + (q & 1)] = y;
+    };
     const float2* prel2 = reinterpret_cast<const float2*>(prel);
     const uint32_t li = level_index(dep);
     const int64_t nl = (int64_t)1 << (2 * dep);
@@ -888,7 +901,7 @@ __global__ void __launch_bounds__(32 * kNearWarps, 9)
                     const float ox = __shfl_sync(0xffffffffu, mox, t), oy = __shfl_sync(0xffffffffu, moy, t);
                     if (b0 + lane < take) {
                         const float2 t2 = prel2[fT + (q - eT)];
-                        buf[fill + b0 + lane] = make_float2(t2.x + ox, t2.y + oy);
+                        stage(fill + b0 + lane, t2.x + ox, t2.y + oy);
                     }
                 }
                 fill += take;
@@ -897,7 +910,7 @@ __global__ void __launch_bounds__(32 * kNearWarps, 9)
         }
         if (fill > 0) {
             const uint32_t n8 = (fill + 8u * g - 1u) & ~(8u * g - 1u);
-            for (uint32_t q = fill + lane; q < n8; q += 32) buf[q] = make_float2(kFarAway, kFarAway);
+            for (uint32_t q = fill + lane; q < n8; q += 32) stage(q, kFarAway, kFarAway);
             __syncwarp();
             if (act) p2p_staged(ker, buf4, n8 / 2, r, g, px, py, gx, gy, zs);
             __syncwarp();

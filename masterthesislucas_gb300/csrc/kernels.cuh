@@ -39,6 +39,43 @@ __device__ __forceinline__ float rsqrt_approx(float x)
     return r;
 }
 
+// Packed FP32 pairs (fma/add/sub/mul.rn.ftz.f32x2, sm_100 and later): two
+// sources' coordinates in one 64-bit register, one instruction for both.
+__device__ __forceinline__ unsigned long long f2_pack(float a, float b)
+{
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(unsigned long long v, float& a, float& b)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b, unsigned long long c)
+{
+    unsigned long long d;
+    asm("fma.rn.ftz.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ unsigned long long f2_add(unsigned long long a, unsigned long long b)
+{
+    unsigned long long d;
+    asm("add.rn.ftz.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b)
+{
+    unsigned long long d;
+    asm("sub.rn.ftz.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsigned long long b)
+{
+    unsigned long long d;
+    asm("mul.rn.ftz.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
 // Student-t kernel of the t-SNE repulsion: F(R) = R (1+r^2)^-2, pair term (1+r^2)^-1
 template <typename real>
 struct KTsne {
@@ -63,6 +100,16 @@ struct KTsne {
         const float fd = rcp_approx(fmaf(Ry, Ry, fmaf(Rx, Rx, 1.0f)));
         D1 = fd * fd;
         t = fd;
+    }
+    // near_xy of two sources at once (packed): D1 = sign * a, t = sign * tt
+    static constexpr float kSign = 1.0f;
+    __device__ __forceinline__ void near_xy2(unsigned long long Rx, unsigned long long Ry, unsigned long long& a,
+                                             unsigned long long& tt) const
+    {
+        float u0, u1;
+        f2_unpack(f2_fma(Ry, Ry, f2_fma(Rx, Rx, f2_pack(1.0f, 1.0f))), u0, u1);
+        tt = f2_pack(rcp_approx(u0), rcp_approx(u1));
+        a = f2_mul(tt, tt);
     }
 };
 
@@ -92,6 +139,17 @@ struct KGrav {
         const float isq = rsqrt_approx(fmaf(Ry, Ry, fmaf(Rx, Rx, (float)eps2)));
         D1 = -(isq * isq) * isq;
         t = -isq;
+    }
+    // near_xy of two sources at once (packed): D1 = sign * a, t = sign * tt
+    static constexpr float kSign = -1.0f;
+    __device__ __forceinline__ void near_xy2(unsigned long long Rx, unsigned long long Ry, unsigned long long& a,
+                                             unsigned long long& tt) const
+    {
+        const float e = (float)eps2;
+        float u0, u1;
+        f2_unpack(f2_fma(Ry, Ry, f2_fma(Rx, Rx, f2_pack(e, e))), u0, u1);
+        tt = f2_pack(rsqrt_approx(u0), rsqrt_approx(u1));
+        a = f2_mul(f2_mul(tt, tt), tt);
     }
 };
 

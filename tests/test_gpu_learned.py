@@ -158,3 +158,102 @@ def test_trained_controller_meets_tolerance_with_mixed_orders():
     orders = np.concatenate([s.list_orders(l) for l in range(1, s.depth() + 1)])
     assert len(orders) > 0 and np.bincount(orders, minlength=5)[:4].sum() > 0  # not everything at order 12
     s.close()
+
+
+def _m2l_flops(p):
+    K = lambda q: (q + 1) * (q + 2) // 2  # noqa: E731
+    return 10 * K(p) + 2 * sum((k + 1) * K(p - k) for k in range(p + 1))
+
+
+def _work(s):
+    """Interaction flops of the last solve: 20 per particle pair plus each
+    accepted pair's M2L at the order it was evaluated at."""
+    orders = np.concatenate([s.list_orders(l) for l in range(1, s.depth() + 1)])
+    m2l = sum(int(c) * _m2l_flops(learned.ORDERS[o]) for o, c in enumerate(np.bincount(orders, minlength=5)))
+    return 20.0 * s.counters()["p2p_pairs"] + m2l
+
+
+def test_trained_controller_gain_over_plain_order12_at_1e4():
+    """What the network buys: at a median error below 1e-4 against the FP64
+    direct sum, the learned controller's interaction work (particle pairs and
+    per-order M2L flops, the network's own inference not counted) is below
+    that of the plain fixed-order-12 FMM at its cheapest angle meeting the same
+    error, on the same tree."""
+    import torch
+    from masterthesislucas_gb300 import NBodySolverFMM_SYM_MORTON, datasets, solver
+    X, E = learned.generate(n_systems=2, n_particles=200000, per_level=20000, seed=12)
+    c, _ = learned.fit(X, E, steps=3000, batch=8192, lr=2e-3, seed=2)
+    n = 262144
+    pos = datasets.two_disks(n, seed=98).astype(np.float64)
+    rows = np.random.default_rng(2).choice(n, 2048, replace=False)
+    ref, _ = solver.direct(pos, kernel="gravity", softening=1e-3, precision="fp64", rows=rows)
+    depth = 9
+    s, g, _ = _solve(pos, c, tau=3e-5, depth=depth)
+    e_l = float(np.median(_rel_err(g[rows], ref)))
+    w_l = _work(s)
+    s.close()
+    assert e_l < 1e-4, e_l
+    pd = torch.from_numpy(pos).cuda()
+    gd = torch.zeros_like(pd)
+    td = torch.zeros(1, dtype=torch.float64, device="cuda")
+    best = None
+    for theta in (0.95, 0.9, 0.85, 0.8, 0.75, 0.7, 0.65, 0.6, 0.55, 0.5):
+        p = NBodySolverFMM_SYM_MORTON("gravity", max_children=32, tree_depth=depth, theta=theta, softening=1e-3,
+                                      order=12, mac="bmax")
+        p.update_tree_device(pd)
+        p.solve_device(gd, td)
+        torch.cuda.synchronize()
+        e_p = float(np.median(_rel_err(gd.cpu().numpy()[rows], ref)))
+        nn = p.counters()["m2l"]
+        w_p = 20.0 * p.counters()["p2p_pairs"] + nn * _m2l_flops(12)
+        p.close()
+        if e_p <= e_l:
+            best = w_p
+            break
+    assert best is not None
+    print("work learned", w_l, "plain p12", best, "gain", best / w_l)
+    assert w_l < best
+
+
+def test_checked_solve_falls_back_to_the_plain_fmm():
+    """A step whose sampled error exceeds the tolerance is redone by the plain
+    FMM (same bits as the plain solver alone); a step within it is kept."""
+    import torch
+    from masterthesislucas_gb300 import NBodySolverFMM_SYM_MORTON, datasets
+    n = 60000
+    pos = datasets.two_disks(n, seed=8).astype(np.float64)
+    pd = torch.from_numpy(pos).cuda()
+    g = torch.zeros_like(pd)
+    t = torch.zeros(1, dtype=torch.float64, device="cuda")
+
+    def plain_solver():
+        return NBodySolverFMM_SYM_MORTON("gravity", max_children=32, theta=0.6, softening=1e-3, order=8, mac="bmax")
+
+    def learned_solver(ctrl):
+        s = NBodySolverFMM_SYM_MORTON("gravity", max_children=32, theta=1.0, softening=1e-3, order=12)
+        s.set_controller(ctrl, 1e-4)
+        return s
+    plain = plain_solver()
+    plain.update_tree_device(pd)
+    plain.solve_device(g, t)
+    torch.cuda.synchronize()
+    g_plain = g.cpu().numpy().copy()
+    # accepts every candidate at order 4: far above the tolerance
+    sloppy = learned.CheckedSolve(learned_solver(_analytic_controller([-10.0] * 5, [0.0] * 5)), plain_solver(), n,
+                                  tol=1e-4)
+    err = sloppy.step(pd, g, t)
+    assert err > 1e-4 and sloppy.recomputed == 1
+    np.testing.assert_array_equal(g.cpu().numpy(), g_plain)
+    # opens every candidate (the direct sum): within the tolerance, kept
+    exact = learned.CheckedSolve(learned_solver(_analytic_controller([10.0] * 5, [0.0] * 5)), plain_solver(), n,
+                                 tol=1e-4)
+    err = exact.step(pd, g, t)
+    assert err < 1e-5 and exact.recomputed == 0
+    # the asynchronous form of the check, enqueued on a stream, measures the same error
+    st = torch.cuda.Stream()
+    e_async = torch.zeros(1, dtype=torch.float64, device="cuda")
+    exact.check_async(pd, g, e_async, st)
+    st.synchronize()
+    assert float(e_async.item()) == pytest.approx(err, rel=1e-12, abs=1e-15)
+    for s in (plain, sloppy.learned, sloppy.plain, exact.learned, exact.plain):
+        s.close()
