@@ -5,6 +5,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <new>
 #include <vector>
 
@@ -325,6 +326,12 @@ int tc_destroy(tc_handle* t)
     if (h.step_graph) cudaGraphExecDestroy(h.step_graph);
     if (h.h_total) cudaFreeHost(h.h_total);
     if (h.h_words) cudaFreeHost(h.h_words);
+    if (h.copy_stream) {
+        cudaStreamSynchronize(h.copy_stream);
+        cudaStreamDestroy(h.copy_stream);
+    }
+    if (h.ev_tree) cudaEventDestroy(h.ev_tree);
+    if (h.ev_grad) cudaEventDestroy(h.ev_grad);
     if (h.own_stream && h.stream) cudaStreamDestroy(h.stream);
     delete t;
     return TC_OK;
@@ -339,7 +346,19 @@ int tc_set_theta(tc_handle* t, double theta)
     return TC_OK;
 }
 
-static int update_common(Handle& h, const double* d_pos, int64_t n, const double* mn, const double* mx)
+static int ensure_copy_stream(Handle& h)
+{
+    if (h.copy_stream) return TC_OK;
+    TC_CUDA_TRY(cudaStreamCreateWithFlags(&h.copy_stream, cudaStreamNonBlocking));
+    TC_CUDA_TRY(cudaEventCreateWithFlags(&h.ev_tree, cudaEventDisableTiming));
+    TC_CUDA_TRY(cudaEventCreateWithFlags(&h.ev_grad, cudaEventDisableTiming));
+    return TC_OK;
+}
+
+// after_tree (may be null) is called once the sorted records are enqueued, before the interaction lists
+// are built (the list build waits on the host for the list sizes)
+static int update_common(Handle& h, const double* d_pos, int64_t n, const double* mn, const double* mx,
+                         const std::function<int()>& after_tree)
 {
     if (n <= 0 || n > (int64_t)0x7FFFFFFF) {
         tc_set_error("n must be in [1, 2^31)");
@@ -351,6 +370,7 @@ static int update_common(Handle& h, const double* d_pos, int64_t n, const double
     }
     int rc = build_tree(h, d_pos, n, mn[0], mn[1], mx[0], mx[1]);
     if (rc) return rc;
+    if ((rc = after_tree())) return rc;
     rc = build_lists(h);  // synchronises the stream (list sizes), except in no-sync mode
     if (rc) return rc;
     TC_CUDA_TRY(cudaMemcpyAsync(h.h_words + 8, h.err.p, 4, cudaMemcpyDeviceToHost, h.stream));
@@ -375,21 +395,33 @@ int tc_update_tree(tc_handle* t, double* pos_xy, int32_t* ids, int64_t n, const 
     TC_CUDA_TRY(cudaSetDevice(h.cfg.device));
     h.launches = 0;
     int rc;
-    if ((rc = ensure(h.pos_in, (size_t)n * 16))) return rc;
+    if ((rc = ensure(h.pos_in, (size_t)n * 16)) || (rc = ensure_copy_stream(h))) return rc;
+    if (ids && (rc = ensure(h.ids_dev, (size_t)n * 8))) return rc;
+    cudaStream_t c = h.copy_stream;
+    int32_t* ids_in = ids ? P<int32_t>(h.ids_dev) : nullptr;
     TC_CUDA_TRY(cudaMemcpyAsync(h.pos_in.p, pos_xy, (size_t)n * 16, cudaMemcpyHostToDevice, h.stream));
-    if ((rc = update_common(h, P<double>(h.pos_in), n, min_xy, max_xy))) return rc;
-    TC_CUDA_TRY(cudaMemcpyAsync(pos_xy, h.pos64.p, (size_t)n * 16, cudaMemcpyDeviceToHost, h.stream));
-    if (ids) {
-        // the records' IDs move with them on the device: no host gather
-        if ((rc = ensure(h.ids_dev, (size_t)n * 8))) return rc;
-        int32_t* ids_in = P<int32_t>(h.ids_dev);
-        int32_t* ids_out = ids_in + n;
-        TC_CUDA_TRY(cudaMemcpyAsync(ids_in, ids, (size_t)n * 4, cudaMemcpyHostToDevice, h.stream));
-        k_gather_ids<<<grid_for(n, 256), 256, 0, h.stream>>>(ids_in, P<uint32_t>(h.perm), n, ids_out);
-        TC_CUDA_TRY(cudaGetLastError());
-        h.launches++;
-        TC_CUDA_TRY(cudaMemcpyAsync(ids, ids_out, (size_t)n * 4, cudaMemcpyDeviceToHost, h.stream));
-    }
+    if (ids) TC_CUDA_TRY(cudaMemcpyAsync(ids_in, ids, (size_t)n * 4, cudaMemcpyHostToDevice, c));
+    // the sorted positions and IDs travel back to the caller on the copy stream while the interaction
+    // lists are built: the reference's updateTree returns its points reordered
+    auto back = [&]() -> int {
+        TC_CUDA_TRY(cudaEventRecord(h.ev_tree, h.stream));
+        TC_CUDA_TRY(cudaStreamWaitEvent(c, h.ev_tree, 0));
+        TC_CUDA_TRY(cudaMemcpyAsync(pos_xy, h.pos64.p, (size_t)n * 16, cudaMemcpyDeviceToHost, c));
+        if (ids) {
+            // the records' IDs move with them on the device: no host gather
+            int32_t* ids_out = ids_in + n;
+            k_gather_ids<<<grid_for(n, 256), 256, 0, c>>>(ids_in, P<uint32_t>(h.perm), n, ids_out);
+            TC_CUDA_TRY(cudaGetLastError());
+            h.launches++;
+            TC_CUDA_TRY(cudaMemcpyAsync(ids, ids_out, (size_t)n * 4, cudaMemcpyDeviceToHost, c));
+        }
+        return TC_OK;
+    };
+    rc = update_common(h, P<double>(h.pos_in), n, min_xy, max_xy, back);
+    // the copy stream's work is finished before returning, on every path
+    const cudaError_t ec = cudaStreamSynchronize(c);
+    if (rc) return rc;
+    if (ec != cudaSuccess) return tc_cuda_fail(ec, "tc_update_tree");
     TC_CUDA_TRY(cudaStreamSynchronize(h.stream));
     return TC_OK;
 }
@@ -414,7 +446,7 @@ int tc_update_tree_device(tc_handle* t, const double* d_pos_xy, int64_t n, const
         int rc = device_bbox(h, d_pos_xy, n, mn, mx);
         if (rc) return rc;
     }
-    return update_common(h, d_pos_xy, n, mn, mx);
+    return update_common(h, d_pos_xy, n, mn, mx, []() { return TC_OK; });
 }
 
 int tc_solve_device(tc_handle* t, double* d_grad_xy, double* d_total, int accumulate, int scatter)
@@ -449,18 +481,34 @@ int tc_solve(tc_handle* t, double* total, const double* pos_xy, double* grad_xy,
     TC_CUDA_TRY(cudaSetDevice(h.cfg.device));
     h.launches = 0;
     int rc;
-    if ((rc = ensure(h.grad_acc, (size_t)n * 16)) || (rc = ensure(h.dtotal, 64))) return rc;
+    if ((rc = ensure(h.grad_acc, (size_t)n * 16)) || (rc = ensure(h.dtotal, 64)) || (rc = ensure_copy_stream(h)))
+        return rc;
+    // the forces add to the caller's (applyForces accumulates into derivative): the sum is taken on the
+    // device, result + grad_xy[i] in one FP64 add per component, and copied straight back.  The caller's
+    // gradient comes in on the copy stream; the order-p solve waits for it only before its near-field
+    // kernel (the first to touch it), so the copy overlaps the far field
+    TC_CUDA_TRY(cudaMemcpyAsync(h.grad_acc.p, grad_xy, (size_t)n * 16, cudaMemcpyHostToDevice, h.copy_stream));
+    TC_CUDA_TRY(cudaEventRecord(h.ev_grad, h.copy_stream));
     if (pos_xy) {
         TC_CUDA_TRY(cudaMemcpyAsync(h.pos64.p, pos_xy, (size_t)n * 16, cudaMemcpyHostToDevice, h.stream));
         if ((rc = refresh_positions(h))) return rc;
     }
-    // the forces add to the caller's (applyForces accumulates into derivative): the sum is taken on the
-    // device, result + grad_xy[i] in one FP64 add per component, and copied straight back
-    TC_CUDA_TRY(cudaMemcpyAsync(h.grad_acc.p, grad_xy, (size_t)n * 16, cudaMemcpyHostToDevice, h.stream));
     TC_CUDA_TRY(cudaMemsetAsync(h.dtotal.p, 0, 8, h.stream));
-    rc = h.cfg.order ? solve_fmm_order(h, P<double>(h.grad_acc), P<double>(h.dtotal), 1, 0)
-                     : solve_fmm(h, P<double>(h.grad_acc), P<double>(h.dtotal), 1, 0);
-    if (rc) return rc;
+    if (h.cfg.order) {
+        h.wait_grad = true;
+        rc = solve_fmm_order(h, P<double>(h.grad_acc), P<double>(h.dtotal), 1, 0);
+        if (h.wait_grad) {  // a path that never reached the near field still orders the copy before returning
+            h.wait_grad = false;
+            if (!rc) TC_CUDA_TRY(cudaStreamWaitEvent(h.stream, h.ev_grad, 0));
+        }
+    } else {
+        TC_CUDA_TRY(cudaStreamWaitEvent(h.stream, h.ev_grad, 0));
+        rc = solve_fmm(h, P<double>(h.grad_acc), P<double>(h.dtotal), 1, 0);
+    }
+    if (rc) {
+        cudaStreamSynchronize(h.copy_stream);
+        return rc;
+    }
     TC_CUDA_TRY(cudaMemcpyAsync(grad_xy, h.grad_acc.p, (size_t)n * 16, cudaMemcpyDeviceToHost, h.stream));
     TC_CUDA_TRY(cudaMemcpyAsync(h.h_total, h.dtotal.p, 8, cudaMemcpyDeviceToHost, h.stream));
     TC_CUDA_TRY(cudaStreamSynchronize(h.stream));

@@ -814,7 +814,10 @@ __device__ __forceinline__ void p2p_staged(const KN& ker, const float4* __restri
 // * A chunk of m sinks gives each sink g = 2^floor(log2(32/m)) lanes that
 //   split its sources; their partial forces are summed by shuffles.
 template <int P, typename KN>
-__global__ void __launch_bounds__(32 * kNearWarps, 9)
+#ifndef TC_NEAR_MIN_BLOCKS
+#define TC_NEAR_MIN_BLOCKS 10  // resident blocks per SM the near field's registers are held to (measured: 9 and 12 slower)
+#endif
+__global__ void __launch_bounds__(32 * kNearWarps, TC_NEAR_MIN_BLOCKS)
     k_near_p(KN ker, int dep, float h, const uint32_t* __restrict__ count, const uint32_t* __restrict__ first,
              const float* __restrict__ comrel, const float* __restrict__ loc, const uint32_t* __restrict__ near_ptr,
              const uint32_t* __restrict__ near_idx, const uint32_t* __restrict__ chunk_ptr,
@@ -1169,6 +1172,11 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
     }
     uint32_t* nchunk = P<uint32_t>(h.cnt_tmp);
     uint32_t* chunk_ptr = P<uint32_t>(h.chunk);
+    if (h.wait_grad) {
+        // the caller's gradient, copied in on the copy stream behind the far field, is added to from here on
+        TC_CUDA_TRY(cudaStreamWaitEvent(s, h.ev_grad, 0));
+        h.wait_grad = false;
+    }
     k_chunks<<<grid_for(nleaf, 256), 256, 0, s>>>(dep, count, nchunk);
     if ((rc = exclusive_scan_u32(nchunk, chunk_ptr, nleaf, P<uint32_t>(h.tmp), s))) return rc;
     k_chunk_leaf<<<grid_for(nleaf, 256), 256, 0, s>>>(dep, chunk_ptr, P<uint32_t>(h.chunk_leaf), (uint32_t)wmax);

@@ -41,6 +41,12 @@ struct Handle {
     tc_config cfg;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    // host-buffer entry points: copies that overlap the kernels run on copy_stream (created on first use);
+    // ev_tree marks the sorted records, ev_grad the caller's gradient on the device, which the order-p solve
+    // waits for before its near-field kernel adds to it (wait_grad)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_tree = nullptr, ev_grad = nullptr;
+    bool wait_grad = false;
     int depth = -1;
     int64_t n = 0;
     int64_t nnodes = 0;
