@@ -132,6 +132,13 @@ int tc_set_expansion_centre(tc_handle* h, int centre);
 #define TC_M2L_TENSOR_ALL 2
 int tc_set_m2l_engine(tc_handle* h, int engine);
 
+/* Order-p solves run their near field (P2P) on a second, internal stream
+ * beside the far field (M2L, L2L): it reads only the tree and its lists.  The
+ * L2P, which adds the final local expansions to the near-field forces, waits
+ * for both.  on = 0 runs the two in sequence on the handle's stream (the
+ * results are identical either way).  Default on.                          */
+int tc_set_near_overlap(tc_handle* h, int on);
+
 /* Per-pair expansion order on a TC_MAC_BMAX handle of order p in {6, 8, 10,
  * 12} (no counterpart in the reference): an accepted pair with ratio
  * r = (b_A + b_B)/|com_A - com_B| < theta is evaluated at the lowest order
@@ -199,10 +206,12 @@ int tc_get_node_boxes(tc_handle* h, int level, double* boxes, int64_t cap, int64
 int tc_last_launch_count(tc_handle* h);
 
 /* Device time of the stages of the last update + solve, in milliseconds,
- * from CUDA events on the handle's stream: [0] Morton codes + radix sort,
- * [1] leaf build + upward pass, [2] interaction lists, [3] M2L,
- * [4] near field (P2P, M2P, P2L, L2P), [5] Z reduction.  Synchronises.   */
-#define TC_NSTAGES 6
+ * from CUDA events: [0] Morton codes + radix sort, [1] leaf build + upward
+ * pass, [2] interaction lists, [3] far field (M2L, L2L), [4] near field (P2P,
+ * M2P, P2L; of an order-p solve, on its own stream and overlapping [3] unless
+ * tc_set_near_overlap(h, 0)), [5] L2P of an order-p solve (0 otherwise: the
+ * reference-order near field includes it), [6] Z reduction.  Synchronises. */
+#define TC_NSTAGES 7
 int tc_get_stage_times(tc_handle* h, double* ms);
 /* Interaction counts of the last solve: [0] P2P pair evaluations, [1] M2P,
  * [2] P2L, [3] M2L (directed; each unordered reference pair counts twice). */

@@ -65,6 +65,7 @@ SIGNATURES = {
     "tc_perplexity_device": (_I, [_P, _I64, _I, ctypes.c_double, _I, ctypes.c_double, _P, _P]),
     "tc_symmetrize_device": (_I, [_P, _P, _I64, _I, _P, _P, _P, _P, _P]),
     "tc_set_m2l_engine": (_I, [_P, _I]),
+    "tc_set_near_overlap": (_I, [_P, _I]),
     "tc_set_adaptive_order": (_I, [_P, _D]),
     "tc_set_leaf_p2p": (_I, [_P, _I]),
     "tc_pm_solve": (_I, [_I, _D, _I, _P, _I64, _P, _P]),

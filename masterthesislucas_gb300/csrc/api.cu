@@ -65,14 +65,26 @@ void release(Buf& b)
     b.bytes = 0;
 }
 
-int record(Handle& h, int i)
+int record_on(Handle& h, int i, cudaStream_t s)
 {
     if (h.nosync) return TC_OK;  // stage timing events stay out of captured graphs
     if (!h.ev_ready) {
         for (auto& e : h.ev) TC_CUDA_TRY(cudaEventCreate(&e));
         h.ev_ready = true;
     }
-    TC_CUDA_TRY(cudaEventRecord(h.ev[i], h.stream));
+    if (i == 4) h.stage_split = false;
+    TC_CUDA_TRY(cudaEventRecord(h.ev[i], s));
+    return TC_OK;
+}
+
+int record(Handle& h, int i) { return record_on(h, i, h.stream); }
+
+int ensure_near_stream(Handle& h)
+{
+    if (h.near_stream) return TC_OK;
+    TC_CUDA_TRY(cudaStreamCreateWithFlags(&h.near_stream, cudaStreamNonBlocking));
+    TC_CUDA_TRY(cudaEventCreateWithFlags(&h.ev_fork, cudaEventDisableTiming));
+    TC_CUDA_TRY(cudaEventCreateWithFlags(&h.ev_join, cudaEventDisableTiming));
     return TC_OK;
 }
 
@@ -318,9 +330,11 @@ int tc_destroy(tc_handle* t)
     Handle& h = t->h;
     cudaSetDevice(h.cfg.device);
     if (h.stream) cudaStreamSynchronize(h.stream);
+    if (h.near_stream) cudaStreamSynchronize(h.near_stream);
+    if (h.copy_stream) cudaStreamSynchronize(h.copy_stream);
     Buf* bufs[] = {&h.codes, &h.perm, &h.alt_keys, &h.alt_vals, &h.pos_in, &h.pos64, &h.prel, &h.grad_acc,
                    &h.count, &h.first, &h.com64, &h.m0, &h.m2, &h.bbc, &h.bblen, &h.comrel, &h.m0r, &h.m2t,
-                   &h.loc, &h.locfin, &h.mu, &h.chunk, &h.zwork, &h.zloc, &h.counters, &h.ptr_pool, &h.idx_pool, &h.cnt_tmp, &h.lstat, &h.ord_pool, &h.nfeat, &h.dec, &h.bigleaf, &h.chunk_leaf, &h.act, &h.act_pos, &h.bmax, &h.celloff, &h.mqueue, &h.tc_ops, &h.tc_mubf, &h.diagpart, &h.ctrl_w, &h.tmp, &h.err, &h.zpart, &h.dtotal, &h.sumtmp,
+                   &h.loc, &h.locfin, &h.mu, &h.chunk, &h.zwork, &h.zloc, &h.counters, &h.ptr_pool, &h.idx_pool, &h.cnt_tmp, &h.lstat, &h.ord_pool, &h.nfeat, &h.dec, &h.bigleaf, &h.chunk_leaf, &h.act, &h.act_pos, &h.bmax, &h.celloff, &h.mqueue, &h.nearf, &h.tc_ops, &h.tc_mubf, &h.diagpart, &h.ctrl_w, &h.tmp, &h.err, &h.zpart, &h.dtotal, &h.sumtmp,
                    &h.host_stage, &h.ids_dev};
     for (Buf* b : bufs) release(*b);
     if (h.step_graph) cudaGraphExecDestroy(h.step_graph);
@@ -330,6 +344,11 @@ int tc_destroy(tc_handle* t)
         cudaStreamSynchronize(h.copy_stream);
         cudaStreamDestroy(h.copy_stream);
     }
+    if (h.near_stream) cudaStreamDestroy(h.near_stream);
+    if (h.ev_ready)
+        for (auto& e : h.ev) cudaEventDestroy(e);
+    if (h.ev_fork) cudaEventDestroy(h.ev_fork);
+    if (h.ev_join) cudaEventDestroy(h.ev_join);
     if (h.ev_tree) cudaEventDestroy(h.ev_tree);
     if (h.ev_grad) cudaEventDestroy(h.ev_grad);
     if (h.own_stream && h.stream) cudaStreamDestroy(h.stream);
@@ -640,12 +659,15 @@ int tc_get_stage_times(tc_handle* t, double* ms)
     if (!h.ev_ready) return TC_ERR_STATE;
     TC_CUDA_TRY(cudaSetDevice(h.cfg.device));
     TC_CUDA_TRY(cudaStreamSynchronize(h.stream));
-    // stage k spans events (a, b)
-    const int a[TC_NSTAGES] = {0, 1, 2, 4, 5, 6};
-    const int b[TC_NSTAGES] = {1, 2, 3, 5, 6, 7};
+    if (h.near_stream) TC_CUDA_TRY(cudaStreamSynchronize(h.near_stream));
+    // stage k spans events (a, b); a < 0: the stage does not exist on this path
+    const int split_a[TC_NSTAGES] = {0, 1, 2, 11, 8, 10, 6}, split_b[TC_NSTAGES] = {1, 2, 3, 5, 9, 6, 7};
+    const int plain_a[TC_NSTAGES] = {0, 1, 2, 4, 5, -1, 6}, plain_b[TC_NSTAGES] = {1, 2, 3, 5, 6, -1, 7};
+    const int* a = h.stage_split ? split_a : plain_a;
+    const int* b = h.stage_split ? split_b : plain_b;
     for (int k = 0; k < TC_NSTAGES; k++) {
         float f = 0.f;
-        cudaError_t e = cudaEventElapsedTime(&f, h.ev[a[k]], h.ev[b[k]]);
+        cudaError_t e = a[k] < 0 ? cudaSuccess : cudaEventElapsedTime(&f, h.ev[a[k]], h.ev[b[k]]);
         ms[k] = e == cudaSuccess ? (double)f : -1.0;
     }
     cudaGetLastError();
@@ -745,6 +767,13 @@ extern "C" int tc_set_m2l_engine(tc_handle* t, int engine)
     }
     t->h.m2l_tc = engine != TC_M2L_SIMT;
     t->h.m2l_tc_all = engine == TC_M2L_TENSOR_ALL;
+    return TC_OK;
+}
+
+extern "C" int tc_set_near_overlap(tc_handle* t, int on)
+{
+    if (!t) return TC_ERR_INVALID;
+    t->h.near_overlap = on != 0;
     return TC_OK;
 }
 

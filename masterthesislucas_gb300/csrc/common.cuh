@@ -45,6 +45,28 @@ __host__ __device__ inline uint32_t compact16(uint32_t x)
 // first node of level l in the level-dense layout: (4^l - 1) / 3
 __host__ __device__ inline uint32_t level_index(int l) { return (uint32_t)((((uint64_t)1 << (2 * l)) - 1) / 3); }
 
+// x widened to a double with integer operations (exact, as the IEEE formats
+// relate): the FP32 -> FP64 conversion instruction shares GB300's narrow FP64
+// pipe.  Normal numbers rebias the exponent (+896) and move the fraction up 29
+// bits; subnormals are normalised; zeros, infinities and NaNs keep their form.
+__device__ __forceinline__ double f64_of_f32(float x)
+{
+    const uint32_t b = __float_as_uint(x);
+    const uint32_t sign = b & 0x80000000u, e = (b >> 23) & 0xFFu, m = b & 0x7FFFFFu;
+    unsigned long long r;
+    if (e == 0u) {
+        if (m == 0u) {
+            r = 0ull;
+        } else {
+            const uint32_t t = 31u - (uint32_t)__clz(m);  // value m * 2^-149 = 2^(t - 149) * (m / 2^t)
+            r = ((unsigned long long)(t + 874u) << 52) | ((unsigned long long)(m ^ (1u << t)) << (52u - t));
+        }
+    } else {
+        r = ((unsigned long long)(e == 0xFFu ? 0x7FFu : e + 896u) << 52) | ((unsigned long long)m << 29);
+    }
+    return __longlong_as_double((long long)(r | ((unsigned long long)sign << 32)));
+}
+
 template <typename T>
 __device__ inline T warp_sum(T v)
 {

@@ -804,8 +804,10 @@ __device__ __forceinline__ void p2p_staged(const KN& ker, const float4* __restri
     zs += KN::kSign * (a0 + a1);
 }
 
-// One warp per work item (leaf S, chunk of m <= 32 sinks): L2P of the final
-// local expansion of S plus direct P2P with every particle of near(S).
+// One warp per work item (leaf S, chunk of m <= 32 sinks): direct P2P with
+// every particle of near(S); the sink's FP32 force goes to nearf (sorted
+// order) for the L2P kernel, the pair sum to zwork.  It reads nothing the far
+// field writes, so it runs on a stream of its own beside the far field.
 // * The near list is read 32 entries at a time, one per lane (index, first
 //   particle, count, frame offset), and broadcast by shuffles.
 // * Its particles are staged into shared memory shifted into S's
@@ -813,19 +815,17 @@ __device__ __forceinline__ void p2p_staged(const KN& ker, const float4* __restri
 //   unrolled pass over a flat array, padded with far-away sources.
 // * A chunk of m sinks gives each sink g = 2^floor(log2(32/m)) lanes that
 //   split its sources; their partial forces are summed by shuffles.
-template <int P, typename KN>
+template <typename KN>
 #ifndef TC_NEAR_MIN_BLOCKS
-#define TC_NEAR_MIN_BLOCKS 10  // resident blocks per SM the near field's registers are held to (measured: 9 and 12 slower)
+#define TC_NEAR_MIN_BLOCKS 10  // resident blocks per SM the near field's registers are held to (48: no spills)
 #endif
 __global__ void __launch_bounds__(32 * kNearWarps, TC_NEAR_MIN_BLOCKS)
     k_near_p(KN ker, int dep, float h, const uint32_t* __restrict__ count, const uint32_t* __restrict__ first,
-             const float* __restrict__ comrel, const float* __restrict__ loc, const uint32_t* __restrict__ near_ptr,
-             const uint32_t* __restrict__ near_idx, const uint32_t* __restrict__ chunk_ptr,
-             const uint32_t* __restrict__ item_leaf, uint32_t cap, const float* __restrict__ prel,
-             const uint32_t* __restrict__ perm, double* __restrict__ grad, int accumulate, int scatter,
-             double* __restrict__ zwork, unsigned long long* __restrict__ counters)
+             const uint32_t* __restrict__ near_ptr, const uint32_t* __restrict__ near_idx,
+             const uint32_t* __restrict__ chunk_ptr, const uint32_t* __restrict__ item_leaf, uint32_t cap,
+             const float* __restrict__ prel, uint32_t n, float2* __restrict__ nearf, double* __restrict__ zwork,
+             unsigned long long* __restrict__ counters)
 {
-    constexpr int KW = ncoef(P - 1);
     // staged sources, two per 16-byte slot as (x0, x1, y0, y1)
     __shared__ __align__(16) float s_src[kNearWarps][2 * kNearBuf];
     uint32_t n_pp = 0;
@@ -839,7 +839,6 @@ __global__ void __launch_bounds__(32 * kNearWarps, TC_NEAR_MIN_BLOCKS)
     const float2* prel2 = reinterpret_cast<const float2*>(prel);
     const uint32_t li = level_index(dep);
     const int64_t nl = (int64_t)1 << (2 * dep);
-    const float ih = 1.0f / h;
     const uint32_t nwork = min(chunk_ptr[nl], cap);
     const int64_t wstride = (int64_t)gridDim.x * kNearWarps;
     for (int64_t wi = blockIdx.x * (int64_t)kNearWarps + w; wi < nwork; wi += wstride) {
@@ -874,7 +873,9 @@ __global__ void __launch_bounds__(32 * kNearWarps, TC_NEAR_MIN_BLOCKS)
             }
             // the batch's particles as one flat range [0, tot): position q
             // belongs to entry t with ex_t <= q < ex_t + c_t (exclusive
-            // prefix ex over the lanes), found by a binary search over lanes
+            // prefix ex over the lanes).  Every entry is a non-empty leaf, so
+            // the entries' first positions are distinct and t is the number
+            // of entries starting at or before q, minus one
             uint32_t inc = mc;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -893,17 +894,19 @@ __global__ void __launch_bounds__(32 * kNearWarps, TC_NEAR_MIN_BLOCKS)
                 }
                 const uint32_t take = min(tot - q0, (uint32_t)kNearBuf - fill);
                 for (uint32_t b0 = 0; b0 < take; b0 += 32) {
-                    const uint32_t q = q0 + b0 + lane;
-                    uint32_t t = 0;
-#pragma unroll
-                    for (uint32_t step = 16; step > 0; step >>= 1) {
-                        const uint32_t e = __shfl_sync(0xffffffffu, ex, t + step);
-                        if (t + step < nt && e <= q) t += step;
-                    }
+                    const uint32_t base = q0 + b0, q = base + lane;
+                    // entries starting before this run of 32 positions, and a bit per entry starting in it
+                    const uint32_t before = __popc(__ballot_sync(0xffffffffu, lane < nt && ex < base));
+                    const uint32_t d = ex - base;  // < 32 only for an entry starting in the run
+                    const uint32_t bits = __reduce_or_sync(0xffffffffu, (lane < nt && d < 32u) ? 1u << d : 0u);
+                    // in [0, nt): entry 0 starts at position 0
+                    const uint32_t t = before + __popc(bits & (0xffffffffu >> (31u - lane))) - 1u;
                     const uint32_t fT = __shfl_sync(0xffffffffu, mf, t), eT = __shfl_sync(0xffffffffu, ex, t);
                     const float ox = __shfl_sync(0xffffffffu, mox, t), oy = __shfl_sync(0xffffffffu, moy, t);
                     if (b0 + lane < take) {
-                        const float2 t2 = prel2[fT + (q - eT)];
+                        // the particle index stays below n even for a list that broke the non-empty rule
+                        const uint32_t src = fT + (q - eT);
+                        const float2 t2 = src < n ? prel2[src] : make_float2(kFarAway, kFarAway);
                         stage(fill + b0 + lane, t2.x + ox, t2.y + oy);
                     }
                 }
@@ -926,19 +929,6 @@ __global__ void __launch_bounds__(32 * kNearWarps, TC_NEAR_MIN_BLOCKS)
             gy += __shfl_xor_sync(0xffffffffu, gy, o);
         }
         if (act && r == 0) {
-            // L2P: F = (1/h) sum_b L_b d^(b - e) / (b - e)!
-            float wv[KW];
-            monomials<P - 1>((px - comrel[2 * S]) * ih, (py - comrel[2 * S + 1]) * ih, wv);
-            const float* L = loc + S * kstride(P);
-            float lx = 0.f, ly = 0.f;
-#pragma unroll
-            for (int k = 0; k < P; k++)
-#pragma unroll
-                for (int b = 0; b <= k; b++) {
-                    const int a = k - b;
-                    lx += L[cidx(a + 1, b)] * wv[cidx(a, b)];
-                    ly += L[cidx(a, b + 1)] * wv[cidx(a, b)];
-                }
             n_pp += staged;
             if (has_self) {
                 // the staged sources included the sink itself: R = 0 adds no
@@ -948,8 +938,165 @@ __global__ void __launch_bounds__(32 * kNearWarps, TC_NEAR_MIN_BLOCKS)
                 zs -= t0;
                 n_pp--;
             }
-            const int64_t o = scatter ? (int64_t)perm[s] : (int64_t)s;
-            double ox2 = (double)(lx * ih + gx), oy2 = (double)(ly * ih + gy);
+            nearf[s] = make_float2(gx, gy);
+        }
+        // the chunk's pair sum: FP32 over the lanes (each lane's partial is an FP32 sum already), FP64 after
+        const float z = warp_sum(act ? zs : 0.0f);
+        if (lane == 0) zwork[wi] = (double)z;
+    }
+    const unsigned long long a = warp_sum((unsigned long long)n_pp);
+    if (lane == 0 && a) atomicAdd(counters + 0, a);
+}
+
+// L2P of the final local expansion of each particle's leaf plus the particle's
+// near-field force: F = (1/h) sum_b L_b d^(b - e) / (b - e)! + nearf, written
+// (or added) in FP64.  Each thread takes kL2pPer consecutive particles in
+// sorted order (16-byte loads of their codes, positions, near-field forces and
+// permutation entries), a block a tile of 128 * kL2pPer.  A tile's particles lie
+// in a few consecutive leaves (their sorted Morton codes say which): the tile
+// stages those leaves' expansions and centres in shared memory once, with
+// coalesced loads, and every particle reads its leaf's coefficients from there
+// as broadcasts.  A tile of more than kL2pSlots leaves reads the rest from
+// global memory.
+constexpr int kL2pPer = 4;
+constexpr int kL2pTile = 128 * kL2pPer;
+constexpr int kL2pSlots = 64;
+constexpr int kL2pBlocksPerSM = 8;
+
+template <int P>
+__device__ __forceinline__ void l2p_eval(const float* L, float dx, float dy, float& lx, float& ly)
+{
+    constexpr int KW = ncoef(P - 1);
+    float wv[KW];
+    monomials<P - 1>(dx, dy, wv);
+    lx = 0.f;
+    ly = 0.f;
+#pragma unroll
+    for (int kk = 0; kk < P; kk++)
+#pragma unroll
+        for (int b = 0; b <= kk; b++) {
+            const int a = kk - b;
+            lx += L[cidx(a + 1, b)] * wv[cidx(a, b)];
+            ly += L[cidx(a, b + 1)] * wv[cidx(a, b)];
+        }
+}
+
+template <int P>
+__global__ void __launch_bounds__(128, kL2pBlocksPerSM)
+    k_l2p_p(int dep, float h, int64_t n, const uint32_t* __restrict__ codes, const float* __restrict__ comrel,
+            const float* __restrict__ loc, const float* __restrict__ prel, const float2* __restrict__ nearf,
+            const uint32_t* __restrict__ perm, double* __restrict__ grad, int accumulate, int scatter)
+{
+    constexpr int K = ncoef(P);
+    constexpr int KR = K | 1;  // odd row stride: neighbouring slots' rows start in different banks
+    __shared__ float sL[kL2pSlots][KR];
+    __shared__ float sC[kL2pSlots][2];
+    __shared__ uint32_t sNode[kL2pSlots];
+    __shared__ uint32_t wlead[4];
+    const uint32_t li = level_index(dep);
+    const int shift = 32 - 2 * dep;
+    const float ih = 1.0f / h;
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const float2* prel2 = reinterpret_cast<const float2*>(prel);
+    auto leaf_of = [&](uint32_t c) { return dep ? c >> shift : 0u; };
+    const int64_t ntile = (n + kL2pTile - 1) / kL2pTile;
+    for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+        const int64_t k0 = tile * kL2pTile + (int64_t)threadIdx.x * kL2pPer;
+        uint32_t leaf[kL2pPer], pm[kL2pPer];
+        float2 p2[kL2pPer], f2[kL2pPer];
+        if (k0 + kL2pPer <= n) {
+            // k0 is a multiple of 4: 16-byte aligned in every array
+            const uint4 c4 = *reinterpret_cast<const uint4*>(codes + k0);
+            const float4 pa = *reinterpret_cast<const float4*>(prel2 + k0);
+            const float4 pb = *reinterpret_cast<const float4*>(prel2 + k0 + 2);
+            const float4 fa = *reinterpret_cast<const float4*>(nearf + k0);
+            const float4 fb = *reinterpret_cast<const float4*>(nearf + k0 + 2);
+            const uint4 m4 = scatter ? *reinterpret_cast<const uint4*>(perm + k0) : make_uint4(0, 0, 0, 0);
+            leaf[0] = leaf_of(c4.x), leaf[1] = leaf_of(c4.y), leaf[2] = leaf_of(c4.z), leaf[3] = leaf_of(c4.w);
+            p2[0] = make_float2(pa.x, pa.y), p2[1] = make_float2(pa.z, pa.w);
+            p2[2] = make_float2(pb.x, pb.y), p2[3] = make_float2(pb.z, pb.w);
+            f2[0] = make_float2(fa.x, fa.y), f2[1] = make_float2(fa.z, fa.w);
+            f2[2] = make_float2(fb.x, fb.y), f2[3] = make_float2(fb.z, fb.w);
+            pm[0] = m4.x, pm[1] = m4.y, pm[2] = m4.z, pm[3] = m4.w;
+        } else {
+#pragma unroll
+            for (int u = 0; u < kL2pPer; u++) {
+                const int64_t k = k0 + u;
+                const bool v = k < n;
+                leaf[u] = v ? leaf_of(codes[k]) : 0u;
+                p2[u] = v ? prel2[k] : make_float2(0.f, 0.f);
+                f2[u] = v ? nearf[k] : make_float2(0.f, 0.f);
+                pm[u] = v && scatter ? perm[k] : 0u;
+            }
+        }
+        // the first particle of each leaf in the tile leads it; the leaf's slot is the number of leaders up
+        // to and including its own, minus one
+        uint32_t prev = __shfl_up_sync(0xffffffffu, leaf[kL2pPer - 1], 1);
+        if (lane == 0 && threadIdx.x > 0 && k0 - 1 < n) prev = leaf_of(codes[k0 - 1]);
+        uint32_t cum[kL2pPer], nlead = 0;
+#pragma unroll
+        for (int u = 0; u < kL2pPer; u++) {
+            const bool lead = k0 + u < n && ((threadIdx.x == 0 && u == 0) || leaf[u] != (u ? leaf[u - 1] : prev));
+            nlead += lead ? 1u : 0u;
+            cum[u] = nlead;
+        }
+        uint32_t incl = nlead;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += v;
+        }
+        if (lane == 31) wlead[w] = incl;
+        __syncthreads();
+        uint32_t before = 0, total = 0;
+#pragma unroll
+        for (uint32_t i = 0; i < 4; i++) {
+            const uint32_t c = wlead[i];
+            before += i < w ? c : 0u;
+            total += c;
+        }
+        const uint32_t excl = before + incl - nlead;
+        int slot[kL2pPer];
+#pragma unroll
+        for (int u = 0; u < kL2pPer; u++) {
+            slot[u] = (int)(excl + cum[u]) - 1;
+            const bool lead = cum[u] != (u ? cum[u - 1] : 0u);
+            if (lead && slot[u] < kL2pSlots) sNode[slot[u]] = li + leaf[u];
+        }
+        __syncthreads();
+        const int ns = min((int)total, kL2pSlots);
+        // the slots' coefficients, eight loads per thread in flight before their stores
+        for (int i0 = 0; i0 < ns * K; i0 += 8 * 128) {
+            float v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int i = i0 + u * 128 + (int)threadIdx.x, sl = i / K;
+                v[u] = i < ns * K ? loc[(int64_t)sNode[sl] * kstride(P) + (i - sl * K)] : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int i = i0 + u * 128 + (int)threadIdx.x, sl = i / K;
+                if (i < ns * K) sL[sl][i - sl * K] = v[u];
+            }
+        }
+        if ((int)threadIdx.x < 2 * ns)
+            sC[threadIdx.x >> 1][threadIdx.x & 1] = comrel[2 * (int64_t)sNode[threadIdx.x >> 1] + (threadIdx.x & 1)];
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < kL2pPer; u++) {
+            const int64_t k = k0 + u;
+            if (k >= n) continue;
+            float lx, ly;
+            const int sl = slot[u];
+            if (sl < kL2pSlots) {
+                l2p_eval<P>(sL[sl], (p2[u].x - sC[sl][0]) * ih, (p2[u].y - sC[sl][1]) * ih, lx, ly);
+            } else {
+                const int64_t S = li + leaf[u];
+                l2p_eval<P>(loc + S * kstride(P), (p2[u].x - comrel[2 * S]) * ih, (p2[u].y - comrel[2 * S + 1]) * ih,
+                            lx, ly);
+            }
+            const int64_t o = scatter ? (int64_t)pm[u] : k;
+            double ox2 = f64_of_f32(lx * ih + f2[u].x), oy2 = f64_of_f32(ly * ih + f2[u].y);
             if (accumulate) {
                 ox2 += grad[2 * o];
                 oy2 += grad[2 * o + 1];
@@ -957,11 +1104,8 @@ __global__ void __launch_bounds__(32 * kNearWarps, TC_NEAR_MIN_BLOCKS)
             grad[2 * o] = ox2;
             grad[2 * o + 1] = oy2;
         }
-        const double z = warp_sum(act ? (double)zs : 0.0);
-        if (lane == 0) zwork[wi] = z;
+        __syncthreads();  // the next tile restages the slots
     }
-    const unsigned long long a = warp_sum((unsigned long long)n_pp);
-    if (lane == 0 && a) atomicAdd(counters + 0, a);
 }
 
 __global__ void k_sum_z2(const double* __restrict__ a, int64_t na, const double* __restrict__ c,
@@ -1079,9 +1223,40 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
         (rc = ensure(h.counters, 64)) || (rc = ensure(h.chunk, (nleaf + 1) * 4)) ||
         (rc = ensure(h.zwork, wmax * 8)) || (rc = ensure(h.chunk_leaf, wmax * 4)) ||
         (rc = ensure(h.cnt_tmp, nleaf * 4 + 64)) ||
-        (rc = ensure(h.tmp, scan_tmp_words(nleaf) * 4)) || (rc = record(h, 4)))
+        (rc = ensure(h.tmp, scan_tmp_words(nleaf) * 4)) || (rc = ensure(h.nearf, h.n * 8)) ||
+        (rc = ensure_near_stream(h)) || (rc = record(h, 4)))
         return rc;
     TC_CUDA_TRY(cudaMemsetAsync(h.counters.p, 0, 64, s));
+    h.stage_split = true;
+    // the near field (P2P) reads only the tree and its lists: it runs on a second stream from here, beside
+    // the far field, and the L2P after both joins the two
+    cudaStream_t sn = s;
+    if (h.near_overlap) {
+        sn = h.near_stream;
+        TC_CUDA_TRY(cudaEventRecord(h.ev_fork, s));
+        TC_CUDA_TRY(cudaStreamWaitEvent(sn, h.ev_fork, 0));
+    }
+    const uint32_t* count_n = P<uint32_t>(h.count);
+    uint32_t* nchunk = P<uint32_t>(h.cnt_tmp);
+    uint32_t* chunk_ptr = P<uint32_t>(h.chunk);
+    if ((rc = record_on(h, 8, sn))) return rc;
+    k_chunks<<<grid_for(nleaf, 256), 256, 0, sn>>>(dep, count_n, nchunk);
+    if ((rc = exclusive_scan_u32(nchunk, chunk_ptr, nleaf, P<uint32_t>(h.tmp), sn))) return rc;
+    k_chunk_leaf<<<grid_for(nleaf, 256), 256, 0, sn>>>(dep, chunk_ptr, P<uint32_t>(h.chunk_leaf), (uint32_t)wmax);
+    {
+        const int64_t wblk = (wmax + kNearWarps - 1) / kNearWarps;
+        const uint32_t* ptr_n = P<uint32_t>(h.ptr_pool);
+        const uint32_t* idx_n = P<uint32_t>(h.idx_pool);
+        k_near_p<KN><<<(unsigned)(wblk < sm_count() * 256 ? wblk : sm_count() * 256), 32 * kNearWarps, 0, sn>>>(
+            ker, dep, (float)(h.L / (double)(1u << dep)), count_n, P<uint32_t>(h.first),
+            ptr_n + h.lists.near_ptr_off[dep], idx_n + h.lists.near_idx_off[dep], chunk_ptr,
+            P<uint32_t>(h.chunk_leaf), (uint32_t)wmax, P<float>(h.prel), (uint32_t)h.n, P<float2>(h.nearf),
+            P<double>(h.zwork),
+            P<unsigned long long>(h.counters));
+    }
+    if ((rc = record_on(h, 9, sn))) return rc;
+    if (h.near_overlap) TC_CUDA_TRY(cudaEventRecord(h.ev_join, sn));
+    if ((rc = record(h, 11))) return rc;  // the far field starts
     float* mu = P<float>(h.mu);
     float* loc = P<float>(h.loc);
     double* zp = P<double>(h.zpart);
@@ -1170,27 +1345,23 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
         else
             k_l2l<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, loc, P<uint32_t>(h.act), P<uint32_t>(h.act_pos));
     }
-    uint32_t* nchunk = P<uint32_t>(h.cnt_tmp);
-    uint32_t* chunk_ptr = P<uint32_t>(h.chunk);
+    if ((rc = record(h, 5))) return rc;
+    if (h.near_overlap) TC_CUDA_TRY(cudaStreamWaitEvent(s, h.ev_join, 0));
     if (h.wait_grad) {
-        // the caller's gradient, copied in on the copy stream behind the far field, is added to from here on
+        // the caller's gradient, copied in on the copy stream behind the far and near fields, is added to
+        // from here on
         TC_CUDA_TRY(cudaStreamWaitEvent(s, h.ev_grad, 0));
         h.wait_grad = false;
     }
-    k_chunks<<<grid_for(nleaf, 256), 256, 0, s>>>(dep, count, nchunk);
-    if ((rc = exclusive_scan_u32(nchunk, chunk_ptr, nleaf, P<uint32_t>(h.tmp), s))) return rc;
-    k_chunk_leaf<<<grid_for(nleaf, 256), 256, 0, s>>>(dep, chunk_ptr, P<uint32_t>(h.chunk_leaf), (uint32_t)wmax);
-    if ((rc = record(h, 5))) return rc;
-    const int64_t wblk = (wmax + kNearWarps - 1) / kNearWarps;
-    k_near_p<ORD, KN><<<(unsigned)(wblk < sm_count() * 256 ? wblk : sm_count() * 256), 32 * kNearWarps, 0, s>>>(
-        ker, dep, hl(dep), count, P<uint32_t>(h.first), comrel, loc, ptr + h.lists.near_ptr_off[dep],
-        idx + h.lists.near_idx_off[dep], chunk_ptr, P<uint32_t>(h.chunk_leaf), (uint32_t)wmax, P<float>(h.prel),
-        P<uint32_t>(h.perm), d_grad, accumulate, scatter, P<double>(h.zwork), P<unsigned long long>(h.counters));
+    if ((rc = record(h, 10))) return rc;
+    k_l2p_p<ORD><<<grid_for(h.n, kL2pTile, sm_count() * kL2pBlocksPerSM), 128, 0, s>>>(dep, hl(dep), h.n, P<uint32_t>(h.codes), comrel, loc,
+                                                     P<float>(h.prel), P<float2>(h.nearf), P<uint32_t>(h.perm),
+                                                     d_grad, accumulate, scatter);
     if ((rc = record(h, 6))) return rc;
     if ((rc = ensure(h.sumtmp, sum_tmp_doubles() * 8)) ||
         (rc = sum_f64(zp, nn, P<double>(h.zwork), chunk_ptr + nleaf, d_total, 1, P<double>(h.sumtmp), s)))
         return rc;
-    h.launches += 3 + 2 * dep + 6 - nfused;
+    h.launches += 3 + 2 * dep + 7 - nfused;
     TC_CUDA_TRY(cudaGetLastError());
     if (tc_m2l) {
         // the tensor-core M2L's status word (list offsets beyond its operators, a bounded wait that gave up)

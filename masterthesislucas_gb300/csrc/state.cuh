@@ -47,6 +47,12 @@ struct Handle {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_tree = nullptr, ev_grad = nullptr;
     bool wait_grad = false;
+    // order-p solves: the near field on near_stream beside the far field (forked by ev_fork, joined by
+    // ev_join before the L2P), its FP32 forces in nearf (sorted order)
+    bool near_overlap = true;
+    cudaStream_t near_stream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    Buf nearf;
     int depth = -1;
     int64_t n = 0;
     int64_t nnodes = 0;
@@ -106,8 +112,9 @@ struct Handle {
     // stage timing (CUDA events on the handle's stream) and interaction counters
     cudaGraphExec_t step_graph = nullptr;  // a captured update + solve (tc_step_capture)
     int graph_launches = 0;
-    cudaEvent_t ev[TC_NSTAGES + 2] = {};
+    cudaEvent_t ev[12] = {};
     bool ev_ready = false;
+    bool stage_split = false;  // the last solve recorded the order-p events (8-11)
     Buf counters;  // u64: p2p pairs, m2p, p2l (device)
     double* h_total = nullptr;     // pinned
     uint32_t* h_words = nullptr;   // pinned, 64 words
@@ -116,10 +123,15 @@ struct Handle {
 int ensure(Buf& b, size_t bytes);
 void release(Buf& b);
 
-// stage boundaries recorded on the handle's stream (index into Handle::ev):
-// 0 update start, 1 sorted, 2 tree built, 3 lists built, 4 solve start,
-// 5 M2L done, 6 near field done, 7 solve done
+// stage boundaries (index into Handle::ev), on the handle's stream unless
+// noted: 0 update start, 1 sorted, 2 tree built, 3 lists built, 4 solve
+// start, 5 far field done, 6 near field done (order p: L2P done), 7 solve
+// done; order-p solves also: 8 / 9 near field start / done (near_stream),
+// 10 L2P start, 11 far field start
 int record(Handle& h, int i);
+int record_on(Handle& h, int i, cudaStream_t s);
+// the order-p near field's stream and fork/join events (created on first use, never inside a capture)
+int ensure_near_stream(Handle& h);
 
 template <typename T>
 inline T* P(const Buf& b) { return reinterpret_cast<T*>(b.p); }

@@ -66,7 +66,7 @@ class NBodySolverFMM_SYM_MORTON:
     def __init__(self, kernel: str = "tsne", max_children: int = 16, tree_depth: int | None = None,
                  theta: float = 0.5, softening: float = 1e-3, precision: str = "fp32", device: int = 0,
                  stream=None, order: int = 0, mac: str = "cell", slack: float = 1.0, leaf_p2p: int = 0,
-                 centre: str = "com", m2l: str = "simt"):
+                 centre: str = "com", m2l: str = "simt", near_overlap: bool = True):
         """mac (order p only): "cell", the reference's (L_A + L_B)/theta <
         |dcom| with cell sizes L; "bmax", (b_A + b_B)/theta < |dcom| with b
         the largest distance of a node's particles from its COM;
@@ -80,7 +80,9 @@ class NBodySolverFMM_SYM_MORTON:
         the level and the grid offset of a pair).
         m2l (centre "box"): "simt" FP32 kernels, or "tensor" the tensor-core
         M2L (BF16 hi/lo split, FP32 accumulation) on the levels with enough
-        nodes to fill the GPU, or "tensor_all" on every level."""
+        nodes to fill the GPU, or "tensor_all" on every level.
+        near_overlap (order p): the near field runs on a second stream beside
+        the far field (False: in sequence; the results are identical)."""
         if centre not in ("com", "box"):
             raise ValueError("centre must be 'com' or 'box'")
         if m2l not in ("simt", "tensor", "tensor_all"):
@@ -113,8 +115,11 @@ class NBodySolverFMM_SYM_MORTON:
         if m2l != "simt":
             check(lib().tc_set_m2l_engine(self._h, _lib.TC_M2L_TENSOR if m2l == "tensor"
                                           else _lib.TC_M2L_TENSOR_ALL))
+        if not near_overlap:
+            check(lib().tc_set_near_overlap(self._h, 0))
         self.centre = centre
         self.m2l = m2l
+        self.near_overlap = near_overlap
         self.maxChildren = max_children
         self._cfg_depth = cfg.depth
         self._theta = theta
@@ -204,7 +209,7 @@ class NBodySolverFMM_SYM_MORTON:
     def launches(self) -> int:
         return int(lib().tc_last_launch_count(self._h))
 
-    STAGES = ("sort", "build", "lists", "far", "near", "reduce")
+    STAGES = ("sort", "build", "lists", "far", "near", "l2p", "reduce")
 
     def stage_times(self) -> dict:
         """Device milliseconds per stage of the last update + solve (CUDA events)."""

@@ -40,7 +40,8 @@ def test_median_error_is_relative_per_particle():
 def _fake_arm(order, err, ms):
     return {"t_total": ms * 20 / 1e3, "depth": 11, "order": order, "theta": 0.75, "mac": "bmax", "tau": None,
             "err": (err, 3 * err, 50 * err), "graph": True, "launches": 2460,
-            "stages": {"sort": 0.25, "build": 0.55, "lists": 0.45, "far": 0.7, "near": 1.4, "reduce": 0.03},
+            "stages": {"sort": 0.25, "build": 0.55, "lists": 0.45, "far": 0.7, "near": 1.3, "l2p": 0.1,
+                       "reduce": 0.03},
             "counters": {"p2p_pairs": 2_359_484_542, "m2p": 0, "p2l": 0, "m2l": 14_200_000},
             "clocks": {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": [], "samples": 17, "source": "nvml"},
             "nonempty_nodes": 600_000, "near_pairs": 9_000_000}
@@ -72,6 +73,8 @@ def test_headline_line_stays_small_with_every_trial_recorded():
         assert k in line
     sr = line["step_roofline"]
     assert 0 < sr["achieved"] < 1 and sr["t_stages_ms"] == pytest.approx(3.38)
+    # overlapping stages: the step roofline is taken against the measured step, not the stage sum
+    assert sr["t_step_ms"] == pytest.approx(3.1) and sr["achieved"] == pytest.approx(sr["t_roof_ms"] / 3.1, rel=1e-3)
     assert "learned_speedup_vs_plain_p12" in line["comparison"]
 
 
