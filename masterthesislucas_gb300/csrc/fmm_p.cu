@@ -949,154 +949,61 @@ __global__ void __launch_bounds__(32 * kNearWarps, TC_NEAR_MIN_BLOCKS)
 }
 
 // L2P of the final local expansion of each particle's leaf plus the particle's
-// near-field force: F = (1/h) sum_b L_b d^(b - e) / (b - e)! + nearf, written
-// (or added) in FP64.  Each thread takes kL2pPer consecutive particles in
-// sorted order (16-byte loads of their codes, positions, near-field forces and
-// permutation entries), a block a tile of 128 * kL2pPer.  A tile's particles lie
-// in a few consecutive leaves (their sorted Morton codes say which): the tile
-// stages those leaves' expansions and centres in shared memory once, with
-// coalesced loads, and every particle reads its leaf's coefficients from there
-// as broadcasts.  A tile of more than kL2pSlots leaves reads the rest from
-// global memory.
-constexpr int kL2pPer = 4;
-constexpr int kL2pTile = 128 * kL2pPer;
-constexpr int kL2pSlots = 64;
-constexpr int kL2pBlocksPerSM = 8;
-
+// near-field force, written (or added) in FP64:
+//   F_x = (1/h) sum_{a+b<P} L_{a+1,b} w_{a,b},  F_y = (1/h) sum L_{a,b+1} w_{a,b},
+// w_{a,b} = dx^a/a! dy^b/b!.  One thread per particle in sorted order; the
+// leaf comes from the particle's sorted Morton code.  The leaf's coefficients
+// are read in storage order, 16 bytes at a time (a warp's particles lie in a
+// few leaves, so each read is a few L1 lines), and each goes to the x and y
+// sums it belongs to.  (Staging a tile's leaves in shared memory costs more:
+// a leaf holds about ten particles, so the per-leaf copy is as long as the
+// evaluation.)
 template <int P>
-__device__ __forceinline__ void l2p_eval(const float* L, float dx, float dy, float& lx, float& ly)
+__global__ void __launch_bounds__(128) k_l2p_p(int dep, float h, int64_t n, const uint32_t* __restrict__ codes,
+                                             const float* __restrict__ comrel, const float* __restrict__ loc,
+                                             const float* __restrict__ prel, const float2* __restrict__ nearf,
+                                             const uint32_t* __restrict__ perm, double* __restrict__ grad,
+                                             int accumulate, int scatter, int vec16)
 {
-    constexpr int KW = ncoef(P - 1);
-    float wv[KW];
-    monomials<P - 1>(dx, dy, wv);
-    lx = 0.f;
-    ly = 0.f;
-#pragma unroll
-    for (int kk = 0; kk < P; kk++)
-#pragma unroll
-        for (int b = 0; b <= kk; b++) {
-            const int a = kk - b;
-            lx += L[cidx(a + 1, b)] * wv[cidx(a, b)];
-            ly += L[cidx(a, b + 1)] * wv[cidx(a, b)];
-        }
-}
-
-template <int P>
-__global__ void __launch_bounds__(128, kL2pBlocksPerSM)
-    k_l2p_p(int dep, float h, int64_t n, const uint32_t* __restrict__ codes, const float* __restrict__ comrel,
-            const float* __restrict__ loc, const float* __restrict__ prel, const float2* __restrict__ nearf,
-            const uint32_t* __restrict__ perm, double* __restrict__ grad, int accumulate, int scatter)
-{
-    constexpr int K = ncoef(P);
-    constexpr int KR = K | 1;  // odd row stride: neighbouring slots' rows start in different banks
-    __shared__ float sL[kL2pSlots][KR];
-    __shared__ float sC[kL2pSlots][2];
-    __shared__ uint32_t sNode[kL2pSlots];
-    __shared__ uint32_t wlead[4];
+    constexpr int K = ncoef(P), KS = kstride(P), KW = ncoef(P - 1);
     const uint32_t li = level_index(dep);
     const int shift = 32 - 2 * dep;
     const float ih = 1.0f / h;
-    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const float2* prel2 = reinterpret_cast<const float2*>(prel);
-    auto leaf_of = [&](uint32_t c) { return dep ? c >> shift : 0u; };
-    const int64_t ntile = (n + kL2pTile - 1) / kL2pTile;
-    for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
-        const int64_t k0 = tile * kL2pTile + (int64_t)threadIdx.x * kL2pPer;
-        uint32_t leaf[kL2pPer], pm[kL2pPer];
-        float2 p2[kL2pPer], f2[kL2pPer];
-        if (k0 + kL2pPer <= n) {
-            // k0 is a multiple of 4: 16-byte aligned in every array
-            const uint4 c4 = *reinterpret_cast<const uint4*>(codes + k0);
-            const float4 pa = *reinterpret_cast<const float4*>(prel2 + k0);
-            const float4 pb = *reinterpret_cast<const float4*>(prel2 + k0 + 2);
-            const float4 fa = *reinterpret_cast<const float4*>(nearf + k0);
-            const float4 fb = *reinterpret_cast<const float4*>(nearf + k0 + 2);
-            const uint4 m4 = scatter ? *reinterpret_cast<const uint4*>(perm + k0) : make_uint4(0, 0, 0, 0);
-            leaf[0] = leaf_of(c4.x), leaf[1] = leaf_of(c4.y), leaf[2] = leaf_of(c4.z), leaf[3] = leaf_of(c4.w);
-            p2[0] = make_float2(pa.x, pa.y), p2[1] = make_float2(pa.z, pa.w);
-            p2[2] = make_float2(pb.x, pb.y), p2[3] = make_float2(pb.z, pb.w);
-            f2[0] = make_float2(fa.x, fa.y), f2[1] = make_float2(fa.z, fa.w);
-            f2[2] = make_float2(fb.x, fb.y), f2[3] = make_float2(fb.z, fb.w);
-            pm[0] = m4.x, pm[1] = m4.y, pm[2] = m4.z, pm[3] = m4.w;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t S = li + (dep ? (codes[k] >> shift) : 0u);
+        const float2 p2 = prel2[k];
+        const float2 f = nearf[k];
+        const uint32_t pm = scatter ? perm[k] : 0u;
+        float wv[KW];
+        monomials<P - 1>((p2.x - comrel[2 * S]) * ih, (p2.y - comrel[2 * S + 1]) * ih, wv);
+        const float4* L4 = reinterpret_cast<const float4*>(loc + S * KS);
+        float lx = 0.f, ly = 0.f;
+#pragma unroll
+        for (int c = 0; c < KS / 4; c++) {
+            const float4 q = L4[c];
+            const float qv[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int i = 4 * c + j;
+                if (i >= K) continue;
+                const int d = cdeg(i), bb = i - d * (d + 1) / 2, aa = d - bb;  // coefficient (aa, bb)
+                if (aa >= 1) lx = fmaf(qv[j], wv[cidx(aa - 1, bb)], lx);
+                if (bb >= 1) ly = fmaf(qv[j], wv[cidx(aa, bb - 1)], ly);
+            }
+        }
+        const int64_t o = scatter ? (int64_t)pm : k;
+        double ox2 = f64_of_f32(lx * ih + f.x), oy2 = f64_of_f32(ly * ih + f.y);
+        if (vec16) {
+            // one 16-byte access per particle (the scattered order makes each its own transaction)
+            double2* g2 = reinterpret_cast<double2*>(grad) + o;
+            if (accumulate) {
+                const double2 a = *g2;
+                ox2 += a.x;
+                oy2 += a.y;
+            }
+            *g2 = make_double2(ox2, oy2);
         } else {
-#pragma unroll
-            for (int u = 0; u < kL2pPer; u++) {
-                const int64_t k = k0 + u;
-                const bool v = k < n;
-                leaf[u] = v ? leaf_of(codes[k]) : 0u;
-                p2[u] = v ? prel2[k] : make_float2(0.f, 0.f);
-                f2[u] = v ? nearf[k] : make_float2(0.f, 0.f);
-                pm[u] = v && scatter ? perm[k] : 0u;
-            }
-        }
-        // the first particle of each leaf in the tile leads it; the leaf's slot is the number of leaders up
-        // to and including its own, minus one
-        uint32_t prev = __shfl_up_sync(0xffffffffu, leaf[kL2pPer - 1], 1);
-        if (lane == 0 && threadIdx.x > 0 && k0 - 1 < n) prev = leaf_of(codes[k0 - 1]);
-        uint32_t cum[kL2pPer], nlead = 0;
-#pragma unroll
-        for (int u = 0; u < kL2pPer; u++) {
-            const bool lead = k0 + u < n && ((threadIdx.x == 0 && u == 0) || leaf[u] != (u ? leaf[u - 1] : prev));
-            nlead += lead ? 1u : 0u;
-            cum[u] = nlead;
-        }
-        uint32_t incl = nlead;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= (uint32_t)o) incl += v;
-        }
-        if (lane == 31) wlead[w] = incl;
-        __syncthreads();
-        uint32_t before = 0, total = 0;
-#pragma unroll
-        for (uint32_t i = 0; i < 4; i++) {
-            const uint32_t c = wlead[i];
-            before += i < w ? c : 0u;
-            total += c;
-        }
-        const uint32_t excl = before + incl - nlead;
-        int slot[kL2pPer];
-#pragma unroll
-        for (int u = 0; u < kL2pPer; u++) {
-            slot[u] = (int)(excl + cum[u]) - 1;
-            const bool lead = cum[u] != (u ? cum[u - 1] : 0u);
-            if (lead && slot[u] < kL2pSlots) sNode[slot[u]] = li + leaf[u];
-        }
-        __syncthreads();
-        const int ns = min((int)total, kL2pSlots);
-        // the slots' coefficients, eight loads per thread in flight before their stores
-        for (int i0 = 0; i0 < ns * K; i0 += 8 * 128) {
-            float v[8];
-#pragma unroll
-            for (int u = 0; u < 8; u++) {
-                const int i = i0 + u * 128 + (int)threadIdx.x, sl = i / K;
-                v[u] = i < ns * K ? loc[(int64_t)sNode[sl] * kstride(P) + (i - sl * K)] : 0.f;
-            }
-#pragma unroll
-            for (int u = 0; u < 8; u++) {
-                const int i = i0 + u * 128 + (int)threadIdx.x, sl = i / K;
-                if (i < ns * K) sL[sl][i - sl * K] = v[u];
-            }
-        }
-        if ((int)threadIdx.x < 2 * ns)
-            sC[threadIdx.x >> 1][threadIdx.x & 1] = comrel[2 * (int64_t)sNode[threadIdx.x >> 1] + (threadIdx.x & 1)];
-        __syncthreads();
-#pragma unroll
-        for (int u = 0; u < kL2pPer; u++) {
-            const int64_t k = k0 + u;
-            if (k >= n) continue;
-            float lx, ly;
-            const int sl = slot[u];
-            if (sl < kL2pSlots) {
-                l2p_eval<P>(sL[sl], (p2[u].x - sC[sl][0]) * ih, (p2[u].y - sC[sl][1]) * ih, lx, ly);
-            } else {
-                const int64_t S = li + leaf[u];
-                l2p_eval<P>(loc + S * kstride(P), (p2[u].x - comrel[2 * S]) * ih, (p2[u].y - comrel[2 * S + 1]) * ih,
-                            lx, ly);
-            }
-            const int64_t o = scatter ? (int64_t)pm[u] : k;
-            double ox2 = f64_of_f32(lx * ih + f2[u].x), oy2 = f64_of_f32(ly * ih + f2[u].y);
             if (accumulate) {
                 ox2 += grad[2 * o];
                 oy2 += grad[2 * o + 1];
@@ -1104,7 +1011,6 @@ __global__ void __launch_bounds__(128, kL2pBlocksPerSM)
             grad[2 * o] = ox2;
             grad[2 * o + 1] = oy2;
         }
-        __syncthreads();  // the next tile restages the slots
     }
 }
 
@@ -1354,9 +1260,10 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
         h.wait_grad = false;
     }
     if ((rc = record(h, 10))) return rc;
-    k_l2p_p<ORD><<<grid_for(h.n, kL2pTile, sm_count() * kL2pBlocksPerSM), 128, 0, s>>>(dep, hl(dep), h.n, P<uint32_t>(h.codes), comrel, loc,
+    k_l2p_p<ORD><<<grid_for(h.n, 128, sm_count() * 12), 128, 0, s>>>(dep, hl(dep), h.n, P<uint32_t>(h.codes), comrel, loc,
                                                      P<float>(h.prel), P<float2>(h.nearf), P<uint32_t>(h.perm),
-                                                     d_grad, accumulate, scatter);
+                                                     d_grad, accumulate, scatter,
+                                                     (reinterpret_cast<uintptr_t>(d_grad) & 15) == 0);
     if ((rc = record(h, 6))) return rc;
     if ((rc = ensure(h.sumtmp, sum_tmp_doubles() * 8)) ||
         (rc = sum_f64(zp, nn, P<double>(h.zwork), chunk_ptr + nleaf, d_total, 1, P<double>(h.sumtmp), s)))

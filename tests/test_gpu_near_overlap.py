@@ -107,3 +107,25 @@ def test_overlap_through_the_host_buffer_entry_points():
         s.close()
     assert np.array_equal(out[0][2], out[1][2])
     assert np.array_equal(out[0][0], out[1][0]) and out[0][1] == out[1][1]
+
+
+def test_gradient_buffer_off_a_16_byte_boundary():
+    """The L2P writes each particle's force as one 16-byte store when the caller's gradient allows it, two
+    8-byte stores otherwise: the same values either way, accumulated or not."""
+    import torch
+    pos = datasets.two_disks(100000, seed=45).astype(np.float64)
+    pd = torch.from_numpy(pos).cuda()
+    s = NBodySolverFMM_SYM_MORTON("gravity", max_children=64, theta=0.75, softening=1e-3, order=8, mac="bmax")
+    s.update_tree_device(pd)
+    n = len(pos)
+    for acc in (False, True):
+        g_al = torch.full((n, 2), 0.5, dtype=torch.float64, device="cuda")
+        flat = torch.full((2 * n + 1,), 0.5, dtype=torch.float64, device="cuda")
+        g_off = flat[1:].view(n, 2)
+        assert g_al.data_ptr() % 16 == 0 and g_off.data_ptr() % 16 == 8
+        t = torch.zeros(1, dtype=torch.float64, device="cuda")
+        s.solve_device(g_al, t, accumulate=acc)
+        s.solve_device(g_off, t, accumulate=acc)
+        torch.cuda.synchronize()
+        assert torch.equal(g_al, g_off)
+    s.close()
