@@ -82,9 +82,13 @@ int record(Handle& h, int i) { return record_on(h, i, h.stream); }
 int ensure_near_stream(Handle& h)
 {
     if (h.near_stream) return TC_OK;
-    TC_CUDA_TRY(cudaStreamCreateWithFlags(&h.near_stream, cudaStreamNonBlocking));
+    int least = 0, greatest = 0;
+    TC_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    TC_CUDA_TRY(cudaStreamCreateWithPriority(&h.near_stream, cudaStreamNonBlocking, least));
+    TC_CUDA_TRY(cudaStreamCreateWithPriority(&h.far_stream, cudaStreamNonBlocking, greatest));
     TC_CUDA_TRY(cudaEventCreateWithFlags(&h.ev_fork, cudaEventDisableTiming));
     TC_CUDA_TRY(cudaEventCreateWithFlags(&h.ev_join, cudaEventDisableTiming));
+    TC_CUDA_TRY(cudaEventCreateWithFlags(&h.ev_far, cudaEventDisableTiming));
     return TC_OK;
 }
 
@@ -331,6 +335,7 @@ int tc_destroy(tc_handle* t)
     cudaSetDevice(h.cfg.device);
     if (h.stream) cudaStreamSynchronize(h.stream);
     if (h.near_stream) cudaStreamSynchronize(h.near_stream);
+    if (h.far_stream) cudaStreamSynchronize(h.far_stream);
     if (h.copy_stream) cudaStreamSynchronize(h.copy_stream);
     Buf* bufs[] = {&h.codes, &h.perm, &h.alt_keys, &h.alt_vals, &h.pos_in, &h.pos64, &h.prel, &h.grad_acc,
                    &h.count, &h.first, &h.com64, &h.m0, &h.m2, &h.bbc, &h.bblen, &h.comrel, &h.m0r, &h.m2t,
@@ -345,6 +350,8 @@ int tc_destroy(tc_handle* t)
         cudaStreamDestroy(h.copy_stream);
     }
     if (h.near_stream) cudaStreamDestroy(h.near_stream);
+    if (h.far_stream) cudaStreamDestroy(h.far_stream);
+    if (h.ev_far) cudaEventDestroy(h.ev_far);
     if (h.ev_ready)
         for (auto& e : h.ev) cudaEventDestroy(e);
     if (h.ev_fork) cudaEventDestroy(h.ev_fork);
@@ -660,6 +667,7 @@ int tc_get_stage_times(tc_handle* t, double* ms)
     TC_CUDA_TRY(cudaSetDevice(h.cfg.device));
     TC_CUDA_TRY(cudaStreamSynchronize(h.stream));
     if (h.near_stream) TC_CUDA_TRY(cudaStreamSynchronize(h.near_stream));
+    if (h.far_stream) TC_CUDA_TRY(cudaStreamSynchronize(h.far_stream));
     // stage k spans events (a, b); a < 0: the stage does not exist on this path
     const int split_a[TC_NSTAGES] = {0, 1, 2, 11, 8, 10, 6}, split_b[TC_NSTAGES] = {1, 2, 3, 5, 9, 6, 7};
     const int plain_a[TC_NSTAGES] = {0, 1, 2, 4, 5, -1, 6}, plain_b[TC_NSTAGES] = {1, 2, 3, 5, 6, -1, 7};
@@ -831,7 +839,8 @@ extern "C" int tc_step_capture(tc_handle* t, const double* d_pos_xy, int64_t n, 
         if (g) cudaGraphDestroy(g);
         return rc ? rc : tc_cuda_fail(ee, "cudaStreamEndCapture");
     }
-    const cudaError_t ei = cudaGraphInstantiate(&h.step_graph, g, 0);
+    // kernel nodes keep their capture stream's priority (the far field above the near field)
+    const cudaError_t ei = cudaGraphInstantiate(&h.step_graph, g, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(g);
     if (ei != cudaSuccess) {
         h.step_graph = nullptr;

@@ -1162,6 +1162,20 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
     }
     if ((rc = record_on(h, 9, sn))) return rc;
     if (h.near_overlap) TC_CUDA_TRY(cudaEventRecord(h.ev_join, sn));
+    // the far field: beside the near field it runs on a stream of higher priority, so that its chain of
+    // dependent launches takes SMs first as near-field blocks retire (the handle's stream points there
+    // until the join; the guard restores it on every exit)
+    const cudaStream_t s_call = s;
+    struct StreamSwap {
+        Handle& hh;
+        cudaStream_t saved;
+        ~StreamSwap() { hh.stream = saved; }
+    } swap{h, h.stream};
+    if (h.near_overlap) {
+        TC_CUDA_TRY(cudaStreamWaitEvent(h.far_stream, h.ev_fork, 0));
+        h.stream = h.far_stream;
+        s = h.far_stream;
+    }
     if ((rc = record(h, 11))) return rc;  // the far field starts
     float* mu = P<float>(h.mu);
     float* loc = P<float>(h.loc);
@@ -1252,7 +1266,13 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
             k_l2l<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, loc, P<uint32_t>(h.act), P<uint32_t>(h.act_pos));
     }
     if ((rc = record(h, 5))) return rc;
-    if (h.near_overlap) TC_CUDA_TRY(cudaStreamWaitEvent(s, h.ev_join, 0));
+    if (h.near_overlap) {
+        TC_CUDA_TRY(cudaEventRecord(h.ev_far, s));
+        h.stream = swap.saved;
+        s = s_call;
+        TC_CUDA_TRY(cudaStreamWaitEvent(s, h.ev_far, 0));
+        TC_CUDA_TRY(cudaStreamWaitEvent(s, h.ev_join, 0));
+    }
     if (h.wait_grad) {
         // the caller's gradient, copied in on the copy stream behind the far and near fields, is added to
         // from here on

@@ -47,11 +47,12 @@ struct Handle {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_tree = nullptr, ev_grad = nullptr;
     bool wait_grad = false;
-    // order-p solves: the near field on near_stream beside the far field (forked by ev_fork, joined by
-    // ev_join before the L2P), its FP32 forces in nearf (sorted order)
+    // order-p solves: the near field on near_stream beside the far field on far_stream (higher priority),
+    // both forked by ev_fork and joined by ev_join / ev_far before the L2P; the near field's FP32 forces
+    // in nearf (sorted order)
     bool near_overlap = true;
-    cudaStream_t near_stream = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaStream_t near_stream = nullptr, far_stream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_far = nullptr;
     Buf nearf;
     int depth = -1;
     int64_t n = 0;
@@ -130,7 +131,7 @@ void release(Buf& b);
 // 10 L2P start, 11 far field start
 int record(Handle& h, int i);
 int record_on(Handle& h, int i, cudaStream_t s);
-// the order-p near field's stream and fork/join events (created on first use, never inside a capture)
+// the order-p near and far fields' streams and fork/join events (created on first use, never inside a capture)
 int ensure_near_stream(Handle& h);
 
 template <typename T>

@@ -438,7 +438,7 @@ int build_exec(tc_tsne_batch* b, int k)
     cudaError_t e = cudaSuccess;
     for (size_t i = 0; i < b->sys.size() && e == cudaSuccess; i++)
         e = cudaGraphAddChildGraphNode(&b->node[k][i], root, nullptr, 0, b->g[i][k]);
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec[k], root, 0);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec[k], root, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(root);
     if (e != cudaSuccess) {
         b->exec[k] = nullptr;
