@@ -89,6 +89,7 @@ int ensure_near_stream(Handle& h)
     TC_CUDA_TRY(cudaEventCreateWithFlags(&h.ev_fork, cudaEventDisableTiming));
     TC_CUDA_TRY(cudaEventCreateWithFlags(&h.ev_join, cudaEventDisableTiming));
     TC_CUDA_TRY(cudaEventCreateWithFlags(&h.ev_far, cudaEventDisableTiming));
+    TC_CUDA_TRY(cudaEventCreateWithFlags(&h.ev_mu, cudaEventDisableTiming));
     return TC_OK;
 }
 
@@ -352,6 +353,7 @@ int tc_destroy(tc_handle* t)
     if (h.near_stream) cudaStreamDestroy(h.near_stream);
     if (h.far_stream) cudaStreamDestroy(h.far_stream);
     if (h.ev_far) cudaEventDestroy(h.ev_far);
+    if (h.ev_mu) cudaEventDestroy(h.ev_mu);
     if (h.ev_ready)
         for (auto& e : h.ev) cudaEventDestroy(e);
     if (h.ev_fork) cudaEventDestroy(h.ev_fork);
@@ -394,10 +396,32 @@ static int update_common(Handle& h, const double* d_pos, int64_t n, const double
         tc_set_error("bounding box is not finite");
         return TC_ERR_INVALID;
     }
-    int rc = build_tree(h, d_pos, n, mn[0], mn[1], mx[0], mx[1]);
-    if (rc) return rc;
-    if ((rc = after_tree())) return rc;
-    rc = build_lists(h);  // synchronises the stream (list sizes), except in no-sync mode
+    // order-p multipoles without the learned controller (whose list build reads them): built on a side
+    // stream beside the interaction lists, which need only the tree, and joined before the update returns
+    // (streams are never created inside a capture: a captured update follows an ordinary one)
+    const bool split = h.cfg.order && !h.ctrl_on && h.near_overlap && (h.near_stream || !h.nosync);
+    h.split_mu = split;
+    int rc = split ? ensure_near_stream(h) : TC_OK;
+    if (!rc) rc = build_tree(h, d_pos, n, mn[0], mn[1], mx[0], mx[1]);
+    h.split_mu = false;
+    bool forked = false;
+    if (!rc && split) {
+        TC_CUDA_TRY(cudaEventRecord(h.ev_fork, h.stream));
+        TC_CUDA_TRY(cudaStreamWaitEvent(h.near_stream, h.ev_fork, 0));
+        forked = true;
+        const cudaStream_t main = h.stream;
+        h.stream = h.near_stream;
+        rc = build_multipoles(h);
+        h.stream = main;
+        const cudaError_t e = cudaEventRecord(h.ev_mu, h.near_stream);
+        if (!rc && e != cudaSuccess) rc = tc_cuda_fail(e, "cudaEventRecord");
+    }
+    if (!rc && (rc = after_tree()) == TC_OK)
+        rc = build_lists(h);  // synchronises the stream (list sizes), except in no-sync mode
+    if (forked) {
+        const cudaError_t e = cudaStreamWaitEvent(h.stream, h.ev_mu, 0);
+        if (!rc && e != cudaSuccess) rc = tc_cuda_fail(e, "cudaStreamWaitEvent");
+    }
     if (rc) return rc;
     TC_CUDA_TRY(cudaMemcpyAsync(h.h_words + 8, h.err.p, 4, cudaMemcpyDeviceToHost, h.stream));
     if (h.nosync) return TC_OK;  // the caller reads the flags after its own synchronisation

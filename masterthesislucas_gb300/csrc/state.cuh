@@ -53,6 +53,10 @@ struct Handle {
     bool near_overlap = true;
     cudaStream_t near_stream = nullptr, far_stream = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_far = nullptr;
+    // the update's multipoles on near_stream beside the list build (ev_mu marks them done); build_tree
+    // leaves them out while split_mu is set
+    bool split_mu = false;
+    cudaEvent_t ev_mu = nullptr;
     Buf nearf;
     int depth = -1;
     int64_t n = 0;

@@ -484,7 +484,7 @@ int build_tree(Handle& h, const double* d_pos, int64_t n, double minx, double mi
     TC_CUDA_TRY(cudaGetLastError());
     if (h.cfg.order && (rc = build_active(h))) return rc;
     // order-p multipoles belong to the tree: the list builder's controller reads them
-    if (h.cfg.order && (rc = build_multipoles(h))) return rc;
+    if (h.cfg.order && !h.split_mu && (rc = build_multipoles(h))) return rc;
     if ((rc = record(h, 2))) return rc;
     h.tree_ready = true;
     return TC_OK;
