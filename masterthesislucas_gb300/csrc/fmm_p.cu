@@ -740,24 +740,38 @@ constexpr int64_t kM2lWarpLevelNodes = (int64_t)1 << 16;
 // ------------------------------------------------------------------ near field
 constexpr int kNearWarps = 4;
 
-__global__ void k_chunks(int dep, const uint32_t* __restrict__ count, uint32_t* __restrict__ nchunk)
+// sinks per block item: leaves of more than 32 particles are split into
+// items of this many sinks, a block (four warps of 32 sinks) each
+constexpr uint32_t kBlockSinks = 32u * kNearWarps;
+
+// per leaf: warp items (a leaf of 1..32 particles) and block items (a larger
+// leaf, one per kBlockSinks of its particles)
+__global__ void k_chunks(int dep, const uint32_t* __restrict__ count, uint32_t* __restrict__ nwarp,
+                         uint32_t* __restrict__ nblock)
 {
     const uint32_t li = level_index(dep);
     const int64_t nl = (int64_t)1 << (2 * dep);
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x)
-        nchunk[i] = (count[li + i] + 31u) / 32u;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = count[li + i];
+        nwarp[i] = c >= 1u && c <= 32u ? 1u : 0u;
+        nblock[i] = c > 32u ? (c + kBlockSinks - 1u) / kBlockSinks : 0u;
+    }
 }
 
-// work item -> leaf, from the exclusive scan of the chunk counts (items of
-// one leaf are consecutive); cap bounds the map's storage
-__global__ void k_chunk_leaf(int dep, const uint32_t* __restrict__ chunk_ptr, uint32_t* __restrict__ item_leaf,
-                             uint32_t cap)
+// item -> leaf for both kinds, from the exclusive scans of their counts (items
+// of one leaf are consecutive), and the number of pair-sum words the near
+// field writes (warp items first, then block items); cap bounds every map
+__global__ void k_chunk_leaf(int dep, const uint32_t* __restrict__ wptr, const uint32_t* __restrict__ bptr,
+                             uint32_t* __restrict__ witem, uint32_t* __restrict__ bitem, uint32_t cap,
+                             uint32_t* __restrict__ nz)
 {
     const int64_t nl = (int64_t)1 << (2 * dep);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t c1 = min(chunk_ptr[i + 1], cap);
-        for (uint32_t c = chunk_ptr[i]; c < c1; c++) item_leaf[c] = (uint32_t)i;
+        const uint32_t w1 = min(wptr[i + 1], cap), b1 = min(bptr[i + 1], cap);
+        for (uint32_t c = wptr[i]; c < w1; c++) witem[c] = (uint32_t)i;
+        for (uint32_t c = bptr[i]; c < b1; c++) bitem[c] = (uint32_t)i;
     }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *nz = min(min(wptr[nl], cap) + min(bptr[nl], cap), cap);
 }
 
 // Sources staged per warp (float2, in the sink leaf's frame).  The whole near
@@ -804,17 +818,154 @@ __device__ __forceinline__ void p2p_staged(const KN& ker, const float4* __restri
     zs += KN::kSign * (a0 + a1);
 }
 
-// One warp per work item (leaf S, chunk of m <= 32 sinks): direct P2P with
-// every particle of near(S); the sink's FP32 force goes to nearf (sorted
-// order) for the L2P kernel, the pair sum to zwork.  It reads nothing the far
-// field writes, so it runs on a stream of its own beside the far field.
+// Direct P2P of a leaf S's sinks with every particle of near(S); each sink's
+// FP32 force goes to nearf (sorted order).  It reads nothing the far field
+// writes, so it runs on a stream of its own beside the far field.
 // * The near list is read 32 entries at a time, one per lane (index, first
 //   particle, count, frame offset), and broadcast by shuffles.
 // * Its particles are staged into shared memory shifted into S's
 //   cell-relative frame (x_T + (cell_T - cell_S) h), so the inner loop is one
 //   unrolled pass over a flat array, padded with far-away sources.
-// * A chunk of m sinks gives each sink g = 2^floor(log2(32/m)) lanes that
-//   split its sources; their partial forces are summed by shuffles.
+// * A warp's m sinks get g = 2^floor(log2(32/m)) lanes each, which split the
+//   sources; their partial forces are summed by shuffles.
+// One item routine serves both kinds of work item: a warp item (a leaf of up
+// to 32 particles, a warp staging into its own buffer) and a block item (up
+// to kBlockSinks sinks of a larger leaf: the four warps stage the list once
+// into the block's buffer, each warp a different run of 32 positions, and
+// each computes its own 32 sinks against it; a warp past the leaf's end only
+// stages).  Every count that steers the staging is the same in all the
+// item's warps (they read the same entries), so the block's barriers are
+// reached uniformly.  Returns the warp's pair sum.
+template <bool kBlk, typename KN>
+__device__ __forceinline__ float near_item(const KN& ker, int dep, float h, const uint32_t* __restrict__ count,
+                                           const uint32_t* __restrict__ first, const uint32_t* __restrict__ near_ptr,
+                                           const uint32_t* __restrict__ near_idx, const float2* __restrict__ prel2,
+                                           uint32_t n, float2* __restrict__ nearf, int64_t si, uint32_t c0,
+                                           uint32_t m, float* buf, uint32_t cap, uint32_t& n_pp)
+{
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t run0 = kBlk ? 32u * w : 0u, rstep = kBlk ? 32u * kNearWarps : 32u;
+    auto sync = [&]() {
+        if constexpr (kBlk)
+            __syncthreads();
+        else
+            __syncwarp();
+    };
+    const float4* buf4 = reinterpret_cast<const float4*>(buf);
+    auto stage = [&](uint32_t q, float x, float y) {
+        buf[(q >> 1) * 4 + (q & 1)] = x;
+        buf[(q >> 1) * 4 + 2 + (q & 1)] = y;
+    };
+    const uint32_t li = level_index(dep);
+    const int64_t S = li + si;
+    const uint32_t fS = first[S];
+    uint32_t g = 32u, r = lane, sk = 0u;
+    if (m > 0u) {
+        const uint32_t lg = 5u - (32u - __clz(m - 1u));  // log2 g, g * m <= 32
+        g = 1u << lg;
+        r = lane & (g - 1u);
+        sk = lane >> lg;
+    }
+    const bool act = sk < m;
+    const uint32_t s = fS + c0 + (act ? sk : 0u);
+    const int isx = (int)compact16((uint32_t)si), isy = (int)compact16((uint32_t)si >> 1);
+    const float2 p2 = act ? prel2[s] : make_float2(0.f, 0.f);
+    const float px = p2.x, py = p2.y;
+    float gx = 0.f, gy = 0.f, zs = 0.f;
+    uint32_t fill = 0, staged = 0;
+    bool has_self = false;
+    const uint32_t e0 = near_ptr[si], e1 = near_ptr[si + 1];
+    for (uint32_t eb = e0; eb < e1; eb += 32) {
+        const uint32_t nt = min(32u, e1 - eb);
+        uint32_t mf = 0, mc = 0;
+        float mox = 0.f, moy = 0.f;
+        if (lane < nt) {
+            const uint32_t ti = near_idx[eb + lane];
+            mf = first[li + ti];
+            mc = count[li + ti];
+            mox = (float)((int)compact16(ti) - isx) * h;
+            moy = (float)((int)compact16(ti >> 1) - isy) * h;
+            has_self |= ti == (uint32_t)si;
+        }
+        // the batch's particles as one flat range [0, tot): position q
+        // belongs to entry t with ex_t <= q < ex_t + c_t (exclusive
+        // prefix ex over the lanes).  Every entry is a non-empty leaf, so
+        // the entries' first positions are distinct and t is the number
+        // of entries starting at or before q, minus one
+        uint32_t inc = mc;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= (uint32_t)o) inc += v;
+        }
+        const uint32_t ex = inc - mc, tot = __shfl_sync(0xffffffffu, inc, 31);
+        for (uint32_t q0 = 0; q0 < tot;) {
+            if (fill == cap) {
+                // evaluate the staged sources (cap is a multiple of 8g)
+                sync();
+                if (act) p2p_staged(ker, buf4, cap / 2, r, g, px, py, gx, gy, zs);
+                sync();
+                staged += fill;
+                fill = 0;
+            }
+            const uint32_t take = min(tot - q0, cap - fill);
+            for (uint32_t b0 = run0; b0 < take; b0 += rstep) {
+                const uint32_t base = q0 + b0, q = base + lane;
+                // entries starting before this run of 32 positions, and a bit per entry starting in it
+                const uint32_t before = __popc(__ballot_sync(0xffffffffu, lane < nt && ex < base));
+                const uint32_t d = ex - base;  // < 32 only for an entry starting in the run
+                const uint32_t bits = __reduce_or_sync(0xffffffffu, (lane < nt && d < 32u) ? 1u << d : 0u);
+                // in [0, nt): entry 0 starts at position 0
+                const uint32_t t = before + __popc(bits & (0xffffffffu >> (31u - lane))) - 1u;
+                const uint32_t fT = __shfl_sync(0xffffffffu, mf, t), eT = __shfl_sync(0xffffffffu, ex, t);
+                const float ox = __shfl_sync(0xffffffffu, mox, t), oy = __shfl_sync(0xffffffffu, moy, t);
+                if (b0 + lane < take) {
+                    // the particle index stays below n even for a list that broke the non-empty rule
+                    const uint32_t src = fT + (q - eT);
+                    const float2 t2 = src < n ? prel2[src] : make_float2(kFarAway, kFarAway);
+                    stage(fill + b0 + lane, t2.x + ox, t2.y + oy);
+                }
+            }
+            fill += take;
+            q0 += take;
+        }
+    }
+    if (fill > 0) {
+        // padded with far-away sources to a multiple of 8g (block items: of 8 * 32, every warp's g)
+        const uint32_t pad = kBlk ? 256u : 8u * g;
+        const uint32_t n8 = (fill + pad - 1u) / pad * pad;
+        for (uint32_t q = fill + (kBlk ? threadIdx.x : lane); q < n8; q += kBlk ? 32u * kNearWarps : 32u)
+            stage(q, kFarAway, kFarAway);
+        sync();
+        if (act) p2p_staged(ker, buf4, ((fill + 8u * g - 1u) / (8u * g) * (8u * g)) / 2, r, g, px, py, gx, gy, zs);
+        sync();
+        staged += fill;
+    }
+    has_self = __any_sync(0xffffffffu, has_self);
+    // the g lanes of a sink hold partial forces: sum them into lane r = 0
+    for (uint32_t o = g >> 1; o > 0; o >>= 1) {
+        gx += __shfl_xor_sync(0xffffffffu, gx, o);
+        gy += __shfl_xor_sync(0xffffffffu, gy, o);
+    }
+    if (act && r == 0) {
+        n_pp += staged;
+        if (has_self) {
+            // the staged sources included the sink itself: R = 0 adds no
+            // force but adds the kernel's pair term at r = 0, removed here
+            float D1, t0;
+            ker.near_xy(0.0f, 0.0f, D1, t0);
+            zs -= t0;
+            n_pp--;
+        }
+        nearf[s] = make_float2(gx, gy);
+    }
+    // the warp's pair sum: FP32 over the lanes (each lane's partial is an FP32 sum already)
+    return warp_sum(act ? zs : 0.0f);
+}
+
+// Block items first (each block takes whole items), then warp items (each
+// warp its own); per item one FP64 pair-sum word in zwork: warp items at
+// [0, nw), block items after them.
 template <typename KN>
 #ifndef TC_NEAR_MIN_BLOCKS
 #define TC_NEAR_MIN_BLOCKS 10  // resident blocks per SM the near field's registers are held to (48: no spills)
@@ -822,126 +973,44 @@ template <typename KN>
 __global__ void __launch_bounds__(32 * kNearWarps, TC_NEAR_MIN_BLOCKS)
     k_near_p(KN ker, int dep, float h, const uint32_t* __restrict__ count, const uint32_t* __restrict__ first,
              const uint32_t* __restrict__ near_ptr, const uint32_t* __restrict__ near_idx,
-             const uint32_t* __restrict__ chunk_ptr, const uint32_t* __restrict__ item_leaf, uint32_t cap,
+             const uint32_t* __restrict__ wptr, const uint32_t* __restrict__ witem,
+             const uint32_t* __restrict__ bptr, const uint32_t* __restrict__ bitem, uint32_t cap,
              const float* __restrict__ prel, uint32_t n, float2* __restrict__ nearf, double* __restrict__ zwork,
              unsigned long long* __restrict__ counters)
 {
-    // staged sources, two per 16-byte slot as (x0, x1, y0, y1)
-    __shared__ __align__(16) float s_src[kNearWarps][2 * kNearBuf];
+    // staged sources, two per 16-byte slot as (x0, x1, y0, y1): the whole
+    // array for a block item, a quarter per warp for warp items
+    __shared__ __align__(16) float s_src[kNearWarps * 2 * kNearBuf];
+    __shared__ float s_z[kNearWarps];
     uint32_t n_pp = 0;
     const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    float* buf = s_src[w];
-    const float4* buf4 = reinterpret_cast<const float4*>(s_src[w]);
-    auto stage = [&](uint32_t q, float x, float y) {
-        buf[(q >> 1) * 4 + (q & 1)] = x;
-        buf[(q >> 1) * 4 + 2 + (q & 1)] = y;
-    };
     const float2* prel2 = reinterpret_cast<const float2*>(prel);
     const uint32_t li = level_index(dep);
     const int64_t nl = (int64_t)1 << (2 * dep);
-    const uint32_t nwork = min(chunk_ptr[nl], cap);
-    const int64_t wstride = (int64_t)gridDim.x * kNearWarps;
-    for (int64_t wi = blockIdx.x * (int64_t)kNearWarps + w; wi < nwork; wi += wstride) {
-        const int64_t si = item_leaf[wi];
-        const int64_t S = li + si;
-        const uint32_t cS = count[S], fS = first[S];
-        const uint32_t c0 = ((uint32_t)wi - chunk_ptr[si]) * 32u;
-        const uint32_t m = min(32u, cS - c0);  // >= 1: a chunk exists only for sinks
-        const uint32_t lg = 5u - (32u - __clz(m - 1u));  // log2 g, g * m <= 32
-        const uint32_t g = 1u << lg, r = lane & (g - 1u), sk = lane >> lg;
-        const bool act = sk < m;
-        const uint32_t s = fS + c0 + (act ? sk : 0u);
-        const int isx = (int)compact16((uint32_t)si), isy = (int)compact16((uint32_t)si >> 1);
-        const float2 p2 = prel2[s];
-        const float px = p2.x, py = p2.y;
-        float gx = 0.f, gy = 0.f, zs = 0.f;
-        // warp-uniform: fill and every count
-        uint32_t fill = 0, staged = 0;
-        bool has_self = false;
-        const uint32_t e0 = near_ptr[si], e1 = near_ptr[si + 1];
-        for (uint32_t eb = e0; eb < e1; eb += 32) {
-            const uint32_t nt = min(32u, e1 - eb);
-            uint32_t mf = 0, mc = 0;
-            float mox = 0.f, moy = 0.f;
-            if (lane < nt) {
-                const uint32_t ti = near_idx[eb + lane];
-                mf = first[li + ti];
-                mc = count[li + ti];
-                mox = (float)((int)compact16(ti) - isx) * h;
-                moy = (float)((int)compact16(ti >> 1) - isy) * h;
-                has_self |= ti == (uint32_t)si;
-            }
-            // the batch's particles as one flat range [0, tot): position q
-            // belongs to entry t with ex_t <= q < ex_t + c_t (exclusive
-            // prefix ex over the lanes).  Every entry is a non-empty leaf, so
-            // the entries' first positions are distinct and t is the number
-            // of entries starting at or before q, minus one
-            uint32_t inc = mc;
+    const uint32_t nw = min(wptr[nl], cap), nb = min(bptr[nl], cap);
+    for (uint32_t bi = blockIdx.x; bi < nb; bi += gridDim.x) {
+        const int64_t si = bitem[bi];
+        const uint32_t cS = count[li + si];
+        const uint32_t c0 = (bi - bptr[si]) * kBlockSinks + 32u * w;
+        const uint32_t m = cS > c0 ? min(32u, cS - c0) : 0u;
+        const float z = near_item<true>(ker, dep, h, count, first, near_ptr, near_idx, prel2, n, nearf, si, c0, m,
+                                        s_src, (uint32_t)(kNearWarps * kNearBuf), n_pp);
+        if (lane == 0) s_z[w] = z;
+        __syncthreads();
+        if (threadIdx.x == 0 && nw + bi < cap) {
+            float zb = 0.f;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
-                if (lane >= (uint32_t)o) inc += v;
-            }
-            const uint32_t ex = inc - mc, tot = __shfl_sync(0xffffffffu, inc, 31);
-            for (uint32_t q0 = 0; q0 < tot;) {
-                if (fill == (uint32_t)kNearBuf) {
-                    // evaluate the staged sources (kNearBuf is a multiple of 8g)
-                    __syncwarp();
-                    if (act) p2p_staged(ker, buf4, kNearBuf / 2, r, g, px, py, gx, gy, zs);
-                    __syncwarp();
-                    staged += fill;
-                    fill = 0;
-                }
-                const uint32_t take = min(tot - q0, (uint32_t)kNearBuf - fill);
-                for (uint32_t b0 = 0; b0 < take; b0 += 32) {
-                    const uint32_t base = q0 + b0, q = base + lane;
-                    // entries starting before this run of 32 positions, and a bit per entry starting in it
-                    const uint32_t before = __popc(__ballot_sync(0xffffffffu, lane < nt && ex < base));
-                    const uint32_t d = ex - base;  // < 32 only for an entry starting in the run
-                    const uint32_t bits = __reduce_or_sync(0xffffffffu, (lane < nt && d < 32u) ? 1u << d : 0u);
-                    // in [0, nt): entry 0 starts at position 0
-                    const uint32_t t = before + __popc(bits & (0xffffffffu >> (31u - lane))) - 1u;
-                    const uint32_t fT = __shfl_sync(0xffffffffu, mf, t), eT = __shfl_sync(0xffffffffu, ex, t);
-                    const float ox = __shfl_sync(0xffffffffu, mox, t), oy = __shfl_sync(0xffffffffu, moy, t);
-                    if (b0 + lane < take) {
-                        // the particle index stays below n even for a list that broke the non-empty rule
-                        const uint32_t src = fT + (q - eT);
-                        const float2 t2 = src < n ? prel2[src] : make_float2(kFarAway, kFarAway);
-                        stage(fill + b0 + lane, t2.x + ox, t2.y + oy);
-                    }
-                }
-                fill += take;
-                q0 += take;
-            }
+            for (int i = 0; i < kNearWarps; i++) zb += s_z[i];
+            zwork[nw + bi] = (double)zb;
         }
-        if (fill > 0) {
-            const uint32_t n8 = (fill + 8u * g - 1u) & ~(8u * g - 1u);
-            for (uint32_t q = fill + lane; q < n8; q += 32) stage(q, kFarAway, kFarAway);
-            __syncwarp();
-            if (act) p2p_staged(ker, buf4, n8 / 2, r, g, px, py, gx, gy, zs);
-            __syncwarp();
-            staged += fill;
-        }
-        has_self = __any_sync(0xffffffffu, has_self);
-        // the g lanes of a sink hold partial forces: sum them into lane r = 0
-        for (uint32_t o = g >> 1; o > 0; o >>= 1) {
-            gx += __shfl_xor_sync(0xffffffffu, gx, o);
-            gy += __shfl_xor_sync(0xffffffffu, gy, o);
-        }
-        if (act && r == 0) {
-            n_pp += staged;
-            if (has_self) {
-                // the staged sources included the sink itself: R = 0 adds no
-                // force but adds the kernel's pair term at r = 0, removed here
-                float D1, t0;
-                ker.near_xy(0.0f, 0.0f, D1, t0);
-                zs -= t0;
-                n_pp--;
-            }
-            nearf[s] = make_float2(gx, gy);
-        }
-        // the chunk's pair sum: FP32 over the lanes (each lane's partial is an FP32 sum already), FP64 after
-        const float z = warp_sum(act ? zs : 0.0f);
+        __syncthreads();
+    }
+    const int64_t wstride = (int64_t)gridDim.x * kNearWarps;
+    for (int64_t wi = blockIdx.x * (int64_t)kNearWarps + w; wi < nw; wi += wstride) {
+        const int64_t si = witem[wi];
+        const uint32_t cS = count[li + si];  // 1..32
+        const float z = near_item<false>(ker, dep, h, count, first, near_ptr, near_idx, prel2, n, nearf, si, 0u, cS,
+                                         s_src + w * 2 * kNearBuf, (uint32_t)kNearBuf, n_pp);
         if (lane == 0) zwork[wi] = (double)z;
     }
     const unsigned long long a = warp_sum((unsigned long long)n_pp);
@@ -1126,10 +1195,10 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
     int rc;
     if ((rc = ensure(h.mu, nn * kstride(ORD) * 4)) || (rc = ensure(h.loc, nn * kstride(ORD) * 4)) ||
         (rc = ensure(h.zpart, nn * 8 + 64)) ||
-        (rc = ensure(h.counters, 64)) || (rc = ensure(h.chunk, (nleaf + 1) * 4)) ||
-        (rc = ensure(h.zwork, wmax * 8)) || (rc = ensure(h.chunk_leaf, wmax * 4)) ||
-        (rc = ensure(h.cnt_tmp, nleaf * 4 + 64)) ||
-        (rc = ensure(h.tmp, scan_tmp_words(nleaf) * 4)) || (rc = ensure(h.nearf, h.n * 8)) ||
+        (rc = ensure(h.counters, 64)) || (rc = ensure(h.chunk, (2 * (nleaf + 1) + 1) * 4)) ||
+        (rc = ensure(h.zwork, wmax * 8)) || (rc = ensure(h.chunk_leaf, 2 * wmax * 4)) ||
+        (rc = ensure(h.cnt_tmp, 2 * nleaf * 4 + 64)) ||
+        (rc = ensure(h.tmp, 2 * scan_tmp_words(nleaf) * 4)) || (rc = ensure(h.nearf, h.n * 8)) ||
         (rc = ensure_near_stream(h)) || (rc = record(h, 4)))
         return rc;
     TC_CUDA_TRY(cudaMemsetAsync(h.counters.p, 0, 64, s));
@@ -1143,21 +1212,25 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
         TC_CUDA_TRY(cudaStreamWaitEvent(sn, h.ev_fork, 0));
     }
     const uint32_t* count_n = P<uint32_t>(h.count);
-    uint32_t* nchunk = P<uint32_t>(h.cnt_tmp);
-    uint32_t* chunk_ptr = P<uint32_t>(h.chunk);
+    uint32_t* nwarp = P<uint32_t>(h.cnt_tmp);
+    uint32_t* nblock = nwarp + nleaf;
+    uint32_t* wptr = P<uint32_t>(h.chunk);
+    uint32_t* bptr = wptr + (nleaf + 1);
+    uint32_t* nz = bptr + (nleaf + 1);  // pair-sum words the near field writes
+    uint32_t* witem = P<uint32_t>(h.chunk_leaf);
+    uint32_t* bitem = witem + wmax;
     if ((rc = record_on(h, 8, sn))) return rc;
-    k_chunks<<<grid_for(nleaf, 256), 256, 0, sn>>>(dep, count_n, nchunk);
-    if ((rc = exclusive_scan_u32(nchunk, chunk_ptr, nleaf, P<uint32_t>(h.tmp), sn))) return rc;
-    k_chunk_leaf<<<grid_for(nleaf, 256), 256, 0, sn>>>(dep, chunk_ptr, P<uint32_t>(h.chunk_leaf), (uint32_t)wmax);
+    k_chunks<<<grid_for(nleaf, 256), 256, 0, sn>>>(dep, count_n, nwarp, nblock);
+    if ((rc = exclusive_scan2_u32(nwarp, wptr, nblock, bptr, nleaf, P<uint32_t>(h.tmp), sn))) return rc;
+    k_chunk_leaf<<<grid_for(nleaf, 256), 256, 0, sn>>>(dep, wptr, bptr, witem, bitem, (uint32_t)wmax, nz);
     {
         const int64_t wblk = (wmax + kNearWarps - 1) / kNearWarps;
         const uint32_t* ptr_n = P<uint32_t>(h.ptr_pool);
         const uint32_t* idx_n = P<uint32_t>(h.idx_pool);
         k_near_p<KN><<<(unsigned)(wblk < sm_count() * 256 ? wblk : sm_count() * 256), 32 * kNearWarps, 0, sn>>>(
             ker, dep, (float)(h.L / (double)(1u << dep)), count_n, P<uint32_t>(h.first),
-            ptr_n + h.lists.near_ptr_off[dep], idx_n + h.lists.near_idx_off[dep], chunk_ptr,
-            P<uint32_t>(h.chunk_leaf), (uint32_t)wmax, P<float>(h.prel), (uint32_t)h.n, P<float2>(h.nearf),
-            P<double>(h.zwork),
+            ptr_n + h.lists.near_ptr_off[dep], idx_n + h.lists.near_idx_off[dep], wptr, witem, bptr, bitem,
+            (uint32_t)wmax, P<float>(h.prel), (uint32_t)h.n, P<float2>(h.nearf), P<double>(h.zwork),
             P<unsigned long long>(h.counters));
     }
     if ((rc = record_on(h, 9, sn))) return rc;
@@ -1286,7 +1359,7 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
                                                      (reinterpret_cast<uintptr_t>(d_grad) & 15) == 0);
     if ((rc = record(h, 6))) return rc;
     if ((rc = ensure(h.sumtmp, sum_tmp_doubles() * 8)) ||
-        (rc = sum_f64(zp, nn, P<double>(h.zwork), chunk_ptr + nleaf, d_total, 1, P<double>(h.sumtmp), s)))
+        (rc = sum_f64(zp, nn, P<double>(h.zwork), nz, d_total, 1, P<double>(h.sumtmp), s)))
         return rc;
     h.launches += 3 + 2 * dep + 7 - nfused;
     TC_CUDA_TRY(cudaGetLastError());
