@@ -47,7 +47,7 @@ def _flags(src: str) -> list:
         f.append("-fmad=false")
     if src in FTZ:
         f.append("-ftz=true")
-    # extra nvcc flags for every translation unit (tuning builds, e.g. -DTC_NEAR_MIN_BLOCKS=10)
+    # extra nvcc flags for every translation unit (tuning builds, e.g. -DTC_NEAR_MIN_WARPS=40)
     f += os.environ.get("TREECODE_NVCC_FLAGS", "").split()
     return f
 

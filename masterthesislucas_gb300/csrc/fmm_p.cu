@@ -741,7 +741,7 @@ constexpr int64_t kM2lWarpLevelNodes = (int64_t)1 << 16;
 constexpr int kNearWarps = 4;
 
 // sinks per block item: leaves of more than 32 particles are split into
-// items of this many sinks, a block (four warps of 32 sinks) each
+// items of this many sinks, a block (a warp per 32 sinks) each
 constexpr uint32_t kBlockSinks = 32u * kNearWarps;
 
 // per leaf: warp items (a leaf of 1..32 particles) and block items (a larger
@@ -830,7 +830,7 @@ __device__ __forceinline__ void p2p_staged(const KN& ker, const float4* __restri
 //   sources; their partial forces are summed by shuffles.
 // One item routine serves both kinds of work item: a warp item (a leaf of up
 // to 32 particles, a warp staging into its own buffer) and a block item (up
-// to kBlockSinks sinks of a larger leaf: the four warps stage the list once
+// to kBlockSinks sinks of a larger leaf: the block's warps stage the list once
 // into the block's buffer, each warp a different run of 32 positions, and
 // each computes its own 32 sinks against it; a warp past the leaf's end only
 // stages).  Every count that steers the staging is the same in all the
@@ -967,10 +967,10 @@ __device__ __forceinline__ float near_item(const KN& ker, int dep, float h, cons
 // warp its own); per item one FP64 pair-sum word in zwork: warp items at
 // [0, nw), block items after them.
 template <typename KN>
-#ifndef TC_NEAR_MIN_BLOCKS
-#define TC_NEAR_MIN_BLOCKS 10  // resident blocks per SM the near field's registers are held to (48: no spills)
+#ifndef TC_NEAR_MIN_WARPS
+#define TC_NEAR_MIN_WARPS 40  // resident warps per SM the near field's registers are held to (48: no spills)
 #endif
-__global__ void __launch_bounds__(32 * kNearWarps, TC_NEAR_MIN_BLOCKS)
+__global__ void __launch_bounds__(32 * kNearWarps, TC_NEAR_MIN_WARPS / kNearWarps)
     k_near_p(KN ker, int dep, float h, const uint32_t* __restrict__ count, const uint32_t* __restrict__ first,
              const uint32_t* __restrict__ near_ptr, const uint32_t* __restrict__ near_idx,
              const uint32_t* __restrict__ wptr, const uint32_t* __restrict__ witem,
