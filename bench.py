@@ -1017,6 +1017,9 @@ def compact_calib(calib):
 # (dram__bytes_read.sum + dram__bytes_write.sum), keyed by (n, depth, order, opening criterion, theta, leaf P2P,
 # expansion centre).
 NEAR_TRAFFIC = {
+    (4194304, 11, 8, "bmax", 0.75, 64, "com"): (75632128 + 12529664,
+                                          "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_near_p launch "
+                                          "of the force step at this configuration (P2P only; bit-exact tree)"),
 }
 
 
