@@ -90,6 +90,7 @@ int ensure_near_stream(Handle& h)
     TC_CUDA_TRY(cudaEventCreateWithFlags(&h.ev_join, cudaEventDisableTiming));
     TC_CUDA_TRY(cudaEventCreateWithFlags(&h.ev_far, cudaEventDisableTiming));
     TC_CUDA_TRY(cudaEventCreateWithFlags(&h.ev_mu, cudaEventDisableTiming));
+    TC_CUDA_TRY(cudaEventCreateWithFlags(&h.ev_lists, cudaEventDisableTiming));
     return TC_OK;
 }
 
@@ -340,7 +341,7 @@ int tc_destroy(tc_handle* t)
     if (h.copy_stream) cudaStreamSynchronize(h.copy_stream);
     Buf* bufs[] = {&h.codes, &h.perm, &h.alt_keys, &h.alt_vals, &h.pos_in, &h.pos64, &h.prel, &h.grad_acc,
                    &h.count, &h.first, &h.com64, &h.m0, &h.m2, &h.bbc, &h.bblen, &h.comrel, &h.m0r, &h.m2t,
-                   &h.loc, &h.locfin, &h.mu, &h.chunk, &h.zwork, &h.zloc, &h.counters, &h.ptr_pool, &h.idx_pool, &h.cnt_tmp, &h.lstat, &h.ord_pool, &h.nfeat, &h.dec, &h.bigleaf, &h.chunk_leaf, &h.act, &h.act_pos, &h.bmax, &h.celloff, &h.mqueue, &h.nearf, &h.tc_ops, &h.tc_mubf, &h.diagpart, &h.ctrl_w, &h.tmp, &h.err, &h.zpart, &h.dtotal, &h.sumtmp,
+                   &h.loc, &h.locfin, &h.mu, &h.chunk, &h.zwork, &h.zloc, &h.counters, &h.ptr_pool, &h.idx_pool, &h.cnt_tmp, &h.lstat, &h.ord_pool, &h.nfeat, &h.dec, &h.bigleaf, &h.chunk_leaf, &h.act, &h.act_pos, &h.bmax, &h.celloff, &h.mqueue, &h.nearf, &h.items_cnt, &h.items_tmp, &h.tc_ops, &h.tc_mubf, &h.diagpart, &h.ctrl_w, &h.tmp, &h.err, &h.zpart, &h.dtotal, &h.sumtmp,
                    &h.host_stage, &h.ids_dev};
     for (Buf* b : bufs) release(*b);
     if (h.step_graph) cudaGraphExecDestroy(h.step_graph);
@@ -354,6 +355,7 @@ int tc_destroy(tc_handle* t)
     if (h.far_stream) cudaStreamDestroy(h.far_stream);
     if (h.ev_far) cudaEventDestroy(h.ev_far);
     if (h.ev_mu) cudaEventDestroy(h.ev_mu);
+    if (h.ev_lists) cudaEventDestroy(h.ev_lists);
     if (h.ev_ready)
         for (auto& e : h.ev) cudaEventDestroy(e);
     if (h.ev_fork) cudaEventDestroy(h.ev_fork);
@@ -398,29 +400,46 @@ static int update_common(Handle& h, const double* d_pos, int64_t n, const double
     }
     // order-p multipoles without the learned controller (whose list build reads them): built on a side
     // stream beside the interaction lists, which need only the tree, and joined before the update returns
-    // (streams are never created inside a capture: a captured update follows an ordinary one)
+    // (streams are never created inside a capture: a captured update follows an ordinary one).  The near
+    // field's work-item tables follow them there; in a captured step (whose list build has no host round
+    // trip that could redo the lists) so do the far field's coarse levels, once their lists are built.
     const bool split = h.cfg.order && !h.ctrl_on && h.near_overlap && (h.near_stream || !h.nosync);
+    const bool coarse = split && h.nosync && far_coarse_applies(h);
+    h.items_ready = false;
+    h.coarse_ready = false;
     h.split_mu = split;
     int rc = split ? ensure_near_stream(h) : TC_OK;
     if (!rc) rc = build_tree(h, d_pos, n, mn[0], mn[1], mx[0], mx[1]);
     h.split_mu = false;
     bool forked = false;
+    const cudaStream_t main = h.stream;
     if (!rc && split) {
         TC_CUDA_TRY(cudaEventRecord(h.ev_fork, h.stream));
         TC_CUDA_TRY(cudaStreamWaitEvent(h.near_stream, h.ev_fork, 0));
         forked = true;
-        const cudaStream_t main = h.stream;
         h.stream = h.near_stream;
         rc = build_multipoles(h);
+        if (!rc) rc = near_items(h);
         h.stream = main;
-        const cudaError_t e = cudaEventRecord(h.ev_mu, h.near_stream);
-        if (!rc && e != cudaSuccess) rc = tc_cuda_fail(e, "cudaEventRecord");
+        h.items_ready = rc == TC_OK;
     }
-    if (!rc && (rc = after_tree()) == TC_OK)
+    if (!rc && (rc = after_tree()) == TC_OK) {
+        h.lists_event_level = coarse ? kFarCoarseLevel : -1;
         rc = build_lists(h);  // synchronises the stream (list sizes), except in no-sync mode
+        h.lists_event_level = -1;
+    }
+    if (!rc && coarse) {
+        TC_CUDA_TRY(cudaStreamWaitEvent(h.near_stream, h.ev_lists, 0));
+        h.stream = h.near_stream;
+        const int rcc = build_far_coarse(h);  // 1: skipped, the solve runs the coarse levels itself
+        h.stream = main;
+        h.coarse_ready = rcc == TC_OK;
+        if (rcc < 0) rc = rcc;
+    }
     if (forked) {
-        const cudaError_t e = cudaStreamWaitEvent(h.stream, h.ev_mu, 0);
-        if (!rc && e != cudaSuccess) rc = tc_cuda_fail(e, "cudaStreamWaitEvent");
+        cudaError_t e = cudaEventRecord(h.ev_mu, h.near_stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(h.stream, h.ev_mu, 0);
+        if (!rc && e != cudaSuccess) rc = tc_cuda_fail(e, "side-stream join");
     }
     if (rc) return rc;
     TC_CUDA_TRY(cudaMemcpyAsync(h.h_words + 8, h.err.p, 4, cudaMemcpyDeviceToHost, h.stream));

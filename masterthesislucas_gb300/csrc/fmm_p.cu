@@ -1195,10 +1195,7 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
     int rc;
     if ((rc = ensure(h.mu, nn * kstride(ORD) * 4)) || (rc = ensure(h.loc, nn * kstride(ORD) * 4)) ||
         (rc = ensure(h.zpart, nn * 8 + 64)) ||
-        (rc = ensure(h.counters, 64)) || (rc = ensure(h.chunk, (2 * (nleaf + 1) + 1) * 4)) ||
-        (rc = ensure(h.zwork, wmax * 8)) || (rc = ensure(h.chunk_leaf, 2 * wmax * 4)) ||
-        (rc = ensure(h.cnt_tmp, 2 * nleaf * 4 + 64)) ||
-        (rc = ensure(h.tmp, 2 * scan_tmp_words(nleaf) * 4)) || (rc = ensure(h.nearf, h.n * 8)) ||
+        (rc = ensure(h.counters, 64)) || (rc = ensure(h.zwork, wmax * 8)) || (rc = ensure(h.nearf, h.n * 8)) ||
         (rc = ensure_near_stream(h)) || (rc = record(h, 4)))
         return rc;
     TC_CUDA_TRY(cudaMemsetAsync(h.counters.p, 0, 64, s));
@@ -1212,17 +1209,20 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
         TC_CUDA_TRY(cudaStreamWaitEvent(sn, h.ev_fork, 0));
     }
     const uint32_t* count_n = P<uint32_t>(h.count);
-    uint32_t* nwarp = P<uint32_t>(h.cnt_tmp);
-    uint32_t* nblock = nwarp + nleaf;
-    uint32_t* wptr = P<uint32_t>(h.chunk);
-    uint32_t* bptr = wptr + (nleaf + 1);
-    uint32_t* nz = bptr + (nleaf + 1);  // pair-sum words the near field writes
-    uint32_t* witem = P<uint32_t>(h.chunk_leaf);
-    uint32_t* bitem = witem + wmax;
     if ((rc = record_on(h, 8, sn))) return rc;
-    k_chunks<<<grid_for(nleaf, 256), 256, 0, sn>>>(dep, count_n, nwarp, nblock);
-    if ((rc = exclusive_scan2_u32(nwarp, wptr, nblock, bptr, nleaf, P<uint32_t>(h.tmp), sn))) return rc;
-    k_chunk_leaf<<<grid_for(nleaf, 256), 256, 0, sn>>>(dep, wptr, bptr, witem, bitem, (uint32_t)wmax, nz);
+    if (!h.items_ready) {
+        // the work-item tables, unless the update built them beside its list build
+        const cudaStream_t main = h.stream;
+        h.stream = sn;
+        rc = near_items(h);
+        h.stream = main;
+        if (rc) return rc;
+    }
+    const uint32_t* wptr = P<uint32_t>(h.chunk);
+    const uint32_t* bptr = wptr + (nleaf + 1);
+    const uint32_t* nz = bptr + (nleaf + 1);  // pair-sum words the near field writes
+    const uint32_t* witem = P<uint32_t>(h.chunk_leaf);
+    const uint32_t* bitem = witem + wmax;
     {
         const int64_t wblk = (wmax + kNearWarps - 1) / kNearWarps;
         const uint32_t* ptr_n = P<uint32_t>(h.ptr_pool);
@@ -1260,9 +1260,6 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
         tc_set_error("order-p solve: multipoles of another order (update the tree first)");
         return TC_ERR_STATE;
     }
-    TC_CUDA_TRY(cudaMemsetAsync(loc, 0, kstride(ORD) * 4, s));
-    TC_CUDA_TRY(cudaMemsetAsync(zp, 0, nn * 8, s));
-    TC_CUDA_TRY(cudaMemsetAsync(zp, 0, 8, s));
     const uint32_t* ptr = P<uint32_t>(h.ptr_pool);
     const uint32_t* idx = P<uint32_t>(h.idx_pool);
     // fixed order below 10: the fine levels' L2L runs inside their M2L launch (after the coarse levels' L2L)
@@ -1271,6 +1268,12 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
     else if constexpr (ORD >= 6) per_pair = h.adapt;
     const bool tc_m2l = h.m2l_tc;
     const bool fuse = ORD < 10 && !per_pair && !tc_m2l;
+    // a captured step's update ran the coarse levels (and the clearing) beside its list build
+    const bool coarse_done = h.coarse_ready && fuse;
+    if (!coarse_done) {
+        TC_CUDA_TRY(cudaMemsetAsync(loc, 0, kstride(ORD) * 4, s));
+        TC_CUDA_TRY(cudaMemsetAsync(zp, 0, nn * 8, s));
+    }
     int nfused = 0;
     if (tc_m2l) {
         if ((rc = m2l_tensor<ORD>(h, pp))) return rc;
@@ -1278,6 +1281,7 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
     for (int l = 1; l <= dep && !tc_m2l; l++) {
         const int64_t nl = (int64_t)1 << (2 * l);
         if (fuse && nl > kM2lWarpLevelNodes) continue;
+        if (coarse_done && nl <= kM2lWarpLevelNodes) continue;
         const uint32_t* np_ = ptr + h.lists.nn_ptr_off[l];
         const uint32_t* ni_ = idx + h.lists.nn_idx_off[l];
         bool mixed = false;
@@ -1324,6 +1328,7 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
     }
     for (int l = 1; l <= dep; l++) {
         const int64_t nl = (int64_t)1 << (2 * l);
+        if (coarse_done && nl <= kM2lWarpLevelNodes) continue;
         if constexpr (ORD < 10) {
             if (fuse && nl > kM2lWarpLevelNodes) {
                 k_m2l_p<ORD, true><<<grid_for(nl, 128), 128, 0, s>>>(
@@ -1361,7 +1366,9 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
     if ((rc = ensure(h.sumtmp, sum_tmp_doubles() * 8)) ||
         (rc = sum_f64(zp, nn, P<double>(h.zwork), nz, d_total, 1, P<double>(h.sumtmp), s)))
         return rc;
-    h.launches += 3 + 2 * dep + 7 - nfused;
+    // far field (an M2L and an L2L launch per level, one fused launch per fine level), the near field, the
+    // L2P and the two-kernel pair sum; the item tables and a captured update's coarse levels count themselves
+    h.launches += 2 * dep - nfused + 4 - (coarse_done ? 2 * kFarCoarseLevel : 0);
     TC_CUDA_TRY(cudaGetLastError());
     if (tc_m2l) {
         // the tensor-core M2L's status word (list offsets beyond its operators, a bounded wait that gave up)
@@ -1412,8 +1419,8 @@ int multipoles_p(Handle& h)
     return TC_OK;
 }
 
-template <int P>
-int dispatch_kernel(Handle& h, double* d_grad, int accumulate, int scatter, double* d_total)
+// the kernel's parameters for the expansion kernels
+PotParams make_pp(const Handle& h)
 {
     PotParams pp;
     pp.kind = h.cfg.kernel;
@@ -1422,12 +1429,63 @@ int dispatch_kernel(Handle& h, double* d_grad, int accumulate, int scatter, doub
         pp.nu = 0.5f;
         pp.c = (float)(h.cfg.softening * h.cfg.softening);
         pp.kappa = -1.0f;
-        return solve_p<P>(h, KGrav<float>{pp.c}, pp, d_grad, accumulate, scatter, d_total);
+    } else {
+        pp.nu = 1.0f;
+        pp.c = 1.0f;
+        pp.kappa = -2.0f;
     }
-    pp.nu = 1.0f;
-    pp.c = 1.0f;
-    pp.kappa = -2.0f;
+    return pp;
+}
+
+template <int P>
+int dispatch_kernel(Handle& h, double* d_grad, int accumulate, int scatter, double* d_total)
+{
+    const PotParams pp = make_pp(h);
+    if (h.cfg.kernel == TC_KERNEL_GRAVITY)
+        return solve_p<P>(h, KGrav<float>{pp.c}, pp, d_grad, accumulate, scatter, d_total);
     return solve_p<P>(h, KTsne<float>{}, pp, d_grad, accumulate, scatter, d_total);
+}
+
+// The fused fixed-order path's coarse levels: the local expansions zeroed
+// (root) and the pair-sum parts cleared, M2L of levels 1..kFarCoarseLevel (a
+// warp per sink node), then their L2L in order.  The solve continues from
+// level kFarCoarseLevel + 1.  Returns 1, queueing nothing, when an earlier
+// solve has not sized the buffers for this tree and order (nothing may be
+// allocated here: the call runs inside a captured update).
+template <int ORD>
+int far_coarse_p(Handle& h, const PotParams& pp)
+{
+    cudaStream_t s = h.stream;
+    if (h.mu_stride != kstride(ORD) || h.loc.bytes < (size_t)h.nnodes * kstride(ORD) * 4 ||
+        h.zpart.bytes < (size_t)h.nnodes * 8)
+        return 1;
+    const int dep = h.depth;
+    const int lc = dep < kFarCoarseLevel ? dep : kFarCoarseLevel;
+    float* mu = P<float>(h.mu);
+    float* loc = P<float>(h.loc);
+    double* zp = P<double>(h.zpart);
+    const float* comrel = P<float>(h.comrel);
+    const uint32_t* count = P<uint32_t>(h.count);
+    const uint32_t* ptr = P<uint32_t>(h.ptr_pool);
+    const uint32_t* idx = P<uint32_t>(h.idx_pool);
+    const uint32_t* act = P<uint32_t>(h.act);
+    const uint32_t* act_pos = P<uint32_t>(h.act_pos);
+    auto hl = [&](int l) { return (float)(h.L / (double)(1u << l)); };
+    TC_CUDA_TRY(cudaMemsetAsync(loc, 0, kstride(ORD) * 4, s));
+    TC_CUDA_TRY(cudaMemsetAsync(zp, 0, h.nnodes * 8, s));
+    for (int l = 1; l <= lc; l++) {
+        const int64_t nl = (int64_t)1 << (2 * l);
+        k_m2l_warp<ORD><<<grid_for(nl * 32, 128), 128, 0, s>>>(l, hl(l), pp, ptr + h.lists.nn_ptr_off[l],
+                                                               idx + h.lists.nn_idx_off[l], comrel, mu, loc, zp, act,
+                                                               act_pos);
+    }
+    for (int l = 1; l <= lc; l++) {
+        const int64_t nl = (int64_t)1 << (2 * l);
+        k_l2l<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, loc, act, act_pos);
+    }
+    h.launches += 2 * lc;
+    TC_CUDA_TRY(cudaGetLastError());
+    return TC_OK;
 }
 
 }  // namespace
@@ -1439,6 +1497,8 @@ template <int P>
 int multipoles_order(Handle& h);
 template <int P>
 int solve_order(Handle& h, double* d_grad, double* d_total, int accumulate, int scatter);
+template <int P>
+int far_coarse_order(Handle& h);
 
 #ifdef TC_FMM_ORDER
 template <int P>
@@ -1453,9 +1513,63 @@ int solve_order(Handle& h, double* d_grad, double* d_total, int accumulate, int 
     return dispatch_kernel<P>(h, d_grad, accumulate, scatter, d_total);
 }
 
+template <int P>
+int far_coarse_order(Handle& h)
+{
+    if constexpr (P < 10)
+        return far_coarse_p<P>(h, make_pp(h));
+    else
+        return TC_ERR_STATE;
+}
+
 template int multipoles_order<TC_FMM_ORDER>(Handle& h);
+template int far_coarse_order<TC_FMM_ORDER>(Handle& h);
 template int solve_order<TC_FMM_ORDER>(Handle& h, double* d_grad, double* d_total, int accumulate, int scatter);
 #else
+int near_items(Handle& h)
+{
+    cudaStream_t s = h.stream;
+    const int dep = h.depth;
+    const int64_t nleaf = (int64_t)1 << (2 * dep);
+    const int64_t wmax = h.n / 32 + (h.n < nleaf ? h.n : nleaf) + 1;
+    int rc;
+    if ((rc = ensure(h.chunk, (2 * (nleaf + 1) + 1) * 4)) || (rc = ensure(h.chunk_leaf, 2 * wmax * 4)) ||
+        (rc = ensure(h.items_cnt, 2 * nleaf * 4 + 64)) || (rc = ensure(h.items_tmp, 2 * scan_tmp_words(nleaf) * 4)))
+        return rc;
+    uint32_t* nwarp = P<uint32_t>(h.items_cnt);
+    uint32_t* nblock = nwarp + nleaf;
+    uint32_t* wptr = P<uint32_t>(h.chunk);
+    uint32_t* bptr = wptr + (nleaf + 1);
+    uint32_t* nz = bptr + (nleaf + 1);
+    uint32_t* witem = P<uint32_t>(h.chunk_leaf);
+    k_chunks<<<grid_for(nleaf, 256), 256, 0, s>>>(dep, P<uint32_t>(h.count), nwarp, nblock);
+    if ((rc = exclusive_scan2_u32(nwarp, wptr, nblock, bptr, nleaf, P<uint32_t>(h.items_tmp), s))) return rc;
+    k_chunk_leaf<<<grid_for(nleaf, 256), 256, 0, s>>>(dep, wptr, bptr, witem, witem + wmax, (uint32_t)wmax, nz);
+    h.launches += 2 + (nleaf <= 2048 ? 1 : 3);
+    TC_CUDA_TRY(cudaGetLastError());
+    return TC_OK;
+}
+
+bool far_coarse_applies(const Handle& h)
+{
+    const int o = h.cfg.order;
+    return (o == 3 || o == 4 || o == 6 || o == 8) && !h.adapt && !h.ctrl_on && !h.m2l_tc &&
+           h.depth > kFarCoarseLevel;
+}
+
+int build_far_coarse(Handle& h)
+{
+    switch (h.cfg.order) {
+    case 3: return far_coarse_order<3>(h);
+    case 4: return far_coarse_order<4>(h);
+    case 6: return far_coarse_order<6>(h);
+    case 8: return far_coarse_order<8>(h);
+    default:
+        tc_set_error("coarse far field: fixed orders 3, 4, 6, 8 only");
+        return TC_ERR_INVALID;
+    }
+}
+
 int build_multipoles(Handle& h)
 {
     switch (h.cfg.order) {

@@ -720,6 +720,8 @@ int build_lists(Handle& h)
                              L.nn_cap[l], nrp, P<uint32_t>(h.idx_pool) + L.near_idx_off[l], L.near_cap[l], 1)))
                 return rc;
             h.launches += 2 + (nl <= 2048 ? 1 : 3);  // count, fill, scan
+            // the levels so far are final: work that reads only them may start on another stream
+            if (l == h.lists_event_level) TC_CUDA_TRY(cudaEventRecord(h.ev_lists, s));
         }
         if (h.nosync) {
             // captured step: the overflow flag lands in pinned memory for the caller to check

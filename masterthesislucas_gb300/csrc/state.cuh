@@ -57,6 +57,14 @@ struct Handle {
     // leaves them out while split_mu is set
     bool split_mu = false;
     cudaEvent_t ev_mu = nullptr;
+    // also on that side stream: the near field's work-item tables (items_ready; their own scratch, items_cnt
+    // and items_tmp, since the list build uses cnt_tmp and tmp meanwhile) and, in a captured step, the far
+    // field's coarse levels once their lists are built (coarse_ready; ev_lists marks list level
+    // lists_event_level built).  The next update clears both flags.
+    bool items_ready = false, coarse_ready = false;
+    int lists_event_level = -1;
+    cudaEvent_t ev_lists = nullptr;
+    Buf items_cnt, items_tmp;
     Buf nearf;
     int depth = -1;
     int64_t n = 0;
@@ -150,6 +158,15 @@ int solve_fmm(Handle& h, double* d_grad, double* d_total, int accumulate, int sc
 // fmm_p.cu (tc_config.order != 0)
 int solve_fmm_order(Handle& h, double* d_grad, double* d_total, int accumulate, int scatter);
 int build_multipoles(Handle& h);
+// the order-p near field's work-item tables on the handle's stream (leaf counts only)
+int near_items(Handle& h);
+// the order-p far field's coarse levels (M2L and L2L of the levels of at most 4^8 nodes) on the handle's
+// stream, for the fused fixed-order path (1, nothing queued, when no earlier solve sized its buffers);
+// far_coarse_applies says whether the handle takes that path
+bool far_coarse_applies(const Handle& h);
+int build_far_coarse(Handle& h);
+// the last level far_coarse covers
+constexpr int kFarCoarseLevel = 8;
 // order-p FP32 tree (tree_p.cu): the node records after the gather of the
 // sorted particles
 int build_records_p(Handle& h, double hleaf);

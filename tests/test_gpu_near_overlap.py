@@ -129,3 +129,42 @@ def test_gradient_buffer_off_a_16_byte_boundary():
         torch.cuda.synchronize()
         assert torch.equal(g_al, g_off)
     s.close()
+
+
+@pytest.mark.parametrize("kernel,order", [("gravity", 8), ("tsne", 4)])
+def test_captured_step_with_coarse_far_field_in_the_update(kernel, order):
+    """A captured step at depth 10 runs the far field's coarse levels (and the near field's item tables) on a
+    side stream of the update, beside its list build; the step's forces and pair sum equal an ordinary
+    update + solve bit for bit, replay after replay."""
+    import torch
+    pos = datasets.two_disks(300000, seed=46).astype(np.float64)
+    pd = torch.from_numpy(pos).cuda()
+    box = np.concatenate([pos.min(0), pos.max(0)])
+    mk = lambda: NBodySolverFMM_SYM_MORTON(kernel, max_children=64, tree_depth=10, theta=0.75, softening=1e-3,  # noqa: E731
+                                           order=order, mac="bmax", leaf_p2p=64)
+    ref = mk()
+    g_ref = torch.zeros_like(pd)
+    t_ref = torch.zeros(1, dtype=torch.float64, device="cuda")
+    ref.update_tree_device(pd, box[:2], box[2:])
+    ref.solve_device(g_ref, t_ref)
+    torch.cuda.synchronize()
+    assert ref.depth() == 10
+    s = mk()
+    g = torch.zeros_like(pd)
+    t = torch.zeros(1, dtype=torch.float64, device="cuda")
+    s.update_tree_device(pd, box[:2], box[2:])
+    s.capture_step(pd, g, t, box=box)
+    for _ in range(3):
+        g.zero_()
+        s.launch_step()
+        torch.cuda.synchronize()
+        assert s.async_status() == 0
+        assert torch.equal(g, g_ref) and float(t.item()) == float(t_ref.item())
+    # an ordinary solve on the captured handle's tree afterwards still matches (it redoes the coarse levels)
+    s.update_tree_device(pd, box[:2], box[2:])
+    g2 = torch.zeros_like(pd)
+    s.solve_device(g2, t)
+    torch.cuda.synchronize()
+    assert torch.equal(g2, g_ref)
+    ref.close()
+    s.close()
