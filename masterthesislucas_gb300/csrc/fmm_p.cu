@@ -1343,6 +1343,11 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
         else
             k_l2l<ORD><<<grid_for(nl, 128), 128, 0, s>>>(l, hl(l), count, comrel, loc, P<uint32_t>(h.act), P<uint32_t>(h.act_pos));
     }
+    // the far field's pair-sum parts, one word per node, summed on its stream while the near field runs
+    const int64_t nsum = sum_tmp_doubles();
+    if ((rc = ensure(h.sumtmp, (2 * nsum + 1) * 8))) return rc;
+    double* zfar = P<double>(h.sumtmp) + 2 * nsum;
+    if ((rc = sum_f64(zp, nn, nullptr, nullptr, zfar, 0, P<double>(h.sumtmp), s))) return rc;
     if ((rc = record(h, 5))) return rc;
     if (h.near_overlap) {
         TC_CUDA_TRY(cudaEventRecord(h.ev_far, s));
@@ -1363,12 +1368,11 @@ int solve_p(Handle& h, KN ker, const PotParams& pp, double* d_grad, int accumula
                                                      d_grad, accumulate, scatter,
                                                      (reinterpret_cast<uintptr_t>(d_grad) & 15) == 0);
     if ((rc = record(h, 6))) return rc;
-    if ((rc = ensure(h.sumtmp, sum_tmp_doubles() * 8)) ||
-        (rc = sum_f64(zp, nn, P<double>(h.zwork), nz, d_total, 1, P<double>(h.sumtmp), s)))
-        return rc;
+    // the pair sum: the far field's total plus the near field's per-item words
+    if ((rc = sum_f64(zfar, 1, P<double>(h.zwork), nz, d_total, 1, P<double>(h.sumtmp) + nsum, s))) return rc;
     // far field (an M2L and an L2L launch per level, one fused launch per fine level), the near field, the
-    // L2P and the two-kernel pair sum; the item tables and a captured update's coarse levels count themselves
-    h.launches += 2 * dep - nfused + 4 - (coarse_done ? 2 * kFarCoarseLevel : 0);
+    // L2P and two two-kernel sums; the item tables and a captured update's coarse levels count themselves
+    h.launches += 2 * dep - nfused + 6 - (coarse_done ? 2 * kFarCoarseLevel : 0);
     TC_CUDA_TRY(cudaGetLastError());
     if (tc_m2l) {
         // the tensor-core M2L's status word (list offsets beyond its operators, a bounded wait that gave up)

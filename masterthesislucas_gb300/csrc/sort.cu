@@ -11,7 +11,10 @@ namespace tc {
 namespace {
 
 constexpr int RT = 256;           // threads per tile
-constexpr int RI = 8;             // keys per thread
+#ifndef TC_SORT_RI
+#define TC_SORT_RI 8
+#endif
+constexpr int RI = TC_SORT_RI;    // keys per thread
 constexpr int RTILE = RT * RI;    // keys per tile
 constexpr int RADIX = 256;
 constexpr int NW = RT / 32;

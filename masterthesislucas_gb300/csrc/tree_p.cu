@@ -153,71 +153,106 @@ __global__ void k_leaf_big_p(int depth, double minx, double miny, double h, cons
     }
 }
 
-// level l from level l + 1: counts, first particle (lowest non-empty child),
-// mass-weighted COM and second moment in the node's cell-relative frame
-// (child centre = node centre + (+-h/4, +-h/4), bit 0 of the child slot is x)
+// node i of level l from level l + 1: counts, first particle (lowest
+// non-empty child), mass-weighted COM and second moment in the node's
+// cell-relative frame (child centre = node centre + (+-h/4, +-h/4), bit 0 of
+// the child slot is x)
+__device__ __forceinline__ void bottom_up_node(int l, int64_t i, double minx, double miny, double hl,
+                                               uint32_t* __restrict__ count, uint32_t* __restrict__ first,
+                                               double2* __restrict__ com64, double* __restrict__ m0,
+                                               double* __restrict__ m2, double2* __restrict__ bbc,
+                                               double* __restrict__ bblen, float* __restrict__ comrel,
+                                               float* __restrict__ m0r, float* __restrict__ m2t,
+                                               float* __restrict__ bmax, int box)
+{
+    const uint32_t li = level_index(l), lc = level_index(l + 1);
+    const float q = (float)(0.25 * hl);
+    const float2* cr2 = reinterpret_cast<const float2*>(comrel);
+    const int64_t node = li + i;
+    const int64_t fc = lc + 4 * i;
+    const uint32_t c4[4] = {count[fc], count[fc + 1], count[fc + 2], count[fc + 3]};
+    const uint32_t cnt = c4[0] + c4[1] + c4[2] + c4[3];
+    if (cnt == 0) {
+        count[node] = 0;
+        first[node] = 0;
+        return;
+    }
+    uint32_t fp = 0;
+    float sx = 0.f, sy = 0.f;
+    float2 g[4];
+    double2 bbox = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int j = 3; j >= 0; j--) {
+        g[j] = make_float2(0.f, 0.f);
+        if (c4[j] == 0) continue;
+        fp = first[fc + j];
+        // bottomUpNodeConstruction's box (:381-470): offset[j] * L_child + BBcentre_child, the lowest
+        // non-empty child last (bit 0 of the child slot is x)
+        const double cl = bblen[fc + j];
+        const double2 cb = bbc[fc + j];
+        bbox = make_double2(__dadd_rn(__dmul_rn((j & 1) ? -0.5 : 0.5, cl), cb.x),
+                           __dadd_rn(__dmul_rn((j & 2) ? -0.5 : 0.5, cl), cb.y));
+        const float2 r = cr2[fc + j];
+        g[j] = make_float2(r.x + ((j & 1) ? q : -q), r.y + ((j & 2) ? q : -q));
+        sx = fmaf((float)c4[j], g[j].x, sx);
+        sy = fmaf((float)c4[j], g[j].y, sy);
+    }
+    const float ic = 1.0f / (float)cnt;
+    sx *= ic;
+    sy *= ic;
+    // box-centred expansions: the node's frame is its cell centre, and bmax bounds its particles'
+    // distance from there
+    if (box) sx = sy = 0.f;
+    float a = 0.f, b = 0.f, d = 0.f, br = 0.f;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        if (c4[j] == 0) continue;
+        const float w = (float)c4[j];
+        const float rx = g[j].x - sx, ry = g[j].y - sy;
+        a += w * (m2t[3 * (fc + j)] + rx * rx);
+        b += w * (m2t[3 * (fc + j) + 1] + rx * ry);
+        d += w * (m2t[3 * (fc + j) + 2] + ry * ry);
+        // every particle of child j lies within bmax_j of the child's COM
+        br = fmaxf(br, sqrtf(fmaf(rx, rx, ry * ry)) + bmax[fc + j]);
+    }
+    count[node] = cnt;
+    first[node] = fp;
+    write_node(node, cell_centre(i, minx, miny, hl), bbox, hl, cnt, sx, sy, a, b, d, br, com64, m0, m2, bbc, bblen,
+               comrel, m0r, m2t, bmax);
+}
+
+// level l from level l + 1, a thread per node
 __global__ void k_bottom_up_p(int l, double minx, double miny, double hl, uint32_t* __restrict__ count,
                               uint32_t* __restrict__ first, double2* __restrict__ com64, double* __restrict__ m0,
                               double* __restrict__ m2, double2* __restrict__ bbc, double* __restrict__ bblen,
                               float* __restrict__ comrel, float* __restrict__ m0r, float* __restrict__ m2t,
                               float* __restrict__ bmax, int box)
 {
-    const uint32_t li = level_index(l), lc = level_index(l + 1);
     const int64_t nl = (int64_t)1 << (2 * l);
-    const float q = (float)(0.25 * hl);
-    const float2* cr2 = reinterpret_cast<const float2*>(comrel);
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t node = li + i;
-        const int64_t fc = lc + 4 * i;
-        const uint32_t c4[4] = {count[fc], count[fc + 1], count[fc + 2], count[fc + 3]};
-        const uint32_t cnt = c4[0] + c4[1] + c4[2] + c4[3];
-        if (cnt == 0) {
-            count[node] = 0;
-            first[node] = 0;
-            continue;
-        }
-        uint32_t fp = 0;
-        float sx = 0.f, sy = 0.f;
-        float2 g[4];
-        double2 bbox = make_double2(0.0, 0.0);
-#pragma unroll
-        for (int j = 3; j >= 0; j--) {
-            g[j] = make_float2(0.f, 0.f);
-            if (c4[j] == 0) continue;
-            fp = first[fc + j];
-            // bottomUpNodeConstruction's box (:381-470): offset[j] * L_child + BBcentre_child, the lowest
-            // non-empty child last (bit 0 of the child slot is x)
-            const double cl = bblen[fc + j];
-            const double2 cb = bbc[fc + j];
-            bbox = make_double2(__dadd_rn(__dmul_rn((j & 1) ? -0.5 : 0.5, cl), cb.x),
-                               __dadd_rn(__dmul_rn((j & 2) ? -0.5 : 0.5, cl), cb.y));
-            const float2 r = cr2[fc + j];
-            g[j] = make_float2(r.x + ((j & 1) ? q : -q), r.y + ((j & 2) ? q : -q));
-            sx = fmaf((float)c4[j], g[j].x, sx);
-            sy = fmaf((float)c4[j], g[j].y, sy);
-        }
-        const float ic = 1.0f / (float)cnt;
-        sx *= ic;
-        sy *= ic;
-        // box-centred expansions: the node's frame is its cell centre, and bmax bounds its particles'
-        // distance from there
-        if (box) sx = sy = 0.f;
-        float a = 0.f, b = 0.f, d = 0.f, br = 0.f;
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            if (c4[j] == 0) continue;
-            const float w = (float)c4[j];
-            const float rx = g[j].x - sx, ry = g[j].y - sy;
-            a += w * (m2t[3 * (fc + j)] + rx * rx);
-            b += w * (m2t[3 * (fc + j) + 1] + rx * ry);
-            d += w * (m2t[3 * (fc + j) + 2] + ry * ry);
-            // every particle of child j lies within bmax_j of the child's COM
-            br = fmaxf(br, sqrtf(fmaf(rx, rx, ry * ry)) + bmax[fc + j]);
-        }
-        count[node] = cnt;
-        first[node] = fp;
-        write_node(node, cell_centre(i, minx, miny, hl), bbox, hl, cnt, sx, sy, a, b, d, br, com64, m0, m2, bbc,
-                   bblen, comrel, m0r, m2t, bmax);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x)
+        bottom_up_node(l, i, minx, miny, hl, count, first, com64, m0, m2, bbc, bblen, comrel, m0r, m2t, bmax, box);
+}
+
+// levels l0 .. 0 in one block (the coarse levels, a few thousand nodes at
+// most: per-level launches would cost more than their work), a barrier
+// between levels; hl0 is level l0's cell size
+constexpr int kBottomUpCoarseLevel = 6;
+__global__ void __launch_bounds__(1024) k_bottom_up_coarse(int l0, double minx, double miny, double hl0,
+                                                           uint32_t* __restrict__ count, uint32_t* __restrict__ first,
+                                                           double2* __restrict__ com64, double* __restrict__ m0,
+                                                           double* __restrict__ m2, double2* __restrict__ bbc,
+                                                           double* __restrict__ bblen, float* __restrict__ comrel,
+                                                           float* __restrict__ m0r, float* __restrict__ m2t,
+                                                           float* __restrict__ bmax, int box)
+{
+    double hl = hl0;
+    for (int l = l0; l >= 0; l--) {
+        const int64_t nl = (int64_t)1 << (2 * l);
+        for (int64_t i = threadIdx.x; i < nl; i += blockDim.x)
+            bottom_up_node(l, i, minx, miny, hl, count, first, com64, m0, m2, bbc, bblen, comrel, m0r, m2t, bmax,
+                           box);
+        __syncthreads();
+        hl *= 2.0;
     }
 }
 
@@ -242,7 +277,7 @@ int build_records_p(Handle& h, double hleaf)
         P<double2>(h.com64), P<double>(h.m0), P<double>(h.m2), P<double2>(h.bbc), P<double>(h.bblen),
         P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t), P<uint32_t>(h.bigleaf), P<float>(h.bmax), box);
     h.launches += 2;
-    for (int l = depth - 1; l >= 0; l--) {
+    for (int l = depth - 1; l > kBottomUpCoarseLevel; l--) {
         const double hl = h.L / (double)(1u << l);
         const int64_t nl = (int64_t)1 << (2 * l);
         k_bottom_up_p<<<grid_for(nl, 128), 128, 0, s>>>(l, h.minx, h.miny, hl, P<uint32_t>(h.count),
@@ -250,6 +285,15 @@ int build_records_p(Handle& h, double hleaf)
                                                         P<double>(h.m2), P<double2>(h.bbc), P<double>(h.bblen),
                                                         P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t),
                                                         P<float>(h.bmax), box);
+        h.launches++;
+    }
+    if (depth > 0) {
+        const int l0 = depth - 1 < kBottomUpCoarseLevel ? depth - 1 : kBottomUpCoarseLevel;
+        k_bottom_up_coarse<<<1, 1024, 0, s>>>(l0, h.minx, h.miny, h.L / (double)(1u << l0), P<uint32_t>(h.count),
+                                              P<uint32_t>(h.first), P<double2>(h.com64), P<double>(h.m0),
+                                              P<double>(h.m2), P<double2>(h.bbc), P<double>(h.bblen),
+                                              P<float>(h.comrel), P<float>(h.m0r), P<float>(h.m2t), P<float>(h.bmax),
+                                              box);
         h.launches++;
     }
     TC_CUDA_TRY(cudaGetLastError());
