@@ -66,8 +66,11 @@ __device__ inline bool mac_accept_fast(int dix, int diy, real hl, real thr2, con
     return variant ? mac_accept_m(a, b, len, theta) : mac_accept(a, b, len, inv_theta);
 }
 
-// levels of up to this many cells (4^8) build their lists with a warp per node
-constexpr int64_t kListsWarpLevelNodes = (int64_t)1 << 16;
+// levels of up to this many cells (4^TC_LISTS_WARP_LEVEL) build their lists with a warp per node
+#ifndef TC_LISTS_WARP_LEVEL
+#define TC_LISTS_WARP_LEVEL 8
+#endif
+constexpr int64_t kListsWarpLevelNodes = (int64_t)1 << (2 * TC_LISTS_WARP_LEVEL);
 
 // Squared-ratio thresholds of the per-pair order rule: an accepted pair with
 // (b_A + b_B)^2 <= t[o] |dcom|^2 takes order bucket o (orders 4, 6, 8, 10, 12);
