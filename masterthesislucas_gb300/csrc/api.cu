@@ -424,9 +424,23 @@ static int update_common(Handle& h, const double* d_pos, int64_t n, const double
         h.items_ready = rc == TC_OK;
     }
     if (!rc && (rc = after_tree()) == TC_OK) {
+        // beside the side stream's work the list build (the update's critical path) runs on the
+        // high-priority stream, forked from and joined back to the handle's stream
+        const bool hp = forked && h.far_stream;
+        if (hp) {
+            TC_CUDA_TRY(cudaEventRecord(h.ev_fork, main));
+            TC_CUDA_TRY(cudaStreamWaitEvent(h.far_stream, h.ev_fork, 0));
+            h.stream = h.far_stream;
+        }
         h.lists_event_level = coarse ? kFarCoarseLevel : -1;
         rc = build_lists(h);  // synchronises the stream (list sizes), except in no-sync mode
         h.lists_event_level = -1;
+        h.stream = main;
+        if (hp) {
+            cudaError_t e = cudaEventRecord(h.ev_far, h.far_stream);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(main, h.ev_far, 0);
+            if (!rc && e != cudaSuccess) rc = tc_cuda_fail(e, "list-build join");
+        }
     }
     if (!rc && coarse) {
         TC_CUDA_TRY(cudaStreamWaitEvent(h.near_stream, h.ev_lists, 0));
