@@ -426,7 +426,10 @@ static int update_common(Handle& h, const double* d_pos, int64_t n, const double
     if (!rc && (rc = after_tree()) == TC_OK) {
         // beside the side stream's work the list build (the update's critical path) runs on the
         // high-priority stream, forked from and joined back to the handle's stream
-        const bool hp = forked && h.far_stream;
+#ifndef TC_LISTS_PRIORITY
+#define TC_LISTS_PRIORITY 1
+#endif
+        const bool hp = TC_LISTS_PRIORITY && forked && h.far_stream;
         if (hp) {
             TC_CUDA_TRY(cudaEventRecord(h.ev_fork, main));
             TC_CUDA_TRY(cudaStreamWaitEvent(h.far_stream, h.ev_fork, 0));
