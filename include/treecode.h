@@ -136,7 +136,8 @@ int tc_set_m2l_engine(tc_handle* h, int engine);
  * beside the far field (M2L, L2L): it reads only the tree and its lists.  The
  * L2P, which adds the final local expansions to the near-field forces, waits
  * for both.  on = 0 runs the two in sequence on the handle's stream (the
- * results are identical either way).  Default on.                          */
+ * results are identical either way).  Default on; tc_tsne_batch_create
+ * turns it off for its systems (their graphs already run side by side).    */
 int tc_set_near_overlap(tc_handle* h, int on);
 
 /* Per-pair expansion order on a TC_MAC_BMAX handle of order p in {6, 8, 10,

@@ -50,7 +50,10 @@ struct Handle {
     // order-p solves: the near field on near_stream beside the far field on far_stream (higher priority),
     // both forked by ev_fork and joined by ev_join / ev_far before the L2P; the near field's FP32 forces
     // in nearf (sorted order)
-    bool near_overlap = true;
+#ifndef TC_NEAR_OVERLAP_DEFAULT
+#define TC_NEAR_OVERLAP_DEFAULT 1
+#endif
+    bool near_overlap = TC_NEAR_OVERLAP_DEFAULT;
     cudaStream_t near_stream = nullptr, far_stream = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_far = nullptr;
     // the update's multipoles on near_stream beside the list build (ev_mu marks them done); build_tree

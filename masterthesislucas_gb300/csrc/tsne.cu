@@ -493,6 +493,9 @@ int tc_tsne_batch_create(tc_tsne* const* systems, int count, double margin, tc_t
     // list regions twice the last exact totals: while the embeddings grow, a region that
     // overflows costs an uncaptured re-step and a re-capture of that system
     for (tc_tsne* t : b->sys) t->hs->cap_slack = 1.0;
+    // one graph holds all the systems, which already run side by side: each system's near field stays on its
+    // own stream after its far field (its fork/join branches and priorities measured slower in the batch)
+    for (tc_tsne* t : b->sys) t->hs->near_overlap = false;
     cudaError_t e = cudaStreamCreateWithFlags(&b->s0, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_prm, 64);
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_ext, 64);
