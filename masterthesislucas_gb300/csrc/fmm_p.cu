@@ -450,8 +450,11 @@ __device__ __forceinline__ void l2l_into(int64_t node, int l, float ih, const fl
 // L2L, plus the parent's final local expansion shifted to A (the level's L2L
 // fused in: A's sum is not written and read back), held to the unfused form's
 // registers so the M2L loop keeps its resident warps
+#ifndef TC_M2L_FUSED_MIN_BLOCKS
+#define TC_M2L_FUSED_MIN_BLOCKS 4  // resident blocks per SM of the order-8 fused M2L + L2L
+#endif
 template <int P, bool L2L = false>
-__global__ void __launch_bounds__(128, L2L ? (P >= 8 ? 4 : P >= 6 ? 5 : 7) : 1) k_m2l_p(int l, float hl, PotParams pp, const uint32_t* __restrict__ nn_ptr,
+__global__ void __launch_bounds__(128, L2L ? (P >= 8 ? TC_M2L_FUSED_MIN_BLOCKS : P >= 6 ? 5 : 7) : 1) k_m2l_p(int l, float hl, PotParams pp, const uint32_t* __restrict__ nn_ptr,
                                                const uint32_t* __restrict__ nn_idx, const uint32_t* __restrict__ count,
                                                const float* __restrict__ comrel, const float* __restrict__ mu,
                                                float* __restrict__ loc, double* __restrict__ zpart, const uint32_t* __restrict__ act, const uint32_t* __restrict__ act_pos)
