@@ -84,3 +84,17 @@ def test_direct_rejects_more_rows_than_points_without_a_row_list(L, fn):
     assert b"invalid" in L.tc_last_error()
     # an unknown precision code is rejected the same way
     assert f(1, 1e-3, 7, fake, 100, None, 10, fake, None, None) == -1
+
+
+def test_stage_names_match_the_header():
+    """tc_get_stage_times writes TC_NSTAGES doubles; the Python mirror names each of them."""
+    from masterthesislucas_gb300 import NBodySolverFMM_SYM_MORTON
+    src = open(os.path.join(ROOT, "include", "treecode.h")).read()
+    n = int(re.search(r"#define\s+TC_NSTAGES\s+(\d+)", src).group(1))
+    assert len(NBodySolverFMM_SYM_MORTON.STAGES) == n
+    assert NBodySolverFMM_SYM_MORTON.STAGES[-1] == "reduce" and "l2p" in NBodySolverFMM_SYM_MORTON.STAGES
+
+
+def test_near_overlap_switch_needs_no_gpu(L):
+    """Setting the near/far overlap is host state only (a null handle is rejected)."""
+    assert L.tc_set_near_overlap(None, 0) == _lib.TC_ERR_INVALID
