@@ -777,9 +777,13 @@ __global__ void k_chunk_leaf(int dep, const uint32_t* __restrict__ wptr, const u
     if (blockIdx.x == 0 && threadIdx.x == 0) *nz = min(min(wptr[nl], cap) + min(bptr[nl], cap), cap);
 }
 
-// Sources staged per warp (float2, in the sink leaf's frame).  The whole near
-// list of a sink leaf is usually a few hundred particles, so one or two fills.
-constexpr int kNearBuf = 256;
+// Sources staged per warp (a block item stages kNearWarps times as many), in
+// the sink leaf's frame.  The whole near list of a sink leaf is usually a few
+// hundred particles, so one or two fills (256 measured 0.4 % slower per step).
+#ifndef TC_NEAR_BUF
+#define TC_NEAR_BUF 512
+#endif
+constexpr int kNearBuf = TC_NEAR_BUF;
 // Padding source: far enough that its force factor underflows to zero and its
 // pair term (~1e-18 gravity, ~1e-36 t-SNE) is absorbed by any real sum.
 constexpr float kFarAway = 1.0e18f;
