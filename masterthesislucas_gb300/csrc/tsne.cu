@@ -313,6 +313,9 @@ struct tc_tsne_batch {
     int device = 0;
     cudaStream_t s0 = nullptr;
     cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};
+    // the graphs exec[k] was instantiated from: node[k] belongs to root[k], and an in-place update of one
+    // system's child node needs that graph alive
+    cudaGraph_t root[3] = {nullptr, nullptr, nullptr};
     Buf prm, ext;
     double* h_prm = nullptr;
     uint64_t* h_ext = nullptr;
@@ -432,6 +435,10 @@ int build_exec(tc_tsne_batch* b, int k)
         cudaGraphExecDestroy(b->exec[k]);
         b->exec[k] = nullptr;
     }
+    if (b->root[k]) {
+        cudaGraphDestroy(b->root[k]);
+        b->root[k] = nullptr;
+    }
     cudaGraph_t root = nullptr;
     TC_CUDA_TRY(cudaGraphCreate(&root, 0));
     b->node[k].assign(b->sys.size(), nullptr);
@@ -439,21 +446,29 @@ int build_exec(tc_tsne_batch* b, int k)
     for (size_t i = 0; i < b->sys.size() && e == cudaSuccess; i++)
         e = cudaGraphAddChildGraphNode(&b->node[k][i], root, nullptr, 0, b->g[i][k]);
     if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec[k], root, cudaGraphInstantiateFlagUseNodePriority);
-    cudaGraphDestroy(root);
     if (e != cudaSuccess) {
+        cudaGraphDestroy(root);
         b->exec[k] = nullptr;
+        b->node[k].assign(b->sys.size(), nullptr);
         return tc_cuda_fail(e, "batch graph");
     }
+    // kept: a re-captured system is swapped in through its node (cudaGraphExecChildGraphNodeSetParams)
+    b->root[k] = root;
     return TC_OK;
 }
 
 void drop_all(tc_tsne_batch* b)
 {
-    for (int k = 0; k < 3; k++)
+    for (int k = 0; k < 3; k++) {
         if (b->exec[k]) {
             cudaGraphExecDestroy(b->exec[k]);
             b->exec[k] = nullptr;
         }
+        if (b->root[k]) {
+            cudaGraphDestroy(b->root[k]);
+            b->root[k] = nullptr;
+        }
+    }
     for (auto& gs : b->g)
         for (cudaGraph_t& g : gs)
             if (g) {
