@@ -779,7 +779,8 @@ __global__ void k_chunk_leaf(int dep, const uint32_t* __restrict__ wptr, const u
 
 // Sources staged per warp (a block item stages kNearWarps times as many), in
 // the sink leaf's frame.  The whole near list of a sink leaf is usually a few
-// hundred particles, so one or two fills (256 measured 0.4 % slower per step).
+// hundred particles, so one or two fills (256 measured 0.4 % slower per step; 768,
+// whose 24 KB per block leaves room for one block fewer per SM, 1.6 % slower).
 #ifndef TC_NEAR_BUF
 #define TC_NEAR_BUF 512
 #endif
